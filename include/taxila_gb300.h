@@ -1,0 +1,193 @@
+/*
+ * taxila_gb300.h - C ABI of the GB300 Shan-Chen lattice-Boltzmann step.
+ *
+ * This library is a drop-in for the flow part of Taxila LBM's time step.  The
+ * reference runs, once per step, the Fortran module procedures
+ *
+ *   FlowCollision              (src/lbm/lbm_flow.F90:936-958)
+ *   DistributionCommunicateFi  (src/lbm/lbm_distribution_function.F90:309-314)
+ *   FlowStream                 (src/lbm/lbm_flow.F90:810-814)
+ *   FlowBounceback             (src/lbm/lbm_flow.F90:816-820)
+ *   FlowApplyBCs               (src/lbm/lbm_flow.F90:1958-1991)
+ *   FlowUpdateFlux             (src/lbm/lbm_flow.F90:458-464)
+ *
+ * from LBMRun2 (src/lbm/lbm.F90:279-406), and FlowFiInit + FlowUpdateMoments
+ * from LBMInit2 (src/lbm/lbm.F90:212, :238).  tx_init and tx_step replace those
+ * calls; the Fortran host keeps the options deck, the plugins, I/O and the
+ * loop.  All arrays crossing this boundary are host arrays in the reference's
+ * natural (PETSc global vector) order: for a field with `dof` values per
+ * lattice site the value (d, i, j, k) is at d + dof*(i + NX*(j + NY*k)),
+ * i.e. the dof index fastest, then x, y, z.  Populations use
+ * dof = m + s*n (component fastest), exactly as the reference's fi vector
+ * (src/lbm/lbm_distribution_function.F90:197-202).
+ *
+ * Every entry point returns 0 on success and a nonzero TX_ERR_* code on
+ * failure (the reference's PetscErrorCode convention, src/lbm/lbm.F90:122-136);
+ * tx_last_error() gives the message.  The device never traps: NaN/Inf
+ * populations and exhausted step budgets come back as status codes.
+ * A handle is single-threaded and owns one CUDA stream and all device memory.
+ */
+#ifndef TAXILA_GB300_H
+#define TAXILA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TX_MAX_COMPONENTS 4  /* reference NMAX_COMPONENTS = 5 (include/lbm_definitions.h:79) */
+#define TX_MAX_MINERALS 16
+
+/* discretization enum values of include/lbm_definitions.h:9-11 */
+#define TX_D3Q19 1
+#define TX_D2Q9 2
+
+/* relaxation modes, include/lbm_definitions.h:68-69 */
+#define TX_RELAX_SRT 0
+#define TX_RELAX_MRT 1
+
+/* per-face flow BC kinds, include/lbm_definitions.h:31-44 (subset on this path) */
+#define TX_BC_NULL 0     /* non-periodic face closed by ghost walls (bounceback) */
+#define TX_BC_PERIODIC 1
+#define TX_BC_DENSITY 6  /* Dirichlet density face (BC_DIRICHLET + BC_DENSITY) */
+
+/* faces, include/lbm_definitions.h:47-52 (index = value - 1 in arrays below) */
+#define TX_XM 1
+#define TX_XP 2
+#define TX_YM 3
+#define TX_YP 4
+#define TX_ZM 5
+#define TX_ZP 6
+
+/* storage/arithmetic forms */
+#define TX_PREC_F64 0      /* plain form: FP64 populations and arithmetic */
+#define TX_PREC_F32 1      /* FP32 arithmetic, FP32 populations stored as f - w_n*rho0 */
+#define TX_PREC_F32_F16 2  /* FP32 arithmetic, FP16 populations stored as f - w_n*rho0 */
+
+/* fields for tx_download / tx_delta_norm */
+#define TX_FIELD_FI 1      /* s*Q dof: populations after the step (reference fi)          */
+#define TX_FIELD_RHO 2     /* s dof: component densities (reference rho)                  */
+#define TX_FIELD_FLUX 3    /* s*ndims dof: reference flux array = common velocity u_eq    */
+#define TX_FIELD_FORCES 4  /* s*ndims dof: Shan-Chen + fluid-solid + body forces          */
+#define TX_FIELD_PRS 5     /* 1 dof: pressure diagnostic (FlowUpdateDiagnostics)          */
+#define TX_FIELD_VELT 6    /* ndims dof: total velocity diagnostic                        */
+#define TX_FIELD_RHOT 7    /* 1 dof: total mass density diagnostic                        */
+#define TX_FIELD_WALLS 8   /* 1 dof: wall codes as uploaded                               */
+
+/* error codes */
+#define TX_OK 0
+#define TX_ERR_ARG 1       /* invalid argument / unsupported parameter combination */
+#define TX_ERR_STATE 2     /* call out of order (e.g. tx_step before tx_init) */
+#define TX_ERR_CUDA 3      /* CUDA runtime error (message has the CUDA string) */
+#define TX_ERR_NOMEM 4     /* device allocation failed or over the memory budget */
+#define TX_ERR_NONFINITE 5 /* NaN/Inf detected in a reduction */
+#define TX_ERR_NODEVICE 6  /* no CUDA device / kernels not built for this device */
+
+typedef struct tx_params {
+  int32_t discretization;   /* TX_D2Q9 or TX_D3Q19 (-discretization) */
+  int32_t nx, ny, nz;       /* -NX -NY -NZ (nz = 1 for D2Q9) */
+  int32_t ncomponents;      /* -ncomponents, 1..TX_MAX_COMPONENTS */
+  int32_t nminerals;        /* -nminerals, 0..TX_MAX_MINERALS */
+  int32_t relaxation_mode;  /* -flow_relaxation_mode */
+  int32_t isotropy_order;   /* -isotropy_order / -derivative_order: 4, 8 (D2Q9 also 10) */
+  int32_t bc_flags[6];      /* TX_BC_* per face XM..ZP; periodic faces come in pairs */
+  double tau[TX_MAX_COMPONENTS];  /* -tau_<c> (SRT) */
+  double s_c[TX_MAX_COMPONENTS];  /* -s_c_<c> .. -s_m_<c> (MRT rates) */
+  double s_e[TX_MAX_COMPONENTS];
+  double s_e2[TX_MAX_COMPONENTS];
+  double s_q[TX_MAX_COMPONENTS];
+  double s_nu[TX_MAX_COMPONENTS];
+  double s_pi[TX_MAX_COMPONENTS];
+  double s_m[TX_MAX_COMPONENTS];
+  double mm[TX_MAX_COMPONENTS];                       /* -mm_<c> molecular masses */
+  double g[TX_MAX_COMPONENTS][TX_MAX_COMPONENTS];     /* -g_<mn>: g[m][n] */
+  double gw[TX_MAX_MINERALS][TX_MAX_COMPONENTS];      /* -gw_<mineral>_<c> */
+  int32_t body_forces;      /* 1 when -gvt was given */
+  double gvt[3];            /* -gvt */
+  double bc_density[6][TX_MAX_COMPONENTS];  /* -bc_density_<face>_<c> for TX_BC_DENSITY faces */
+  int32_t literal_kind;     /* 4: the reference's default-REAL literals (1./6. etc.) are
+                               single precision, as built without -fdefault-real-8; 8: double */
+  int32_t precision;        /* TX_PREC_* */
+  int32_t exact;            /* 1: reference operation order, IEEE divides, no FMA (FP64 only) */
+  double rho0;              /* reference density of the shifted storage (precision forms) */
+} tx_params;
+
+typedef struct tx_handle tx_handle;
+
+/* Fill *p with the reference's defaults (lbm_options.F90:105-148,
+ * lbm_relaxation.F90:65-84, lbm_component.F90:99-111). */
+int tx_params_default(tx_params* p);
+
+/* LBMSetUp (src/lbm/lbm.F90:140-175) for the flow: validates the parameters
+ * (FlowSetFromOptions, lbm_flow.F90:188-284) and allocates device state. */
+int tx_create(const tx_params* p, tx_handle** out);
+
+/* LBMDestroy (src/lbm/lbm.F90:99-108). */
+int tx_destroy(tx_handle* h);
+
+/* Last error message of this handle (or of the last failed tx_create when h is NULL). */
+const char* tx_last_error(const tx_handle* h);
+
+/* WallsSetValues (src/lbm/lbm_walls.F90:151-177): natural-order wall codes,
+ * NX*NY*NZ doubles.  0 = pore, 1..nminerals = mineral, other positive values
+ * (e.g. 800, 999) = plain wall.  Ghost walls on non-periodic faces are added
+ * by the library (WallsSetGhostNodes, lbm_walls.F90:179-231). */
+int tx_upload_walls(tx_handle* h, const double* walls);
+
+/* The initialize_state plugin's output (src/lbm/lbm.F90:444-453): rho
+ * (s dof) and u (s*ndims dof, the reference flux array) in natural order;
+ * u may be NULL for a fluid at rest. */
+int tx_upload_state(tx_handle* h, const double* rho, const double* u);
+
+/* -ic_file / restart (src/lbm/lbm.F90:482-544): populations, s*Q dof. */
+int tx_upload_fi(tx_handle* h, const double* fi);
+
+/* The initialize_bcs plugin's face arrays (src/lbm/lbm_bc.F90:215-228):
+ * vals has nbcs = s*ndims values per face node (component fastest, only the
+ * first s used for density faces), face nodes in natural order of the two
+ * tangential axes.  Optional: tx_create fills faces from bc_density. */
+int tx_upload_bc_values(tx_handle* h, int32_t face, const double* vals);
+
+/* LBMInit2 for istep = 0 (src/lbm/lbm.F90:183-253): FlowFiInit (unless
+ * populations were uploaded) then FlowUpdateMoments. */
+int tx_init(tx_handle* h);
+
+/* nsteps iterations of the flow part of LBMRun2's loop body (lbm.F90:283-363). */
+int tx_step(tx_handle* h, int32_t nsteps);
+
+/* DistributionCalcDeltaNorm (lbm_distribution_function.F90:809-833):
+ * ||(old - new)/new||_inf of TX_FIELD_RHO or TX_FIELD_FI against the values
+ * saved by the previous call (first call: against zero).  Sites where new
+ * is 0 contribute 0.  FP64 device reduction. */
+int tx_delta_norm(tx_handle* h, int32_t field, double* norm);
+
+/* Copy a field to a host array in natural order (see TX_FIELD_*). */
+int tx_download(tx_handle* h, int32_t field, double* out);
+
+/* Number of doubles tx_download writes for a field. */
+int64_t tx_field_size(const tx_handle* h, int32_t field);
+
+/* Block until all work queued on the handle's stream is done. */
+int tx_sync(tx_handle* h);
+
+/* ---- instrumentation (no counterpart in the reference; used by bench.py) ---- */
+
+/* Per-kernel CUDA-event timing of tx_step on the handle's stream (resets the totals). */
+int tx_set_timing(tx_handle* h, int32_t on);
+
+/* Accumulated milliseconds of the collide-push and density launches and the
+ * number of kernel launches since tx_set_timing. */
+int tx_get_timing(tx_handle* h, double* ms_step, double* ms_density, int64_t* launches);
+
+/* The handle's cudaStream_t (as void*), for callers that order their own work after it. */
+void* tx_get_stream(tx_handle* h);
+
+/* Name of the kernel variant selected by tx_create. */
+const char* tx_kernel_name(const tx_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TAXILA_GB300_H */

@@ -1,0 +1,567 @@
+// C ABI of the GB300 Shan-Chen step (include/taxila_gb300.h): handle, device
+// memory, parameter translation and kernel dispatch.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/taxila_gb300.h"
+#include "tx_dispatch.h"
+
+using namespace tx;
+
+static std::string g_create_error;
+
+struct tx_handle {
+  tx_params p{};
+  int D = 3, S = 1, Q = 19;
+  Geo g{};
+  Phys ph{};
+  Faces faces{};
+  KernelSet ks{};
+  cudaStream_t stream = nullptr;
+  size_t pop_bytes = 0;       // bytes of one population element
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;                // f[cur] holds the current state
+  void* rho = nullptr;        // forcing density
+  size_t rho_bytes = 0;
+  uint8_t* mask = nullptr;
+  double* faceval[6] = {nullptr};
+  long long face_n[6] = {0};
+  double* stage = nullptr;    // natural-order staging buffer (largest field)
+  double* old_rho = nullptr;
+  double* old_fi = nullptr;
+  double* uic = nullptr;
+  unsigned long long* red = nullptr;  // [0] max bits, [1] non-finite count
+  std::vector<uint8_t> host_mask;
+  bool have_walls = false, have_state = false, have_fi = false, inited = false;
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_step_ms = 0.0, t_density_ms = 0.0;
+  long long n_step_launch = 0, n_density_launch = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(tx_handle* h, int code, const std::string& msg) {
+  if (h)
+    h->err = msg;
+  else
+    g_create_error = msg;
+  return code;
+}
+
+#define TX_CUDA(h, call)                                                                   \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(h, TX_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+int check_launch(tx_handle* h, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, TX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return TX_OK;
+}
+
+StepArgs args(tx_handle* h, int in, int out) {
+  StepArgs a{};
+  a.fin = h->f[in];
+  a.fout = h->f[out];
+  a.rho = h->rho;
+  a.mask = h->mask;
+  a.g = h->g;
+  a.faces = h->faces;
+  return a;
+}
+
+long long field_dof(const tx_handle* h, int field) {
+  switch (field) {
+    case TX_FIELD_FI: return (long long)h->S * h->Q;
+    case TX_FIELD_RHO: return h->S;
+    case TX_FIELD_FLUX:
+    case TX_FIELD_FORCES: return (long long)h->S * h->D;
+    case TX_FIELD_PRS:
+    case TX_FIELD_RHOT:
+    case TX_FIELD_WALLS: return 1;
+    case TX_FIELD_VELT: return h->D;
+  }
+  return -1;
+}
+
+int validate(const tx_params* p, std::string* why) {
+  auto bad = [&](const std::string& s) {
+    *why = s;
+    return TX_ERR_ARG;
+  };
+  if (p->discretization != TX_D3Q19 && p->discretization != TX_D2Q9) return bad("discretization must be TX_D3Q19 or TX_D2Q9");
+  const int D = p->discretization == TX_D3Q19 ? 3 : 2;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1) return bad("lattice sizes must be >= 1");
+  if (D == 2 && p->nz != 1) return bad("D2Q9 needs nz = 1");
+  if (p->ncomponents < 1 || p->ncomponents > TX_MAX_COMPONENTS) return bad("ncomponents out of range");
+  if (p->ncomponents > kMaxBuiltComponents)
+    return bad("ncomponents > " + std::to_string(kMaxBuiltComponents) + " is not built into this library");
+  if (p->nminerals < 0 || p->nminerals > TX_MAX_MINERALS) return bad("nminerals out of range");
+  if (p->relaxation_mode != TX_RELAX_SRT && p->relaxation_mode != TX_RELAX_MRT) return bad("relaxation_mode must be 0 or 1");
+  if (!(p->isotropy_order == 4 || p->isotropy_order == 8 || (D == 2 && p->isotropy_order == 10)))
+    return bad(D == 3 ? "isotropy_order must be 4 or 8 for D3Q19 (the reference errors on 10)"
+                      : "isotropy_order must be 4, 8 or 10");
+  if (p->precision < TX_PREC_F64 || p->precision > TX_PREC_F32_F16) return bad("unknown precision form");
+  if (p->exact && p->precision != TX_PREC_F64) return bad("exact operation order exists for the FP64 form only");
+  for (int a = 0; a < D; ++a) {
+    const int lo = p->bc_flags[2 * a], hi = p->bc_flags[2 * a + 1];
+    if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
+    for (int f : {2 * a, 2 * a + 1}) {
+      const int v = p->bc_flags[f];
+      if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
+        return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
+    }
+  }
+  for (int m = 0; m < p->ncomponents; ++m) {
+    if (p->relaxation_mode == TX_RELAX_SRT && !(p->tau[m] > 0.0)) return bad("tau must be > 0");
+    if (!(p->mm[m] > 0.0)) return bad("molecular masses must be > 0");
+  }
+  return TX_OK;
+}
+
+void fill_phys(tx_handle* h) {
+  const tx_params& p = h->p;
+  Phys& P = h->ph;
+  std::memset(&P, 0, sizeof(P));
+  const int S = h->S;
+  for (int m = 0; m < S; ++m) {
+    P.tau[m] = p.tau[m];
+    P.inv_tau[m] = 1.0 / p.tau[m];
+    P.cs2[m] = 1.0 / 3.0;                     // lbm_relaxation.F90:82
+    P.inv_cs2[m] = 3.0;
+    P.dk[m] = 1. - 2. / (3. * p.mm[m]);        // lbm_component.F90:158
+    P.mm[m] = p.mm[m];
+    const double s_c = p.relaxation_mode == TX_RELAX_SRT ? 1.0 / p.tau[m] : p.s_c[m];  // lbm_relaxation.F90:133
+    P.mmot[m] = p.mm[m] * s_c;
+    for (int k = 0; k < S; ++k) P.g[m][k] = p.g[m][k];
+    const double rates[7] = {p.s_c[m], p.s_e[m], p.s_e2[m], p.s_q[m], p.s_nu[m], p.s_pi[m], p.s_m[m]};
+    for (int k = 0; k < h->Q; ++k) {
+      const int r = h->D == 3 ? rate_of<3>(k) : rate_of<2>(k);
+      const int mmt = h->D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
+      P.srate[m][k] = rates[r];
+      P.srate_mmt[m][k] = rates[r] / mmt;
+    }
+  }
+  for (int q = 0; q < p.nminerals; ++q)
+    for (int m = 0; m < S; ++m) P.gw[q + 1][m] = p.gw[q][m];
+  for (int d = 0; d < 3; ++d) P.gvt[d] = p.gvt[d];
+  // isotropy weights (lbm_discretization_d3q19.F90:199-230, d2q9:119-142)
+  const int iso = p.isotropy_order;
+  double* w = P.ffw;
+  if (h->D == 3) {
+    if (iso == 4) { w[1] = 1.0 / 6.0; w[2] = 1.0 / 12.0; }
+    if (iso == 8) {
+      w[1] = 4.0 / 45.0; w[2] = 1.0 / 21.0; w[3] = 2.0 / 105.0; w[4] = 5.0 / 504.0;
+      w[5] = 1.0 / 315.0; w[6] = 1.0 / 630.0; w[8] = 1.0 / 5040.0;
+    }
+  } else {
+    if (iso == 4) { w[1] = 1.0 / 3.0; w[2] = 1.0 / 12.0; }
+    if (iso == 8) { w[1] = 4.0 / 21.0; w[2] = 4.0 / 45.0; w[4] = 1.0 / 60.0; w[5] = 2.0 / 315.0; w[8] = 1.0 / 5040.0; }
+    if (iso == 10) {
+      w[1] = 262.0 / 1785.0; w[2] = 93.0 / 1190.0; w[4] = 7.0 / 340.0; w[5] = 6.0 / 595.0;
+      w[8] = 9.0 / 9520.0; w[9] = 2.0 / 5355.0; w[10] = 1.0 / 7140.0;
+    }
+  }
+  P.c0 = 6.0;  // disc%c_0
+  // fluid-solid weights 1./6., 1./12. (D3) and 1./3., 1./12. (D2): default-REAL literals
+  if (p.literal_kind == 8) {
+    P.fs_w_axis = h->D == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
+    P.fs_w_diag = 1.0 / 12.0;
+  } else {
+    P.fs_w_axis = h->D == 3 ? (double)(1.0f / 6.0f) : (double)(1.0f / 3.0f);
+    P.fs_w_diag = (double)(1.0f / 12.0f);
+  }
+  const double eps15 = (double)1.e-15f;
+  for (int m = 0; m < S; ++m)
+    for (int k = 0; k < S; ++k)
+      if (std::fabs(p.g[m][k]) > eps15) P.ff_on = 1;
+  for (int q = 0; q < p.nminerals; ++q)
+    for (int m = 0; m < S; ++m)
+      if (std::fabs(p.gw[q][m]) > eps15) P.fs_on = 1;
+  P.body_on = p.body_forces != 0;
+  P.rho0 = p.precision == TX_PREC_F64 ? 0.0 : p.rho0;
+}
+
+__global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red) {
+  double mx = 0.0;
+  unsigned long long bad = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double c = cur[i];
+    if (!isfinite(c)) ++bad;
+    const double v = c != 0.0 ? fabs((old[i] - c) / c) : 0.0;
+    if (v > mx) mx = v;
+    old[i] = c;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&red[0], (unsigned long long)__double_as_longlong(mx));
+    if (bad) atomicAdd(&red[1], bad);
+  }
+}
+
+int sync_stream(tx_handle* h) {
+  TX_CUDA(h, cudaStreamSynchronize(h->stream));
+  return TX_OK;
+}
+
+// populations of state cur -> natural order staging
+int stage_field(tx_handle* h, int field) {
+  const long long N = h->g.n;
+  if (field == TX_FIELD_FI) {
+    h->ks.to_natural(h->f[h->cur], h->mask, N, h->ph.rho0, h->stage, h->stream);
+  } else if (field == TX_FIELD_WALLS) {
+    return TX_ERR_ARG;
+  } else {
+    const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
+                   : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : 7;
+    h->ks.moments(args(h, h->cur, h->cur), h->ph, what, h->stage, h->stream);
+  }
+  return check_launch(h, "download kernel");
+}
+
+}  // namespace
+
+extern "C" {
+
+int tx_params_default(tx_params* p) {
+  if (!p) return TX_ERR_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->discretization = TX_D3Q19;
+  p->nx = p->ny = p->nz = 1;
+  p->ncomponents = 1;
+  p->nminerals = 1;
+  p->relaxation_mode = TX_RELAX_SRT;
+  p->isotropy_order = 4;
+  for (int m = 0; m < TX_MAX_COMPONENTS; ++m) {
+    p->tau[m] = 1.0;
+    p->s_c[m] = p->s_e[m] = p->s_e2[m] = p->s_q[m] = p->s_nu[m] = p->s_pi[m] = p->s_m[m] = 1.0;
+    p->mm[m] = 1.0;
+  }
+  p->literal_kind = 4;
+  p->precision = TX_PREC_F64;
+  p->rho0 = 1.0;
+  return TX_OK;
+}
+
+const char* tx_last_error(const tx_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int tx_create(const tx_params* p, tx_handle** out) {
+  if (!p || !out) return fail(nullptr, TX_ERR_ARG, "null argument");
+  *out = nullptr;
+  std::string why;
+  int rc = validate(p, &why);
+  if (rc) return fail(nullptr, rc, why);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(nullptr, TX_ERR_NODEVICE, "no CUDA device");
+  tx_handle* h = new tx_handle();
+  h->p = *p;
+  h->D = p->discretization == TX_D3Q19 ? 3 : 2;
+  h->S = p->ncomponents;
+  h->Q = h->D == 3 ? 19 : 9;
+  h->g.nx = p->nx;
+  h->g.ny = p->ny;
+  h->g.nz = h->D == 3 ? p->nz : 1;
+  for (int a = 0; a < 3; ++a) h->g.per[a] = a < h->D ? p->bc_flags[2 * a] == TX_BC_PERIODIC : 1;
+  h->g.n = (long long)h->g.nx * h->g.ny * h->g.nz;
+  fill_phys(h);
+  const bool mrt = p->relaxation_mode == TX_RELAX_MRT;
+  using Fn = bool (*)(int, int, bool, KernelSet*);
+  // [form][dimension 3/2][components 1/2]; form 0 exact FP64, 1 FP64, 2 FP32, 3 FP32/FP16
+  static const Fn table[4][2][2] = {
+      {{kernels_d3_exact_s1, kernels_d3_exact_s2}, {kernels_d2_exact_s1, kernels_d2_exact_s2}},
+      {{kernels_d3_f64_s1, kernels_d3_f64_s2}, {kernels_d2_f64_s1, kernels_d2_f64_s2}},
+      {{kernels_d3_f32_s1, kernels_d3_f32_s2}, {kernels_d2_f32_s1, kernels_d2_f32_s2}},
+      {{kernels_d3_f16_s1, kernels_d3_f16_s2}, {kernels_d2_f16_s1, kernels_d2_f16_s2}}};
+  const int form = p->precision == TX_PREC_F64 ? (p->exact ? 0 : 1) : (p->precision == TX_PREC_F32 ? 2 : 3);
+  const bool ok = table[form][h->D == 3 ? 0 : 1][h->S - 1](h->S, p->isotropy_order, mrt, &h->ks);
+  if (!ok) {
+    delete h;
+    return fail(nullptr, TX_ERR_ARG, "no kernel built for this parameter combination");
+  }
+  const long long N = h->g.n;
+  h->pop_bytes = p->precision == TX_PREC_F64 ? 8 : (p->precision == TX_PREC_F32 ? 4 : 2);
+  h->rho_bytes = p->precision == TX_PREC_F64 ? 8 : 4;
+  auto cleanup = [&](const std::string& msg, int code) {
+    tx_destroy(h);
+    return fail(nullptr, code, msg);
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup("cudaStreamCreate failed", TX_ERR_CUDA);
+  const size_t popb = (size_t)N * h->S * h->Q * h->pop_bytes;
+  const size_t stageb = (size_t)N * h->S * h->Q * sizeof(double);
+  if (cudaMalloc(&h->f[0], popb) != cudaSuccess || cudaMalloc(&h->f[1], popb) != cudaSuccess ||
+      cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
+      cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->stage, stageb) != cudaSuccess ||
+      cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess)
+    return cleanup("device allocation failed", TX_ERR_NOMEM);
+  cudaMemsetAsync(h->f[0], 0, popb, h->stream);
+  cudaMemsetAsync(h->f[1], 0, popb, h->stream);
+  cudaMemsetAsync(h->rho, 0, (size_t)N * h->S * h->rho_bytes, h->stream);
+  cudaMemsetAsync(h->mask, 0, (size_t)N, h->stream);
+  h->host_mask.assign((size_t)N, 0);
+  // Dirichlet density faces (FlowSetUpBCsD3/D2, lbm_flow.F90:1311-1956): uniform values
+  for (int f = 0; f < 2 * h->D; ++f) {
+    if (p->bc_flags[f] != TX_BC_DENSITY) continue;
+    const int a = f / 2;
+    long long area = h->D == 2 ? (a == 0 ? h->g.ny : h->g.nx)
+                               : (a == 0 ? (long long)h->g.ny * h->g.nz : a == 1 ? (long long)h->g.nx * h->g.nz
+                                                                                 : (long long)h->g.nx * h->g.ny);
+    h->face_n[f] = area;
+    std::vector<double> v((size_t)area * h->S);
+    for (int m = 0; m < h->S; ++m)
+      for (long long q = 0; q < area; ++q) v[(size_t)m * area + q] = p->bc_density[f][m];
+    if (cudaMalloc(&h->faceval[f], v.size() * sizeof(double)) != cudaSuccess) return cleanup("device allocation failed", TX_ERR_NOMEM);
+    cudaMemcpy(h->faceval[f], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+    h->faces.on[f] = 1;
+    h->faces.vals[f] = h->faceval[f];
+  }
+  for (int i = 0; i < 4; ++i) cudaEventCreate(&h->ev[i]);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cleanup("stream sync failed", TX_ERR_CUDA);
+  *out = h;
+  return TX_OK;
+}
+
+int tx_destroy(tx_handle* h) {
+  if (!h) return TX_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->f[0]);
+  cudaFree(h->f[1]);
+  cudaFree(h->rho);
+  cudaFree(h->mask);
+  cudaFree(h->stage);
+  cudaFree(h->old_rho);
+  cudaFree(h->old_fi);
+  cudaFree(h->uic);
+  cudaFree(h->red);
+  for (int f = 0; f < 6; ++f) cudaFree(h->faceval[f]);
+  for (int i = 0; i < 4; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return TX_OK;
+}
+
+int tx_upload_walls(tx_handle* h, const double* walls) {
+  if (!h || !walls) return TX_ERR_ARG;
+  const long long N = h->g.n;
+  for (long long i = 0; i < N; ++i) {
+    const double v = walls[i];
+    uint8_t code;
+    if (v == 0.0) {
+      code = 0;
+    } else if (!(v > 0.0) || !std::isfinite(v)) {
+      return fail(h, TX_ERR_ARG, "wall codes must be 0 (pore) or positive");
+    } else if (v == 900.0 || v == 901.0 || v == 902.0) {
+      return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 are not supported by the device path");
+    } else {
+      const int mineral = (int)v;
+      code = (v < 998.0 && mineral >= 1 && mineral <= h->p.nminerals) ? (uint8_t)mineral : (uint8_t)255;
+    }
+    h->host_mask[(size_t)i] = code;
+  }
+  TX_CUDA(h, cudaMemcpyAsync(h->mask, h->host_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  h->have_walls = true;
+  return sync_stream(h);
+}
+
+int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
+  if (!h || !rho) return TX_ERR_ARG;
+  const long long N = h->g.n;
+  const int S = h->S, D = h->D;
+  // rho: natural (m fastest) -> [m][cell] in the rho storage type
+  std::vector<double> rt((size_t)N * S);
+  for (long long i = 0; i < N; ++i)
+    for (int m = 0; m < S; ++m) rt[(size_t)m * N + i] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] : 0.0;
+  if (h->rho_bytes == 8) {
+    TX_CUDA(h, cudaMemcpyAsync(h->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    TX_CUDA(h, cudaStreamSynchronize(h->stream));
+  } else {
+    std::vector<float> rf(rt.begin(), rt.end());
+    TX_CUDA(h, cudaMemcpyAsync(h->rho, rf.data(), rf.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    TX_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  cudaFree(h->uic);
+  h->uic = nullptr;
+  if (u) {
+    std::vector<double> ut((size_t)N * S * D);
+    for (long long i = 0; i < N; ++i)
+      for (int d = 0; d < D; ++d)
+        for (int m = 0; m < S; ++m) ut[((size_t)(m * D + d)) * N + i] = u[(i * D + d) * S + m];
+    TX_CUDA(h, cudaMalloc(&h->uic, ut.size() * sizeof(double)));
+    TX_CUDA(h, cudaMemcpy(h->uic, ut.data(), ut.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  h->have_state = true;
+  h->have_fi = false;
+  h->inited = false;
+  return TX_OK;
+}
+
+int tx_upload_fi(tx_handle* h, const double* fi) {
+  if (!h || !fi) return TX_ERR_ARG;
+  const long long N = h->g.n;
+  const size_t bytes = (size_t)N * h->S * h->Q * sizeof(double);
+  TX_CUDA(h, cudaMemcpyAsync(h->stage, fi, bytes, cudaMemcpyHostToDevice, h->stream));
+  h->ks.from_natural(h->stage, h->mask, N, h->ph.rho0, h->f[h->cur], h->stream);
+  int rc = check_launch(h, "k_pops_from_natural");
+  if (rc) return rc;
+  h->have_fi = true;
+  h->have_state = false;
+  h->inited = false;
+  return sync_stream(h);
+}
+
+int tx_upload_bc_values(tx_handle* h, int32_t face, const double* vals) {
+  if (!h || !vals) return TX_ERR_ARG;
+  const int f = face - 1;
+  if (f < 0 || f >= 2 * h->D || !h->faceval[f]) return fail(h, TX_ERR_ARG, "face is not a density face");
+  const long long area = h->face_n[f];
+  const int nbcs = h->S * h->D;
+  std::vector<double> v((size_t)area * h->S);
+  for (long long q = 0; q < area; ++q)
+    for (int m = 0; m < h->S; ++m) v[(size_t)m * area + q] = vals[q * nbcs + m];
+  TX_CUDA(h, cudaMemcpy(h->faceval[f], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return TX_OK;
+}
+
+int tx_init(tx_handle* h) {
+  if (!h) return TX_ERR_ARG;
+  if (!h->have_walls) return fail(h, TX_ERR_STATE, "tx_upload_walls must come before tx_init");
+  if (!h->have_state && !h->have_fi) return fail(h, TX_ERR_STATE, "tx_upload_state or tx_upload_fi must come before tx_init");
+  if (!h->have_fi) {
+    // FlowFiInit: the state buffer becomes (1 - P/2) feq of the initial moments
+    h->ks.init(args(h, h->cur, h->cur), h->ph, h->uic, h->stream);
+    int rc = check_launch(h, "k_init");
+    if (rc) return rc;
+  }
+  // FlowUpdateMoments: the forcing density is the plain population sum
+  h->ks.density(args(h, h->cur, h->cur), h->ph, 1, h->stream);
+  int rc = check_launch(h, "k_density");
+  if (rc) return rc;
+  rc = sync_stream(h);
+  if (rc) return rc;
+  cudaFree(h->uic);
+  h->uic = nullptr;
+  h->inited = true;
+  return TX_OK;
+}
+
+int tx_step(tx_handle* h, int32_t nsteps) {
+  if (!h) return TX_ERR_ARG;
+  if (!h->inited) return fail(h, TX_ERR_STATE, "tx_init must come before tx_step");
+  if (nsteps < 0) return fail(h, TX_ERR_ARG, "nsteps must be >= 0");
+  for (int t = 0; t < nsteps; ++t) {
+    const int nxt = 1 - h->cur;
+    StepArgs a = args(h, h->cur, nxt);
+    if (h->timing) cudaEventRecord(h->ev[0], h->stream);
+    h->ks.step(a, h->ph, h->stream);
+    if (h->timing) cudaEventRecord(h->ev[1], h->stream);
+    h->ks.density(a, h->ph, 0, h->stream);
+    if (h->timing) cudaEventRecord(h->ev[2], h->stream);
+    int rc = check_launch(h, "k_step/k_density");
+    if (rc) return rc;
+    h->cur = nxt;
+    h->n_step_launch++;
+    h->n_density_launch++;
+    if (h->timing) {
+      TX_CUDA(h, cudaEventSynchronize(h->ev[2]));
+      float a_ms = 0.f, b_ms = 0.f;
+      cudaEventElapsedTime(&a_ms, h->ev[0], h->ev[1]);
+      cudaEventElapsedTime(&b_ms, h->ev[1], h->ev[2]);
+      h->t_step_ms += a_ms;
+      h->t_density_ms += b_ms;
+    }
+  }
+  return TX_OK;
+}
+
+int tx_sync(tx_handle* h) {
+  if (!h) return TX_ERR_ARG;
+  return sync_stream(h);
+}
+
+int64_t tx_field_size(const tx_handle* h, int32_t field) {
+  if (!h) return -1;
+  const long long dof = field_dof(h, field);
+  return dof < 0 ? -1 : dof * h->g.n;
+}
+
+int tx_download(tx_handle* h, int32_t field, double* out) {
+  if (!h || !out) return TX_ERR_ARG;
+  const long long dof = field_dof(h, field);
+  if (dof < 0) return fail(h, TX_ERR_ARG, "unknown field");
+  const long long N = h->g.n;
+  if (field == TX_FIELD_WALLS) {
+    // the uploaded codes are kept on the host in mask form; report them as the reference walls vector
+    for (long long i = 0; i < N; ++i) {
+      const uint8_t c = h->host_mask[(size_t)i];
+      out[i] = c == 255 ? 999.0 : (double)c;
+    }
+    return TX_OK;
+  }
+  if (!h->inited) return fail(h, TX_ERR_STATE, "tx_init must come before tx_download");
+  int rc = stage_field(h, field);
+  if (rc) return rc;
+  TX_CUDA(h, cudaMemcpyAsync(out, h->stage, (size_t)(N * dof) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync_stream(h);
+}
+
+int tx_delta_norm(tx_handle* h, int32_t field, double* norm) {
+  if (!h || !norm) return TX_ERR_ARG;
+  if (field != TX_FIELD_RHO && field != TX_FIELD_FI) return fail(h, TX_ERR_ARG, "delta norm over rho or fi only");
+  if (!h->inited) return fail(h, TX_ERR_STATE, "tx_init must come before tx_delta_norm");
+  const long long n = tx_field_size(h, field);
+  double*& old = field == TX_FIELD_RHO ? h->old_rho : h->old_fi;
+  if (!old) {
+    TX_CUDA(h, cudaMalloc(&old, (size_t)n * sizeof(double)));
+    TX_CUDA(h, cudaMemsetAsync(old, 0, (size_t)n * sizeof(double), h->stream));
+  }
+  int rc = stage_field(h, field);
+  if (rc) return rc;
+  TX_CUDA(h, cudaMemsetAsync(h->red, 0, 2 * sizeof(unsigned long long), h->stream));
+  k_delta_norm<<<1216, 256, 0, h->stream>>>(h->stage, old, n, h->red);
+  rc = check_launch(h, "k_delta_norm");
+  if (rc) return rc;
+  unsigned long long r[2];
+  TX_CUDA(h, cudaMemcpyAsync(r, h->red, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+  rc = sync_stream(h);
+  if (rc) return rc;
+  double v;
+  std::memcpy(&v, &r[0], sizeof(v));
+  *norm = v;
+  if (r[1]) return fail(h, TX_ERR_NONFINITE, "non-finite values in the field (" + std::to_string(r[1]) + " sites)");
+  return TX_OK;
+}
+
+/* ------------------------------------------------------- instrumentation */
+int tx_set_timing(tx_handle* h, int32_t on) {
+  if (!h) return TX_ERR_ARG;
+  h->timing = on != 0;
+  h->t_step_ms = h->t_density_ms = 0.0;
+  h->n_step_launch = h->n_density_launch = 0;
+  return TX_OK;
+}
+
+int tx_get_timing(tx_handle* h, double* ms_step, double* ms_density, int64_t* launches) {
+  if (!h) return TX_ERR_ARG;
+  if (ms_step) *ms_step = h->t_step_ms;
+  if (ms_density) *ms_density = h->t_density_ms;
+  if (launches) *launches = h->n_step_launch + h->n_density_launch;
+  return TX_OK;
+}
+
+void* tx_get_stream(tx_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+const char* tx_kernel_name(const tx_handle* h) { return h ? h->ks.name : ""; }
+
+}  // extern "C"

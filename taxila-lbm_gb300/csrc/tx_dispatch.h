@@ -1,0 +1,76 @@
+// Kernel tables: one KernelSet per (dimension, components, isotropy, MRT,
+// exactness, storage form); built by the tx_inst_*.cu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tx_kernels.cuh"
+
+namespace tx {
+
+struct KernelSet {
+  void (*step)(const StepArgs&, const Phys&, cudaStream_t);
+  void (*density)(const StepArgs&, const Phys&, int mode, cudaStream_t);
+  void (*init)(const StepArgs&, const Phys&, const double* uic, cudaStream_t);
+  void (*moments)(const StepArgs&, const Phys&, int what, double* out, cudaStream_t);
+  void (*to_natural)(const void* f, const uint8_t* mask, long long N, double rho0, double* out, cudaStream_t);
+  void (*from_natural)(const double* in, const uint8_t* mask, long long N, double rho0, void* f, cudaStream_t);
+  const char* name;
+};
+
+// Component counts compiled into the library.
+constexpr int kMaxBuiltComponents = 2;
+
+bool kernels_d3_exact_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_exact_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_exact_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_exact_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f64_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f64_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f64_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f64_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f32_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f32_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f32_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f32_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f16_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d3_f16_s2(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f16_s1(int S, int ISO, bool MRT, KernelSet* ks);
+bool kernels_d2_f16_s2(int S, int ISO, bool MRT, KernelSet* ks);
+
+inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace tx
+
+// Instantiates the launchers of one storage/arithmetic form for one dimension.
+#define TX_FORM_LAUNCHERS(D, S, ISO, MRT, EXACT, T, R, RT) TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)
+#define TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)                                                  \
+  struct L_##S##_##ISO##_##MRT {                                                                             \
+    static void step(const StepArgs& a, const Phys& p, cudaStream_t s) {                                      \
+      k_step<D, S, ISO, MRT, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p);                     \
+    }                                                                                                         \
+    static void density(const StepArgs& a, const Phys& p, int mode, cudaStream_t s) {                         \
+      k_density<D, S, T, R, RT><<<grid_for(a.g.n, 256), 256, 0, s>>>(a, p, mode);                             \
+    }                                                                                                         \
+    static void init(const StepArgs& a, const Phys& p, const double* u, cudaStream_t s) {                     \
+      k_init<D, S, ISO, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p, u);                       \
+    }                                                                                                         \
+    static void moments(const StepArgs& a, const Phys& p, int what, double* out, cudaStream_t s) {            \
+      k_moments<D, S, ISO, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p, what, out);            \
+    }                                                                                                         \
+    static void to_nat(const void* f, const uint8_t* m, long long N, double r0, double* o, cudaStream_t s) {  \
+      k_pops_to_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, r0, o); \
+    }                                                                                                         \
+    static void from_nat(const double* i, const uint8_t* m, long long N, double r0, void* f, cudaStream_t s) { \
+      k_pops_from_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(i, m, N, r0, reinterpret_cast<T*>(f)); \
+    }                                                                                                         \
+  };
+
+#define TX_FORM_CASE(S, ISO, MRT) TX_FORM_CASE_(S, ISO, MRT)
+#define TX_FORM_CASE_(S, ISO, MRT)                                                                               \
+  if (s == S && iso == ISO && mrt == MRT) {                                                                    \
+    *ks = KernelSet{&L_##S##_##ISO##_##MRT::step,   &L_##S##_##ISO##_##MRT::density,                           \
+                    &L_##S##_##ISO##_##MRT::init,   &L_##S##_##ISO##_##MRT::moments,                           \
+                    &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat, #S "c iso" #ISO " mrt" #MRT}; \
+    return true;                                                                                               \
+  }

@@ -1,0 +1,32 @@
+// Body of one tx_inst_*.cu translation unit: the kernel table of one
+// (dimension, exactness, storage) combination for one component count, isotropy order and relaxation mode.  The including file defines
+// TX_D, TX_S, TX_EXACT, TX_T, TX_R, TX_RT and TX_FN before including this.
+#include "tx_dispatch.h"
+
+namespace tx {
+namespace {
+#define TX_L(ISO, MRT) TX_FORM_LAUNCHERS(TX_D, TX_S, ISO, MRT, TX_EXACT, TX_T, TX_R, TX_RT)
+TX_L(4, false)
+TX_L(4, true)
+TX_L(8, false)
+TX_L(8, true)
+#if TX_D == 2
+TX_L(10, false)
+TX_L(10, true)
+#endif
+#undef TX_L
+}  // namespace
+
+bool TX_FN(int s, int iso, bool mrt, KernelSet* ks) {
+  TX_FORM_CASE(TX_S, 4, false)
+  TX_FORM_CASE(TX_S, 4, true)
+  TX_FORM_CASE(TX_S, 8, false)
+  TX_FORM_CASE(TX_S, 8, true)
+#if TX_D == 2
+  TX_FORM_CASE(TX_S, 10, false)
+  TX_FORM_CASE(TX_S, 10, true)
+#endif
+  return false;
+}
+
+}  // namespace tx

@@ -1,0 +1,9 @@
+// Kernel table: D2, 2 component(s), reference operation order (built with --fmad=false), storage double, arithmetic double.
+#define TX_D 2
+#define TX_S 2
+#define TX_EXACT true
+#define TX_T double
+#define TX_R double
+#define TX_RT double
+#define TX_FN kernels_d2_exact_s2
+#include "tx_inst.cuh"

@@ -1,0 +1,9 @@
+// Kernel table: D2, 2 component(s), fast arithmetic, storage __half, arithmetic float.
+#define TX_D 2
+#define TX_S 2
+#define TX_EXACT false
+#define TX_T __half
+#define TX_R float
+#define TX_RT float
+#define TX_FN kernels_d2_f16_s2
+#include "tx_inst.cuh"

@@ -1,0 +1,9 @@
+// Kernel table: D3, 1 component(s), reference operation order (built with --fmad=false), storage double, arithmetic double.
+#define TX_D 3
+#define TX_S 1
+#define TX_EXACT true
+#define TX_T double
+#define TX_R double
+#define TX_RT double
+#define TX_FN kernels_d3_exact_s1
+#include "tx_inst.cuh"

@@ -1,0 +1,720 @@
+// CUDA kernels of the Shan-Chen flow step (sm_103a).
+//
+// Device state between steps is the reference's fi after FlowApplyBCs (the
+// post-stream, post-boundary populations) in SoA layout f[(m*Q + n)*N + cell],
+// cell = x + nx*(y + ny*z), plus the density used for forcing, rho[m*N + cell].
+// One step of LBMRun2 (src/lbm/lbm.F90:283-363) is two launches:
+//
+//   k_step     per pore site: forces (fluid-solid, body, Shan-Chen), flux and
+//              common velocity (FlowUpdateFlux), equilibrium, forcing prefactor
+//              and BGK/MRT collision (FlowCollision), then push-streaming with
+//              bounceback folded in (FlowStream + FlowBounceback): population n
+//              goes to x + c_n, or back to x as opp(n) when x + c_n is a wall
+//              (periodic axes wrap; non-periodic faces are ghost walls).
+//   k_density  per pore site of the pushed populations: Dirichlet density
+//              faces (BCApplyDirichletNode) and the forcing density
+//              (DistributionCalcDensity + BCApplyDirichletToRho).
+//
+// The forces and velocity of a step are recomputed at the start of the next
+// k_step from (f, rho), so they are the values the reference stores between
+// steps.  Template parameters:
+//   D      2 (D2Q9) or 3 (D3Q19)        S    number of components
+//   ISO    isotropy order 4, 8, 10      MRT  MRT (true) or BGK (false)
+//   EXACT  reference operation order: no FMA (its translation unit is built
+//          with --fmad=false), IEEE divides, the reference's expression shapes
+//   T      population storage type (double; float/half hold f - w_n*rho0)
+//   R      arithmetic type              RT   storage type of rho
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "tx_ff_stencil.cuh"
+#include "tx_lattice.cuh"
+
+namespace tx {
+
+constexpr int MAXC = 4;
+constexpr int MAXMIN = 16;
+
+struct Geo {
+  int nx, ny, nz;
+  int per[3];
+  long long n;
+};
+
+// Parameters in FP64; kernels convert to R.
+struct Phys {
+  double tau[MAXC], inv_tau[MAXC], cs2[MAXC], inv_cs2[MAXC], dk[MAXC], mm[MAXC], mmot[MAXC];
+  double g[MAXC][MAXC];
+  double gw[MAXMIN + 1][MAXC];  // row = mineral id (row 0 unused)
+  double gvt[3];
+  double ffw[12];
+  double c0, fs_w_axis, fs_w_diag;
+  double srate[MAXC][19];   // MRT rate of moment k
+  double srate_mmt[MAXC][19];  // rate / diag(M M^T)
+  double rho0;              // shift of the reduced-precision storage
+  int ff_on, fs_on, body_on;
+};
+
+struct Faces {
+  int on[6];                // Dirichlet density face flags, XM..ZP
+  const double* vals[6];    // [m * area + node], node in natural order of the tangential axes
+};
+
+struct StepArgs {
+  const void* fin;
+  void* fout;
+  void* rho;                // RT [m * N + cell]
+  const uint8_t* mask;      // 0 pore, 1..16 mineral, 255 other wall
+  Geo g;
+  Faces faces;
+};
+
+// ----------------------------------------------------------------- storage
+template <class T>
+struct St;
+template <>
+struct St<double> {
+  __device__ static __forceinline__ double ld(const double* p) { return __ldg(p); }
+  __device__ static __forceinline__ void st(double* p, double v) { *p = v; }
+};
+template <>
+struct St<float> {
+  __device__ static __forceinline__ float ld(const float* p) { return __ldg(p); }
+  __device__ static __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <>
+struct St<__half> {
+  __device__ static __forceinline__ float ld(const __half* p) { return __half2float(__ldg(p)); }
+  __device__ static __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+template <class T>
+constexpr bool kShifted = !std::is_same<T, double>::value;
+
+// --------------------------------------------------------------- geometry
+__device__ __forceinline__ int wrap_axis(int v, int n) {
+  while (v < 0) v += n;
+  while (v >= n) v -= n;
+  return v;
+}
+
+// Linear index of (x+dx, y+dy, z+dz), or -1 outside a non-periodic axis
+// (the ghost walls of WallsSetGhostNodesD3/D2, lbm_walls.F90:179-231).
+__device__ __forceinline__ long long nbr(const Geo& g, int x, int y, int z, int dx, int dy, int dz) {
+  int xx = x + dx, yy = y + dy, zz = z + dz;
+  if (xx < 0 || xx >= g.nx) {
+    if (!g.per[0]) return -1;
+    xx = wrap_axis(xx, g.nx);
+  }
+  if (yy < 0 || yy >= g.ny) {
+    if (!g.per[1]) return -1;
+    yy = wrap_axis(yy, g.ny);
+  }
+  if (zz < 0 || zz >= g.nz) {
+    if (!g.per[2]) return -1;
+    zz = wrap_axis(zz, g.nz);
+  }
+  return (long long)xx + (long long)g.nx * ((long long)yy + (long long)g.ny * zz);
+}
+
+__device__ __forceinline__ bool is_pore(const uint8_t* mask, long long i) { return i >= 0 && __ldg(mask + i) == 0; }
+
+__device__ __forceinline__ bool on_face(const Geo& g, int f, int x, int y, int z) {
+  switch (f) {
+    case 0: return x == 0;
+    case 1: return x == g.nx - 1;
+    case 2: return y == 0;
+    case 3: return y == g.ny - 1;
+    case 4: return z == 0;
+    default: return z == g.nz - 1;
+  }
+}
+
+template <int D>
+__device__ __forceinline__ long long face_node(const Geo& g, int f, int x, int y, int z) {
+  const int a = f >> 1;
+  if (D == 2) return a == 0 ? y : x;
+  if (a == 0) return y + (long long)g.ny * z;
+  if (a == 1) return x + (long long)g.nx * z;
+  return x + (long long)g.nx * y;
+}
+
+template <int D>
+__device__ __forceinline__ long long face_area(const Geo& g, int f) {
+  const int a = f >> 1;
+  if (D == 2) return a == 0 ? g.ny : g.nx;
+  if (a == 0) return (long long)g.ny * g.nz;
+  if (a == 1) return (long long)g.nx * g.nz;
+  return (long long)g.nx * g.ny;
+}
+
+template <int D>
+__device__ __forceinline__ bool any_dirichlet(const Geo& g, const Faces& fc, int x, int y, int z) {
+  bool r = false;
+#pragma unroll
+  for (int f = 0; f < 2 * D; ++f) r = r || (fc.on[f] && on_face(g, f, x, y, z));
+  return r;
+}
+
+template <int D>
+__host__ __device__ constexpr FFTerm ffterm(int t) {
+  return D == 3 ? ff_d3(t) : ff_d2(t);
+}
+
+// ------------------------------------------------------------------ forces
+// FlowCalcForces (lbm_flow.F90:760-808) for one pore site: zero, then
+// fluid-solid (lbm_forcing.F90:1326-1421), body (:1440-1496) and the
+// wall-aware Shan-Chen term (:51-958 / :960-1299), in that order.
+template <int D, int S, int ISO, bool EXACT, class R, class RT>
+__device__ __forceinline__ void cell_forces(const Geo& g, const Phys& P, const uint8_t* mask, const RT* rho,
+                                            int x, int y, int z, const R rf[S], R F[S][D]) {
+  using L = Lat<D>;
+#pragma unroll
+  for (int m = 0; m < S; ++m)
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[m][d] = R(0);
+
+  if (P.fs_on) {
+    sfor<1, L::Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      const long long q = nbr(g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
+      const int mk = q >= 0 ? (int)__ldg(mask + q) : 255;
+      if (mk >= 1 && mk <= MAXMIN) {
+        const R wgt = R(n <= L::NAXIS ? P.fs_w_axis : P.fs_w_diag);
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          constexpr int c = L::c(n, d);
+          if constexpr (c != 0) {
+#pragma unroll
+            for (int m = 0; m < S; ++m) {
+              const R t = wgt * rf[m] * R(P.gw[mk][m]);
+              F[m][d] = c > 0 ? F[m][d] - t : F[m][d] + t;
+            }
+          }
+        });
+      }
+    });
+  }
+  if (P.body_on) {
+#pragma unroll
+    for (int m = 0; m < S; ++m)
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[m][d] = F[m][d] + R(P.gvt[d]) * R(P.mm[m]) * rf[m];
+  }
+  if (P.ff_on) {
+    R gr[S][D];
+    R ws[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      ws[d] = R(0);
+#pragma unroll
+      for (int m = 0; m < S; ++m) gr[m][d] = R(0);
+    }
+    constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+    sfor<0, NT>([&](auto tt) {
+      constexpr FFTerm T = ffterm<D>(decltype(tt)::value);
+      if constexpr (T.level <= ISO) {
+        const long long pi = nbr(g, x, y, z, T.e[0], T.e[1], T.e[2]);
+        bool ok = is_pore(mask, pi);
+        if constexpr (T.naux > 0) {
+          unsigned bits = 0;
+          sfor<0, T.naux>([&](auto qq) {
+            constexpr FFTerm U = ffterm<D>(decltype(tt)::value);
+            constexpr int q = decltype(qq)::value;
+            if (is_pore(mask, nbr(g, x, y, z, U.aux[q][0], U.aux[q][1], U.aux[q][2]))) bits |= 1u << q;
+          });
+          ok = ok && ((T.truth >> bits) & 1u);
+        }
+        if (ok) {
+          sfor<0, D>([&](auto dd) {
+            constexpr FFTerm U = ffterm<D>(decltype(tt)::value);
+            constexpr int d = decltype(dd)::value;
+            constexpr int e = U.e[d];
+            constexpr int wi = U.w;
+            if constexpr (e != 0) {
+              const R coef = R(double(e) * P.ffw[wi]);
+#pragma unroll
+              for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * (R(rho[(long long)m * g.n + pi]) - rf[m]);
+              ws[d] = ws[d] + R(P.ffw[wi] * double(e * e));
+            }
+          });
+        }
+      }
+    });
+    const R eps = R((double)1.e-12f);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (ws[d] > eps) {
+        R q[S];
+        if constexpr (EXACT) {
+#pragma unroll
+          for (int m = 0; m < S; ++m) q[m] = gr[m][d] / ws[d];
+        } else {
+          const R inv = R(1) / ws[d];
+#pragma unroll
+          for (int m = 0; m < S; ++m) q[m] = gr[m][d] * inv;
+        }
+#pragma unroll
+        for (int m = 0; m < S; ++m) {
+          R acc = R(0);
+#pragma unroll
+          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * q[k];
+          F[m][d] = F[m][d] - R(P.c0) * rf[m] * acc;
+        }
+      }
+    }
+  }
+}
+
+// Load the site's populations (shifted storage adds w_n * rho0 back).
+template <int D, int S, class T, class R>
+__device__ __forceinline__ void load_pops(const T* f, long long N, long long idx, R rho0, R fv[S][Lat<D>::Q]) {
+  using L = Lat<D>;
+#pragma unroll
+  for (int m = 0; m < S; ++m)
+    sfor<0, L::Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      R v = R(St<T>::ld(f + ((long long)(m * L::Q + n)) * N + idx));
+      if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
+      fv[m][n] = v;
+    });
+}
+
+template <int D, int S, class R>
+__device__ __forceinline__ R pop_sum(const R fv[S][Lat<D>::Q], int m) {
+  R acc = R(0);
+  sfor<0, Lat<D>::Q>([&](auto nn) { acc = acc + fv[m][decltype(nn)::value]; });
+  return acc;
+}
+
+// sum_n f c_n,d in direction order (DistributionCalcFluxD3/D2,
+// lbm_distribution_function.F90:451-508); zero terms add nothing
+template <int D, int S, class R>
+__device__ __forceinline__ R pop_flux(const R fv[S][Lat<D>::Q], int m, int d0) {
+  R acc = R(0);
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    if (d == d0) {
+      sfor<0, Lat<D>::Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        constexpr int c = Lat<D>::c(n, d);
+        if constexpr (c > 0) acc = acc + fv[m][n];
+        if constexpr (c < 0) acc = acc - fv[m][n];
+      });
+    }
+  });
+  return acc;
+}
+
+// Moments of a pore site from its post-stream populations: the density of the
+// collision (rc: Dirichlet nodes re-summed as in BCUpdateRho, lbm_bc.F90:436-611),
+// forces, and the common velocity of FlowUpdateUED3/D2 (lbm_flow.F90:494-574).
+template <int D, int S, int ISO, bool EXACT, class R, class RT>
+__device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, int x, int y, int z, long long idx,
+                                             const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
+  const RT* rho = reinterpret_cast<const RT*>(a.rho);
+#pragma unroll
+  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * a.g.n + idx]);
+  const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
+#pragma unroll
+  for (int m = 0; m < S; ++m) rc[m] = dn ? pop_sum<D, S, R>(fv, m) : rf[m];
+  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    R num = R(0), den = R(0);
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      const R ue = pop_flux<D, S, R>(fv, m, d) + R(.5) * F[m][d];
+      num = num + ue * R(P.mmot[m]);
+    }
+#pragma unroll
+    for (int m = 0; m < S; ++m) den = den + rc[m] * R(P.mmot[m]);
+    if constexpr (EXACT)
+      up[d] = num / den;
+    else
+      up[d] = num * (R(1) / den);
+  }
+}
+
+// Equilibrium (DiscretizationEquilf_D3Q19, lbm_discretization_d3q19.F90:265-305;
+// _D2Q9, lbm_discretization_d2q9.F90:168-205) and forcing prefactor
+// (FlowFiBarEqPrefactor, lbm_flow.F90:836-851) of component m, direction n.
+template <int D, int n, bool EXACT, class R>
+__device__ __forceinline__ void feq_pf(const Phys& P, int m, R r, const R u[D], R usqr, const R Fm[D], R& feq, R& pf) {
+  using L = Lat<D>;
+  const R cs2 = R(P.cs2[m]), dk = R(P.dk[m]);
+  R udote = R(0);
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    constexpr int c = L::c(n, d);
+    if constexpr (c > 0) udote = udote + u[d];
+    if constexpr (c < 0) udote = udote - u[d];
+  });
+  if constexpr (n == 0) {
+    if constexpr (D == 3)
+      feq = r * (dk - usqr / R(2.));
+    else
+      feq = r * ((R(1.) + dk * R(5.)) / R(6.) - R(2.) * usqr / R(3.));
+  } else if constexpr (EXACT) {
+    feq = R(L::w(n)) * r *
+          (R(1.5) * (R(1.) - dk) + udote / cs2 + udote * udote / (R(2.) * cs2 * cs2) - usqr / (R(2.) * cs2));
+  } else {
+    const R ic = R(P.inv_cs2[m]);
+    feq = R(L::w(n)) * r * (R(1.5) * (R(1.) - dk) + udote * ic + R(0.5) * udote * udote * ic * ic - R(0.5) * usqr * ic);
+  }
+  R acc = R(0);
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    acc = acc + Fm[d] * (R(L::c(n, d)) - u[d]);
+  });
+  if constexpr (EXACT)
+    pf = acc / (r * cs2);
+  else
+    pf = acc * (R(1) / (r * cs2));
+}
+
+// ------------------------------------------------------------------ step
+template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_step(StepArgs a, Phys P) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.g.n) return;
+  if (__ldg(a.mask + idx) != 0) return;
+  const int x = (int)(idx % a.g.nx);
+  const long long yz = idx / a.g.nx;
+  const int y = (int)(yz % a.g.ny);
+  const int z = (int)(yz / a.g.ny);
+  const long long N = a.g.n;
+  const R rho0 = R(P.rho0);
+
+  R fv[S][Q];
+  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, idx, rho0, fv);
+  R rc[S], rf[S], F[S][D], up[D];
+  cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
+  R usqr = R(0);
+#pragma unroll
+  for (int d = 0; d < D; ++d) usqr = usqr + up[d] * up[d];
+
+  // destinations of the push: x + c_n, or x itself (as opp(n)) at walls
+  long long dst[Q];
+  sfor<0, Q>([&](auto nn) {
+    constexpr int n = decltype(nn)::value;
+    if constexpr (n == 0) {
+      dst[0] = idx;
+    } else {
+      const long long q = nbr(a.g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
+      dst[n] = is_pore(a.mask, q) ? q : -1;
+    }
+  });
+  T* fout = reinterpret_cast<T*>(a.fout);
+
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R feq[Q], pf[Q];
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq[n], pf[n]);
+    });
+    R* f = fv[m];
+    if constexpr (!MRT) {
+      // RelaxationCollideSRT (lbm_relaxation.F90:171-180) then f += P feq
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        const R fb = (R(1.) - R(.5) * pf[n]) * feq[n];
+        if constexpr (EXACT)
+          f[n] = f[n] - (f[n] - fb) / R(P.tau[m]);
+        else
+          f[n] = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
+        f[n] = f[n] + pf[n] * feq[n];
+      });
+    } else {
+      // RelaxationCollideMRT (lbm_relaxation.F90:182-200): coef_k from the
+      // pre-collision differences, then each f_i subtracts coef_k mt(i,k) in k order
+      R dfi[Q];
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        dfi[n] = f[n] - (R(1.) - R(.5) * pf[n]) * feq[n];
+      });
+      R coef[Q];
+      sfor<0, Q>([&](auto kk) {
+        constexpr int k = decltype(kk)::value;
+        R md = R(0);
+        sfor<0, Q>([&](auto ii) {
+          constexpr int i = decltype(ii)::value;
+          constexpr int v = L::mt(i, k);
+          if constexpr (v == 1) md = md + dfi[i];
+          else if constexpr (v == -1) md = md - dfi[i];
+          else if constexpr (v != 0) md = md + R(v) * dfi[i];
+        });
+        if constexpr (EXACT)
+          coef[k] = R(P.srate[m][k]) * md / R(L::mmt(k));
+        else
+          coef[k] = R(P.srate_mmt[m][k]) * md;
+      });
+      sfor<0, Q>([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
+        R v = f[i];
+        sfor<0, Q>([&](auto kk) {
+          constexpr int k = decltype(kk)::value;
+          constexpr int c = L::mt(i, k);
+          if constexpr (c == 1) v = v - coef[k];
+          else if constexpr (c == -1) v = v + coef[k];
+          else if constexpr (c != 0) v = v - coef[k] * R(c);
+        });
+        f[i] = v + pf[i] * feq[i];
+      });
+    }
+    // push (DistributionStreamD3/D2 + DistributionBouncebackD3/D2)
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      constexpr int o = opp<D>(n);
+      R v = f[n];
+      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
+      if (dst[n] >= 0)
+        St<T>::st(fout + (long long)(m * Q + n) * N + dst[n], v);
+      else
+        St<T>::st(fout + (long long)(m * Q + o) * N + idx, v);  // w(opp n) == w(n): same shift
+    });
+  }
+}
+
+// -------------------------------------------------- Dirichlet density node
+// BCApplyDirichletNode (lbm_bc.F90:1273-1333) in the local frame of
+// DiscSetLocalDirections (lbm_discretization_d3q19.F90:566-714; d2q9:372-434):
+// normal axis a, inward sign sg, tangential axes in CARDINAL order.
+template <int D, int S, class R>
+__device__ __forceinline__ void dirichlet_node(int f, const R pv[S], R fv[S][Lat<D>::Q]) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const int a = f >> 1;
+  const int sg = (f & 1) == 0 ? 1 : -1;
+  int tang[2];
+  int nt;
+  if (D == 3) {
+    tang[0] = a == 0 ? 1 : (a == 1 ? 2 : 0);
+    tang[1] = a == 0 ? 2 : (a == 1 ? 0 : 1);
+    nt = 2;
+  } else {
+    tang[0] = a == 0 ? 1 : 0;
+    tang[1] = 0;
+    nt = 1;
+  }
+  R wsn = R(0);
+  for (int n = 1; n < Q; ++n)
+    if (sg * L::c(n, a) == 1) wsn = wsn + R(L::w(n));
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R Qv[3] = {R(0), R(0), R(0)};
+    R sum = R(0);
+    for (int n = 0; n < Q; ++n) sum = sum + fv[m][n];
+    Qv[a] = R(sg) * (pv[m] - sum) / wsn;
+    for (int p = 0; p < nt; ++p) {
+      const int t = tang[p];
+      R mom = R(0), wst = R(0);
+      for (int n = 1; n < Q; ++n) {
+        mom = mom + fv[m][n] * R(L::c(n, t));
+        if (sg * L::c(n, a) == 1 && L::c(n, t) != 0) wst = wst + R(L::w(n));
+      }
+      Qv[t] = -(mom / wst);
+    }
+    for (int n = 1; n < Q; ++n) {
+      if (sg * L::c(n, a) != 1) continue;
+      R cq = R(0);
+      for (int d = 0; d < D; ++d) cq = cq + R(L::c(n, d)) * Qv[d];
+      fv[m][n] = fv[m][n] + R(L::w(n)) * cq;
+    }
+  }
+}
+
+// -------------------------------------------------------------- density
+// mode 0 (after a step): Dirichlet faces in XM..ZP order (BCApplyDirichletD3/D2,
+// lbm_bc.F90:1091-1271), forcing density = the face value
+// (BCApplyDirichletToRho, :252-434) on face nodes, sum of populations elsewhere.
+// mode 1 (FlowUpdateMoments at init, lbm_flow.F90:466-478): plain sums.
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(256) k_density(StepArgs a, Phys P, int mode) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.g.n) return;
+  if (__ldg(a.mask + idx) != 0) return;
+  const long long N = a.g.n;
+  const R rho0 = R(P.rho0);
+  RT* rho = reinterpret_cast<RT*>(a.rho);
+  T* fcur = reinterpret_cast<T*>(a.fout);
+  const int x = (int)(idx % a.g.nx);
+  const long long yz = idx / a.g.nx;
+  const int y = (int)(yz % a.g.ny);
+  const int z = (int)(yz / a.g.ny);
+  const bool dn = mode == 0 && any_dirichlet<D>(a.g, a.faces, x, y, z);
+  if (!dn) {
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      R acc = R(0);
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        R v = R(St<T>::ld(fcur + (long long)(m * Q + n) * N + idx));
+        if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
+        acc = acc + v;
+      });
+      rho[(long long)m * N + idx] = RT(acc);
+    }
+    return;
+  }
+  R fv[S][Q];
+  load_pops<D, S, T, R>(fcur, N, idx, rho0, fv);
+  R rf[S];
+  for (int f = 0; f < 2 * D; ++f) {
+    if (!a.faces.on[f] || !on_face(a.g, f, x, y, z)) continue;
+    const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
+    R pv[S];
+#pragma unroll
+    for (int m = 0; m < S; ++m) pv[m] = R(a.faces.vals[f][(long long)m * area + node]);
+    dirichlet_node<D, S, R>(f, pv, fv);
+#pragma unroll
+    for (int m = 0; m < S; ++m) rf[m] = pv[m];
+  }
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    rho[(long long)m * N + idx] = RT(rf[m]);
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      R v = fv[m][n];
+      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
+      St<T>::st(fcur + (long long)(m * Q + n) * N + idx, v);
+    });
+  }
+}
+
+// -------------------------------------------------------------------- init
+// FlowFiInit (lbm_flow.F90:923-934): forces from the initial density, the
+// equilibrium at the initial velocity, f = (1 - P/2) feq (FlowFeqBarD3/D2).
+// uic is [(m*D + d) * N + cell]; rho holds the initial density.
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_init(StepArgs a, Phys P, const double* uic) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.g.n) return;
+  if (__ldg(a.mask + idx) != 0) return;
+  const long long N = a.g.n;
+  const int x = (int)(idx % a.g.nx);
+  const long long yz = idx / a.g.nx;
+  const int y = (int)(yz % a.g.ny);
+  const int z = (int)(yz / a.g.ny);
+  const RT* rho = reinterpret_cast<const RT*>(a.rho);
+  R rf[S], F[S][D];
+#pragma unroll
+  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
+  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+  T* fout = reinterpret_cast<T*>(a.fout);
+  const R rho0 = R(P.rho0);
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R u[D];
+    R usqr = R(0);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      u[d] = uic ? R(uic[(long long)(m * D + d) * N + idx]) : R(0);
+      usqr = usqr + u[d] * u[d];
+    }
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      R feq, pf;
+      feq_pf<D, n, EXACT, R>(P, m, rf[m], u, usqr, F[m], feq, pf);
+      R v = (R(1.) - R(0.5) * pf) * feq;
+      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
+      St<T>::st(fout + (long long)(m * Q + n) * N + idx, v);
+    });
+  }
+}
+
+// -------------------------------------------------------------- downloads
+// Fields of the current state in natural order (component fastest).
+// what: 2 rho, 3 flux (common velocity), 4 forces, 5 prs, 6 velt, 7 rhot
+// (FlowUpdateDiagnosticsD3/D2, lbm_flow.F90:654-758, for psi = rho).
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_moments(StepArgs a, Phys P, int what, double* out) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.g.n) return;
+  const bool wall = __ldg(a.mask + idx) != 0;
+  const int dof = what == 2 ? S : (what == 3 || what == 4) ? S * D : (what == 6 ? D : 1);
+  if (wall) {
+    for (int q = 0; q < dof; ++q) out[idx * dof + q] = 0.0;
+    return;
+  }
+  const long long N = a.g.n;
+  const int x = (int)(idx % a.g.nx);
+  const long long yz = idx / a.g.nx;
+  const int y = (int)(yz % a.g.ny);
+  const int z = (int)(yz / a.g.ny);
+  R fv[S][Q];
+  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, idx, R(P.rho0), fv);
+  R rc[S], rf[S], F[S][D], up[D];
+  cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
+  if (what == 2) {
+    for (int m = 0; m < S; ++m) out[idx * S + m] = double(rc[m]);
+  } else if (what == 3 || what == 4) {
+    for (int d = 0; d < D; ++d)
+      for (int m = 0; m < S; ++m) out[(idx * D + d) * S + m] = double(what == 3 ? up[d] : F[m][d]);
+  } else {
+    R rt = R(0);
+    for (int m = 0; m < S; ++m) rt = rt + rc[m] * R(P.mm[m]);
+    if (what == 7) {
+      out[idx] = double(rt);
+    } else if (what == 5) {
+      R pr = rt / R(3.);
+      if (S > 1) {
+        for (int m = 0; m < S; ++m) {
+          R acc = R(0);
+          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * rc[k];
+          pr = pr + R(P.c0) / R(2.) * rc[m] * acc;
+        }
+      }
+      out[idx] = double(pr);
+    } else {
+      for (int d = 0; d < D; ++d) {
+        R acc = R(0);
+        for (int m = 0; m < S; ++m) acc = acc + (pop_flux<D, S, R>(fv, m, d) + R(.5) * F[m][d]) * R(P.mm[m]);
+        out[idx * D + d] = double(acc / rt);
+      }
+    }
+  }
+}
+
+// Natural-order populations <-> SoA state.
+template <int D, int S, class T, class R>
+__global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, double rho0, double* out) {
+  constexpr int Q = Lat<D>::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N) return;
+  const bool wall = __ldg(mask + idx) != 0;
+  for (int n = 0; n < Q; ++n)
+    for (int m = 0; m < S; ++m) {
+      double v = 0.0;
+      if (!wall) {
+        v = double(St<T>::ld(f + (long long)(m * Q + n) * N + idx));
+        if constexpr (kShifted<T>) v = double(R(v) + R(Lat<D>::w(n)) * R(rho0));
+      }
+      out[(idx * Q + n) * S + m] = v;
+    }
+}
+
+template <int D, int S, class T, class R>
+__global__ void k_pops_from_natural(const double* in, const uint8_t* mask, long long N, double rho0, T* f) {
+  constexpr int Q = Lat<D>::Q;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N) return;
+  const bool wall = __ldg(mask + idx) != 0;
+  for (int n = 0; n < Q; ++n)
+    for (int m = 0; m < S; ++m) {
+      R v = wall ? R(0) : R(in[(idx * Q + n) * S + m]);
+      if constexpr (kShifted<T>) v = v - R(Lat<D>::w(n)) * R(rho0);
+      St<T>::st(f + (long long)(m * Q + n) * N + idx, v);
+    }
+}
+
+}  // namespace tx

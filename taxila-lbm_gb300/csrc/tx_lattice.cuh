@@ -1,0 +1,124 @@
+// Lattice constants of D2Q9 and D3Q19 as compile-time functions.
+//
+// Direction order, velocities, weights, the MRT transform M^T and diag(M M^T)
+// are those of DiscretizationSetup_D3Q19 (src/lbm/lbm_discretization_d3q19.F90:
+// 64-232) and DiscretizationSetUp_D2Q9 (src/lbm/lbm_discretization_d2q9.F90:
+// 53-144); the order has to be the reference's because populations cross the
+// C ABI in the reference's layout and the MRT moment order fixes rounding.
+// Everything here is constexpr so that kernels unrolled with sfor<> fold
+// zero and unit MRT coefficients away at compile time.
+#pragma once
+#include <type_traits>
+
+namespace tx {
+
+template <int B, int E, class F>
+__host__ __device__ __forceinline__ void sfor(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    sfor<B + 1, E>(f);
+  }
+}
+
+template <int D>
+struct Lat;
+
+template <>
+struct Lat<3> {
+  static constexpr int ND = 3;
+  static constexpr int Q = 19;
+  static constexpr int NAXIS = 6;  // directions 1..6 are the axis links
+  __host__ __device__ static constexpr int c(int n, int d) {
+    const int cx[19] = {0, 1, 0, -1, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 0, 0, 0, 0};
+    const int cy[19] = {0, 0, 1, 0, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, -1, 1};
+    const int cz[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+    return d == 0 ? cx[n] : (d == 1 ? cy[n] : cz[n]);
+  }
+  __host__ __device__ static constexpr double w(int n) {
+    return n == 0 ? 1.0 / 3.0 : (n <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+  }
+  // mt(i, k) = M^T(i, k): value of moment k's basis vector at direction i
+  __host__ __device__ static constexpr int mt(int i, int k) {
+    const signed char m[19][19] = {
+        {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1},
+        {-30, -11, -11, -11, -11, -11, -11, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8},
+        {12, -4, -4, -4, -4, -4, -4, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1},
+        {0, 1, 0, -1, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 0, 0, 0, 0},
+        {0, -4, 0, 4, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 0, 0, 0, 0},
+        {0, 0, 1, 0, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, -1, 1},
+        {0, 0, -4, 0, 4, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, -1, 1},
+        {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1},
+        {0, 0, 0, 0, 0, -4, 4, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1},
+        {0, 2, -1, 2, -1, -1, -1, 1, 1, 1, 1, 1, 1, 1, 1, -2, -2, -2, -2},
+        {0, -4, 2, -4, 2, 2, 2, 1, 1, 1, 1, 1, 1, 1, 1, -2, -2, -2, -2},
+        {0, 0, 1, 0, 1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0},
+        {0, 0, -2, 0, -2, 2, 2, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, -1, 1, -1},
+        {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 1, -1, -1, 1, -1, 1, 1, -1, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, -1, -1, 1, 1, 0, 0, 0, 0, 1, -1, -1, 1},
+        {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, -1, -1, -1, -1, 1, 1}};
+    return m[k][i];
+  }
+  __host__ __device__ static constexpr int mmt(int k) {
+    const int v[19] = {19, 2394, 252, 10, 40, 10, 40, 10, 40, 36, 72, 12, 24, 4, 4, 4, 8, 8, 8};
+    return v[k];
+  }
+};
+
+template <>
+struct Lat<2> {
+  static constexpr int ND = 2;
+  static constexpr int Q = 9;
+  static constexpr int NAXIS = 4;
+  __host__ __device__ static constexpr int c(int n, int d) {
+    const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    const int cy[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    return d == 0 ? cx[n] : (d == 1 ? cy[n] : 0);
+  }
+  __host__ __device__ static constexpr double w(int n) {
+    return n == 0 ? 4.0 / 9.0 : (n <= 4 ? 1.0 / 9.0 : 1.0 / 36.0);
+  }
+  __host__ __device__ static constexpr int mt(int i, int k) {
+    const signed char m[9][9] = {{1, 1, 1, 1, 1, 1, 1, 1, 1},   {-4, -1, -1, -1, -1, 2, 2, 2, 2},
+                                 {4, -2, -2, -2, -2, 1, 1, 1, 1}, {0, 1, 0, -1, 0, 1, -1, -1, 1},
+                                 {0, -2, 0, 2, 0, 1, -1, -1, 1},  {0, 0, 1, 0, -1, 1, 1, -1, -1},
+                                 {0, 0, -2, 0, 2, 1, 1, -1, -1},  {0, 1, -1, 1, -1, 0, 0, 0, 0},
+                                 {0, 0, 0, 0, 0, 1, -1, 1, -1}};
+    return m[k][i];
+  }
+  __host__ __device__ static constexpr int mmt(int k) {
+    const int v[9] = {9, 36, 36, 6, 12, 6, 12, 4, 4};
+    return v[k];
+  }
+};
+
+// the direction with all velocity components negated (disc%opposites)
+template <int D>
+__host__ __device__ constexpr int opp(int n) {
+  int r = 0;
+  for (int m = 0; m < Lat<D>::Q; ++m) {
+    bool ok = true;
+    for (int d = 0; d < D; ++d) ok = ok && (Lat<D>::c(m, d) == -Lat<D>::c(n, d));
+    if (ok) r = m;
+  }
+  return r;
+}
+
+// MRT rate index map of DiscretizationSetupRelax_D3Q19 (:234-263) / _D2Q9
+// (:147-166): which of s_c, s_e, s_e2, s_q, s_nu, s_pi, s_m relaxes moment k
+enum { R_C = 0, R_E, R_E2, R_Q, R_NU, R_PI, R_M };
+template <int D>
+__host__ __device__ constexpr int rate_of(int k) {
+  if (D == 3) {
+    const int r[19] = {R_C, R_E, R_E2, R_C, R_Q, R_C, R_Q, R_C, R_Q, R_NU,
+                       R_PI, R_NU, R_PI, R_NU, R_NU, R_NU, R_M, R_M, R_M};
+    return r[k];
+  } else {
+    const int r[9] = {R_C, R_E, R_E2, R_C, R_Q, R_C, R_Q, R_NU, R_NU};
+    return r[k];
+  }
+}
+
+}  // namespace tx

@@ -1,0 +1,234 @@
+"""The reference's input deck (a PETSc options file) mapped onto tx_params.
+
+Mirrors OptionsSetUp (lbm_options.F90:163-365), FlowSetFromOptions
+(lbm_flow.F90:188-284), FlowParseBC (lbm_flow.F90:1031-1309) for periodic and
+density faces, ComponentSetFromOptions (lbm_component.F90:131-176),
+RelaxationSetFromOptions (lbm_relaxation.F90:117-151), MineralSetFromOptions
+(lbm_mineral.F90:103-134), GridSetFromOptions/InfoSetFromOptions
+(lbm_grid.F90:97-132, lbm_info.F90:116-238) and FlowSetPhysicalScales
+(lbm_flow.F90:295-376).  Option names and defaults are the reference's, so an
+unchanged deck drives this library.
+"""
+from dataclasses import dataclass, field
+
+from . import params as P
+
+
+class DeckError(ValueError):
+    """Raised where the reference would call LBMError on the deck."""
+
+
+def parse_deck_text(text):
+    """PETSc options-file syntax: ``-name value`` per line, ``#`` comments."""
+    opts = {}
+    for raw in text.splitlines():
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        parts = line.split(None, 1)
+        key = parts[0]
+        if not key.startswith("-"):
+            raise DeckError("option must start with '-': %r" % raw)
+        opts[key[1:]] = parts[1].strip() if len(parts) > 1 else None
+    return opts
+
+
+def _bool(v):
+    if v is None:
+        return True
+    s = v.strip().lower()
+    if s in ("1", "true", "yes", "on"):
+        return True
+    if s in ("0", "false", "no", "off"):
+        return False
+    raise DeckError("not a boolean: %r" % v)
+
+
+def _reals(v):
+    return [float(x) for x in v.replace(" ", "").split(",") if x != ""]
+
+
+@dataclass
+class RunOptions:
+    """Driver-level options that stay on the host (the time loop's controls)."""
+    npasses: int = 1
+    ntimes: int = 1
+    kwrite: int = -1
+    istep: int = 0
+    run_to_steadystate: bool = False
+    steadystate_tolerance: float = 1e-6
+    steadystate_field_rho: bool = True
+    steadystate_field_fi: bool = False
+    walls_type: int = 1
+    walls_file: str = "geometry.dat"
+    output_prefix: str = ""
+    output_flow_fi: bool = False
+    ic_file: str = ""
+    ic_file_rho: str = ""
+    component_names: list = field(default_factory=list)
+    mineral_names: list = field(default_factory=list)
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nsteps(self):
+        return self.ntimes * self.npasses
+
+
+def params_from_options(opts):
+    """Return (tx_params, RunOptions) for a parsed options dict."""
+    p = P.default_params()
+    run = RunOptions()
+    get = opts.get
+
+    def has(k):
+        return k in opts
+
+    # discretization (lbm_options.F90:303-324)
+    name = get("flow_discretization") or get("discretization") or "D3Q19"
+    name = name.strip().lower()
+    if name.startswith("d3q19"):
+        p.discretization = P.D3Q19
+    elif name.startswith("d2q9"):
+        p.discretization = P.D2Q9
+    else:
+        raise DeckError("Invalid Discretization")
+    nd = p.ndims
+
+    # grid (lbm_info.F90:150-163)
+    p.nx = int(get("NX", -1))
+    p.ny = int(get("NY", -1))
+    p.nz = int(get("NZ", -1)) if nd == 3 else 1
+    if p.nx < 1 or p.ny < 1 or p.nz < 1:
+        raise DeckError("grid size -NX/-NY(/-NZ) must be given")
+    for a, ax in enumerate("xyz"[:nd]):
+        if has("bc_periodic_" + ax) and _bool(get("bc_periodic_" + ax)):
+            p.bc_flags[2 * a] = P.BC_PERIODIC
+            p.bc_flags[2 * a + 1] = P.BC_PERIODIC
+
+    p.relaxation_mode = int(get("flow_relaxation_mode", 0))
+    p.ncomponents = int(get("ncomponents", 1))
+    p.nminerals = int(get("nminerals", 1))
+    if not 1 <= p.ncomponents <= P.MAXC:
+        raise DeckError("ncomponents must be 1..%d" % P.MAXC)
+    if not 0 <= p.nminerals <= P.MAXMIN:
+        raise DeckError("nminerals must be 0..%d" % P.MAXMIN)
+    if has("isotropy_order"):
+        p.isotropy_order = int(get("isotropy_order"))
+    elif has("derivative_order"):
+        p.isotropy_order = int(get("derivative_order"))
+    if _bool(get("flow_use_nonideal_eos", "0")):
+        raise DeckError("-flow_use_nonideal_eos: only psi = rho is on this path")
+
+    # components (lbm_component.F90:82-176, lbm_relaxation.F90:117-151)
+    s = p.ncomponents
+    names = []
+    for m in range(s):
+        nm = get("component%d_name" % (m + 1)) or "component%d" % (m + 1)
+        names.append(nm.strip())
+    run.component_names = names
+    viscosity = [-999.0] * s
+    density = [-999.0] * s
+    for m, nm in enumerate(names):
+        if p.relaxation_mode == P.SRT:
+            if has("tau_" + nm):
+                p.tau[m] = float(get("tau_" + nm))
+        else:
+            for key in ("s_c", "s_e", "s_e2", "s_q", "s_nu", "s_pi", "s_m"):
+                if has(key + "_" + nm):
+                    getattr(p, key)[m] = float(get(key + "_" + nm))
+        if has("mm_" + nm):
+            p.mm[m] = float(get("mm_" + nm))
+        if has("viscosity_" + nm):
+            viscosity[m] = float(get("viscosity_" + nm))
+        if has("density_" + nm):
+            density[m] = float(get("density_" + nm))
+        for q in range(s):
+            key = "g_%d%d" % (m + 1, q + 1)
+            if has(key):
+                p.g[m][q] = float(get(key))
+
+    # minerals (lbm_mineral.F90:64-134)
+    mnames = []
+    for q in range(p.nminerals):
+        nm = get("mineral%d_name" % (q + 1)) or "mineral%d" % (q + 1)
+        mnames.append(nm.strip())
+        for m in range(s):
+            key = "gw_%s_%s" % (nm.strip(), names[m])
+            if has(key):
+                p.gw[q][m] = float(get(key))
+    run.mineral_names = mnames
+
+    # body force (lbm_flow.F90:224-231)
+    if has("gvt"):
+        g = _reals(get("gvt"))
+        p.body_forces = 1
+        for d in range(min(nd, len(g))):
+            p.gvt[d] = g[d]
+
+    # boundary conditions (lbm_flow.F90:1031-1309): periodic and density
+    for f, fname in enumerate(P.FACE_NAMES[: 2 * nd]):
+        if has("bc_density_" + fname) and _bool(get("bc_density_" + fname)):
+            if p.bc_flags[f] == P.BC_PERIODIC:
+                raise DeckError("Multiple BCs provided for boundary " + fname)
+            p.bc_flags[f] = P.BC_DENSITY
+            for m in range(s):
+                key = ("bc_density_%s_value" % fname) if s == 1 else ("bc_density_%s_%s" % (fname, names[m]))
+                p.bc_density[f][m] = float(get(key, -1.0))
+        for other in ("reflecting", "pressure", "pressure_inlet", "pressure_outlet", "flux",
+                      "flux_inlet", "flux_outlet", "momentum", "velocity"):
+            if has("bc_%s_%s" % (other, fname)) and _bool(get("bc_%s_%s" % (other, fname))):
+                raise DeckError("-bc_%s_%s: only periodic and density faces are on this path" % (other, fname))
+
+    _physical_scales(p, viscosity, density)
+
+    # driver options (lbm_options.F90:184-262)
+    run.npasses = int(get("npasses", 1))
+    run.ntimes = int(get("ntimes", 1))
+    run.kwrite = int(get("kwrite", -1))
+    run.istep = int(get("istep", 0))
+    run.run_to_steadystate = _bool(get("run_to_steadystate", "0"))
+    if run.run_to_steadystate:
+        run.steadystate_tolerance = float(get("steadystate_tolerance", 1e-6))
+        run.steadystate_field_rho = _bool(get("steadystate_field_rho", "1"))
+        run.steadystate_field_fi = _bool(get("steadystate_field_fi", "0"))
+    run.walls_type = int(get("walls_type", 1))
+    run.walls_file = (get("walls_file") or "geometry.dat").strip()
+    run.output_prefix = (get("output_file_prefix") or "").strip()
+    run.output_flow_fi = _bool(get("output_flow_fi", "0"))
+    run.ic_file = (get("ic_file") or "").strip()
+    run.ic_file_rho = (get("ic_file_rho") or "").strip()
+    run.extra = dict(opts)
+    return p, run
+
+
+def _physical_scales(p, viscosity, density, length_scale=1.0):
+    """FlowSetPhysicalScales (lbm_flow.F90:295-376): tau / mm consistency.
+
+    Component 1's tau and mm are taken as correct; other components' tau/mm
+    are derived from -viscosity_<c>/-density_<c> when those are given."""
+    eps = 1.e-8
+    if viscosity[0] < -990.0:
+        time_scale = 1.0
+    else:
+        time_scale = length_scale * length_scale * (p.tau[0] - 0.5) / (viscosity[0] * 3.)
+    if density[0] < -990.0:
+        density[0] = 1.0
+    mass_scale = p.mm[0] * density[0] * length_scale ** 3
+    for m in range(1, p.ncomponents):
+        if viscosity[m] >= -990.0:
+            consistent_tau = (3. * time_scale * viscosity[m]) / (length_scale * length_scale) + 0.5
+            if abs(p.tau[m] - 1.) < eps:
+                p.tau[m] = consistent_tau
+            elif abs(p.tau[m] - consistent_tau) > eps:
+                raise DeckError("Viscosities and relaxation times specified for components are not consistent.")
+        if density[m] >= -990.0:
+            consistent_mm = mass_scale / density[0] / length_scale ** 3
+            if abs(p.mm[m] - 1.) < eps:
+                p.mm[m] = consistent_mm
+            elif abs(p.mm[m] - consistent_mm) > eps:
+                raise DeckError("Densities and molecular masses specified for components are not consistent.")
+
+
+def load_deck(path):
+    with open(path) as f:
+        return params_from_options(parse_deck_text(f.read()))

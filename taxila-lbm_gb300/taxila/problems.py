@@ -1,0 +1,79 @@
+"""Problem plugins: initial states and wall geometries, natural order.
+
+The reference fills host arrays through link-time plugins
+(``initialize_state``, ``initialize_walls``; src/lbm/lbm.F90:444-453,
+src/lbm/lbm_walls.F90:172).  These functions produce the same arrays as numpy
+vectors for tx_upload_state / tx_upload_walls: rho has s values per site
+(component fastest), walls one code per site, x fastest then y, z.
+"""
+import numpy as np
+
+
+def _grid(nx, ny, nz):
+    k, j, i = np.meshgrid(np.arange(1, nz + 1), np.arange(1, ny + 1), np.arange(1, nx + 1), indexing="ij")
+    return i, j, k
+
+
+def bubble_box_state(nx, ny, nz, rho_inner, rho_outer, half, walls=None, only_pore=True):
+    """The reference tests' bubble (tests/bubble_2D/initialize_state.F90:149-206,
+    :45-124): rho_inner on the box (N+1)/2 +- half (integer division), 1-based
+    inclusive bounds, rho_outer elsewhere; ``only_pore`` skips wall sites like
+    the bubble_2D plugin (the *_hots plugin sets every site)."""
+    s = len(rho_inner)
+    i, j, k = _grid(nx, ny, nz)
+    inside = (i >= (nx + 1) // 2 - half) & (i <= (nx + 1) // 2 + half)
+    inside &= (j >= (ny + 1) // 2 - half) & (j <= (ny + 1) // 2 + half)
+    if nz > 1:
+        inside &= (k >= (nz + 1) // 2 - half) & (k <= (nz + 1) // 2 + half)
+    rho = np.where(inside.ravel()[:, None], np.asarray(rho_inner, float)[None, :], np.asarray(rho_outer, float)[None, :])
+    if only_pore and walls is not None:
+        rho[np.asarray(walls).ravel() != 0] = 0.0
+    return rho.reshape(-1, s).ravel()
+
+
+def bubble_ball_state(nx, ny, nz, radius, rho_in, rho_out):
+    """Centred disk (2D) or sphere (3D) of radius ``radius`` in 1-based cell
+    centres: rho_in inside (distance <= radius), rho_out outside."""
+    i, j, k = _grid(nx, ny, nz)
+    r2 = (i - (nx + 1) / 2.0) ** 2 + (j - (ny + 1) / 2.0) ** 2
+    if nz > 1:
+        r2 = r2 + (k - (nz + 1) / 2.0) ** 2
+    inside = (r2 <= radius * radius).ravel()
+    return np.where(inside[:, None], np.asarray(rho_in, float)[None, :], np.asarray(rho_out, float)[None, :]).ravel()
+
+
+def sphere_pack(shape, porosity, rmin, rmax, seed, periodic=True, max_spheres=1_000_000):
+    """Seeded random overlapping spheres added until the pore fraction drops
+    to ``porosity``.  shape = (nz, ny, nx); radii uniform in [rmin, rmax];
+    centres uniform in the box; periodic images wrap when ``periodic``.
+    Returns a bool array (True = solid), natural order."""
+    nz, ny, nx = shape
+    rng = np.random.default_rng(seed)
+    solid = np.zeros(shape, dtype=bool)
+    target = (1.0 - porosity) * solid.size
+    count = 0
+    zz = np.arange(nz)[:, None, None]
+    yy = np.arange(ny)[None, :, None]
+    xx = np.arange(nx)[None, None, :]
+    while solid.sum() < target and count < max_spheres:
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(0, 1, 3) * np.array([nz, ny, nx])
+        dz = zz - c[0]
+        dy = yy - c[1]
+        dx = xx - c[2]
+        if periodic:
+            dz = (dz + nz / 2.0) % nz - nz / 2.0
+            dy = (dy + ny / 2.0) % ny - ny / 2.0
+            dx = (dx + nx / 2.0) % nx - nx / 2.0
+        solid |= (dz * dz + dy * dy + dx * dx) <= r * r
+        count += 1
+    return solid
+
+
+def mineral_walls(solid, seed, nminerals=2):
+    """Split solid voxels among minerals 1..nminerals with a seeded fair coin."""
+    rng = np.random.default_rng(seed + 7919)
+    walls = np.zeros(solid.shape, dtype=np.float64)
+    ids = rng.integers(1, nminerals + 1, size=solid.shape)
+    walls[solid] = ids[solid]
+    return walls.ravel()

@@ -1,0 +1,89 @@
+"""Parameter sets and initial states shared by the oracle and GPU tests."""
+import numpy as np
+
+from taxila import params as P
+from taxila import problems
+
+REF = "/root/reference"
+
+
+def base(disc, shape, ncomp=2, mode=P.SRT, iso=4, periodic=(1, 1, 1)):
+    p = P.default_params()
+    p.discretization = disc
+    p.nz, p.ny, p.nx = shape
+    if disc == P.D2Q9:
+        p.nz = 1
+    p.ncomponents = ncomp
+    p.relaxation_mode = mode
+    p.isotropy_order = iso
+    for a in range(p.ndims):
+        if periodic[a]:
+            p.bc_flags[2 * a] = p.bc_flags[2 * a + 1] = P.BC_PERIODIC
+    return p
+
+
+def bubble_2d_reference_deck():
+    """tests/bubble_2D/input_data of the reference as tx_params."""
+    p = base(P.D2Q9, (1, 128, 128))
+    p.tau[0] = p.tau[1] = 1.0
+    p.g[0][1] = p.g[1][0] = 0.1
+    return p
+
+
+def bubble_2d_reference_state(p):
+    return problems.bubble_box_state(p.nx, p.ny, 1, [0.03, 0.97], [0.97, 0.03], 26, np.zeros(p.nsites))
+
+
+def sc_bubble(disc, shape, mode, iso, g=0.12, r=None, ncomp=2):
+    p = base(disc, shape, ncomp=ncomp, mode=mode, iso=iso)
+    p.tau[0], p.tau[1] = 1.0, 0.8
+    if mode == P.MRT:
+        p.s_nu[0], p.s_nu[1] = 1.0, 1.0 / 0.7
+        p.s_e[0], p.s_q[1] = 1.2, 1.1
+    if ncomp == 2:
+        p.g[0][1] = p.g[1][0] = g
+    z, y, x = p.shape
+    r = r if r is not None else max(2.0, min(x, y) / 5.0)
+    rho = problems.bubble_ball_state(x, y, z, r, [2.0, 0.06][:ncomp], [0.06, 2.0][:ncomp])
+    return p, np.zeros(p.nsites), rho
+
+
+def porous_case(disc, shape, mode=P.SRT, iso=4, seed=3, dirichlet=True, body=False, ncomp=2):
+    """Seeded sphere pack with two minerals, ghost walls on x/y, density faces on z
+    (D2Q9: on y), plus optional body force."""
+    periodic = (0, 0, 1) if disc == P.D3Q19 else (0, 1, 1)
+    if disc == P.D3Q19 and not dirichlet:
+        periodic = (1, 1, 1)
+    p = base(disc, shape, ncomp=ncomp, mode=mode, iso=iso, periodic=periodic)
+    p.nminerals = 2
+    p.tau[0], p.tau[1] = 1.0, 0.9
+    if mode == P.MRT:
+        p.s_nu[0], p.s_nu[1] = 1.0, 1.0 / 0.9
+    if ncomp == 2:
+        p.g[0][1] = p.g[1][0] = 0.1
+        p.gw[0][0], p.gw[0][1] = 0.3, -0.3
+        p.gw[1][0], p.gw[1][1] = -0.3, 0.3
+    else:
+        p.gw[0][0], p.gw[1][0] = 0.05, -0.05
+    z, y, x = p.shape
+    solid = problems.sphere_pack((z, y, x), 0.55, 1.2, 2.5, seed, periodic=True)
+    walls = problems.mineral_walls(solid, seed)
+    rng = np.random.default_rng(seed)
+    s = p.ncomponents
+    rho = np.empty((p.nsites, s))
+    rho[:, 0] = 1.0 + 0.02 * rng.standard_normal(p.nsites)
+    if s == 2:
+        rho[:, 1] = 0.06 + 0.005 * rng.standard_normal(p.nsites)
+    if dirichlet:
+        a = 2 if disc == P.D3Q19 else 1
+        p.bc_flags[2 * a] = P.BC_DENSITY
+        p.bc_flags[2 * a + 1] = P.BC_DENSITY
+        p.bc_density[2 * a][0], p.bc_density[2 * a + 1][0] = 1.03, 0.97
+        if s == 2:
+            p.bc_density[2 * a][1], p.bc_density[2 * a + 1][1] = 0.07, 0.05
+    if body:
+        p.body_forces = 1
+        p.gvt[0], p.gvt[1] = 1e-5, -2e-5
+        if disc == P.D3Q19:
+            p.gvt[2] = 3e-5
+    return p, walls, rho.ravel()

@@ -1,0 +1,51 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    names = []
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(tx_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    for must in ("tx_create", "tx_destroy", "tx_upload_walls", "tx_upload_state", "tx_upload_fi",
+                 "tx_init", "tx_step", "tx_download", "tx_delta_norm", "tx_last_error"):
+        assert must in names
+
+
+def test_library_exports_all_declared():
+    from taxila import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [n for n in declared() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_params_struct_layout():
+    # ctypes mirror matches the C struct (offset of the last field + its size)
+    from taxila import params as P
+    assert ctypes.sizeof(P.TxParams) == P.TxParams.rho0.offset + 8
+
+
+def test_params_default_matches_c():
+    from taxila import _lib
+    from taxila import params as P
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    L = _lib.load()
+    a = P.TxParams()
+    assert L.tx_params_default(ctypes.byref(a)) == 0
+    b = P.default_params()
+    assert bytes(a) == bytes(b)

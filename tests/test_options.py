@@ -1,0 +1,95 @@
+"""Deck parsing mirrors the reference's options (lbm_options.F90, lbm_flow.F90)."""
+import pytest
+
+from taxila import options as O
+from taxila import params as P
+
+DECK_2D = """
+## Bubble problem, in 2D
+-NX 128
+-NY 128
+-flow_relaxation_mode 0 # SRT
+-discretization d2q9
+-ncomponents 2
+-component1_name outer
+-mm_outer 1.0
+-tau_outer 1.0
+-component2_name inner
+-mm_inner 1.0
+-tau_inner 1.0
+-g_11 0.0
+-g_22 0.0
+-g_12 0.1
+-g_21 0.1
+-rho_outer 0.97,0.03
+-rho_inner 0.03,0.97
+-bc_periodic_x
+-bc_periodic_y
+-npasses 100
+-kwrite 100
+-walls_type 2
+-output_file_prefix test_solution/
+-output_flow_fi
+"""
+
+
+def test_bubble_deck():
+    p, run = O.params_from_options(O.parse_deck_text(DECK_2D))
+    assert p.discretization == P.D2Q9 and (p.nx, p.ny, p.nz) == (128, 128, 1)
+    assert p.ncomponents == 2 and p.relaxation_mode == P.SRT and p.isotropy_order == 4
+    assert p.g[0][1] == 0.1 and p.g[1][0] == 0.1 and p.g[0][0] == 0.0
+    assert list(p.bc_flags)[:4] == [P.BC_PERIODIC] * 4
+    assert run.nsteps == 100 and run.kwrite == 100 and run.walls_type == 2
+    assert run.component_names == ["outer", "inner"] and run.output_flow_fi
+    assert O._reals(run.extra["rho_inner"]) == [0.03, 0.97]
+
+
+def test_mrt_and_derivative_order():
+    deck = DECK_2D.replace("-flow_relaxation_mode 0 # SRT", "-flow_relaxation_mode 1\n-derivative_order 10\n-s_e_outer 0.1\n-s_nu_inner 1.5")
+    p, _ = O.params_from_options(O.parse_deck_text(deck))
+    assert p.relaxation_mode == P.MRT and p.isotropy_order == 10
+    assert p.s_e[0] == 0.1 and p.s_nu[1] == 1.5 and p.tau[0] == 1.0
+
+
+def test_density_faces_and_minerals():
+    deck = """-NX 8
+-NY 8
+-NZ 16
+-discretization d3q19
+-ncomponents 2
+-nminerals 2
+-bc_density_zm
+-bc_density_zm_component1 2.1
+-bc_density_zm_component2 0.06
+-bc_density_zp
+-bc_density_zp_component1 1.9
+-bc_density_zp_component2 0.06
+-gw_mineral1_component1 0.3
+-gw_mineral2_component2 -0.3
+-gvt 0,0,1e-6
+"""
+    p, _ = O.params_from_options(O.parse_deck_text(deck))
+    assert p.bc_flags[4] == P.BC_DENSITY and p.bc_flags[5] == P.BC_DENSITY and p.bc_flags[0] == P.BC_NULL
+    assert p.bc_density[4][0] == 2.1 and p.bc_density[5][1] == 0.06
+    assert p.gw[0][0] == 0.3 and p.gw[1][1] == -0.3 and p.gw[0][1] == 0.0
+    assert p.body_forces == 1 and p.gvt[2] == 1e-6
+
+
+def test_conflicting_bcs_rejected():
+    deck = "-NX 4\n-NY 4\n-NZ 4\n-bc_periodic_z\n-bc_density_zm\n"
+    with pytest.raises(O.DeckError):
+        O.params_from_options(O.parse_deck_text(deck))
+
+
+def test_unsupported_bc_rejected():
+    deck = "-NX 4\n-NY 4\n-NZ 4\n-bc_velocity_zm\n"
+    with pytest.raises(O.DeckError):
+        O.params_from_options(O.parse_deck_text(deck))
+
+
+def test_viscosity_consistency():
+    deck = "-NX 4\n-NY 4\n-NZ 4\n-ncomponents 2\n-tau_component1 1.0\n-viscosity_component1 0.1\n-viscosity_component2 0.05\n"
+    p, _ = O.params_from_options(O.parse_deck_text(deck))
+    # time scale = (tau1 - 0.5)/(3 nu1); tau2 = 3 ts nu2 + 0.5
+    ts = (1.0 - 0.5) / (0.1 * 3.0)
+    assert abs(p.tau[1] - (3 * ts * 0.05 + 0.5)) < 1e-15
