@@ -20,6 +20,7 @@ struct tx_handle {
   int D = 3, S = 1, Q = 19;
   Geo g{};
   Phys ph{};
+  Phys* d_phys = nullptr;     // device copy of ph
   Faces faces{};
   KernelSet ks{};
   cudaStream_t stream = nullptr;
@@ -73,6 +74,7 @@ StepArgs args(tx_handle* h, int in, int out) {
   a.fout = h->f[out];
   a.rho = h->rho;
   a.mask = h->mask;
+  a.phys = h->d_phys;
   a.g = h->g;
   a.faces = h->faces;
   return a;
@@ -101,6 +103,8 @@ int validate(const tx_params* p, std::string* why) {
   const int D = p->discretization == TX_D3Q19 ? 3 : 2;
   if (p->nx < 1 || p->ny < 1 || p->nz < 1) return bad("lattice sizes must be >= 1");
   if (D == 2 && p->nz != 1) return bad("D2Q9 needs nz = 1");
+  if ((long long)p->nx * p->ny * p->nz >= (1ll << 31)) return bad("lattices of 2^31 sites or more are not supported");
+  if (p->nz > 65535) return bad("nz must be <= 65535");
   if (p->ncomponents < 1 || p->ncomponents > TX_MAX_COMPONENTS) return bad("ncomponents out of range");
   if (p->ncomponents > kMaxBuiltComponents)
     return bad("ncomponents > " + std::to_string(kMaxBuiltComponents) + " is not built into this library");
@@ -114,6 +118,8 @@ int validate(const tx_params* p, std::string* why) {
   for (int a = 0; a < D; ++a) {
     const int lo = p->bc_flags[2 * a], hi = p->bc_flags[2 * a + 1];
     if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
+    const int ext = a == 0 ? p->nx : (a == 1 ? p->ny : p->nz);
+    if (lo == TX_BC_PERIODIC && ext < 3) return bad("periodic axes need at least 3 sites");
     for (int f : {2 * a, 2 * a + 1}) {
       const int v = p->bc_flags[f];
       if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
@@ -225,7 +231,7 @@ int stage_field(tx_handle* h, int field) {
   } else {
     const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
                    : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : 7;
-    h->ks.moments(args(h, h->cur, h->cur), h->ph, what, h->stage, h->stream);
+    h->ks.moments(args(h, h->cur, h->cur), what, h->stage, h->stream);
   }
   return check_launch(h, "download kernel");
 }
@@ -303,8 +309,11 @@ int tx_create(const tx_params* p, tx_handle** out) {
   if (cudaMalloc(&h->f[0], popb) != cudaSuccess || cudaMalloc(&h->f[1], popb) != cudaSuccess ||
       cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
       cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->stage, stageb) != cudaSuccess ||
-      cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess)
+      cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&h->d_phys, sizeof(Phys)) != cudaSuccess)
     return cleanup("device allocation failed", TX_ERR_NOMEM);
+  if (cudaMemcpy(h->d_phys, &h->ph, sizeof(Phys), cudaMemcpyHostToDevice) != cudaSuccess)
+    return cleanup("parameter upload failed", TX_ERR_CUDA);
   cudaMemsetAsync(h->f[0], 0, popb, h->stream);
   cudaMemsetAsync(h->f[1], 0, popb, h->stream);
   cudaMemsetAsync(h->rho, 0, (size_t)N * h->S * h->rho_bytes, h->stream);
@@ -344,6 +353,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->old_fi);
   cudaFree(h->uic);
   cudaFree(h->red);
+  cudaFree(h->d_phys);
   for (int f = 0; f < 6; ++f) cudaFree(h->faceval[f]);
   for (int i = 0; i < 4; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
@@ -440,12 +450,12 @@ int tx_init(tx_handle* h) {
   if (!h->have_state && !h->have_fi) return fail(h, TX_ERR_STATE, "tx_upload_state or tx_upload_fi must come before tx_init");
   if (!h->have_fi) {
     // FlowFiInit: the state buffer becomes (1 - P/2) feq of the initial moments
-    h->ks.init(args(h, h->cur, h->cur), h->ph, h->uic, h->stream);
+    h->ks.init(args(h, h->cur, h->cur), h->uic, h->stream);
     int rc = check_launch(h, "k_init");
     if (rc) return rc;
   }
   // FlowUpdateMoments: the forcing density is the plain population sum
-  h->ks.density(args(h, h->cur, h->cur), h->ph, 1, h->stream);
+  h->ks.density(args(h, h->cur, h->cur), 1, h->stream);
   int rc = check_launch(h, "k_density");
   if (rc) return rc;
   rc = sync_stream(h);
@@ -464,9 +474,9 @@ int tx_step(tx_handle* h, int32_t nsteps) {
     const int nxt = 1 - h->cur;
     StepArgs a = args(h, h->cur, nxt);
     if (h->timing) cudaEventRecord(h->ev[0], h->stream);
-    h->ks.step(a, h->ph, h->stream);
+    h->ks.step(a, h->stream);
     if (h->timing) cudaEventRecord(h->ev[1], h->stream);
-    h->ks.density(a, h->ph, 0, h->stream);
+    h->ks.density(a, 0, h->stream);
     if (h->timing) cudaEventRecord(h->ev[2], h->stream);
     int rc = check_launch(h, "k_step/k_density");
     if (rc) return rc;

@@ -9,10 +9,10 @@
 namespace tx {
 
 struct KernelSet {
-  void (*step)(const StepArgs&, const Phys&, cudaStream_t);
-  void (*density)(const StepArgs&, const Phys&, int mode, cudaStream_t);
-  void (*init)(const StepArgs&, const Phys&, const double* uic, cudaStream_t);
-  void (*moments)(const StepArgs&, const Phys&, int what, double* out, cudaStream_t);
+  void (*step)(const StepArgs&, cudaStream_t);
+  void (*density)(const StepArgs&, int mode, cudaStream_t);
+  void (*init)(const StepArgs&, const double* uic, cudaStream_t);
+  void (*moments)(const StepArgs&, int what, double* out, cudaStream_t);
   void (*to_natural)(const void* f, const uint8_t* mask, long long N, double rho0, double* out, cudaStream_t);
   void (*from_natural)(const double* in, const uint8_t* mask, long long N, double rho0, void* f, cudaStream_t);
   const char* name;
@@ -40,23 +40,40 @@ bool kernels_d2_f16_s2(int S, int ISO, bool MRT, KernelSet* ks);
 
 inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Lattice kernels run on an (x-tile, y-tile, z) grid of `threads` threads per
+// block: x tiles of up to 128 sites (a multiple of 32), the rest of the block in y.
+struct Launch3 {
+  dim3 grid, block;
+};
+inline Launch3 launch3(const Geo& g, int threads) {
+  int bx = ((g.nx + 31) / 32) * 32;
+  if (bx > 128) bx = 128;
+  if (bx > threads) bx = threads;
+  int by = threads / bx;
+  if (by < 1) by = 1;
+  Launch3 l;
+  l.block = dim3((unsigned)bx, (unsigned)by, 1);
+  l.grid = dim3((unsigned)((g.nx + bx - 1) / bx), (unsigned)((g.ny + by - 1) / by), (unsigned)g.nz);
+  return l;
+}
+
 }  // namespace tx
 
 // Instantiates the launchers of one storage/arithmetic form for one dimension.
 #define TX_FORM_LAUNCHERS(D, S, ISO, MRT, EXACT, T, R, RT) TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)
 #define TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)                                                  \
   struct L_##S##_##ISO##_##MRT {                                                                             \
-    static void step(const StepArgs& a, const Phys& p, cudaStream_t s) {                                      \
-      k_step<D, S, ISO, MRT, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p);                     \
+    static void step(const StepArgs& a, cudaStream_t s) {                                                     \
+      k_step<D, S, ISO, MRT, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a);                        \
     }                                                                                                         \
-    static void density(const StepArgs& a, const Phys& p, int mode, cudaStream_t s) {                         \
-      k_density<D, S, T, R, RT><<<grid_for(a.g.n, 256), 256, 0, s>>>(a, p, mode);                             \
+    static void density(const StepArgs& a, int mode, cudaStream_t s) {                                        \
+      k_density<D, S, T, R, RT><<<launch3(a.g, 256).grid, launch3(a.g, 256).block, 0, s>>>(a, mode);                                \
     }                                                                                                         \
-    static void init(const StepArgs& a, const Phys& p, const double* u, cudaStream_t s) {                     \
-      k_init<D, S, ISO, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p, u);                       \
+    static void init(const StepArgs& a, const double* u, cudaStream_t s) {                                    \
+      k_init<D, S, ISO, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, u);                          \
     }                                                                                                         \
-    static void moments(const StepArgs& a, const Phys& p, int what, double* out, cudaStream_t s) {            \
-      k_moments<D, S, ISO, EXACT, T, R, RT><<<grid_for(a.g.n, 128), 128, 0, s>>>(a, p, what, out);            \
+    static void moments(const StepArgs& a, int what, double* out, cudaStream_t s) {                           \
+      k_moments<D, S, ISO, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, what, out);               \
     }                                                                                                         \
     static void to_nat(const void* f, const uint8_t* m, long long N, double r0, double* o, cudaStream_t s) {  \
       k_pops_to_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, r0, o); \

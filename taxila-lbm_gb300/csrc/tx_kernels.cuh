@@ -66,6 +66,7 @@ struct StepArgs {
   void* fout;
   void* rho;                // RT [m * N + cell]
   const uint8_t* mask;      // 0 pore, 1..16 mineral, 255 other wall
+  const Phys* phys;         // device copy of the handle's parameters
   Geo g;
   Faces faces;
 };
@@ -92,42 +93,50 @@ template <class T>
 constexpr bool kShifted = !std::is_same<T, double>::value;
 
 // --------------------------------------------------------------- geometry
-__device__ __forceinline__ int wrap_axis(int v, int n) {
-  while (v < 0) v += n;
-  while (v >= n) v -= n;
-  return v;
-}
-
 // Linear index of (x+dx, y+dy, z+dz), or -1 outside a non-periodic axis
 // (the ghost walls of WallsSetGhostNodesD3/D2, lbm_walls.F90:179-231).
+// Branch-free, 32-bit; |d| <= 3 and every periodic extent is >= 3 (checked
+// by tx_create), so one wrap suffices.
 __device__ __forceinline__ long long nbr(const Geo& g, int x, int y, int z, int dx, int dy, int dz) {
   int xx = x + dx, yy = y + dy, zz = z + dz;
-  if (xx < 0 || xx >= g.nx) {
-    if (!g.per[0]) return -1;
-    xx = wrap_axis(xx, g.nx);
-  }
-  if (yy < 0 || yy >= g.ny) {
-    if (!g.per[1]) return -1;
-    yy = wrap_axis(yy, g.ny);
-  }
-  if (zz < 0 || zz >= g.nz) {
-    if (!g.per[2]) return -1;
-    zz = wrap_axis(zz, g.nz);
-  }
-  return (long long)xx + (long long)g.nx * ((long long)yy + (long long)g.ny * zz);
+  const bool ox = xx < 0 || xx >= g.nx, oy = yy < 0 || yy >= g.ny, oz = zz < 0 || zz >= g.nz;
+  const bool outside = (ox && !g.per[0]) || (oy && !g.per[1]) || (oz && !g.per[2]);
+  xx += xx < 0 ? g.nx : (xx >= g.nx ? -g.nx : 0);
+  yy += yy < 0 ? g.ny : (yy >= g.ny ? -g.ny : 0);
+  zz += zz < 0 ? g.nz : (zz >= g.nz ? -g.nz : 0);
+  const long long lin = (long long)xx + (long long)g.nx * ((long long)yy + (long long)g.ny * (long long)zz);
+  return outside ? -1ll : lin;
+}
+
+// Site of this thread in a (x-tile, y-tile, z) launch grid; false when outside.
+__device__ __forceinline__ bool site_of(const Geo& g, int& x, int& y, int& z, long long& idx) {
+  x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  z = (int)blockIdx.z;
+  if (x >= g.nx || y >= g.ny || z >= g.nz) return false;
+  idx = (long long)x + (long long)g.nx * ((long long)y + (long long)g.ny * (long long)z);
+  return true;
 }
 
 __device__ __forceinline__ bool is_pore(const uint8_t* mask, long long i) { return i >= 0 && __ldg(mask + i) == 0; }
 
 __device__ __forceinline__ bool on_face(const Geo& g, int f, int x, int y, int z) {
-  switch (f) {
-    case 0: return x == 0;
-    case 1: return x == g.nx - 1;
-    case 2: return y == 0;
-    case 3: return y == g.ny - 1;
-    case 4: return z == 0;
-    default: return z == g.nz - 1;
-  }
+  const int a = f >> 1;
+  const int c = a == 0 ? x : (a == 1 ? y : z);
+  const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+  return (f & 1) ? c == n - 1 : c == 0;
+}
+
+// bit f set <=> face f is a Dirichlet density face (constant-index reads only)
+__device__ __forceinline__ unsigned face_bits(const Faces& fc) {
+  return (fc.on[0] ? 1u : 0u) | (fc.on[1] ? 2u : 0u) | (fc.on[2] ? 4u : 0u) | (fc.on[3] ? 8u : 0u) |
+         (fc.on[4] ? 16u : 0u) | (fc.on[5] ? 32u : 0u);
+}
+
+// bit f set <=> (x, y, z) lies on face f
+__device__ __forceinline__ unsigned site_faces(const Geo& g, int x, int y, int z) {
+  return (x == 0 ? 1u : 0u) | (x == g.nx - 1 ? 2u : 0u) | (y == 0 ? 4u : 0u) | (y == g.ny - 1 ? 8u : 0u) |
+         (z == 0 ? 16u : 0u) | (z == g.nz - 1 ? 32u : 0u);
 }
 
 template <int D>
@@ -150,15 +159,56 @@ __device__ __forceinline__ long long face_area(const Geo& g, int f) {
 
 template <int D>
 __device__ __forceinline__ bool any_dirichlet(const Geo& g, const Faces& fc, int x, int y, int z) {
-  bool r = false;
-#pragma unroll
-  for (int f = 0; f < 2 * D; ++f) r = r || (fc.on[f] && on_face(g, f, x, y, z));
-  return r;
+  const unsigned keep = D == 3 ? 63u : 15u;
+  return (face_bits(fc) & site_faces(g, x, y, z) & keep) != 0u;
 }
 
 template <int D>
 __host__ __device__ constexpr FFTerm ffterm(int t) {
   return D == 3 ? ff_d3(t) : ff_d2(t);
+}
+
+// One term of the wall-aware psi gradient: the neighbour x + e must be pore
+// space and, for long links, the path cells must satisfy the term's truth table.
+template <int D, int S, int ISO, int TI, class R, class RT>
+__device__ __forceinline__ void ff_term(const Geo& g, const Phys& P, const uint8_t* mask, const RT* rho, int x, int y,
+                                        int z, const R rf[S], R gr[S][D], R ws[D]) {
+  constexpr FFTerm T = ffterm<D>(TI);
+  if constexpr (T.level <= ISO) {
+    const long long pi = nbr(g, x, y, z, T.e[0], T.e[1], T.e[2]);
+    bool ok = is_pore(mask, pi);
+    if constexpr (T.naux > 0) {
+      unsigned bits = 0;
+      if constexpr (T.naux > 0) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[0][0], T.aux[0][1], T.aux[0][2])) ? 1u : 0u;
+      if constexpr (T.naux > 1) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[1][0], T.aux[1][1], T.aux[1][2])) ? 2u : 0u;
+      if constexpr (T.naux > 2) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[2][0], T.aux[2][1], T.aux[2][2])) ? 4u : 0u;
+      if constexpr (T.naux > 3) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[3][0], T.aux[3][1], T.aux[3][2])) ? 8u : 0u;
+      ok = ok && ((T.truth >> bits) & 1u);
+    }
+    if (ok) {
+      R dif[S];
+#pragma unroll
+      for (int m = 0; m < S; ++m) dif[m] = R(rho[(long long)m * g.n + pi]) - rf[m];
+      if constexpr (T.e[0] != 0) {
+        const R coef = R(double(T.e[0]) * P.ffw[T.w]);
+#pragma unroll
+        for (int m = 0; m < S; ++m) gr[m][0] = gr[m][0] + coef * dif[m];
+        ws[0] = ws[0] + R(P.ffw[T.w] * double(T.e[0] * T.e[0]));
+      }
+      if constexpr (D > 1 && T.e[1] != 0) {
+        const R coef = R(double(T.e[1]) * P.ffw[T.w]);
+#pragma unroll
+        for (int m = 0; m < S; ++m) gr[m][1] = gr[m][1] + coef * dif[m];
+        ws[1] = ws[1] + R(P.ffw[T.w] * double(T.e[1] * T.e[1]));
+      }
+      if constexpr (D > 2 && T.e[2] != 0) {
+        const R coef = R(double(T.e[2]) * P.ffw[T.w]);
+#pragma unroll
+        for (int m = 0; m < S; ++m) gr[m][D > 2 ? 2 : 0] = gr[m][D > 2 ? 2 : 0] + coef * dif[m];
+        ws[D > 2 ? 2 : 0] = ws[D > 2 ? 2 : 0] + R(P.ffw[T.w] * double(T.e[2] * T.e[2]));
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------------ forces
@@ -211,36 +261,7 @@ __device__ __forceinline__ void cell_forces(const Geo& g, const Phys& P, const u
       for (int m = 0; m < S; ++m) gr[m][d] = R(0);
     }
     constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
-    sfor<0, NT>([&](auto tt) {
-      constexpr FFTerm T = ffterm<D>(decltype(tt)::value);
-      if constexpr (T.level <= ISO) {
-        const long long pi = nbr(g, x, y, z, T.e[0], T.e[1], T.e[2]);
-        bool ok = is_pore(mask, pi);
-        if constexpr (T.naux > 0) {
-          unsigned bits = 0;
-          sfor<0, T.naux>([&](auto qq) {
-            constexpr FFTerm U = ffterm<D>(decltype(tt)::value);
-            constexpr int q = decltype(qq)::value;
-            if (is_pore(mask, nbr(g, x, y, z, U.aux[q][0], U.aux[q][1], U.aux[q][2]))) bits |= 1u << q;
-          });
-          ok = ok && ((T.truth >> bits) & 1u);
-        }
-        if (ok) {
-          sfor<0, D>([&](auto dd) {
-            constexpr FFTerm U = ffterm<D>(decltype(tt)::value);
-            constexpr int d = decltype(dd)::value;
-            constexpr int e = U.e[d];
-            constexpr int wi = U.w;
-            if constexpr (e != 0) {
-              const R coef = R(double(e) * P.ffw[wi]);
-#pragma unroll
-              for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * (R(rho[(long long)m * g.n + pi]) - rf[m]);
-              ws[d] = ws[d] + R(P.ffw[wi] * double(e * e));
-            }
-          });
-        }
-      }
-    });
+    sfor<0, NT>([&](auto tt) { ff_term<D, S, ISO, decltype(tt)::value, R, RT>(g, P, mask, rho, x, y, z, rf, gr, ws); });
     const R eps = R((double)1.e-12f);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -309,16 +330,16 @@ __device__ __forceinline__ R pop_flux(const R fv[S][Lat<D>::Q], int m, int d0) {
 // Moments of a pore site from its post-stream populations: the density of the
 // collision (rc: Dirichlet nodes re-summed as in BCUpdateRho, lbm_bc.F90:436-611),
 // forces, and the common velocity of FlowUpdateUED3/D2 (lbm_flow.F90:494-574).
-template <int D, int S, int ISO, bool EXACT, class R, class RT>
-__device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, int x, int y, int z, long long idx,
-                                             const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
-  const RT* rho = reinterpret_cast<const RT*>(a.rho);
-#pragma unroll
-  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * a.g.n + idx]);
+// Density of the collision (Dirichlet nodes re-summed as in BCUpdateRho,
+// lbm_bc.F90:436-611) and the common velocity of FlowUpdateUED3/D2
+// (lbm_flow.F90:494-574) from the post-stream populations and the forces.
+template <int D, int S, bool EXACT, class R>
+__device__ __forceinline__ void cell_velocity(const StepArgs& a, const Phys& P, int x, int y, int z,
+                                              const R fv[S][Lat<D>::Q], const R rf[S], const R F[S][D], R rc[S],
+                                              R up[D]) {
   const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
 #pragma unroll
   for (int m = 0; m < S; ++m) rc[m] = dn ? pop_sum<D, S, R>(fv, m) : rf[m];
-  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     R num = R(0), den = R(0);
@@ -334,6 +355,18 @@ __device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, i
     else
       up[d] = num * (R(1) / den);
   }
+}
+
+// Moments of a pore site from its post-stream populations: forces from the
+// forcing density, then cell_velocity.
+template <int D, int S, int ISO, bool EXACT, class R, class RT>
+__device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, int x, int y, int z, long long idx,
+                                             const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
+  const RT* rho = reinterpret_cast<const RT*>(a.rho);
+#pragma unroll
+  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * a.g.n + idx]);
+  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+  cell_velocity<D, S, EXACT, R>(a, P, x, y, z, fv, rf, F, rc, up);
 }
 
 // Equilibrium (DiscretizationEquilf_D3Q19, lbm_discretization_d3q19.F90:265-305;
@@ -374,67 +407,111 @@ __device__ __forceinline__ void feq_pf(const Phys& P, int m, R r, const R u[D], 
 }
 
 // ------------------------------------------------------------------ step
+// Each kernel copies its StepArgs parameter into a local before use; the
+// helpers take references to that copy, never to the parameter itself.
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_step(StepArgs a, Phys P) {
+__global__ void __launch_bounds__(128) k_step(StepArgs a_in) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= a.g.n) return;
+  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
+  const Phys& P = *a.phys;
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
   if (__ldg(a.mask + idx) != 0) return;
-  const int x = (int)(idx % a.g.nx);
-  const long long yz = idx / a.g.nx;
-  const int y = (int)(yz % a.g.ny);
-  const int z = (int)(yz / a.g.ny);
   const long long N = a.g.n;
   const R rho0 = R(P.rho0);
 
-  R fv[S][Q];
-  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, idx, rho0, fv);
-  R rc[S], rf[S], F[S][D], up[D];
-  cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
+  // forces first (they need only rho and the mask)
+  R rf[S], F[S][D];
+  {
+    const RT* rho = reinterpret_cast<const RT*>(a.rho);
+#pragma unroll
+    for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
+    cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+  }
+  const T* fin = reinterpret_cast<const T*>(a.fin);
+  // moments pass, one component's populations at a time
+  R rc[S], up[D];
+  {
+    const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
+    R jm[S][D];
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      R f1[1][Q];
+      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, f1);
+#pragma unroll
+      for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
+      rc[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rf[m];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      R num = R(0), den = R(0);
+#pragma unroll
+      for (int m = 0; m < S; ++m) num = num + (jm[m][d] + R(.5) * F[m][d]) * R(P.mmot[m]);
+#pragma unroll
+      for (int m = 0; m < S; ++m) den = den + rc[m] * R(P.mmot[m]);
+      if constexpr (EXACT)
+        up[d] = num / den;
+      else
+        up[d] = num * (R(1) / den);
+    }
+  }
   R usqr = R(0);
 #pragma unroll
   for (int d = 0; d < D; ++d) usqr = usqr + up[d] * up[d];
 
-  // destinations of the push: x + c_n, or x itself (as opp(n)) at walls
-  long long dst[Q];
-  sfor<0, Q>([&](auto nn) {
-    constexpr int n = decltype(nn)::value;
-    if constexpr (n == 0) {
-      dst[0] = idx;
-    } else {
-      const long long q = nbr(a.g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
-      dst[n] = is_pore(a.mask, q) ? q : -1;
-    }
-  });
   T* fout = reinterpret_cast<T*>(a.fout);
+  // push (DistributionStreamD3/D2 + DistributionBouncebackD3/D2): to x + c_n,
+  // or back to x as opp(n) when x + c_n is a wall
+  auto push = [&](auto nn, int m, R v) {
+    constexpr int n = decltype(nn)::value;
+    constexpr int o = opp<D>(n);
+    if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;  // w(opp n) == w(n): same shift
+    long long q = idx;
+    if constexpr (n != 0) {
+      q = nbr(a.g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
+      if (!is_pore(a.mask, q)) q = -1;
+    }
+    if (q >= 0)
+      St<T>::st(fout + (long long)(m * Q + n) * N + q, v);
+    else
+      St<T>::st(fout + (long long)(m * Q + o) * N + idx, v);
+  };
 
 #pragma unroll
   for (int m = 0; m < S; ++m) {
-    R feq[Q], pf[Q];
-    sfor<0, Q>([&](auto nn) {
-      constexpr int n = decltype(nn)::value;
-      feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq[n], pf[n]);
-    });
-    R* f = fv[m];
+    R f[Q];
+    {
+      R fv1[1][Q];
+      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, fv1);
+#pragma unroll
+      for (int n = 0; n < Q; ++n) f[n] = fv1[0][n];
+    }
     if constexpr (!MRT) {
-      // RelaxationCollideSRT (lbm_relaxation.F90:171-180) then f += P feq
+      // RelaxationCollideSRT (lbm_relaxation.F90:171-180) then f += P feq, one direction at a time
       sfor<0, Q>([&](auto nn) {
         constexpr int n = decltype(nn)::value;
-        const R fb = (R(1.) - R(.5) * pf[n]) * feq[n];
+        R feq, pf;
+        feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
+        const R fb = (R(1.) - R(.5) * pf) * feq;
+        R v;
         if constexpr (EXACT)
-          f[n] = f[n] - (f[n] - fb) / R(P.tau[m]);
+          v = f[n] - (f[n] - fb) / R(P.tau[m]);
         else
-          f[n] = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
-        f[n] = f[n] + pf[n] * feq[n];
+          v = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
+        push(nn, m, v + pf * feq);
       });
     } else {
       // RelaxationCollideMRT (lbm_relaxation.F90:182-200): coef_k from the
       // pre-collision differences, then each f_i subtracts coef_k mt(i,k) in k order
-      R dfi[Q];
+      R dfi[Q], pfeq[Q];
       sfor<0, Q>([&](auto nn) {
         constexpr int n = decltype(nn)::value;
-        dfi[n] = f[n] - (R(1.) - R(.5) * pf[n]) * feq[n];
+        R feq, pf;
+        feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
+        dfi[n] = f[n] - (R(1.) - R(.5) * pf) * feq;
+        pfeq[n] = pf * feq;
       });
       R coef[Q];
       sfor<0, Q>([&](auto kk) {
@@ -462,20 +539,9 @@ __global__ void __launch_bounds__(128) k_step(StepArgs a, Phys P) {
           else if constexpr (c == -1) v = v + coef[k];
           else if constexpr (c != 0) v = v - coef[k] * R(c);
         });
-        f[i] = v + pf[i] * feq[i];
+        push(ii, m, v + pfeq[i]);
       });
     }
-    // push (DistributionStreamD3/D2 + DistributionBouncebackD3/D2)
-    sfor<0, Q>([&](auto nn) {
-      constexpr int n = decltype(nn)::value;
-      constexpr int o = opp<D>(n);
-      R v = f[n];
-      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
-      if (dst[n] >= 0)
-        St<T>::st(fout + (long long)(m * Q + n) * N + dst[n], v);
-      else
-        St<T>::st(fout + (long long)(m * Q + o) * N + idx, v);  // w(opp n) == w(n): same shift
-    });
   }
 }
 
@@ -533,20 +599,19 @@ __device__ __forceinline__ void dirichlet_node(int f, const R pv[S], R fv[S][Lat
 // (BCApplyDirichletToRho, :252-434) on face nodes, sum of populations elsewhere.
 // mode 1 (FlowUpdateMoments at init, lbm_flow.F90:466-478): plain sums.
 template <int D, int S, class T, class R, class RT>
-__global__ void __launch_bounds__(256) k_density(StepArgs a, Phys P, int mode) {
+__global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= a.g.n) return;
+  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
+  const Phys& P = *a.phys;
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
   if (__ldg(a.mask + idx) != 0) return;
   const long long N = a.g.n;
   const R rho0 = R(P.rho0);
   RT* rho = reinterpret_cast<RT*>(a.rho);
   T* fcur = reinterpret_cast<T*>(a.fout);
-  const int x = (int)(idx % a.g.nx);
-  const long long yz = idx / a.g.nx;
-  const int y = (int)(yz % a.g.ny);
-  const int z = (int)(yz / a.g.ny);
   const bool dn = mode == 0 && any_dirichlet<D>(a.g, a.faces, x, y, z);
   if (!dn) {
 #pragma unroll
@@ -565,16 +630,20 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a, Phys P, int mode) {
   R fv[S][Q];
   load_pops<D, S, T, R>(fcur, N, idx, rho0, fv);
   R rf[S];
-  for (int f = 0; f < 2 * D; ++f) {
-    if (!a.faces.on[f] || !on_face(a.g, f, x, y, z)) continue;
-    const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
-    R pv[S];
+  const unsigned hit = face_bits(a.faces) & site_faces(a.g, x, y, z);
+  sfor<0, 2 * D>([&](auto ff) {
+    constexpr int f = decltype(ff)::value;
+    if (hit & (1u << f)) {
+      const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
+      const double* vals = a.faces.vals[f];
+      R pv[S];
 #pragma unroll
-    for (int m = 0; m < S; ++m) pv[m] = R(a.faces.vals[f][(long long)m * area + node]);
-    dirichlet_node<D, S, R>(f, pv, fv);
+      for (int m = 0; m < S; ++m) pv[m] = R(vals[(long long)m * area + node]);
+      dirichlet_node<D, S, R>(f, pv, fv);
 #pragma unroll
-    for (int m = 0; m < S; ++m) rf[m] = pv[m];
-  }
+      for (int m = 0; m < S; ++m) rf[m] = pv[m];
+    }
+  });
 #pragma unroll
   for (int m = 0; m < S; ++m) {
     rho[(long long)m * N + idx] = RT(rf[m]);
@@ -592,17 +661,16 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a, Phys P, int mode) {
 // equilibrium at the initial velocity, f = (1 - P/2) feq (FlowFeqBarD3/D2).
 // uic is [(m*D + d) * N + cell]; rho holds the initial density.
 template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_init(StepArgs a, Phys P, const double* uic) {
+__global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= a.g.n) return;
+  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
+  const Phys& P = *a.phys;
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
   if (__ldg(a.mask + idx) != 0) return;
   const long long N = a.g.n;
-  const int x = (int)(idx % a.g.nx);
-  const long long yz = idx / a.g.nx;
-  const int y = (int)(yz % a.g.ny);
-  const int z = (int)(yz / a.g.ny);
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
   R rf[S], F[S][D];
 #pragma unroll
@@ -635,11 +703,14 @@ __global__ void __launch_bounds__(128) k_init(StepArgs a, Phys P, const double* 
 // what: 2 rho, 3 flux (common velocity), 4 forces, 5 prs, 6 velt, 7 rhot
 // (FlowUpdateDiagnosticsD3/D2, lbm_flow.F90:654-758, for psi = rho).
 template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_moments(StepArgs a, Phys P, int what, double* out) {
+__global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double* out) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= a.g.n) return;
+  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
+  const Phys& P = *a.phys;
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
   const bool wall = __ldg(a.mask + idx) != 0;
   const int dof = what == 2 ? S : (what == 3 || what == 4) ? S * D : (what == 6 ? D : 1);
   if (wall) {
@@ -647,10 +718,6 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a, Phys P, int what, d
     return;
   }
   const long long N = a.g.n;
-  const int x = (int)(idx % a.g.nx);
-  const long long yz = idx / a.g.nx;
-  const int y = (int)(yz % a.g.ny);
-  const int z = (int)(yz / a.g.ny);
   R fv[S][Q];
   load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, idx, R(P.rho0), fv);
   R rc[S], rf[S], F[S][D], up[D];
