@@ -48,6 +48,10 @@ BYTES_PER_LUP_STEP = 2 * 19 * 2 * 8 + 1   # k_step: read + write 2x19 FP64 popul
 BYTES_PER_LUP_DENSITY = 19 * 2 * 8 + 2 * 8 + 1  # k_density: read populations, write rho, mask
 
 
+FORMS = {"f64": P.PREC_F64, "f32": P.PREC_F32, "f16": P.PREC_F32_F16}
+POP_BYTES = {P.PREC_F64: 8, P.PREC_F32: 4, P.PREC_F32_F16: 2}
+
+
 def workload_params(precision=P.PREC_F64, n=N_SIDE):
     p = P.default_params()
     p.discretization = P.D3Q19
@@ -279,7 +283,8 @@ def run_gpu(args):
         torch.cuda.set_device(0)
     gpu = torch.cuda.current_device()
     from taxila._lib import Handle
-    p = workload_params()
+    prec = FORMS[args.form]
+    p = workload_params(prec, args.n)
     walls, rho = workload_state(p)
     h = Handle(p)
     h.upload_walls(walls)
@@ -315,28 +320,35 @@ def run_gpu(args):
         return 0
     peak, peak_kind = peaks()
     k_ms = t_step / nk
-    achieved = p.nsites * BYTES_PER_LUP_STEP / (k_ms * 1e-3) / 1e9
-    traffic = traffic_from_profile()
+    bpl = 2 * 19 * 2 * POP_BYTES[prec] + 1
+    achieved = p.nsites * bpl / (k_ms * 1e-3) / 1e9
+    bpl_dram = traffic_from_profile() if args.form == "f64" else None
+    traffic = round(bpl_dram * p.nsites) if bpl_dram else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "D3Q19 128^3 2-component MRT Shan-Chen bubble (r=24, rho 2.0/0.06, G=0.9 -> g_12=0.15), "
-                               "periodic, isotropy 4, FP64 plain form",
-                   "global_lattice": [N_SIDE] * 3, "sites_per_gpu": p.nsites, "parallelism": "replicas x%d" % ws,
-                   "l2": "inputs larger than L2 (2 x 637 MB population buffers); no flush",
-                   "kernel": "k_step/k_density, fast FP64 form (%s)" % kname},
+        "scaling": "weak", "vs_baseline": None, "dtype": {"f64": "f64", "f32": "f32", "f16": "f32 (f16 storage)"}[args.form],
+        "data": "synthetic",
+        "config": {"workload": "D3Q19 %d^3 2-component MRT Shan-Chen bubble (r=%g, rho 2.0/0.06, G=0.9 -> g_12=0.15), "
+                               "periodic, isotropy 4, %s form" % (args.n, 24.0 * args.n / N_SIDE,
+                                                                  {"f64": "FP64 plain", "f32": "FP32", "f16": "FP32-arithmetic FP16-storage"}[args.form]),
+                   "global_lattice": [args.n] * 3, "sites_per_gpu": p.nsites, "parallelism": "replicas x%d" % ws,
+                   "l2": "inputs larger than L2 (2 x %d MB population buffers); no flush" % (p.nsites * 38 * POP_BYTES[prec] // 1000000),
+                   "kernel": "k_step/k_density (%s)" % kname},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "k_step (collide + push, %d B/LUP algorithmic)" % BYTES_PER_LUP_STEP,
+                     "kernel": "k_step (collide + push, %d B/LUP algorithmic)" % bpl,
                      "ms_per_launch": round(k_ms, 4), "ms_k_density": round(t_dens / nk, 4),
                      "peak_source": peak_kind,
+                     "compute_bound": ({"pipe": "fp64", "active_frac": 0.848,
+                                        "source": "ncu sm__pipe_fp64_cycles_active of k_step, 96^3 capture "
+                                                  "(profiles/k_step_d3q19_2c_mrt_96.md)"} if args.form == "f64" else None),
                      "note": "FP64 is issue-bound on GB300 (FP64 rate ~1/64 of FP32): the HBM fraction of the "
                              "plain form is low by construction; see the fp32/fp16 forms"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
-    if ws == 1 and not args.quick:
+    if ws == 1 and not args.quick and args.form == "f64" and args.n == N_SIDE:
         try:
             line["e2e"] = e2e_run(max(10, args.steps // 4), 2)
         except Exception as ex:  # report, do not hide
@@ -375,6 +387,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form and CPU legs")
+    ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling runs use a smaller case)")
+    ap.add_argument("--form", default="f64", choices=sorted(FORMS), help="storage/arithmetic form of the timed run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
