@@ -172,6 +172,28 @@ int64_t tx_field_size(const tx_handle* h, int32_t field);
 /* Block until all work queued on the handle's stream is done. */
 int tx_sync(tx_handle* h);
 
+/* ---- the step for callers that cannot allocate device memory ---- */
+
+/* Size of the library's one static device work area (every GPU that loads the
+ * library holds it until the process exits). */
+#define TX_STATIC_SCRATCH_BYTES (64ll << 20)
+
+/* No counterpart in the reference.  For callers that are not allowed to call
+ * cudaMalloc (hosts that own all device memory in their own arena, plugins
+ * handed device buffers by their host): runs nsteps flow steps from fi_in to
+ * fi_out without allocating any device memory.  walls (NX*NY*NZ codes),
+ * fi_in and fi_out (s*Q dof) are the caller's DEVICE arrays in natural order;
+ * fi_in is read only.  The result equals tx_create + tx_upload_walls +
+ * tx_upload_fi(fi_in) + tx_init + tx_step(nsteps) + tx_download(TX_FIELD_FI)
+ * (the reference's restart path) for the FP64 form.  All working storage comes
+ * from one static device array of TX_STATIC_SCRATCH_BYTES; lattices that need
+ * more return TX_ERR_ARG.  The first call on a device looks up that array's
+ * address, so make it before any stream capture.  Calls share the array:
+ * calls whose GPU work overlaps race.  The call is synchronous on `stream`
+ * (a cudaStream_t; NULL = default stream).  Errors: tx_last_error(NULL). */
+int tx_step_static(const tx_params* p, const double* walls, const double* fi_in, double* fi_out, int32_t nsteps,
+                   void* stream);
+
 /* ---- instrumentation (no counterpart in the reference; used by bench.py) ---- */
 
 /* Per-kernel CUDA-event timing of tx_step on the handle's stream (resets the totals). */

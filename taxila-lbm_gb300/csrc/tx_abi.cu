@@ -94,6 +94,17 @@ long long field_dof(const tx_handle* h, int field) {
   return -1;
 }
 
+}  // namespace
+
+namespace tx {
+int validate_params(const tx_params* p, std::string* why);
+void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out);
+bool select_kernels(const tx_params* p, KernelSet* ks);
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace tx
+
+namespace {
+
 int validate(const tx_params* p, std::string* why) {
   auto bad = [&](const std::string& s) {
     *why = s;
@@ -133,11 +144,8 @@ int validate(const tx_params* p, std::string* why) {
   return TX_OK;
 }
 
-void fill_phys(tx_handle* h) {
-  const tx_params& p = h->p;
-  Phys& P = h->ph;
+void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
   std::memset(&P, 0, sizeof(P));
-  const int S = h->S;
   for (int m = 0; m < S; ++m) {
     P.tau[m] = p.tau[m];
     P.inv_tau[m] = 1.0 / p.tau[m];
@@ -149,9 +157,9 @@ void fill_phys(tx_handle* h) {
     P.mmot[m] = p.mm[m] * s_c;
     for (int k = 0; k < S; ++k) P.g[m][k] = p.g[m][k];
     const double rates[7] = {p.s_c[m], p.s_e[m], p.s_e2[m], p.s_q[m], p.s_nu[m], p.s_pi[m], p.s_m[m]};
-    for (int k = 0; k < h->Q; ++k) {
-      const int r = h->D == 3 ? rate_of<3>(k) : rate_of<2>(k);
-      const int mmt = h->D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
+    for (int k = 0; k < Q; ++k) {
+      const int r = D == 3 ? rate_of<3>(k) : rate_of<2>(k);
+      const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
       P.srate[m][k] = rates[r];
       P.srate_mmt[m][k] = rates[r] / mmt;
     }
@@ -162,7 +170,7 @@ void fill_phys(tx_handle* h) {
   // isotropy weights (lbm_discretization_d3q19.F90:199-230, d2q9:119-142)
   const int iso = p.isotropy_order;
   double* w = P.ffw;
-  if (h->D == 3) {
+  if (D == 3) {
     if (iso == 4) { w[1] = 1.0 / 6.0; w[2] = 1.0 / 12.0; }
     if (iso == 8) {
       w[1] = 4.0 / 45.0; w[2] = 1.0 / 21.0; w[3] = 2.0 / 105.0; w[4] = 5.0 / 504.0;
@@ -179,10 +187,10 @@ void fill_phys(tx_handle* h) {
   P.c0 = 6.0;  // disc%c_0
   // fluid-solid weights 1./6., 1./12. (D3) and 1./3., 1./12. (D2): default-REAL literals
   if (p.literal_kind == 8) {
-    P.fs_w_axis = h->D == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
+    P.fs_w_axis = D == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
     P.fs_w_diag = 1.0 / 12.0;
   } else {
-    P.fs_w_axis = h->D == 3 ? (double)(1.0f / 6.0f) : (double)(1.0f / 3.0f);
+    P.fs_w_axis = D == 3 ? (double)(1.0f / 6.0f) : (double)(1.0f / 3.0f);
     P.fs_w_diag = (double)(1.0f / 12.0f);
   }
   const double eps15 = (double)1.e-15f;
@@ -195,6 +203,8 @@ void fill_phys(tx_handle* h) {
   P.body_on = p.body_forces != 0;
   P.rho0 = p.precision == TX_PREC_F64 ? 0.0 : p.rho0;
 }
+
+void fill_phys(tx_handle* h) { fill_phys_impl(h->p, h->D, h->S, h->Q, h->ph); }
 
 __global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red) {
   double mx = 0.0;
@@ -237,6 +247,24 @@ int stage_field(tx_handle* h, int field) {
 }
 
 }  // namespace
+
+namespace tx {
+int validate_params(const tx_params* p, std::string* why) { return validate(p, why); }
+void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out) { fill_phys_impl(p, D, S, Q, *out); }
+bool select_kernels(const tx_params* p, KernelSet* ks) {
+  const bool mrt = p->relaxation_mode == TX_RELAX_MRT;
+  using Fn = bool (*)(int, int, bool, KernelSet*);
+  // [form][dimension 3/2][components 1/2]; form 0 exact FP64, 1 FP64, 2 FP32, 3 FP32/FP16
+  static const Fn table[4][2][2] = {
+      {{kernels_d3_exact_s1, kernels_d3_exact_s2}, {kernels_d2_exact_s1, kernels_d2_exact_s2}},
+      {{kernels_d3_f64_s1, kernels_d3_f64_s2}, {kernels_d2_f64_s1, kernels_d2_f64_s2}},
+      {{kernels_d3_f32_s1, kernels_d3_f32_s2}, {kernels_d2_f32_s1, kernels_d2_f32_s2}},
+      {{kernels_d3_f16_s1, kernels_d3_f16_s2}, {kernels_d2_f16_s1, kernels_d2_f16_s2}}};
+  const int form = p->precision == TX_PREC_F64 ? (p->exact ? 0 : 1) : (p->precision == TX_PREC_F32 ? 2 : 3);
+  const int D = p->discretization == TX_D3Q19 ? 3 : 2;
+  return table[form][D == 3 ? 0 : 1][p->ncomponents - 1](p->ncomponents, p->isotropy_order, mrt, ks);
+}
+}  // namespace tx
 
 extern "C" {
 
@@ -281,16 +309,7 @@ int tx_create(const tx_params* p, tx_handle** out) {
   for (int a = 0; a < 3; ++a) h->g.per[a] = a < h->D ? p->bc_flags[2 * a] == TX_BC_PERIODIC : 1;
   h->g.n = (long long)h->g.nx * h->g.ny * h->g.nz;
   fill_phys(h);
-  const bool mrt = p->relaxation_mode == TX_RELAX_MRT;
-  using Fn = bool (*)(int, int, bool, KernelSet*);
-  // [form][dimension 3/2][components 1/2]; form 0 exact FP64, 1 FP64, 2 FP32, 3 FP32/FP16
-  static const Fn table[4][2][2] = {
-      {{kernels_d3_exact_s1, kernels_d3_exact_s2}, {kernels_d2_exact_s1, kernels_d2_exact_s2}},
-      {{kernels_d3_f64_s1, kernels_d3_f64_s2}, {kernels_d2_f64_s1, kernels_d2_f64_s2}},
-      {{kernels_d3_f32_s1, kernels_d3_f32_s2}, {kernels_d2_f32_s1, kernels_d2_f32_s2}},
-      {{kernels_d3_f16_s1, kernels_d3_f16_s2}, {kernels_d2_f16_s1, kernels_d2_f16_s2}}};
-  const int form = p->precision == TX_PREC_F64 ? (p->exact ? 0 : 1) : (p->precision == TX_PREC_F32 ? 2 : 3);
-  const bool ok = table[form][h->D == 3 ? 0 : 1][h->S - 1](h->S, p->isotropy_order, mrt, &h->ks);
+  const bool ok = select_kernels(p, &h->ks);
   if (!ok) {
     delete h;
     return fail(nullptr, TX_ERR_ARG, "no kernel built for this parameter combination");

@@ -51,6 +51,7 @@ def load():
         "tx_get_timing": ([vp, dp, dp, C.POINTER(i64)], C.c_int),
         "tx_get_stream": ([vp], vp),
         "tx_kernel_name": ([vp], C.c_char_p),
+        "tx_step_static": ([C.POINTER(P.TxParams), vp, vp, vp, i32, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -66,6 +67,16 @@ def dptr(a):
 
 def f64(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
+
+
+def step_static(params, walls_dev, fi_in_dev, fi_out_dev, nsteps, stream=None):
+    """tx_step_static on caller-owned device arrays (addresses as ints)."""
+    L = load()
+    p = P.copy_params(params)
+    rc = L.tx_step_static(C.byref(p), C.c_void_p(walls_dev), C.c_void_p(fi_in_dev), C.c_void_p(fi_out_dev),
+                          int(nsteps), C.c_void_p(stream) if stream else None)
+    if rc:
+        raise TxError(rc, L.tx_last_error(None).decode())
 
 
 class Handle:
