@@ -18,6 +18,9 @@ LIB = os.path.join(HERE, "libtaxila_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-I" + INCLUDE]
+# extra nvcc options (e.g. -DTX_FLOAT_MIN_BLOCKS=2 to retune the float kernels'
+# occupancy); a change of this value rebuilds every object
+EXTRA = os.environ.get("TX_NVCC_EXTRA", "").split()
 
 
 def _nvcc():
@@ -32,12 +35,12 @@ def _deps():
         [os.path.join(INCLUDE, "taxila_gb300.h")]
 
 
-def _compile(src, extra):
+def _compile(src, extra, stamp):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-    newest_dep = max(os.path.getmtime(p) for p in _deps() + [src])
+    newest_dep = max(os.path.getmtime(p) for p in _deps() + [src, stamp])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, None
-    cmd = [_nvcc()] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
+    cmd = [_nvcc()] + ARCH + FLAGS + EXTRA + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return obj, "%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr)
@@ -46,11 +49,16 @@ def _compile(src, extra):
 
 def build(verbose=True, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "extra_flags.txt")
+    want = " ".join(EXTRA)
+    if not os.path.exists(stamp) or open(stamp).read() != want:
+        with open(stamp, "w") as fh:
+            fh.write(want)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     objs, errors = [], []
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        futs = {ex.submit(_compile, s, ["--fmad=false"] if "_exact_" in os.path.basename(s) else []): s for s in srcs}
+        futs = {ex.submit(_compile, s, ["--fmad=false"] if "_exact_" in os.path.basename(s) else [], stamp): s for s in srcs}
         for fut in cf.as_completed(futs):
             obj, err = fut.result()
             objs.append(obj)

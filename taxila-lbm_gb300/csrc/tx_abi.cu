@@ -21,6 +21,7 @@ struct tx_handle {
   Geo g{};
   Phys ph{};
   Phys* d_phys = nullptr;     // device copy of ph
+  PhysT<float>* d_phys32 = nullptr;  // FP32 copy for the reduced-precision forms
   Faces faces{};
   KernelSet ks{};
   cudaStream_t stream = nullptr;
@@ -74,7 +75,7 @@ StepArgs args(tx_handle* h, int in, int out) {
   a.fout = h->f[out];
   a.rho = h->rho;
   a.mask = h->mask;
-  a.phys = h->d_phys;
+  a.phys = h->p.precision == TX_PREC_F64 ? (const void*)h->d_phys : (const void*)h->d_phys32;
   a.g = h->g;
   a.faces = h->faces;
   return a;
@@ -162,6 +163,26 @@ void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
       const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
       P.srate[m][k] = rates[r];
       P.srate_mmt[m][k] = rates[r] / mmt;
+    }
+    // fast form: base rate = the rate most moments share (1/tau for BGK)
+    if (p.relaxation_mode == TX_RELAX_SRT) {
+      P.s0[m] = 1.0 / p.tau[m];
+      P.spec_mask[m] = 0u;
+    } else {
+      int best = 0, best_count = -1;
+      for (int k = 0; k < Q; ++k) {
+        int c = 0;
+        for (int j = 0; j < Q; ++j) c += P.srate[m][j] == P.srate[m][k];
+        if (c > best_count) { best_count = c; best = k; }
+      }
+      P.s0[m] = P.srate[m][best];
+      P.spec_mask[m] = 0u;
+      for (int k = 0; k < Q; ++k) {
+        if (P.srate[m][k] == P.s0[m]) continue;
+        const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
+        P.spec_mask[m] |= 1u << k;
+        P.dspec[m][k] = (P.srate[m][k] - P.s0[m]) / mmt;
+      }
     }
   }
   for (int q = 0; q < p.nminerals; ++q)
@@ -329,9 +350,13 @@ int tx_create(const tx_params* p, tx_handle** out) {
       cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
       cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->stage, stageb) != cudaSuccess ||
       cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMalloc(&h->d_phys, sizeof(Phys)) != cudaSuccess)
+      cudaMalloc(&h->d_phys, sizeof(Phys)) != cudaSuccess ||
+      cudaMalloc(&h->d_phys32, sizeof(PhysT<float>)) != cudaSuccess)
     return cleanup("device allocation failed", TX_ERR_NOMEM);
-  if (cudaMemcpy(h->d_phys, &h->ph, sizeof(Phys), cudaMemcpyHostToDevice) != cudaSuccess)
+  PhysT<float> ph32{};
+  convert_phys(h->ph, &ph32);
+  if (cudaMemcpy(h->d_phys, &h->ph, sizeof(Phys), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->d_phys32, &ph32, sizeof(ph32), cudaMemcpyHostToDevice) != cudaSuccess)
     return cleanup("parameter upload failed", TX_ERR_CUDA);
   cudaMemsetAsync(h->f[0], 0, popb, h->stream);
   cudaMemsetAsync(h->f[1], 0, popb, h->stream);
@@ -373,6 +398,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->uic);
   cudaFree(h->red);
   cudaFree(h->d_phys);
+  cudaFree(h->d_phys32);
   for (int f = 0; f < 6; ++f) cudaFree(h->faceval[f]);
   for (int i = 0; i < 4; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);

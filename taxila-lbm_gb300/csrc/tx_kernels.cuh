@@ -28,6 +28,13 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+// Resident 128-thread blocks per SM that ptxas must make room for in the
+// float-arithmetic k_step (4 caps it at 128 registers a thread; the FP64 form
+// is bound by the FP64 pipe and keeps its full register budget).
+#ifndef TX_FLOAT_MIN_BLOCKS
+#define TX_FLOAT_MIN_BLOCKS 4
+#endif
+
 #include "tx_ff_stencil.cuh"
 #include "tx_lattice.cuh"
 
@@ -42,19 +49,42 @@ struct Geo {
   long long n;
 };
 
-// Parameters in FP64; kernels convert to R.
-struct Phys {
-  double tau[MAXC], inv_tau[MAXC], cs2[MAXC], inv_cs2[MAXC], dk[MAXC], mm[MAXC], mmot[MAXC];
-  double g[MAXC][MAXC];
-  double gw[MAXMIN + 1][MAXC];  // row = mineral id (row 0 unused)
-  double gvt[3];
-  double ffw[12];
-  double c0, fs_w_axis, fs_w_diag;
-  double srate[MAXC][19];   // MRT rate of moment k
-  double srate_mmt[MAXC][19];  // rate / diag(M M^T)
-  double rho0;              // shift of the reduced-precision storage
+// Parameters in the arithmetic type R of the kernels that read them (the
+// handle keeps an FP64 and an FP32 copy on the device).
+template <class R>
+struct PhysT {
+  R tau[MAXC], inv_tau[MAXC], cs2[MAXC], inv_cs2[MAXC], dk[MAXC], mm[MAXC], mmot[MAXC];
+  R g[MAXC][MAXC];
+  R gw[MAXMIN + 1][MAXC];  // row = mineral id (row 0 unused)
+  R gvt[3];
+  R ffw[12];
+  R c0, fs_w_axis, fs_w_diag;
+  R srate[MAXC][19];       // MRT rate of moment k
+  R srate_mmt[MAXC][19];   // rate / diag(M M^T)
+  R rho0;                  // shift of the reduced-precision storage
+  // fast form: relax every moment at s0, then correct the moments whose rate
+  // differs (bit k of spec_mask) by dspec = (rate_k - s0) / diag(M M^T)_k
+  R s0[MAXC];
+  R dspec[MAXC][19];
+  unsigned spec_mask[MAXC];
   int ff_on, fs_on, body_on;
 };
+using Phys = PhysT<double>;
+
+template <class R, class Src>
+inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
+  auto cp = [](const Src* x, R* y, int n) { for (int i = 0; i < n; ++i) y[i] = R(x[i]); };
+  cp(a.tau, b->tau, MAXC); cp(a.inv_tau, b->inv_tau, MAXC); cp(a.cs2, b->cs2, MAXC); cp(a.inv_cs2, b->inv_cs2, MAXC);
+  cp(a.dk, b->dk, MAXC); cp(a.mm, b->mm, MAXC); cp(a.mmot, b->mmot, MAXC);
+  cp(&a.g[0][0], &b->g[0][0], MAXC * MAXC); cp(&a.gw[0][0], &b->gw[0][0], (MAXMIN + 1) * MAXC);
+  cp(a.gvt, b->gvt, 3); cp(a.ffw, b->ffw, 12);
+  b->c0 = R(a.c0); b->fs_w_axis = R(a.fs_w_axis); b->fs_w_diag = R(a.fs_w_diag);
+  cp(&a.srate[0][0], &b->srate[0][0], MAXC * 19); cp(&a.srate_mmt[0][0], &b->srate_mmt[0][0], MAXC * 19);
+  b->rho0 = R(a.rho0);
+  cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19);
+  for (int m = 0; m < MAXC; ++m) b->spec_mask[m] = a.spec_mask[m];
+  b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
+}
 
 struct Faces {
   int on[6];                // Dirichlet density face flags, XM..ZP
@@ -66,7 +96,7 @@ struct StepArgs {
   void* fout;
   void* rho;                // RT [m * N + cell]
   const uint8_t* mask;      // 0 pore, 1..16 mineral, 255 other wall
-  const Phys* phys;         // device copy of the handle's parameters
+  const void* phys;         // device PhysT<R> of the kernels' arithmetic type
   Geo g;
   Faces faces;
 };
@@ -171,7 +201,7 @@ __host__ __device__ constexpr FFTerm ffterm(int t) {
 // One term of the wall-aware psi gradient: the neighbour x + e must be pore
 // space and, for long links, the path cells must satisfy the term's truth table.
 template <int D, int S, int ISO, int TI, class R, class RT>
-__device__ __forceinline__ void ff_term(const Geo& g, const Phys& P, const uint8_t* mask, const RT* rho, int x, int y,
+__device__ __forceinline__ void ff_term(const Geo& g, const PhysT<R>& P, const uint8_t* mask, const RT* rho, int x, int y,
                                         int z, const R rf[S], R gr[S][D], R ws[D]) {
   constexpr FFTerm T = ffterm<D>(TI);
   if constexpr (T.level <= ISO) {
@@ -190,22 +220,22 @@ __device__ __forceinline__ void ff_term(const Geo& g, const Phys& P, const uint8
 #pragma unroll
       for (int m = 0; m < S; ++m) dif[m] = R(rho[(long long)m * g.n + pi]) - rf[m];
       if constexpr (T.e[0] != 0) {
-        const R coef = R(double(T.e[0]) * P.ffw[T.w]);
+        const R coef = R(T.e[0]) * P.ffw[T.w];
 #pragma unroll
         for (int m = 0; m < S; ++m) gr[m][0] = gr[m][0] + coef * dif[m];
-        ws[0] = ws[0] + R(P.ffw[T.w] * double(T.e[0] * T.e[0]));
+        ws[0] = ws[0] + P.ffw[T.w] * R(T.e[0] * T.e[0]);
       }
       if constexpr (D > 1 && T.e[1] != 0) {
-        const R coef = R(double(T.e[1]) * P.ffw[T.w]);
+        const R coef = R(T.e[1]) * P.ffw[T.w];
 #pragma unroll
         for (int m = 0; m < S; ++m) gr[m][1] = gr[m][1] + coef * dif[m];
-        ws[1] = ws[1] + R(P.ffw[T.w] * double(T.e[1] * T.e[1]));
+        ws[1] = ws[1] + P.ffw[T.w] * R(T.e[1] * T.e[1]);
       }
       if constexpr (D > 2 && T.e[2] != 0) {
-        const R coef = R(double(T.e[2]) * P.ffw[T.w]);
+        const R coef = R(T.e[2]) * P.ffw[T.w];
 #pragma unroll
         for (int m = 0; m < S; ++m) gr[m][D > 2 ? 2 : 0] = gr[m][D > 2 ? 2 : 0] + coef * dif[m];
-        ws[D > 2 ? 2 : 0] = ws[D > 2 ? 2 : 0] + R(P.ffw[T.w] * double(T.e[2] * T.e[2]));
+        ws[D > 2 ? 2 : 0] = ws[D > 2 ? 2 : 0] + P.ffw[T.w] * R(T.e[2] * T.e[2]);
       }
     }
   }
@@ -216,7 +246,7 @@ __device__ __forceinline__ void ff_term(const Geo& g, const Phys& P, const uint8
 // fluid-solid (lbm_forcing.F90:1326-1421), body (:1440-1496) and the
 // wall-aware Shan-Chen term (:51-958 / :960-1299), in that order.
 template <int D, int S, int ISO, bool EXACT, class R, class RT>
-__device__ __forceinline__ void cell_forces(const Geo& g, const Phys& P, const uint8_t* mask, const RT* rho,
+__device__ __forceinline__ void cell_forces(const Geo& g, const PhysT<R>& P, const uint8_t* mask, const RT* rho,
                                             int x, int y, int z, const R rf[S], R F[S][D]) {
   using L = Lat<D>;
 #pragma unroll
@@ -334,7 +364,7 @@ __device__ __forceinline__ R pop_flux(const R fv[S][Lat<D>::Q], int m, int d0) {
 // lbm_bc.F90:436-611) and the common velocity of FlowUpdateUED3/D2
 // (lbm_flow.F90:494-574) from the post-stream populations and the forces.
 template <int D, int S, bool EXACT, class R>
-__device__ __forceinline__ void cell_velocity(const StepArgs& a, const Phys& P, int x, int y, int z,
+__device__ __forceinline__ void cell_velocity(const StepArgs& a, const PhysT<R>& P, int x, int y, int z,
                                               const R fv[S][Lat<D>::Q], const R rf[S], const R F[S][D], R rc[S],
                                               R up[D]) {
   const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
@@ -360,7 +390,7 @@ __device__ __forceinline__ void cell_velocity(const StepArgs& a, const Phys& P, 
 // Moments of a pore site from its post-stream populations: forces from the
 // forcing density, then cell_velocity.
 template <int D, int S, int ISO, bool EXACT, class R, class RT>
-__device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, int x, int y, int z, long long idx,
+__device__ __forceinline__ void cell_moments(const StepArgs& a, const PhysT<R>& P, int x, int y, int z, long long idx,
                                              const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
 #pragma unroll
@@ -373,7 +403,7 @@ __device__ __forceinline__ void cell_moments(const StepArgs& a, const Phys& P, i
 // _D2Q9, lbm_discretization_d2q9.F90:168-205) and forcing prefactor
 // (FlowFiBarEqPrefactor, lbm_flow.F90:836-851) of component m, direction n.
 template <int D, int n, bool EXACT, class R>
-__device__ __forceinline__ void feq_pf(const Phys& P, int m, R r, const R u[D], R usqr, const R Fm[D], R& feq, R& pf) {
+__device__ __forceinline__ void feq_pf(const PhysT<R>& P, int m, R r, const R u[D], R usqr, const R Fm[D], R& feq, R& pf) {
   using L = Lat<D>;
   const R cs2 = R(P.cs2[m]), dk = R(P.dk[m]);
   R udote = R(0);
@@ -410,11 +440,11 @@ __device__ __forceinline__ void feq_pf(const Phys& P, int m, R r, const R u[D], 
 // Each kernel copies its StepArgs parameter into a local before use; the
 // helpers take references to that copy, never to the parameter itself.
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_step(StepArgs a_in) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1) k_step(StepArgs a_in) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
-  const Phys& P = *a.phys;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
@@ -479,68 +509,154 @@ __global__ void __launch_bounds__(128) k_step(StepArgs a_in) {
       St<T>::st(fout + (long long)(m * Q + o) * N + idx, v);
   };
 
-#pragma unroll
-  for (int m = 0; m < S; ++m) {
-    R f[Q];
-    {
-      R fv1[1][Q];
-      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, fv1);
-#pragma unroll
-      for (int n = 0; n < Q; ++n) f[n] = fv1[0][n];
-    }
-    if constexpr (!MRT) {
-      // RelaxationCollideSRT (lbm_relaxation.F90:171-180) then f += P feq, one direction at a time
-      sfor<0, Q>([&](auto nn) {
-        constexpr int n = decltype(nn)::value;
-        R feq, pf;
-        feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
-        const R fb = (R(1.) - R(.5) * pf) * feq;
-        R v;
-        if constexpr (EXACT)
-          v = f[n] - (f[n] - fb) / R(P.tau[m]);
-        else
-          v = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
-        push(nn, m, v + pf * feq);
-      });
-    } else {
-      // RelaxationCollideMRT (lbm_relaxation.F90:182-200): coef_k from the
-      // pre-collision differences, then each f_i subtracts coef_k mt(i,k) in k order
-      R dfi[Q], pfeq[Q];
-      sfor<0, Q>([&](auto nn) {
-        constexpr int n = decltype(nn)::value;
-        R feq, pf;
-        feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
-        dfi[n] = f[n] - (R(1.) - R(.5) * pf) * feq;
-        pfeq[n] = pf * feq;
-      });
-      R coef[Q];
-      sfor<0, Q>([&](auto kk) {
-        constexpr int k = decltype(kk)::value;
-        R md = R(0);
-        sfor<0, Q>([&](auto ii) {
-          constexpr int i = decltype(ii)::value;
-          constexpr int v = L::mt(i, k);
-          if constexpr (v == 1) md = md + dfi[i];
-          else if constexpr (v == -1) md = md - dfi[i];
-          else if constexpr (v != 0) md = md + R(v) * dfi[i];
+  if constexpr (EXACT) {
+  #pragma unroll
+    for (int m = 0; m < S; ++m) {
+      R f[Q];
+      {
+        R fv1[1][Q];
+        load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, fv1);
+  #pragma unroll
+        for (int n = 0; n < Q; ++n) f[n] = fv1[0][n];
+      }
+      if constexpr (!MRT) {
+        // RelaxationCollideSRT (lbm_relaxation.F90:171-180) then f += P feq, one direction at a time
+        sfor<0, Q>([&](auto nn) {
+          constexpr int n = decltype(nn)::value;
+          R feq, pf;
+          feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
+          const R fb = (R(1.) - R(.5) * pf) * feq;
+          R v;
+          if constexpr (EXACT)
+            v = f[n] - (f[n] - fb) / R(P.tau[m]);
+          else
+            v = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
+          push(nn, m, v + pf * feq);
         });
-        if constexpr (EXACT)
-          coef[k] = R(P.srate[m][k]) * md / R(L::mmt(k));
-        else
-          coef[k] = R(P.srate_mmt[m][k]) * md;
-      });
-      sfor<0, Q>([&](auto ii) {
-        constexpr int i = decltype(ii)::value;
-        R v = f[i];
+      } else {
+        // RelaxationCollideMRT (lbm_relaxation.F90:182-200): coef_k from the
+        // pre-collision differences, then each f_i subtracts coef_k mt(i,k) in k order
+        R dfi[Q], pfeq[Q];
+        sfor<0, Q>([&](auto nn) {
+          constexpr int n = decltype(nn)::value;
+          R feq, pf;
+          feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
+          dfi[n] = f[n] - (R(1.) - R(.5) * pf) * feq;
+          pfeq[n] = pf * feq;
+        });
+        R coef[Q];
         sfor<0, Q>([&](auto kk) {
           constexpr int k = decltype(kk)::value;
-          constexpr int c = L::mt(i, k);
-          if constexpr (c == 1) v = v - coef[k];
-          else if constexpr (c == -1) v = v + coef[k];
-          else if constexpr (c != 0) v = v - coef[k] * R(c);
+          R md = R(0);
+          sfor<0, Q>([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            constexpr int v = L::mt(i, k);
+            if constexpr (v == 1) md = md + dfi[i];
+            else if constexpr (v == -1) md = md - dfi[i];
+            else if constexpr (v != 0) md = md + R(v) * dfi[i];
+          });
+          if constexpr (EXACT)
+            coef[k] = R(P.srate[m][k]) * md / R(L::mmt(k));
+          else
+            coef[k] = R(P.srate_mmt[m][k]) * md;
         });
-        push(ii, m, v + pfeq[i]);
-      });
+        sfor<0, Q>([&](auto ii) {
+          constexpr int i = decltype(ii)::value;
+          R v = f[i];
+          sfor<0, Q>([&](auto kk) {
+            constexpr int k = decltype(kk)::value;
+            constexpr int c = L::mt(i, k);
+            if constexpr (c == 1) v = v - coef[k];
+            else if constexpr (c == -1) v = v + coef[k];
+            else if constexpr (c != 0) v = v - coef[k] * R(c);
+          });
+          push(ii, m, v + pfeq[i]);
+        });
+      }
+    }
+  } else {
+    // Fast form.  The equilibrium of every component shares the common
+    // velocity part B_n: feq_n(m) = rho_m * W_n * (A_m,n + B_n) with c_s^2 = 1/3.
+    R B[Q];
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      if constexpr (n == 0) {
+        B[0] = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
+      } else {
+        R ud = R(0);
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          constexpr int c = L::c(n, d);
+          if constexpr (c > 0) ud = ud + up[d];
+          if constexpr (c < 0) ud = ud - up[d];
+        });
+        B[n] = R(3) * ud + R(4.5) * ud * ud - R(1.5) * usqr;
+      }
+    });
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      const R r = rc[m];
+      const R dk = P.dk[m];
+      const R A0 = D == 3 ? dk : (R(1) + R(5) * dk) * R(1.0 / 6.0);
+      const R An = R(1.5) * (R(1) - dk);
+      const R inv = R(3) / r;  // 1 / (rho c_s^2)
+      R Fu = R(0);
+#pragma unroll
+      for (int d = 0; d < D; ++d) Fu = Fu + F[m][d] * up[d];
+      const R s0 = P.s0[m];
+      const unsigned spec = P.spec_mask[m];
+      const T* fm = fin + (long long)m * Q * N + idx;
+      // deviation from the forced equilibrium and the relaxed population of direction n
+      auto relax = [&](auto nn, R& dfi) -> R {
+        constexpr int n = decltype(nn)::value;
+        R f = R(St<T>::ld(fm + (long long)n * N));
+        if constexpr (kShifted<T>) f = f + R(L::w(n)) * rho0;
+        const R feq = r * R(n == 0 ? 1.0 : L::w(n)) * ((n == 0 ? A0 : An) + B[n]);
+        R Fc = R(0);
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          constexpr int c = L::c(n, d);
+          if constexpr (c > 0) Fc = Fc + F[m][d];
+          if constexpr (c < 0) Fc = Fc - F[m][d];
+        });
+        const R pfeq = (Fc - Fu) * inv * feq;
+        dfi = f - (feq - R(0.5) * pfeq);
+        return f - s0 * dfi + pfeq;
+      };
+      if (spec == 0u) {
+        // every moment relaxes at s0 (BGK): one direction at a time
+        sfor<0, Q>([&](auto nn) {
+          R dfi;
+          const R v = relax(nn, dfi);
+          push(nn, m, v);
+        });
+      } else {
+        // moments whose MRT rate differs from s0 get (rate - s0) on top
+        R fo[Q], dfi[Q];
+        sfor<0, Q>([&](auto nn) { fo[decltype(nn)::value] = relax(nn, dfi[decltype(nn)::value]); });
+        sfor<0, Q>([&](auto kk) {
+          constexpr int k = decltype(kk)::value;
+          if (spec & (1u << k)) {
+            R md = R(0);
+            sfor<0, Q>([&](auto ii) {
+              constexpr int i = decltype(ii)::value;
+              constexpr int v = L::mt(i, k);
+              if constexpr (v == 1) md = md + dfi[i];
+              else if constexpr (v == -1) md = md - dfi[i];
+              else if constexpr (v != 0) md = md + R(v) * dfi[i];
+            });
+            const R ck = P.dspec[m][k] * md;
+            sfor<0, Q>([&](auto ii) {
+              constexpr int i = decltype(ii)::value;
+              constexpr int v = L::mt(i, k);
+              if constexpr (v == 1) fo[i] = fo[i] - ck;
+              else if constexpr (v == -1) fo[i] = fo[i] + ck;
+              else if constexpr (v != 0) fo[i] = fo[i] - ck * R(v);
+            });
+          }
+        });
+        sfor<0, Q>([&](auto nn) { push(nn, m, fo[decltype(nn)::value]); });
+      }
     }
   }
 }
@@ -603,7 +719,7 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
-  const Phys& P = *a.phys;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
@@ -665,7 +781,7 @@ __global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) 
   using L = Lat<D>;
   constexpr int Q = L::Q;
   const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
-  const Phys& P = *a.phys;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
@@ -707,7 +823,7 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
   using L = Lat<D>;
   constexpr int Q = L::Q;
   const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
-  const Phys& P = *a.phys;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
