@@ -31,6 +31,7 @@ struct tx_handle {
   void* rho = nullptr;        // forcing density
   size_t rho_bytes = 0;
   uint8_t* mask = nullptr;
+  uint32_t* links = nullptr;  // link masks (k_links), rebuilt with every wall upload
   double* faceval[6] = {nullptr};
   long long face_n[6] = {0};
   double* stage = nullptr;    // natural-order staging buffer (largest field)
@@ -69,12 +70,23 @@ int check_launch(tx_handle* h, const char* what) {
   return TX_OK;
 }
 
+// link masks from the device wall mask (after every change of the mask)
+int update_links(tx_handle* h) {
+  const Launch3 l = launch3(h->g, 256);
+  if (h->D == 3)
+    k_links<3><<<l.grid, l.block, 0, h->stream>>>(h->mask, h->g, h->links);
+  else
+    k_links<2><<<l.grid, l.block, 0, h->stream>>>(h->mask, h->g, h->links);
+  return check_launch(h, "k_links");
+}
+
 StepArgs args(tx_handle* h, int in, int out) {
   StepArgs a{};
   a.fin = h->f[in];
   a.fout = h->f[out];
   a.rho = h->rho;
   a.mask = h->mask;
+  a.links = h->links;
   a.phys = h->p.precision == TX_PREC_F64 ? (const void*)h->d_phys : (const void*)h->d_phys32;
   a.g = h->g;
   a.faces = h->faces;
@@ -105,125 +117,6 @@ void set_global_error(const std::string& msg) { g_create_error = msg; }
 }  // namespace tx
 
 namespace {
-
-int validate(const tx_params* p, std::string* why) {
-  auto bad = [&](const std::string& s) {
-    *why = s;
-    return TX_ERR_ARG;
-  };
-  if (p->discretization != TX_D3Q19 && p->discretization != TX_D2Q9) return bad("discretization must be TX_D3Q19 or TX_D2Q9");
-  const int D = p->discretization == TX_D3Q19 ? 3 : 2;
-  if (p->nx < 1 || p->ny < 1 || p->nz < 1) return bad("lattice sizes must be >= 1");
-  if (D == 2 && p->nz != 1) return bad("D2Q9 needs nz = 1");
-  if ((long long)p->nx * p->ny * p->nz >= (1ll << 31)) return bad("lattices of 2^31 sites or more are not supported");
-  if (p->nz > 65535) return bad("nz must be <= 65535");
-  if (p->ncomponents < 1 || p->ncomponents > TX_MAX_COMPONENTS) return bad("ncomponents out of range");
-  if (p->ncomponents > kMaxBuiltComponents)
-    return bad("ncomponents > " + std::to_string(kMaxBuiltComponents) + " is not built into this library");
-  if (p->nminerals < 0 || p->nminerals > TX_MAX_MINERALS) return bad("nminerals out of range");
-  if (p->relaxation_mode != TX_RELAX_SRT && p->relaxation_mode != TX_RELAX_MRT) return bad("relaxation_mode must be 0 or 1");
-  if (!(p->isotropy_order == 4 || p->isotropy_order == 8 || (D == 2 && p->isotropy_order == 10)))
-    return bad(D == 3 ? "isotropy_order must be 4 or 8 for D3Q19 (the reference errors on 10)"
-                      : "isotropy_order must be 4, 8 or 10");
-  if (p->precision < TX_PREC_F64 || p->precision > TX_PREC_F32_F16) return bad("unknown precision form");
-  if (p->exact && p->precision != TX_PREC_F64) return bad("exact operation order exists for the FP64 form only");
-  for (int a = 0; a < D; ++a) {
-    const int lo = p->bc_flags[2 * a], hi = p->bc_flags[2 * a + 1];
-    if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
-    const int ext = a == 0 ? p->nx : (a == 1 ? p->ny : p->nz);
-    if (lo == TX_BC_PERIODIC && ext < 3) return bad("periodic axes need at least 3 sites");
-    for (int f : {2 * a, 2 * a + 1}) {
-      const int v = p->bc_flags[f];
-      if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
-        return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
-    }
-  }
-  for (int m = 0; m < p->ncomponents; ++m) {
-    if (p->relaxation_mode == TX_RELAX_SRT && !(p->tau[m] > 0.0)) return bad("tau must be > 0");
-    if (!(p->mm[m] > 0.0)) return bad("molecular masses must be > 0");
-  }
-  return TX_OK;
-}
-
-void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
-  std::memset(&P, 0, sizeof(P));
-  for (int m = 0; m < S; ++m) {
-    P.tau[m] = p.tau[m];
-    P.inv_tau[m] = 1.0 / p.tau[m];
-    P.cs2[m] = 1.0 / 3.0;                     // lbm_relaxation.F90:82
-    P.inv_cs2[m] = 3.0;
-    P.dk[m] = 1. - 2. / (3. * p.mm[m]);        // lbm_component.F90:158
-    P.mm[m] = p.mm[m];
-    const double s_c = p.relaxation_mode == TX_RELAX_SRT ? 1.0 / p.tau[m] : p.s_c[m];  // lbm_relaxation.F90:133
-    P.mmot[m] = p.mm[m] * s_c;
-    for (int k = 0; k < S; ++k) P.g[m][k] = p.g[m][k];
-    const double rates[7] = {p.s_c[m], p.s_e[m], p.s_e2[m], p.s_q[m], p.s_nu[m], p.s_pi[m], p.s_m[m]};
-    for (int k = 0; k < Q; ++k) {
-      const int r = D == 3 ? rate_of<3>(k) : rate_of<2>(k);
-      const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
-      P.srate[m][k] = rates[r];
-      P.srate_mmt[m][k] = rates[r] / mmt;
-    }
-    // fast form: base rate = the rate most moments share (1/tau for BGK)
-    if (p.relaxation_mode == TX_RELAX_SRT) {
-      P.s0[m] = 1.0 / p.tau[m];
-      P.spec_mask[m] = 0u;
-    } else {
-      int best = 0, best_count = -1;
-      for (int k = 0; k < Q; ++k) {
-        int c = 0;
-        for (int j = 0; j < Q; ++j) c += P.srate[m][j] == P.srate[m][k];
-        if (c > best_count) { best_count = c; best = k; }
-      }
-      P.s0[m] = P.srate[m][best];
-      P.spec_mask[m] = 0u;
-      for (int k = 0; k < Q; ++k) {
-        if (P.srate[m][k] == P.s0[m]) continue;
-        const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
-        P.spec_mask[m] |= 1u << k;
-        P.dspec[m][k] = (P.srate[m][k] - P.s0[m]) / mmt;
-      }
-    }
-  }
-  for (int q = 0; q < p.nminerals; ++q)
-    for (int m = 0; m < S; ++m) P.gw[q + 1][m] = p.gw[q][m];
-  for (int d = 0; d < 3; ++d) P.gvt[d] = p.gvt[d];
-  // isotropy weights (lbm_discretization_d3q19.F90:199-230, d2q9:119-142)
-  const int iso = p.isotropy_order;
-  double* w = P.ffw;
-  if (D == 3) {
-    if (iso == 4) { w[1] = 1.0 / 6.0; w[2] = 1.0 / 12.0; }
-    if (iso == 8) {
-      w[1] = 4.0 / 45.0; w[2] = 1.0 / 21.0; w[3] = 2.0 / 105.0; w[4] = 5.0 / 504.0;
-      w[5] = 1.0 / 315.0; w[6] = 1.0 / 630.0; w[8] = 1.0 / 5040.0;
-    }
-  } else {
-    if (iso == 4) { w[1] = 1.0 / 3.0; w[2] = 1.0 / 12.0; }
-    if (iso == 8) { w[1] = 4.0 / 21.0; w[2] = 4.0 / 45.0; w[4] = 1.0 / 60.0; w[5] = 2.0 / 315.0; w[8] = 1.0 / 5040.0; }
-    if (iso == 10) {
-      w[1] = 262.0 / 1785.0; w[2] = 93.0 / 1190.0; w[4] = 7.0 / 340.0; w[5] = 6.0 / 595.0;
-      w[8] = 9.0 / 9520.0; w[9] = 2.0 / 5355.0; w[10] = 1.0 / 7140.0;
-    }
-  }
-  P.c0 = 6.0;  // disc%c_0
-  // fluid-solid weights 1./6., 1./12. (D3) and 1./3., 1./12. (D2): default-REAL literals
-  if (p.literal_kind == 8) {
-    P.fs_w_axis = D == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
-    P.fs_w_diag = 1.0 / 12.0;
-  } else {
-    P.fs_w_axis = D == 3 ? (double)(1.0f / 6.0f) : (double)(1.0f / 3.0f);
-    P.fs_w_diag = (double)(1.0f / 12.0f);
-  }
-  const double eps15 = (double)1.e-15f;
-  for (int m = 0; m < S; ++m)
-    for (int k = 0; k < S; ++k)
-      if (std::fabs(p.g[m][k]) > eps15) P.ff_on = 1;
-  for (int q = 0; q < p.nminerals; ++q)
-    for (int m = 0; m < S; ++m)
-      if (std::fabs(p.gw[q][m]) > eps15) P.fs_on = 1;
-  P.body_on = p.body_forces != 0;
-  P.rho0 = p.precision == TX_PREC_F64 ? 0.0 : p.rho0;
-}
 
 void fill_phys(tx_handle* h) { fill_phys_impl(h->p, h->D, h->S, h->Q, h->ph); }
 
@@ -348,7 +241,8 @@ int tx_create(const tx_params* p, tx_handle** out) {
   const size_t stageb = (size_t)N * h->S * h->Q * sizeof(double);
   if (cudaMalloc(&h->f[0], popb) != cudaSuccess || cudaMalloc(&h->f[1], popb) != cudaSuccess ||
       cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
-      cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->stage, stageb) != cudaSuccess ||
+      cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->links, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&h->stage, stageb) != cudaSuccess ||
       cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&h->d_phys, sizeof(Phys)) != cudaSuccess ||
       cudaMalloc(&h->d_phys32, sizeof(PhysT<float>)) != cudaSuccess)
@@ -363,6 +257,10 @@ int tx_create(const tx_params* p, tx_handle** out) {
   cudaMemsetAsync(h->rho, 0, (size_t)N * h->S * h->rho_bytes, h->stream);
   cudaMemsetAsync(h->mask, 0, (size_t)N, h->stream);
   h->host_mask.assign((size_t)N, 0);
+  if (update_links(h) != TX_OK) {
+    const std::string why = h->err;
+    return cleanup(why, TX_ERR_CUDA);
+  }
   // Dirichlet density faces (FlowSetUpBCsD3/D2, lbm_flow.F90:1311-1956): uniform values
   for (int f = 0; f < 2 * h->D; ++f) {
     if (p->bc_flags[f] != TX_BC_DENSITY) continue;
@@ -392,6 +290,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->f[1]);
   cudaFree(h->rho);
   cudaFree(h->mask);
+  cudaFree(h->links);
   cudaFree(h->stage);
   cudaFree(h->old_rho);
   cudaFree(h->old_fi);
@@ -411,21 +310,12 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
   if (!h || !walls) return TX_ERR_ARG;
   const long long N = h->g.n;
   for (long long i = 0; i < N; ++i) {
-    const double v = walls[i];
-    uint8_t code;
-    if (v == 0.0) {
-      code = 0;
-    } else if (!(v > 0.0) || !std::isfinite(v)) {
-      return fail(h, TX_ERR_ARG, "wall codes must be 0 (pore) or positive");
-    } else if (v == 900.0 || v == 901.0 || v == 902.0) {
-      return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 are not supported by the device path");
-    } else {
-      const int mineral = (int)v;
-      code = (v < 998.0 && mineral >= 1 && mineral <= h->p.nminerals) ? (uint8_t)mineral : (uint8_t)255;
-    }
-    h->host_mask[(size_t)i] = code;
+    const char* why = nullptr;
+    if (!wall_code(walls[i], h->p.nminerals, &h->host_mask[(size_t)i], &why)) return fail(h, TX_ERR_ARG, why);
   }
   TX_CUDA(h, cudaMemcpyAsync(h->mask, h->host_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  const int rc = update_links(h);
+  if (rc != TX_OK) return rc;
   h->have_walls = true;
   return sync_stream(h);
 }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tx_host_params.h"
 #include "tx_kernels.cuh"
 
 namespace tx {
@@ -17,9 +18,6 @@ struct KernelSet {
   void (*from_natural)(const double* in, const uint8_t* mask, long long N, double rho0, void* f, cudaStream_t);
   const char* name;
 };
-
-// Component counts compiled into the library.
-constexpr int kMaxBuiltComponents = 2;
 
 bool kernels_d3_exact_s1(int S, int ISO, bool MRT, KernelSet* ks);
 bool kernels_d3_exact_s2(int S, int ISO, bool MRT, KernelSet* ks);

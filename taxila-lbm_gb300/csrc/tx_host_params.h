@@ -1,0 +1,159 @@
+// Host-side parameter handling of the flow step: validation of tx_params,
+// translation into the kernels' parameter block, and the wall-code mapping.
+// Plain C++ (no CUDA calls), shared by the C ABI and the host emulation of
+// the kernels.
+#pragma once
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "../../include/taxila_gb300.h"
+#include "tx_kernels.cuh"
+
+namespace tx {
+
+// Component counts compiled into the library.
+constexpr int kMaxBuiltComponents = 2;
+
+inline int validate(const tx_params* p, std::string* why) {
+  auto bad = [&](const std::string& s) {
+    *why = s;
+    return TX_ERR_ARG;
+  };
+  if (p->discretization != TX_D3Q19 && p->discretization != TX_D2Q9) return bad("discretization must be TX_D3Q19 or TX_D2Q9");
+  const int D = p->discretization == TX_D3Q19 ? 3 : 2;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1) return bad("lattice sizes must be >= 1");
+  if (D == 2 && p->nz != 1) return bad("D2Q9 needs nz = 1");
+  if ((long long)p->nx * p->ny * p->nz >= (1ll << 31)) return bad("lattices of 2^31 sites or more are not supported");
+  if (p->nz > 65535) return bad("nz must be <= 65535");
+  if (p->ncomponents < 1 || p->ncomponents > TX_MAX_COMPONENTS) return bad("ncomponents out of range");
+  if (p->ncomponents > kMaxBuiltComponents)
+    return bad("ncomponents > " + std::to_string(kMaxBuiltComponents) + " is not built into this library");
+  if (p->nminerals < 0 || p->nminerals > TX_MAX_MINERALS) return bad("nminerals out of range");
+  if (p->relaxation_mode != TX_RELAX_SRT && p->relaxation_mode != TX_RELAX_MRT) return bad("relaxation_mode must be 0 or 1");
+  if (!(p->isotropy_order == 4 || p->isotropy_order == 8 || (D == 2 && p->isotropy_order == 10)))
+    return bad(D == 3 ? "isotropy_order must be 4 or 8 for D3Q19 (the reference errors on 10)"
+                      : "isotropy_order must be 4, 8 or 10");
+  if (p->precision < TX_PREC_F64 || p->precision > TX_PREC_F32_F16) return bad("unknown precision form");
+  if (p->exact && p->precision != TX_PREC_F64) return bad("exact operation order exists for the FP64 form only");
+  for (int a = 0; a < D; ++a) {
+    const int lo = p->bc_flags[2 * a], hi = p->bc_flags[2 * a + 1];
+    if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
+    const int ext = a == 0 ? p->nx : (a == 1 ? p->ny : p->nz);
+    if (lo == TX_BC_PERIODIC && ext < 3) return bad("periodic axes need at least 3 sites");
+    for (int f : {2 * a, 2 * a + 1}) {
+      const int v = p->bc_flags[f];
+      if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
+        return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
+    }
+  }
+  for (int m = 0; m < p->ncomponents; ++m) {
+    if (p->relaxation_mode == TX_RELAX_SRT && !(p->tau[m] > 0.0)) return bad("tau must be > 0");
+    if (!(p->mm[m] > 0.0)) return bad("molecular masses must be > 0");
+  }
+  return TX_OK;
+}
+
+inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
+  std::memset(&P, 0, sizeof(P));
+  for (int m = 0; m < S; ++m) {
+    P.tau[m] = p.tau[m];
+    P.inv_tau[m] = 1.0 / p.tau[m];
+    P.cs2[m] = 1.0 / 3.0;                     // lbm_relaxation.F90:82
+    P.inv_cs2[m] = 3.0;
+    P.dk[m] = 1. - 2. / (3. * p.mm[m]);        // lbm_component.F90:158
+    P.mm[m] = p.mm[m];
+    const double s_c = p.relaxation_mode == TX_RELAX_SRT ? 1.0 / p.tau[m] : p.s_c[m];  // lbm_relaxation.F90:133
+    P.mmot[m] = p.mm[m] * s_c;
+    for (int k = 0; k < S; ++k) P.g[m][k] = p.g[m][k];
+    const double rates[7] = {p.s_c[m], p.s_e[m], p.s_e2[m], p.s_q[m], p.s_nu[m], p.s_pi[m], p.s_m[m]};
+    for (int k = 0; k < Q; ++k) {
+      const int r = D == 3 ? rate_of<3>(k) : rate_of<2>(k);
+      const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
+      P.srate[m][k] = rates[r];
+      P.srate_mmt[m][k] = rates[r] / mmt;
+    }
+    // fast form: base rate = the rate most moments share (1/tau for BGK)
+    if (p.relaxation_mode == TX_RELAX_SRT) {
+      P.s0[m] = 1.0 / p.tau[m];
+      P.spec_mask[m] = 0u;
+    } else {
+      int best = 0, best_count = -1;
+      for (int k = 0; k < Q; ++k) {
+        int c = 0;
+        for (int j = 0; j < Q; ++j) c += P.srate[m][j] == P.srate[m][k];
+        if (c > best_count) { best_count = c; best = k; }
+      }
+      P.s0[m] = P.srate[m][best];
+      P.spec_mask[m] = 0u;
+      for (int k = 0; k < Q; ++k) {
+        if (P.srate[m][k] == P.s0[m]) continue;
+        const int mmt = D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k);
+        P.spec_mask[m] |= 1u << k;
+        P.dspec[m][k] = (P.srate[m][k] - P.s0[m]) / mmt;
+      }
+    }
+  }
+  for (int q = 0; q < p.nminerals; ++q)
+    for (int m = 0; m < S; ++m) P.gw[q + 1][m] = p.gw[q][m];
+  for (int d = 0; d < 3; ++d) P.gvt[d] = p.gvt[d];
+  // isotropy weights (lbm_discretization_d3q19.F90:199-230, d2q9:119-142)
+  const int iso = p.isotropy_order;
+  double* w = P.ffw;
+  if (D == 3) {
+    if (iso == 4) { w[1] = 1.0 / 6.0; w[2] = 1.0 / 12.0; }
+    if (iso == 8) {
+      w[1] = 4.0 / 45.0; w[2] = 1.0 / 21.0; w[3] = 2.0 / 105.0; w[4] = 5.0 / 504.0;
+      w[5] = 1.0 / 315.0; w[6] = 1.0 / 630.0; w[8] = 1.0 / 5040.0;
+    }
+  } else {
+    if (iso == 4) { w[1] = 1.0 / 3.0; w[2] = 1.0 / 12.0; }
+    if (iso == 8) { w[1] = 4.0 / 21.0; w[2] = 4.0 / 45.0; w[4] = 1.0 / 60.0; w[5] = 2.0 / 315.0; w[8] = 1.0 / 5040.0; }
+    if (iso == 10) {
+      w[1] = 262.0 / 1785.0; w[2] = 93.0 / 1190.0; w[4] = 7.0 / 340.0; w[5] = 6.0 / 595.0;
+      w[8] = 9.0 / 9520.0; w[9] = 2.0 / 5355.0; w[10] = 1.0 / 7140.0;
+    }
+  }
+  P.c0 = 6.0;  // disc%c_0
+  // fluid-solid weights 1./6., 1./12. (D3) and 1./3., 1./12. (D2): default-REAL literals
+  if (p.literal_kind == 8) {
+    P.fs_w_axis = D == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
+    P.fs_w_diag = 1.0 / 12.0;
+  } else {
+    P.fs_w_axis = D == 3 ? (double)(1.0f / 6.0f) : (double)(1.0f / 3.0f);
+    P.fs_w_diag = (double)(1.0f / 12.0f);
+  }
+  const double eps15 = (double)1.e-15f;
+  for (int m = 0; m < S; ++m)
+    for (int k = 0; k < S; ++k)
+      if (std::fabs(p.g[m][k]) > eps15) P.ff_on = 1;
+  for (int q = 0; q < p.nminerals; ++q)
+    for (int m = 0; m < S; ++m)
+      if (std::fabs(p.gw[q][m]) > eps15) P.fs_on = 1;
+  P.body_on = p.body_forces != 0;
+  P.rho0 = p.precision == TX_PREC_F64 ? 0.0 : p.rho0;
+}
+
+// Reference wall value (lbm_walls.F90:151-177) -> device mask code:
+// 0 pore, 1..nminerals mineral, 255 any other wall (codes >= 998, unknown
+// minerals).  Returns false, with the reason, for values the device path
+// rejects: negative or non-finite values and the specular codes 900-902.
+inline bool wall_code(double v, int nminerals, uint8_t* code, const char** why) {
+  if (v == 0.0) {
+    *code = 0;
+    return true;
+  }
+  if (!(v > 0.0) || !std::isfinite(v)) {
+    *why = "wall codes must be 0 (pore) or positive";
+    return false;
+  }
+  if (v == 900.0 || v == 901.0 || v == 902.0) {
+    *why = "specular (no-stick) wall codes 900-902 are not supported by the device path";
+    return false;
+  }
+  const int mineral = (int)v;
+  *code = (v < 998.0 && mineral >= 1 && mineral <= nminerals) ? (uint8_t)mineral : (uint8_t)255;
+  return true;
+}
+
+}  // namespace tx

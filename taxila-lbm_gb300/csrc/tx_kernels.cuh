@@ -96,6 +96,7 @@ struct StepArgs {
   void* fout;
   void* rho;                // RT [m * N + cell]
   const uint8_t* mask;      // 0 pore, 1..16 mineral, 255 other wall
+  const uint32_t* links;    // link mask of every site (k_links)
   const void* phys;         // device PhysT<R> of the kernels' arithmetic type
   Geo g;
   Faces faces;
@@ -123,19 +124,76 @@ template <class T>
 constexpr bool kShifted = !std::is_same<T, double>::value;
 
 // --------------------------------------------------------------- geometry
-// Linear index of (x+dx, y+dy, z+dz), or -1 outside a non-periodic axis
-// (the ghost walls of WallsSetGhostNodesD3/D2, lbm_walls.F90:179-231).
-// Branch-free, 32-bit; |d| <= 3 and every periodic extent is >= 3 (checked
-// by tx_create), so one wrap suffices.
-__device__ __forceinline__ long long nbr(const Geo& g, int x, int y, int z, int dx, int dy, int dz) {
-  int xx = x + dx, yy = y + dy, zz = z + dz;
-  const bool ox = xx < 0 || xx >= g.nx, oy = yy < 0 || yy >= g.ny, oz = zz < 0 || zz >= g.nz;
-  const bool outside = (ox && !g.per[0]) || (oy && !g.per[1]) || (oz && !g.per[2]);
-  xx += xx < 0 ? g.nx : (xx >= g.nx ? -g.nx : 0);
-  yy += yy < 0 ? g.ny : (yy >= g.ny ? -g.ny : 0);
-  zz += zz < 0 ? g.nz : (zz >= g.nz ? -g.nz : 0);
-  const long long lin = (long long)xx + (long long)g.nx * ((long long)yy + (long long)g.ny * (long long)zz);
-  return outside ? -1ll : lin;
+// Neighbourhood of one site within RCH lattice units.  The linear index of
+// (x+dx, y+dy, z+dz) is ox[dx] + oy[dy] + oz[dz] (32-bit: tx_create checks
+// N < 2^31); bit d+RCH of in_a is clear when coordinate a + d leaves a
+// non-periodic axis (the ghost walls of WallsSetGhostNodesD3/D2,
+// lbm_walls.F90:179-231).  Periodic extents are >= 3 >= RCH, so one wrap
+// suffices; offsets past a non-periodic face are clamped into the lattice so
+// that every index stays a valid address.
+template <int D, int RCH>
+struct Hood {
+  static constexpr int RZ = D == 3 ? RCH : 0;
+  int ox[2 * RCH + 1], oy[2 * RCH + 1], oz[2 * RZ + 1];
+  unsigned in_x, in_y, in_z;
+
+  __device__ static __forceinline__ int wrap(int c, int n, int per, unsigned& in, int bit) {
+    const bool out = c < 0 || c >= n;
+    in |= (!out || per) ? (1u << bit) : 0u;
+    int w = c < 0 ? c + n : (c >= n ? c - n : c);
+    w = w < 0 ? 0 : (w >= n ? n - 1 : w);
+    return w;
+  }
+  __device__ __forceinline__ Hood(const Geo& g, int x, int y, int z) {
+    in_x = in_y = in_z = 0u;
+#pragma unroll
+    for (int d = -RCH; d <= RCH; ++d) {
+      ox[d + RCH] = wrap(x + d, g.nx, g.per[0], in_x, d + RCH);
+      oy[d + RCH] = g.nx * wrap(y + d, g.ny, g.per[1], in_y, d + RCH);
+    }
+#pragma unroll
+    for (int d = -RZ; d <= RZ; ++d) oz[d + RZ] = g.nx * g.ny * wrap(z + d, g.nz, g.per[2], in_z, d + RZ);
+  }
+  template <int dx, int dy, int dz>
+  __device__ __forceinline__ int at() const {
+    static_assert(dx >= -RCH && dx <= RCH && dy >= -RCH && dy <= RCH && dz >= -RZ && dz <= RZ, "offset beyond reach");
+    return ox[dx + RCH] + oy[dy + RCH] + oz[dz + RZ];
+  }
+  template <int dx, int dy, int dz>
+  __device__ __forceinline__ bool inside() const {
+    return ((in_x >> (dx + RCH)) & (in_y >> (dy + RCH)) & (in_z >> (dz + RZ)) & 1u) != 0u;
+  }
+};
+
+// Link mask of a site (k_links): bit 0 set when the site is pore space, bit n
+// (1..Q-1) when x + c_n is a pore site inside the lattice or across a
+// periodic face.  Push streaming, bounceback and the nearest-neighbour
+// stencil terms read it instead of the wall mask.
+template <int D>
+__host__ __device__ constexpr int link_of(int ex, int ey, int ez) {
+  int r = -1;
+  for (int n = 1; n < Lat<D>::Q; ++n)
+    if (Lat<D>::c(n, 0) == ex && Lat<D>::c(n, 1) == ey && (D == 3 ? Lat<D>::c(n, 2) : 0) == ez) r = n;
+  return r;
+}
+
+template <int D>
+__host__ __device__ constexpr uint32_t all_links() {
+  return ((1u << Lat<D>::Q) - 1u) & ~1u;
+}
+
+// pore test of the site at offset (dx, dy, dz): a link bit for lattice links,
+// the wall mask for the longer stencil offsets
+template <int D, int RCH, int dx, int dy, int dz>
+__device__ __forceinline__ bool pore_at(const Hood<D, RCH>& h, uint32_t links, const uint8_t* mask) {
+  constexpr int n = link_of<D>(dx, dy, dz);
+  if constexpr (n > 0) {
+    return ((links >> n) & 1u) != 0u;
+  } else {
+    const bool in = h.template inside<dx, dy, dz>();
+    const bool pore = __ldg(mask + h.template at<dx, dy, dz>()) == 0;
+    return in & pore;
+  }
 }
 
 // Site of this thread in a (x-tile, y-tile, z) launch grid; false when outside.
@@ -147,8 +205,6 @@ __device__ __forceinline__ bool site_of(const Geo& g, int& x, int& y, int& z, lo
   idx = (long long)x + (long long)g.nx * ((long long)y + (long long)g.ny * (long long)z);
   return true;
 }
-
-__device__ __forceinline__ bool is_pore(const uint8_t* mask, long long i) { return i >= 0 && __ldg(mask + i) == 0; }
 
 __device__ __forceinline__ bool on_face(const Geo& g, int f, int x, int y, int z) {
   const int a = f >> 1;
@@ -198,45 +254,64 @@ __host__ __device__ constexpr FFTerm ffterm(int t) {
   return D == 3 ? ff_d3(t) : ff_d2(t);
 }
 
+// Reach of the isotropy-ISO gradient stencil (at least one lattice link).
+template <int D, int ISO>
+__host__ __device__ constexpr int stencil_reach() {
+  int r = 1;
+  const int nt = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  for (int t = 0; t < nt; ++t) {
+    const FFTerm T = ffterm<D>(t);
+    if (T.level > ISO) continue;
+    for (int d = 0; d < 3; ++d) {
+      const int e = T.e[d] < 0 ? -T.e[d] : T.e[d];
+      r = e > r ? e : r;
+      for (int k = 0; k < T.naux; ++k) {
+        const int q = T.aux[k][d] < 0 ? -T.aux[k][d] : T.aux[k][d];
+        r = q > r ? q : r;
+      }
+    }
+  }
+  return r;
+}
+
 // One term of the wall-aware psi gradient: the neighbour x + e must be pore
-// space and, for long links, the path cells must satisfy the term's truth table.
-template <int D, int S, int ISO, int TI, class R, class RT>
-__device__ __forceinline__ void ff_term(const Geo& g, const PhysT<R>& P, const uint8_t* mask, const RT* rho, int x, int y,
-                                        int z, const R rf[S], R gr[S][D], R ws[D]) {
+// space and, for long links, the path cells must satisfy the term's truth
+// table.  EXACT sums the normalising weights in the reference's order; the
+// fast form counts them per weight class and multiplies once (wc).
+template <int D, int S, int ISO, bool EXACT, int TI, int RCH, class R, class RT>
+__device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P, const uint8_t* mask,
+                                        const RT* rho, long long N, const R rf[S], R gr[S][D], R ws[D], int wc[12][D]) {
   constexpr FFTerm T = ffterm<D>(TI);
   if constexpr (T.level <= ISO) {
-    const long long pi = nbr(g, x, y, z, T.e[0], T.e[1], T.e[2]);
-    bool ok = is_pore(mask, pi);
+    constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2];
+    bool ok = pore_at<D, RCH, ex, ey, ez>(h, links, mask);
     if constexpr (T.naux > 0) {
       unsigned bits = 0;
-      if constexpr (T.naux > 0) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[0][0], T.aux[0][1], T.aux[0][2])) ? 1u : 0u;
-      if constexpr (T.naux > 1) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[1][0], T.aux[1][1], T.aux[1][2])) ? 2u : 0u;
-      if constexpr (T.naux > 2) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[2][0], T.aux[2][1], T.aux[2][2])) ? 4u : 0u;
-      if constexpr (T.naux > 3) bits |= is_pore(mask, nbr(g, x, y, z, T.aux[3][0], T.aux[3][1], T.aux[3][2])) ? 8u : 0u;
+      if constexpr (T.naux > 0) bits |= pore_at<D, RCH, T.aux[0][0], T.aux[0][1], T.aux[0][2]>(h, links, mask) ? 1u : 0u;
+      if constexpr (T.naux > 1) bits |= pore_at<D, RCH, T.aux[1][0], T.aux[1][1], T.aux[1][2]>(h, links, mask) ? 2u : 0u;
+      if constexpr (T.naux > 2) bits |= pore_at<D, RCH, T.aux[2][0], T.aux[2][1], T.aux[2][2]>(h, links, mask) ? 4u : 0u;
+      if constexpr (T.naux > 3) bits |= pore_at<D, RCH, T.aux[3][0], T.aux[3][1], T.aux[3][2]>(h, links, mask) ? 8u : 0u;
       ok = ok && ((T.truth >> bits) & 1u);
     }
     if (ok) {
+      constexpr int tw = T.w;
+      const int pi = h.template at<ex, ey, ez>();
       R dif[S];
 #pragma unroll
-      for (int m = 0; m < S; ++m) dif[m] = R(rho[(long long)m * g.n + pi]) - rf[m];
-      if constexpr (T.e[0] != 0) {
-        const R coef = R(T.e[0]) * P.ffw[T.w];
+      for (int m = 0; m < S; ++m) dif[m] = R(rho[(long long)m * N + pi]) - rf[m];
+      sfor<0, D>([&](auto dd) {
+        constexpr int d = decltype(dd)::value;
+        constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
+        if constexpr (e != 0) {
+          const R coef = R(e) * P.ffw[tw];
 #pragma unroll
-        for (int m = 0; m < S; ++m) gr[m][0] = gr[m][0] + coef * dif[m];
-        ws[0] = ws[0] + P.ffw[T.w] * R(T.e[0] * T.e[0]);
-      }
-      if constexpr (D > 1 && T.e[1] != 0) {
-        const R coef = R(T.e[1]) * P.ffw[T.w];
-#pragma unroll
-        for (int m = 0; m < S; ++m) gr[m][1] = gr[m][1] + coef * dif[m];
-        ws[1] = ws[1] + P.ffw[T.w] * R(T.e[1] * T.e[1]);
-      }
-      if constexpr (D > 2 && T.e[2] != 0) {
-        const R coef = R(T.e[2]) * P.ffw[T.w];
-#pragma unroll
-        for (int m = 0; m < S; ++m) gr[m][D > 2 ? 2 : 0] = gr[m][D > 2 ? 2 : 0] + coef * dif[m];
-        ws[D > 2 ? 2 : 0] = ws[D > 2 ? 2 : 0] + P.ffw[T.w] * R(T.e[2] * T.e[2]);
-      }
+          for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * dif[m];
+          if constexpr (EXACT)
+            ws[d] = ws[d] + P.ffw[tw] * R(e * e);
+          else
+            wc[tw][d] += e * e;
+        }
+      });
     }
   }
 }
@@ -245,33 +320,38 @@ __device__ __forceinline__ void ff_term(const Geo& g, const PhysT<R>& P, const u
 // FlowCalcForces (lbm_flow.F90:760-808) for one pore site: zero, then
 // fluid-solid (lbm_forcing.F90:1326-1421), body (:1440-1496) and the
 // wall-aware Shan-Chen term (:51-958 / :960-1299), in that order.
-template <int D, int S, int ISO, bool EXACT, class R, class RT>
-__device__ __forceinline__ void cell_forces(const Geo& g, const PhysT<R>& P, const uint8_t* mask, const RT* rho,
-                                            int x, int y, int z, const R rf[S], R F[S][D]) {
+template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT>
+__device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P,
+                                            const uint8_t* mask, const RT* rho, long long N, const R rf[S],
+                                            R F[S][D]) {
   using L = Lat<D>;
 #pragma unroll
   for (int m = 0; m < S; ++m)
 #pragma unroll
     for (int d = 0; d < D; ++d) F[m][d] = R(0);
 
-  if (P.fs_on) {
+  // only links that end on a wall can carry a fluid-solid force
+  const uint32_t walled = ~links & all_links<D>();
+  if (P.fs_on && walled) {
     sfor<1, L::Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
-      const long long q = nbr(g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
-      const int mk = q >= 0 ? (int)__ldg(mask + q) : 255;
-      if (mk >= 1 && mk <= MAXMIN) {
-        const R wgt = R(n <= L::NAXIS ? P.fs_w_axis : P.fs_w_diag);
-        sfor<0, D>([&](auto dd) {
-          constexpr int d = decltype(dd)::value;
-          constexpr int c = L::c(n, d);
-          if constexpr (c != 0) {
+      constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
+      if ((walled >> n) & 1u) {
+        const int mk = h.template inside<cx, cy, cz>() ? (int)__ldg(mask + h.template at<cx, cy, cz>()) : 255;
+        if (mk >= 1 && mk <= MAXMIN) {
+          const R wgt = R(n <= L::NAXIS ? P.fs_w_axis : P.fs_w_diag);
+          sfor<0, D>([&](auto dd) {
+            constexpr int d = decltype(dd)::value;
+            constexpr int c = L::c(n, d);
+            if constexpr (c != 0) {
 #pragma unroll
-            for (int m = 0; m < S; ++m) {
-              const R t = wgt * rf[m] * R(P.gw[mk][m]);
-              F[m][d] = c > 0 ? F[m][d] - t : F[m][d] + t;
+              for (int m = 0; m < S; ++m) {
+                const R t = wgt * rf[m] * R(P.gw[mk][m]);
+                F[m][d] = c > 0 ? F[m][d] - t : F[m][d] + t;
+              }
             }
-          }
-        });
+          });
+        }
       }
     });
   }
@@ -284,14 +364,25 @@ __device__ __forceinline__ void cell_forces(const Geo& g, const PhysT<R>& P, con
   if (P.ff_on) {
     R gr[S][D];
     R ws[D];
+    int wc[12][D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       ws[d] = R(0);
 #pragma unroll
+      for (int w = 0; w < 12; ++w) wc[w][d] = 0;
+#pragma unroll
       for (int m = 0; m < S; ++m) gr[m][d] = R(0);
     }
     constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
-    sfor<0, NT>([&](auto tt) { ff_term<D, S, ISO, decltype(tt)::value, R, RT>(g, P, mask, rho, x, y, z, rf, gr, ws); });
+    sfor<0, NT>([&](auto tt) {
+      ff_term<D, S, ISO, EXACT, decltype(tt)::value, RCH, R, RT>(h, links, P, mask, rho, N, rf, gr, ws, wc);
+    });
+    if constexpr (!EXACT) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int w = 1; w < 12; ++w) ws[d] = ws[d] + P.ffw[w] * R(wc[w][d]);
+    }
     const R eps = R((double)1.e-12f);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -395,7 +486,8 @@ __device__ __forceinline__ void cell_moments(const StepArgs& a, const PhysT<R>& 
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
 #pragma unroll
   for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * a.g.n + idx]);
-  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+  const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
+  cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, a.g.n, rf, F);
   cell_velocity<D, S, EXACT, R>(a, P, x, y, z, fv, rf, F, rc, up);
 }
 
@@ -448,17 +540,19 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
-  if (__ldg(a.mask + idx) != 0) return;
+  const uint32_t links = __ldg(a.links + idx);
+  if (!(links & 1u)) return;  // wall site
   const long long N = a.g.n;
   const R rho0 = R(P.rho0);
+  const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
 
-  // forces first (they need only rho and the mask)
+  // forces first (they need only rho and the wall layout)
   R rf[S], F[S][D];
   {
     const RT* rho = reinterpret_cast<const RT*>(a.rho);
 #pragma unroll
     for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
-    cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+    cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, N, rf, F);
   }
   const T* fin = reinterpret_cast<const T*>(a.fin);
   // moments pass, one component's populations at a time
@@ -493,20 +587,21 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
 
   T* fout = reinterpret_cast<T*>(a.fout);
   // push (DistributionStreamD3/D2 + DistributionBouncebackD3/D2): to x + c_n,
-  // or back to x as opp(n) when x + c_n is a wall
+  // or back to x as opp(n) when link n ends on a wall
   auto push = [&](auto nn, int m, R v) {
     constexpr int n = decltype(nn)::value;
     constexpr int o = opp<D>(n);
     if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;  // w(opp n) == w(n): same shift
-    long long q = idx;
-    if constexpr (n != 0) {
-      q = nbr(a.g, x, y, z, L::c(n, 0), L::c(n, 1), D == 3 ? L::c(n, 2) : 0);
-      if (!is_pore(a.mask, q)) q = -1;
+    T* dst;
+    if constexpr (n == 0) {
+      dst = fout + (long long)(m * Q) * N + idx;
+    } else {
+      constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
+      const bool pore = ((links >> n) & 1u) != 0u;
+      dst = pore ? fout + (long long)(m * Q + n) * N + h.template at<cx, cy, cz>()
+                 : fout + (long long)(m * Q + o) * N + idx;
     }
-    if (q >= 0)
-      St<T>::st(fout + (long long)(m * Q + n) * N + q, v);
-    else
-      St<T>::st(fout + (long long)(m * Q + o) * N + idx, v);
+    St<T>::st(dst, v);
   };
 
   if constexpr (EXACT) {
@@ -526,11 +621,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
           R feq, pf;
           feq_pf<D, n, EXACT, R>(P, m, rc[m], up, usqr, F[m], feq, pf);
           const R fb = (R(1.) - R(.5) * pf) * feq;
-          R v;
-          if constexpr (EXACT)
-            v = f[n] - (f[n] - fb) / R(P.tau[m]);
-          else
-            v = f[n] + (fb - f[n]) * R(P.inv_tau[m]);
+          const R v = f[n] - (f[n] - fb) / R(P.tau[m]);
           push(nn, m, v + pf * feq);
         });
       } else {
@@ -555,10 +646,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
             else if constexpr (v == -1) md = md - dfi[i];
             else if constexpr (v != 0) md = md + R(v) * dfi[i];
           });
-          if constexpr (EXACT)
-            coef[k] = R(P.srate[m][k]) * md / R(L::mmt(k));
-          else
-            coef[k] = R(P.srate_mmt[m][k]) * md;
+          coef[k] = R(P.srate[m][k]) * md / R(L::mmt(k));
         });
         sfor<0, Q>([&](auto ii) {
           constexpr int i = decltype(ii)::value;
@@ -575,13 +663,18 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       }
     }
   } else {
-    // Fast form.  The equilibrium of every component shares the common
-    // velocity part B_n: feq_n(m) = rho_m * W_n * (A_m,n + B_n) with c_s^2 = 1/3.
-    R B[Q];
+    // Fast form, with c_s^2 = 1/3 and E_n = W~_n (A_m,n + B_n) (W~_0 = 1):
+    //   feq_n   = rho E_n                      (B_n holds the velocity terms)
+    //   P feq_n = 3 E_n (F.c_n - F.u)          (He forcing)
+    //   f'_n    = (1 - s0) f_n + E_n (s0 rho - k F.u + k F.c_n),  k = 3 - 1.5 s0
+    // i.e. f - s0 (f - feq + P feq / 2) + P feq, every moment relaxed at s0.
+    // Moments whose MRT rate differs from s0 are corrected afterwards.
+    // WB_n = W~_n B_n is shared by the components.
+    R WB[Q];
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       if constexpr (n == 0) {
-        B[0] = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
+        WB[0] = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
       } else {
         R ud = R(0);
         sfor<0, D>([&](auto dd) {
@@ -590,7 +683,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
           if constexpr (c > 0) ud = ud + up[d];
           if constexpr (c < 0) ud = ud - up[d];
         });
-        B[n] = R(3) * ud + R(4.5) * ud * ud - R(1.5) * usqr;
+        constexpr double w = L::w(n);
+        WB[n] = ud * (R(3 * w) + R(4.5 * w) * ud) - R(1.5 * w) * usqr;
       }
     });
 #pragma unroll
@@ -599,41 +693,62 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       const R dk = P.dk[m];
       const R A0 = D == 3 ? dk : (R(1) + R(5) * dk) * R(1.0 / 6.0);
       const R An = R(1.5) * (R(1) - dk);
-      const R inv = R(3) / r;  // 1 / (rho c_s^2)
-      R Fu = R(0);
-#pragma unroll
-      for (int d = 0; d < D; ++d) Fu = Fu + F[m][d] * up[d];
+      const R WA_axis = R(L::w(1)) * An, WA_diag = R(L::w(Q - 1)) * An;
       const R s0 = P.s0[m];
+      const R k = R(3) - R(1.5) * s0;
+      const R keep = R(1) - s0;
+      R Fu = R(0), kF[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        Fu = Fu + F[m][d] * up[d];
+        kF[d] = k * F[m][d];
+      }
+      const R G = s0 * r - k * Fu;
       const unsigned spec = P.spec_mask[m];
       const T* fm = fin + (long long)m * Q * N + idx;
-      // deviation from the forced equilibrium and the relaxed population of direction n
-      auto relax = [&](auto nn, R& dfi) -> R {
+      auto E_of = [&](auto nn) -> R {
+        constexpr int n = decltype(nn)::value;
+        if constexpr (n == 0) return A0 + WB[0];
+        else return (n <= L::NAXIS ? WA_axis : WA_diag) + WB[n];
+      };
+      auto pop = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
         R f = R(St<T>::ld(fm + (long long)n * N));
         if constexpr (kShifted<T>) f = f + R(L::w(n)) * rho0;
-        const R feq = r * R(n == 0 ? 1.0 : L::w(n)) * ((n == 0 ? A0 : An) + B[n]);
-        R Fc = R(0);
+        return f;
+      };
+      // sum_d c_n,d v_d
+      auto cdot = [&](auto nn, const R v[D]) -> R {
+        constexpr int n = decltype(nn)::value;
+        R acc = R(0);
         sfor<0, D>([&](auto dd) {
           constexpr int d = decltype(dd)::value;
           constexpr int c = L::c(n, d);
-          if constexpr (c > 0) Fc = Fc + F[m][d];
-          if constexpr (c < 0) Fc = Fc - F[m][d];
+          if constexpr (c > 0) acc = acc + v[d];
+          if constexpr (c < 0) acc = acc - v[d];
         });
-        const R pfeq = (Fc - Fu) * inv * feq;
-        dfi = f - (feq - R(0.5) * pfeq);
-        return f - s0 * dfi + pfeq;
+        return acc;
       };
       if (spec == 0u) {
         // every moment relaxes at s0 (BGK): one direction at a time
         sfor<0, Q>([&](auto nn) {
-          R dfi;
-          const R v = relax(nn, dfi);
-          push(nn, m, v);
+          const R f = pop(nn);
+          push(nn, m, keep * f + E_of(nn) * (G + cdot(nn, kF)));
         });
       } else {
-        // moments whose MRT rate differs from s0 get (rate - s0) on top
+        // deviation from the forced equilibrium: f - E_n (rho + 1.5 F.u - 1.5 F.c_n)
+        const R H = r + R(1.5) * Fu;
+        R hF[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
         R fo[Q], dfi[Q];
-        sfor<0, Q>([&](auto nn) { fo[decltype(nn)::value] = relax(nn, dfi[decltype(nn)::value]); });
+        sfor<0, Q>([&](auto nn) {
+          constexpr int n = decltype(nn)::value;
+          const R f = pop(nn);
+          const R E = E_of(nn);
+          fo[n] = keep * f + E * (G + cdot(nn, kF));
+          dfi[n] = f - E * (H - cdot(nn, hF));
+        });
         sfor<0, Q>([&](auto kk) {
           constexpr int k = decltype(kk)::value;
           if (spec & (1u << k)) {
@@ -659,6 +774,25 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       }
     }
   }
+}
+
+// Link masks of every site from the wall mask (see link_of).
+template <int D>
+__global__ void __launch_bounds__(256) k_links(const uint8_t* mask, Geo g, uint32_t* links) {
+  using L = Lat<D>;
+  int x, y, z;
+  long long idx;
+  if (!site_of(g, x, y, z, idx)) return;
+  const Hood<D, 1> h(g, x, y, z);
+  uint32_t b = __ldg(mask + idx) == 0 ? 1u : 0u;
+  sfor<1, L::Q>([&](auto nn) {
+    constexpr int n = decltype(nn)::value;
+    constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
+    const bool in = h.template inside<cx, cy, cz>();
+    const bool pore = __ldg(mask + h.template at<cx, cy, cz>()) == 0;
+    b |= (in & pore) ? (1u << n) : 0u;
+  });
+  links[idx] = b;
 }
 
 // -------------------------------------------------- Dirichlet density node
@@ -791,7 +925,10 @@ __global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) 
   R rf[S], F[S][D];
 #pragma unroll
   for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
-  cell_forces<D, S, ISO, EXACT, R, RT>(a.g, P, a.mask, rho, x, y, z, rf, F);
+  {
+    const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
+    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, N, rf, F);
+  }
   T* fout = reinterpret_cast<T*>(a.fout);
   const R rho0 = R(P.rho0);
 #pragma unroll

@@ -103,7 +103,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   g.n = (long long)g.nx * g.ny * g.nz;
   const long long N = g.n;
 
-  // carve the scratch array: parameters | mask | rho | face values | populations A | populations B | flag
+  // carve the scratch array: parameters | mask | links | rho | face values | populations A | populations B | flag
   long long area[6] = {0, 0, 0, 0, 0, 0};
   for (int f = 0; f < 2 * D; ++f) {
     if (p->bc_flags[f] != TX_BC_DENSITY) continue;
@@ -116,6 +116,8 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   off = align256(off + sizeof(Phys));
   const size_t o_mask = off;
   off = align256(off + (size_t)N);
+  const size_t o_links = off;
+  off = align256(off + (size_t)N * sizeof(uint32_t));
   const size_t o_rho = off;
   off = align256(off + (size_t)N * S * sizeof(double));
   size_t o_face[6];
@@ -156,6 +158,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   fill_phys_from(*p, D, S, Q, &ph);
   Phys* d_phys = (Phys*)(base + o_phys);
   uint8_t* mask = base + o_mask;
+  uint32_t* links = (uint32_t*)(base + o_links);
   double* rho = (double*)(base + o_rho);
   double* pa = (double*)(base + o_pa);
   double* pb = (double*)(base + o_pb);
@@ -173,6 +176,13 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   TX_SCHK(cudaMemsetAsync(rho, 0, (size_t)N * S * sizeof(double), st));
   TX_SCHK(cudaMemsetAsync(pb, 0, pop_bytes, st));
   k_static_mask<<<grid_for(N, 256), 256, 0, st>>>(walls, N, p->nminerals, mask, flag);
+  {
+    const Launch3 l = launch3(g, 256);
+    if (D == 3)
+      k_links<3><<<l.grid, l.block, 0, st>>>(mask, g, links);
+    else
+      k_links<2><<<l.grid, l.block, 0, st>>>(mask, g, links);
+  }
   Faces faces{};
   for (int f = 0; f < 2 * D; ++f) {
     if (!area[f]) continue;
@@ -186,6 +196,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   StepArgs a{};
   a.rho = rho;
   a.mask = mask;
+  a.links = links;
   a.phys = d_phys;
   a.g = g;
   a.faces = faces;

@@ -87,3 +87,19 @@ def porous_case(disc, shape, mode=P.SRT, iso=4, seed=3, dirichlet=True, body=Fal
         if disc == P.D3Q19:
             p.gvt[2] = 3e-5
     return p, walls, rho.ravel()
+
+
+# (name, case factory, steps): the parity matrix of the GPU and host-emulation tests
+PARITY = [
+    ("d2_srt_iso4", lambda: sc_bubble(P.D2Q9, (1, 40, 48), P.SRT, 4), 30),
+    ("d2_mrt_iso8", lambda: sc_bubble(P.D2Q9, (1, 44, 40), P.MRT, 8), 30),
+    ("d2_mrt_iso10", lambda: sc_bubble(P.D2Q9, (1, 40, 40), P.MRT, 10), 30),
+    ("d3_srt_iso4", lambda: sc_bubble(P.D3Q19, (12, 14, 16), P.SRT, 4), 20),
+    ("d3_mrt_iso4", lambda: sc_bubble(P.D3Q19, (16, 12, 14), P.MRT, 4), 20),
+    ("d3_mrt_iso8", lambda: sc_bubble(P.D3Q19, (14, 16, 12), P.MRT, 8), 20),
+    ("d3_porous_dirichlet_srt", lambda: porous_case(P.D3Q19, (14, 12, 10)), 20),
+    ("d3_porous_dirichlet_mrt_body", lambda: porous_case(P.D3Q19, (12, 10, 14), mode=P.MRT, body=True), 20),
+    ("d3_porous_periodic_iso8", lambda: porous_case(P.D3Q19, (12, 12, 12), iso=8, dirichlet=False), 15),
+    ("d2_porous_dirichlet", lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), 30),
+    ("d3_single_component_porous", lambda: porous_case(P.D3Q19, (10, 12, 14), ncomp=1, body=True), 20),
+]

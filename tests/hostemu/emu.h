@@ -1,0 +1,170 @@
+// Host emulation of the flow step: the kernels of tx_kernels.cuh run one
+// thread at a time on the CPU, with the parameter translation and launch
+// shapes of the C ABI (tx_abi.cu).  Test infrastructure: a sanitizer build
+// checks every index the kernels form, and the results are compared with the
+// oracle on the CPU.
+#pragma once
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tx_host_params.h"
+
+namespace emu {
+
+using namespace tx;
+
+struct Case {
+  tx_params p;
+  int nsteps = 0;
+  int from_fi = 0;            // 0: tx_upload_state + tx_init, 1: tx_upload_fi + tx_init
+  std::vector<double> walls;  // [N]
+  std::vector<double> init;   // rho [N*S] or fi [N*S*Q], natural order
+};
+
+struct Result {
+  std::vector<double> fi, rho, flux, forces;  // natural order, as tx_download
+};
+
+// the library's launch3 shape, walked block by block and thread by thread
+template <class F>
+void launch3(const Geo& g, int threads, F&& f) {
+  int bx = ((g.nx + 31) / 32) * 32;
+  if (bx > 128) bx = 128;
+  if (bx > threads) bx = threads;
+  int by = threads / bx;
+  if (by < 1) by = 1;
+  blockDim = dim3{(unsigned)bx, (unsigned)by, 1};
+  gridDim = dim3{(unsigned)((g.nx + bx - 1) / bx), (unsigned)((g.ny + by - 1) / by), (unsigned)g.nz};
+  for (unsigned bz = 0; bz < gridDim.z; ++bz)
+    for (unsigned byy = 0; byy < gridDim.y; ++byy)
+      for (unsigned bxx = 0; bxx < gridDim.x; ++bxx)
+        for (unsigned ty = 0; ty < blockDim.y; ++ty)
+          for (unsigned tx_ = 0; tx_ < blockDim.x; ++tx_) {
+            blockIdx = dim3{bxx, byy, bz};
+            threadIdx = dim3{tx_, ty, 0};
+            f();
+          }
+}
+
+template <class F>
+void launch1(long long n, int bs, F&& f) {
+  blockDim = dim3{(unsigned)bs, 1, 1};
+  gridDim = dim3{(unsigned)((n + bs - 1) / bs), 1, 1};
+  for (unsigned b = 0; b < gridDim.x; ++b)
+    for (int t = 0; t < bs; ++t) {
+      blockIdx = dim3{b, 0, 0};
+      threadIdx = dim3{(unsigned)t, 0, 0};
+      f();
+    }
+}
+
+template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
+std::string run(const Case& c, Result& out) {
+  constexpr int Q = Lat<D>::Q;
+  const tx_params& p = c.p;
+  Geo g{};
+  g.nx = p.nx;
+  g.ny = p.ny;
+  g.nz = D == 3 ? p.nz : 1;
+  for (int a = 0; a < 3; ++a) g.per[a] = a < D ? p.bc_flags[2 * a] == TX_BC_PERIODIC : 1;
+  g.n = (long long)g.nx * g.ny * g.nz;
+  const long long N = g.n;
+
+  Phys ph{};
+  fill_phys_impl(p, D, S, Q, ph);
+  PhysT<R> P{};
+  if constexpr (std::is_same<R, double>::value)
+    P = ph;
+  else
+    convert_phys(ph, &P);
+
+  std::vector<uint8_t> mask((size_t)N);
+  for (long long i = 0; i < N; ++i) {
+    const char* why = nullptr;
+    if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why)) return why;
+  }
+  std::vector<uint32_t> links((size_t)N);
+  launch3(g, 256, [&] { k_links<D>(mask.data(), g, links.data()); });
+
+  std::vector<T> f0((size_t)N * S * Q), f1((size_t)N * S * Q);
+  std::memset(f0.data(), 0, f0.size() * sizeof(T));
+  std::memset(f1.data(), 0, f1.size() * sizeof(T));
+  std::vector<RT> rho((size_t)N * S, RT(0));
+  std::vector<double> facevals[6];
+  Faces faces{};
+  for (int f = 0; f < 2 * D; ++f) {
+    if (p.bc_flags[f] != TX_BC_DENSITY) continue;
+    const int a = f / 2;
+    const long long area = D == 2 ? (a == 0 ? g.ny : g.nx)
+                                  : (a == 0 ? (long long)g.ny * g.nz : a == 1 ? (long long)g.nx * g.nz
+                                                                              : (long long)g.nx * g.ny);
+    facevals[f].resize((size_t)area * S);
+    for (int m = 0; m < S; ++m)
+      for (long long q = 0; q < area; ++q) facevals[f][(size_t)(m * area + q)] = p.bc_density[f][m];
+    faces.on[f] = 1;
+    faces.vals[f] = facevals[f].data();
+  }
+
+  T* buf[2] = {f0.data(), f1.data()};
+  int cur = 0;
+  auto args = [&](int in, int o) {
+    StepArgs a{};
+    a.fin = buf[in];
+    a.fout = buf[o];
+    a.rho = rho.data();
+    a.mask = mask.data();
+    a.links = links.data();
+    a.phys = &P;
+    a.g = g;
+    a.faces = faces;
+    return a;
+  };
+  const double rho0 = ph.rho0;
+  if (c.from_fi) {
+    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), mask.data(), N, rho0, buf[cur]); });
+  } else {
+    for (long long i = 0; i < N; ++i)
+      for (int m = 0; m < S; ++m)
+        rho[(size_t)(m * N + i)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] : 0.0);
+    const StepArgs a = args(cur, cur);
+    launch3(g, 128, [&] { k_init<D, S, ISO, EXACT, T, R, RT>(a, nullptr); });
+  }
+  {
+    const StepArgs a = args(cur, cur);
+    launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 1); });
+  }
+  for (int t = 0; t < c.nsteps; ++t) {
+    const StepArgs a = args(cur, 1 - cur);
+    launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
+    launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 0); });
+    cur = 1 - cur;
+  }
+  out.fi.assign((size_t)N * S * Q, 0.0);
+  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], mask.data(), N, rho0, out.fi.data()); });
+  const StepArgs a = args(cur, cur);
+  out.rho.assign((size_t)N * S, 0.0);
+  out.flux.assign((size_t)N * S * D, 0.0);
+  out.forces.assign((size_t)N * S * D, 0.0);
+  launch3(g, 128, [&] { k_moments<D, S, ISO, EXACT, T, R, RT>(a, 2, out.rho.data()); });
+  launch3(g, 128, [&] { k_moments<D, S, ISO, EXACT, T, R, RT>(a, 3, out.flux.data()); });
+  launch3(g, 128, [&] { k_moments<D, S, ISO, EXACT, T, R, RT>(a, 4, out.forces.data()); });
+  return "";
+}
+
+// one entry per compiled combination; returns false when none matches
+bool dispatch_d3_iso4(const Case& c, Result& out, std::string* err);
+bool dispatch_d3_iso8(const Case& c, Result& out, std::string* err);
+bool dispatch_d2(const Case& c, Result& out, std::string* err);
+bool dispatch_forms(const Case& c, Result& out, std::string* err);
+
+}  // namespace emu
+
+// selects run<...> when the case's parameters match the combination
+#define EMU_TRY(D_, S_, ISO_, MRT_, EXACT_, PREC_, T_, R_, RT_)                                          \
+  if (c.p.ncomponents == S_ && c.p.isotropy_order == ISO_ && (c.p.relaxation_mode == TX_RELAX_MRT) == MRT_ && \
+      (c.p.exact != 0) == EXACT_ && c.p.precision == PREC_) {                                          \
+    *err = run<D_, S_, ISO_, MRT_, EXACT_, T_, R_, RT_>(c, out);                                       \
+    return true;                                                                                       \
+  }

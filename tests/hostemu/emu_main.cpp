@@ -1,0 +1,58 @@
+// emu <case.bin> <result.bin>: one flow run of the host emulation.
+//
+// case.bin:   tx_params (raw struct) | int32 nsteps | int32 from_fi |
+//             walls [N] f64 | rho [N*S] or fi [N*S*Q] f64 (natural order)
+// result.bin: fi [N*S*Q] | rho [N*S] | flux [N*D*S] | forces [N*D*S], f64
+// Exit status 0 on success, 2 for parameters the library rejects (message on
+// stderr), 3 when the combination is not compiled into the emulation.
+#include <cstdio>
+
+#include "emu.h"
+
+using namespace emu;
+
+static bool read_all(FILE* f, void* p, size_t bytes) { return fread(p, 1, bytes, f) == bytes; }
+
+int main(int argc, char** argv) {
+  if (argc != 3) {
+    fprintf(stderr, "usage: emu case.bin result.bin\n");
+    return 1;
+  }
+  FILE* f = fopen(argv[1], "rb");
+  if (!f) return 1;
+  Case c;
+  int32_t hdr[2];
+  if (!read_all(f, &c.p, sizeof(c.p)) || !read_all(f, hdr, sizeof(hdr))) return 1;
+  c.nsteps = hdr[0];
+  c.from_fi = hdr[1];
+  std::string why;
+  const int rc = validate(&c.p, &why);
+  if (rc) {
+    fprintf(stderr, "%s\n", why.c_str());
+    return 2;
+  }
+  const int D = c.p.discretization == TX_D3Q19 ? 3 : 2, S = c.p.ncomponents, Q = D == 3 ? 19 : 9;
+  const long long N = (long long)c.p.nx * c.p.ny * (D == 3 ? c.p.nz : 1);
+  c.walls.resize((size_t)N);
+  c.init.resize((size_t)(N * S * (c.from_fi ? Q : 1)));
+  if (!read_all(f, c.walls.data(), c.walls.size() * 8) || !read_all(f, c.init.data(), c.init.size() * 8)) return 1;
+  fclose(f);
+
+  Result r;
+  std::string err;
+  const bool found = D == 3 ? (dispatch_d3_iso4(c, r, &err) || dispatch_d3_iso8(c, r, &err) || dispatch_forms(c, r, &err))
+                            : (dispatch_d2(c, r, &err) || dispatch_forms(c, r, &err));
+  if (!found) {
+    fprintf(stderr, "combination not compiled into the emulation\n");
+    return 3;
+  }
+  if (!err.empty()) {
+    fprintf(stderr, "%s\n", err.c_str());
+    return 2;
+  }
+  FILE* o = fopen(argv[2], "wb");
+  if (!o) return 1;
+  for (const std::vector<double>* v : {&r.fi, &r.rho, &r.flux, &r.forces}) fwrite(v->data(), 8, v->size(), o);
+  fclose(o);
+  return 0;
+}

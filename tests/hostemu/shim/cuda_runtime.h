@@ -1,0 +1,25 @@
+// Host stand-ins for the CUDA qualifiers and built-ins used by the flow
+// kernels (taxila-lbm_gb300/csrc/tx_kernels.cuh), so that the kernels compile
+// as plain C++ and run one thread at a time on the CPU.  The kernels use no
+// shared memory, barriers, warp operations or atomics, so a sequential walk
+// over the launch grid computes exactly what the device computes per thread.
+#pragma once
+#include <cstdint>
+
+#define __global__
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __launch_bounds__(...)
+
+struct dim3 {
+  unsigned x, y, z;
+};
+inline dim3 threadIdx, blockIdx, blockDim, gridDim;
+
+template <class T>
+inline T __ldg(const T* p) {
+  return *p;
+}
+
+typedef void* cudaStream_t;

@@ -69,19 +69,7 @@ def compare(o, h, p, walls, exact, rtol=1e-12):
     return out
 
 
-PARITY = [
-    ("d2_srt_iso4", lambda: cases.sc_bubble(P.D2Q9, (1, 40, 48), P.SRT, 4), 30),
-    ("d2_mrt_iso8", lambda: cases.sc_bubble(P.D2Q9, (1, 44, 40), P.MRT, 8), 30),
-    ("d2_mrt_iso10", lambda: cases.sc_bubble(P.D2Q9, (1, 40, 40), P.MRT, 10), 30),
-    ("d3_srt_iso4", lambda: cases.sc_bubble(P.D3Q19, (12, 14, 16), P.SRT, 4), 20),
-    ("d3_mrt_iso4", lambda: cases.sc_bubble(P.D3Q19, (16, 12, 14), P.MRT, 4), 20),
-    ("d3_mrt_iso8", lambda: cases.sc_bubble(P.D3Q19, (14, 16, 12), P.MRT, 8), 20),
-    ("d3_porous_dirichlet_srt", lambda: cases.porous_case(P.D3Q19, (14, 12, 10)), 20),
-    ("d3_porous_dirichlet_mrt_body", lambda: cases.porous_case(P.D3Q19, (12, 10, 14), mode=P.MRT, body=True), 20),
-    ("d3_porous_periodic_iso8", lambda: cases.porous_case(P.D3Q19, (12, 12, 12), iso=8, dirichlet=False), 15),
-    ("d2_porous_dirichlet", lambda: cases.porous_case(P.D2Q9, (1, 30, 26), body=True), 30),
-    ("d3_single_component_porous", lambda: cases.porous_case(P.D3Q19, (10, 12, 14), ncomp=1, body=True), 20),
-]
+PARITY = cases.PARITY
 
 
 @pytest.mark.parametrize("name,make,steps", PARITY, ids=[c[0] for c in PARITY])

@@ -1,0 +1,135 @@
+"""Host emulation of the CUDA kernels against the oracle (CPU only).
+
+The kernels of taxila-lbm_gb300/csrc/tx_kernels.cuh, compiled as C++ with
+AddressSanitizer/UBSan (tests/hostemu), run the GPU parity matrix on the CPU
+with the library's own parameter translation and launch shapes:
+
+* exact FP64 form: populations, densities, velocities and forces identical to
+  the oracle bit for bit (the device build adds only --fmad=false, which the
+  host compiler matches with -ffp-contract=off);
+* fast FP64 form: within 1e-12 relative of the oracle;
+* FP32 arithmetic forms: within the bounds stated in FORM_TOL.
+
+Every index a kernel forms is checked by the sanitizers, so an out-of-bounds
+read or write in a kernel fails here before it reaches a GPU.
+"""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import cases
+from oracle import Oracle
+from taxila import params as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "hostemu"))
+import build_emu  # noqa: E402
+
+FIELDS = ("fi", "rho", "flux", "forces")
+ORACLE_FIELDS = {"fi": P.FIELD_FI, "rho": P.FIELD_RHO, "flux": P.FIELD_FLUX, "forces": P.FIELD_FORCES}
+# bound on max |emu - oracle| / max |oracle| over pore sites after 20 steps of the
+# D3Q19 MRT bubble: FP32 arithmetic and storage; FP32 arithmetic with FP16 storage of
+# f - w rho0 (11-bit significand: ~5e-4 of the deviation; the flux, a small
+# difference of populations, carries the largest relative error)
+FORM_TOL = {P.PREC_F32: {"fi": 2e-5, "rho": 2e-5, "flux": 2e-5, "forces": 2e-5},
+            P.PREC_F32_F16: {"fi": 2e-3, "rho": 2e-3, "flux": 3e-2, "forces": 3e-3}}
+
+
+@pytest.fixture(scope="module")
+def emu_exe():
+    os.environ.setdefault("ASAN_OPTIONS", "detect_leaks=0")
+    return build_emu.build()
+
+
+def run_emu(exe, p, walls, init, steps, from_fi, tmp_path):
+    case = os.path.join(str(tmp_path), "case.bin")
+    res = os.path.join(str(tmp_path), "result.bin")
+    with open(case, "wb") as f:
+        f.write(C.string_at(C.addressof(p), C.sizeof(p)))
+        f.write(np.array([steps, 1 if from_fi else 0], dtype=np.int32).tobytes())
+        f.write(np.ascontiguousarray(walls, dtype=np.float64).tobytes())
+        f.write(np.ascontiguousarray(init, dtype=np.float64).tobytes())
+    r = subprocess.run([exe, case, res], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, "emu exit %d: %s" % (r.returncode, r.stderr[-3000:])
+    raw = np.fromfile(res, dtype=np.float64)
+    n, s, d, q = p.nsites, p.ncomponents, p.ndims, p.Q
+    sizes = {"fi": n * s * q, "rho": n * s, "flux": n * s * d, "forces": n * s * d}
+    out, o = {}, 0
+    for k in FIELDS:
+        out[k] = raw[o:o + sizes[k]]
+        o += sizes[k]
+    assert o == raw.size
+    return out
+
+
+def oracle_run(p, walls, rho, steps, fi=None):
+    o = Oracle(p)
+    o.set_walls(walls)
+    if fi is not None:
+        o.set_fi(fi)
+    else:
+        o.set_state(rho)
+    o.init()
+    if steps:
+        o.step(steps)
+    return {k: o.get(v) for k, v in ORACLE_FIELDS.items()}
+
+
+def compare(ref, got, p, walls, tol):
+    pore = np.asarray(walls).ravel() == 0
+    errs = {}
+    for k in FIELDS:
+        a, b = ref[k], got[k]
+        t = tol[k] if isinstance(tol, dict) else tol
+        m = np.repeat(pore, a.size // p.nsites)
+        assert np.all(b[~m] == 0.0), k
+        if t == 0.0:
+            bad = np.nonzero((a != b) & m)[0]
+            assert bad.size == 0, "%s: %d values differ, first %s: %r vs %r" % (k, bad.size, bad[:3], a[bad[:3]], b[bad[:3]])
+        else:
+            scale = np.max(np.abs(a[m])) or 1.0
+            errs[k] = float(np.max(np.abs(a[m] - b[m])) / scale)
+            assert errs[k] <= t, "%s: max rel err %.3e > %.1e" % (k, errs[k], t)
+    return errs
+
+
+@pytest.mark.parametrize("name,make,steps", cases.PARITY, ids=[c[0] for c in cases.PARITY])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_emulated_kernels_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    compare(ref, got, p, walls, 0.0 if exact else 1e-12)
+
+
+def test_emulated_restart_from_fi(emu_exe, tmp_path):
+    p, walls, rho = cases.porous_case(P.D3Q19, (10, 12, 10), mode=P.MRT, body=True)
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.init()
+    o.step(3)
+    fi = o.get(P.FIELD_FI)
+    ref = oracle_run(p, walls, None, 5, fi=fi)
+    q = P.copy_params(p)
+    q.exact = 1
+    got = run_emu(emu_exe, q, walls, fi, 5, True, tmp_path)
+    compare(ref, got, p, walls, 0.0)
+
+
+@pytest.mark.parametrize("prec", [P.PREC_F32, P.PREC_F32_F16], ids=["f32", "f32_f16"])
+def test_emulated_reduced_precision_forms(emu_exe, tmp_path, prec):
+    p, walls, rho = cases.sc_bubble(P.D3Q19, (12, 12, 14), P.MRT, 4, g=0.15)
+    ref = oracle_run(p, walls, rho, 20)
+    q = P.copy_params(p)
+    q.precision = prec
+    q.rho0 = 1.0
+    got = run_emu(emu_exe, q, walls, rho, 20, False, tmp_path)
+    errs = compare(ref, got, p, walls, FORM_TOL[prec])
+    print("form %d after 20 steps:" % prec, errs)
