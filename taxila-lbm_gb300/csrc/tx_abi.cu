@@ -324,10 +324,10 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
   if (!h || !rho) return TX_ERR_ARG;
   const long long N = h->g.n;
   const int S = h->S, D = h->D;
-  // rho: natural (m fastest) -> [m][cell] in the rho storage type
+  // rho: natural order (component fastest, the device layout too), zero on walls
   std::vector<double> rt((size_t)N * S);
   for (long long i = 0; i < N; ++i)
-    for (int m = 0; m < S; ++m) rt[(size_t)m * N + i] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] : 0.0;
+    for (int m = 0; m < S; ++m) rt[(size_t)(i * S + m)] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] : 0.0;
   if (h->rho_bytes == 8) {
     TX_CUDA(h, cudaMemcpyAsync(h->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, h->stream));
     TX_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -114,6 +114,10 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
       w[8] = 9.0 / 9520.0; w[9] = 2.0 / 5355.0; w[10] = 1.0 / 7140.0;
     }
   }
+  for (int d = 0; d < D; ++d) {
+    const double ws = D == 3 ? full_weight_sum<3>(iso, P.ffw, d) : full_weight_sum<2>(iso, P.ffw, d);
+    P.inv_ws_full[d] = ws > 0.0 ? 1.0 / ws : 0.0;
+  }
   P.c0 = 6.0;  // disc%c_0
   // fluid-solid weights 1./6., 1./12. (D3) and 1./3., 1./12. (D2): default-REAL literals
   if (p.literal_kind == 8) {

@@ -2,7 +2,7 @@
 //
 // Device state between steps is the reference's fi after FlowApplyBCs (the
 // post-stream, post-boundary populations) in SoA layout f[(m*Q + n)*N + cell],
-// cell = x + nx*(y + ny*z), plus the density used for forcing, rho[m*N + cell].
+// cell = x + nx*(y + ny*z), plus the density used for forcing, rho[cell*S + m].
 // One step of LBMRun2 (src/lbm/lbm.F90:283-363) is two launches:
 //
 //   k_step     per pore site: forces (fluid-solid, body, Shan-Chen), flux and
@@ -66,6 +66,7 @@ struct PhysT {
   // differs (bit k of spec_mask) by dspec = (rate_k - s0) / diag(M M^T)_k
   R s0[MAXC];
   R dspec[MAXC][19];
+  R inv_ws_full[3];        // 1 / weight sum of a gradient stencil with every neighbour pore
   unsigned spec_mask[MAXC];
   int ff_on, fs_on, body_on;
 };
@@ -81,7 +82,7 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   b->c0 = R(a.c0); b->fs_w_axis = R(a.fs_w_axis); b->fs_w_diag = R(a.fs_w_diag);
   cp(&a.srate[0][0], &b->srate[0][0], MAXC * 19); cp(&a.srate_mmt[0][0], &b->srate_mmt[0][0], MAXC * 19);
   b->rho0 = R(a.rho0);
-  cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19);
+  cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19); cp(a.inv_ws_full, b->inv_ws_full, 3);
   for (int m = 0; m < MAXC; ++m) b->spec_mask[m] = a.spec_mask[m];
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
 }
@@ -94,7 +95,7 @@ struct Faces {
 struct StepArgs {
   const void* fin;
   void* fout;
-  void* rho;                // RT [m * N + cell]
+  void* rho;                // RT [cell * S + m]
   const uint8_t* mask;      // 0 pore, 1..16 mineral, 255 other wall
   const uint32_t* links;    // link mask of every site (k_links)
   const void* phys;         // device PhysT<R> of the kernels' arithmetic type
@@ -122,6 +123,24 @@ struct St<__half> {
 };
 template <class T>
 constexpr bool kShifted = !std::is_same<T, double>::value;
+
+// The forcing density is stored component-fastest, rho[cell * S + m], so that
+// one vector load brings every component of a neighbour.
+template <int S, class RT, class R>
+__device__ __forceinline__ void rho_at(const RT* rho, unsigned cell, R v[S]) {
+  if constexpr (S == 2 && std::is_same<RT, double>::value) {
+    const double2 t = __ldg(reinterpret_cast<const double2*>(rho) + cell);
+    v[0] = R(t.x);
+    v[1] = R(t.y);
+  } else if constexpr (S == 2 && std::is_same<RT, float>::value) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(rho) + cell);
+    v[0] = R(t.x);
+    v[1] = R(t.y);
+  } else {
+#pragma unroll
+    for (int m = 0; m < S; ++m) v[m] = R(__ldg(rho + (size_t)cell * S + m));
+  }
+}
 
 // --------------------------------------------------------------- geometry
 // Neighbourhood of one site within RCH lattice units.  The linear index of
@@ -155,9 +174,9 @@ struct Hood {
     for (int d = -RZ; d <= RZ; ++d) oz[d + RZ] = g.nx * g.ny * wrap(z + d, g.nz, g.per[2], in_z, d + RZ);
   }
   template <int dx, int dy, int dz>
-  __device__ __forceinline__ int at() const {
+  __device__ __forceinline__ unsigned at() const {
     static_assert(dx >= -RCH && dx <= RCH && dy >= -RCH && dy <= RCH && dz >= -RZ && dz <= RZ, "offset beyond reach");
-    return ox[dx + RCH] + oy[dy + RCH] + oz[dz + RZ];
+    return (unsigned)(ox[dx + RCH] + oy[dy + RCH] + oz[dz + RZ]);
   }
   template <int dx, int dy, int dz>
   __device__ __forceinline__ bool inside() const {
@@ -274,6 +293,31 @@ __host__ __device__ constexpr int stencil_reach() {
   return r;
 }
 
+// True when every term of the isotropy-ISO stencil is a plain lattice link
+// (isotropy 4): the link mask then decides all of them.
+template <int D, int ISO>
+__host__ __device__ constexpr bool stencil_is_links() {
+  const int nt = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  for (int t = 0; t < nt; ++t) {
+    const FFTerm T = ffterm<D>(t);
+    if (T.level > ISO) continue;
+    if (T.naux > 0 || link_of<D>(T.e[0], T.e[1], T.e[2]) < 0) return false;
+  }
+  return true;
+}
+
+// Weight sum of axis d of the isotropy-ISO stencil with every neighbour pore.
+template <int D>
+inline double full_weight_sum(int iso, const double ffw[12], int d) {
+  const int nt = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  double ws = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    const FFTerm T = ffterm<D>(t);
+    if (T.level <= iso) ws += ffw[T.w] * (double)(T.e[d] * T.e[d]);
+  }
+  return ws;
+}
+
 // One term of the wall-aware psi gradient: the neighbour x + e must be pore
 // space and, for long links, the path cells must satisfy the term's truth
 // table.  EXACT sums the normalising weights in the reference's order; the
@@ -295,10 +339,11 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
     }
     if (ok) {
       constexpr int tw = T.w;
-      const int pi = h.template at<ex, ey, ez>();
+      const unsigned pi = h.template at<ex, ey, ez>();
       R dif[S];
+      rho_at<S>(rho, pi, dif);
 #pragma unroll
-      for (int m = 0; m < S; ++m) dif[m] = R(rho[(long long)m * N + pi]) - rf[m];
+      for (int m = 0; m < S; ++m) dif[m] = dif[m] - rf[m];
       sfor<0, D>([&](auto dd) {
         constexpr int d = decltype(dd)::value;
         constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
@@ -361,6 +406,49 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
 #pragma unroll
       for (int d = 0; d < D; ++d) F[m][d] = F[m][d] + R(P.gvt[d]) * R(P.mm[m]) * rf[m];
   }
+  if constexpr (!EXACT && stencil_is_links<D, ISO>()) {
+    // every stencil neighbour pore: the weight sums are constant and the
+    // psi(x) terms cancel, so grad = sum_k w_k e_k psi(x + e_k)
+    if (P.ff_on && (links | 1u) == (all_links<D>() | 1u)) {
+      R gr[S][D];
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int m = 0; m < S; ++m) gr[m][d] = R(0);
+      constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+      sfor<0, NT>([&](auto tt) {
+        constexpr FFTerm T = ffterm<D>(decltype(tt)::value);
+        if constexpr (T.level <= ISO) {
+          constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2], tw = T.w;
+          R v[S];
+          rho_at<S>(rho, h.template at<ex, ey, ez>(), v);
+          sfor<0, D>([&](auto dd) {
+            constexpr int d = decltype(dd)::value;
+            constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
+            if constexpr (e != 0) {
+              const R coef = R(e) * P.ffw[tw];
+#pragma unroll
+              for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * v[m];
+            }
+          });
+        }
+      });
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        R q[S];
+#pragma unroll
+        for (int m = 0; m < S; ++m) q[m] = gr[m][d] * P.inv_ws_full[d];
+#pragma unroll
+        for (int m = 0; m < S; ++m) {
+          R acc = R(0);
+#pragma unroll
+          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * q[k];
+          F[m][d] = F[m][d] - R(P.c0) * rf[m] * acc;
+        }
+      }
+      return;
+    }
+  }
   if (P.ff_on) {
     R gr[S][D];
     R ws[D];
@@ -410,13 +498,13 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
 
 // Load the site's populations (shifted storage adds w_n * rho0 back).
 template <int D, int S, class T, class R>
-__device__ __forceinline__ void load_pops(const T* f, long long N, long long idx, R rho0, R fv[S][Lat<D>::Q]) {
+__device__ __forceinline__ void load_pops(const T* f, long long N, unsigned c, R rho0, R fv[S][Lat<D>::Q]) {
   using L = Lat<D>;
 #pragma unroll
   for (int m = 0; m < S; ++m)
     sfor<0, L::Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
-      R v = R(St<T>::ld(f + ((long long)(m * L::Q + n)) * N + idx));
+      R v = R(St<T>::ld(f + ((long long)(m * L::Q + n)) * N + c));
       if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
       fv[m][n] = v;
     });
@@ -484,8 +572,7 @@ template <int D, int S, int ISO, bool EXACT, class R, class RT>
 __device__ __forceinline__ void cell_moments(const StepArgs& a, const PhysT<R>& P, int x, int y, int z, long long idx,
                                              const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
-#pragma unroll
-  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * a.g.n + idx]);
+  rho_at<S>(rho, (unsigned)idx, rf);
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
   cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, a.g.n, rf, F);
   cell_velocity<D, S, EXACT, R>(a, P, x, y, z, fv, rf, F, rc, up);
@@ -540,7 +627,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
-  const uint32_t links = __ldg(a.links + idx);
+  const unsigned c = (unsigned)idx;  // N < 2^31
+  const uint32_t links = __ldg(a.links + c);
   if (!(links & 1u)) return;  // wall site
   const long long N = a.g.n;
   const R rho0 = R(P.rho0);
@@ -550,8 +638,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
   R rf[S], F[S][D];
   {
     const RT* rho = reinterpret_cast<const RT*>(a.rho);
-#pragma unroll
-    for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
+    rho_at<S>(rho, c, rf);
     cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, N, rf, F);
   }
   const T* fin = reinterpret_cast<const T*>(a.fin);
@@ -563,7 +650,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       R f1[1][Q];
-      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, f1);
+      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, rho0, f1);
 #pragma unroll
       for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
       rc[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rf[m];
@@ -594,12 +681,12 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
     if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;  // w(opp n) == w(n): same shift
     T* dst;
     if constexpr (n == 0) {
-      dst = fout + (long long)(m * Q) * N + idx;
+      dst = fout + (long long)(m * Q) * N + c;
     } else {
       constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
       const bool pore = ((links >> n) & 1u) != 0u;
-      dst = pore ? fout + (long long)(m * Q + n) * N + h.template at<cx, cy, cz>()
-                 : fout + (long long)(m * Q + o) * N + idx;
+      T* const base = fout + (long long)(m * Q + (pore ? n : o)) * N;
+      dst = base + (pore ? h.template at<cx, cy, cz>() : c);
     }
     St<T>::st(dst, v);
   };
@@ -610,7 +697,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       R f[Q];
       {
         R fv1[1][Q];
-        load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, idx, rho0, fv1);
+        load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, rho0, fv1);
   #pragma unroll
         for (int n = 0; n < Q; ++n) f[n] = fv1[0][n];
       }
@@ -671,6 +758,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
     // Moments whose MRT rate differs from s0 are corrected afterwards.
     // WB_n = W~_n B_n is shared by the components.
     R WB[Q];
+    const R cu_axis = R(1.5 * L::w(1)) * usqr, cu_diag = R(1.5 * L::w(Q - 1)) * usqr;
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       if constexpr (n == 0) {
@@ -684,7 +772,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
           if constexpr (c < 0) ud = ud - up[d];
         });
         constexpr double w = L::w(n);
-        WB[n] = ud * (R(3 * w) + R(4.5 * w) * ud) - R(1.5 * w) * usqr;
+        WB[n] = ud * (R(3 * w) + R(4.5 * w) * ud) - (n <= L::NAXIS ? cu_axis : cu_diag);
       }
     });
 #pragma unroll
@@ -705,7 +793,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       }
       const R G = s0 * r - k * Fu;
       const unsigned spec = P.spec_mask[m];
-      const T* fm = fin + (long long)m * Q * N + idx;
+      const T* fm = fin + (long long)m * Q * N;
       auto E_of = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
         if constexpr (n == 0) return A0 + WB[0];
@@ -713,7 +801,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
       };
       auto pop = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
-        R f = R(St<T>::ld(fm + (long long)n * N));
+        R f = R(St<T>::ld(fm + (long long)n * N + c));
         if constexpr (kShifted<T>) f = f + R(L::w(n)) * rho0;
         return f;
       };
@@ -857,7 +945,8 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
-  if (__ldg(a.mask + idx) != 0) return;
+  const unsigned c = (unsigned)idx;  // N < 2^31
+  if (__ldg(a.mask + c) != 0) return;
   const long long N = a.g.n;
   const R rho0 = R(P.rho0);
   RT* rho = reinterpret_cast<RT*>(a.rho);
@@ -869,16 +958,16 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
       R acc = R(0);
       sfor<0, Q>([&](auto nn) {
         constexpr int n = decltype(nn)::value;
-        R v = R(St<T>::ld(fcur + (long long)(m * Q + n) * N + idx));
+        R v = R(St<T>::ld(fcur + (long long)(m * Q + n) * N + c));
         if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
         acc = acc + v;
       });
-      rho[(long long)m * N + idx] = RT(acc);
+      rho[(size_t)c * S + m] = RT(acc);
     }
     return;
   }
   R fv[S][Q];
-  load_pops<D, S, T, R>(fcur, N, idx, rho0, fv);
+  load_pops<D, S, T, R>(fcur, N, c, rho0, fv);
   R rf[S];
   const unsigned hit = face_bits(a.faces) & site_faces(a.g, x, y, z);
   sfor<0, 2 * D>([&](auto ff) {
@@ -896,12 +985,12 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   });
 #pragma unroll
   for (int m = 0; m < S; ++m) {
-    rho[(long long)m * N + idx] = RT(rf[m]);
+    rho[(size_t)c * S + m] = RT(rf[m]);
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       R v = fv[m][n];
       if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
-      St<T>::st(fcur + (long long)(m * Q + n) * N + idx, v);
+      St<T>::st(fcur + (long long)(m * Q + n) * N + c, v);
     });
   }
 }
@@ -923,8 +1012,7 @@ __global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) 
   const long long N = a.g.n;
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
   R rf[S], F[S][D];
-#pragma unroll
-  for (int m = 0; m < S; ++m) rf[m] = R(rho[(long long)m * N + idx]);
+  rho_at<S>(rho, (unsigned)idx, rf);
   {
     const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
     cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, N, rf, F);
@@ -972,7 +1060,7 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
   }
   const long long N = a.g.n;
   R fv[S][Q];
-  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, idx, R(P.rho0), fv);
+  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, (unsigned)idx, R(P.rho0), fv);
   R rc[S], rf[S], F[S][D], up[D];
   cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
   if (what == 2) {

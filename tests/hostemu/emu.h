@@ -127,7 +127,7 @@ std::string run(const Case& c, Result& out) {
   } else {
     for (long long i = 0; i < N; ++i)
       for (int m = 0; m < S; ++m)
-        rho[(size_t)(m * N + i)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] : 0.0);
+        rho[(size_t)(i * S + m)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] : 0.0);
     const StepArgs a = args(cur, cur);
     launch3(g, 128, [&] { k_init<D, S, ISO, EXACT, T, R, RT>(a, nullptr); });
   }

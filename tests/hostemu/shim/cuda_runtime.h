@@ -17,6 +17,13 @@ struct dim3 {
 };
 inline dim3 threadIdx, blockIdx, blockDim, gridDim;
 
+struct float2 {
+  float x, y;
+};
+struct alignas(16) double2 {
+  double x, y;
+};
+
 template <class T>
 inline T __ldg(const T* p) {
   return *p;
