@@ -194,8 +194,65 @@ int tx_sync(tx_handle* h);
 int tx_step_static(const tx_params* p, const double* walls, const double* fi_in, double* fi_out, int32_t nsteps,
                    void* stream);
 
-/* ---- instrumentation (no counterpart in the reference; used by bench.py) ---- */
 
+/* ------------------------------------------------------------ batches
+ * Many independent lattices of one kernel form, stepped together by
+ * persistent tile-table launches that are replayed as a CUDA graph.  There is
+ * no counterpart in the reference, which runs one lattice per process; these
+ * entry points serve batched permeability runs and the request server.
+ * A batch owns one CUDA stream; every call is synchronous with respect to the
+ * host unless stated.  Lattice ids are assigned by tx_batch_add and never
+ * reused within a batch. */
+typedef struct tx_batch tx_batch;
+
+/* Velocity statistics of one lattice from tx_batch_probe, over pore sites:
+ * the largest change of any velocity component since the previous probe
+ * (the first probe compares with zero), the largest component, the sum of
+ * each component, the pore-site count and the steps taken so far. */
+typedef struct {
+  int32_t id;
+  int32_t pad_;
+  double du_max;
+  double u_max;
+  double u_sum[3];
+  int64_t pore_sites;
+  int64_t steps;
+} tx_probe;
+
+/* form: discretization, ncomponents, relaxation_mode, isotropy_order and
+ * precision shared by every lattice of the batch (exact must be 0).
+ * hbm_budget_bytes > 0 caps the device memory of all lattices together;
+ * tx_batch_add fails with TX_ERR_NOMEM above it. */
+int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** out);
+int tx_batch_destroy(tx_batch* b);
+const char* tx_batch_last_error(const tx_batch* b);
+/* device bytes one lattice with these parameters occupies in a batch */
+int64_t tx_batch_lattice_bytes(const tx_params* p);
+int64_t tx_batch_bytes_in_use(const tx_batch* b);
+int32_t tx_batch_count(const tx_batch* b);
+
+/* Adds a lattice (walls and initial state as tx_upload_walls + tx_upload_state,
+ * then tx_init) and returns its id.  It joins the next step of the batch. */
+int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const double* rho, const double* u,
+                 int32_t* id);
+int tx_batch_remove(tx_batch* b, int32_t id);
+/* nsteps flow steps of every lattice in the batch */
+int tx_batch_step(tx_batch* b, int32_t nsteps);
+/* Probes every lattice; writes up to cap records, *n = lattices probed. */
+int tx_batch_probe(tx_batch* b, int32_t cap, tx_probe* out, int32_t* n);
+/* a field of one lattice, as tx_download */
+int tx_batch_download(tx_batch* b, int32_t id, int32_t field, double* out);
+/* tile shape (bx*by*bz must be 128; bz = 1 for D2Q9) and persistent blocks per SM */
+int tx_batch_set_tiles(tx_batch* b, int32_t bx, int32_t by, int32_t bz, int32_t blocks_per_sm);
+/* Times the candidate tile shapes and grid sizes on the lattices in the batch
+ * (steps_per_trial steps each; these are real steps of every lattice) and
+ * keeps the fastest; chosen = {bx, by, bz, blocks_per_sm}. */
+int tx_batch_tune(tx_batch* b, int32_t steps_per_trial, int32_t* chosen);
+/* steps per captured graph (even, >= 2); 0 launches every step directly */
+int tx_batch_set_graph(tx_batch* b, int32_t steps_per_graph);
+void* tx_batch_stream(tx_batch* b);
+
+/* ---- instrumentation (no counterpart in the reference; used by bench.py) ---- */
 /* Per-kernel CUDA-event timing of tx_step on the handle's stream (resets the totals). */
 int tx_set_timing(tx_handle* h, int32_t on);
 

@@ -1,0 +1,137 @@
+// Batched flow step: many independent lattices advanced by one persistent
+// launch per kernel.
+//
+// The lattices of a batch share one kernel form (dimension, components,
+// isotropy, relaxation, storage) but each has its own size, walls, physical
+// parameters and boundary faces.  A tile table lists (lattice, tile origin)
+// for every tile of every active lattice; a tile is one thread block
+// (bx, by, bz).  A fixed grid of persistent blocks walks the table, so the
+// launch configuration never changes when lattices join or leave: the table
+// and its length live in device memory, which is what lets the host capture
+// the step loop once in a CUDA graph and keep replaying it while the table is
+// rewritten between replays.
+//
+// Every site is updated by the same per-site functions as the single-lattice
+// kernels (step_site, density_site), so a lattice's populations do not depend
+// on the tile shape, on the other lattices or on the launch.
+//
+// All lattices of a batch step in lockstep.  flip selects the ping-pong
+// buffer: at flip 0 a lattice's state is in LatDesc::a.fin, at flip 1 in
+// LatDesc::a.fout.
+#pragma once
+#include "tx_kernels.cuh"
+
+namespace tx {
+
+struct LatDesc {
+  StepArgs a;         // fin: state buffer at flip 0; fout: the other buffer
+  double* uold;       // velocity at the previous probe, [d * N + cell]
+  int tile_begin;     // this lattice's tiles in the table
+  int tile_count;
+};
+
+// per-tile partial of a probe: velocity change and velocity statistics over pore sites
+struct ProbePart {
+  double du;          // max over sites and axes of |u - u_old|
+  double umax;        // max over sites and axes of |u|
+  double usum[3];     // sum of u per axis
+  double npore;       // pore sites
+};
+
+struct BatchArgs {
+  const LatDesc* lats;
+  const int4* tiles;  // (lattice slot, x0, y0, z0)
+  const int* ntiles;  // table length (device memory: may change between graph replays)
+  ProbePart* parts;   // [tile]
+};
+
+__device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
+  StepArgs a = s;
+  if (flip) {
+    a.fin = s.fout;
+    a.fout = const_cast<void*>(s.fin);
+  }
+  return a;
+}
+
+template <int D, int S, int ISO, bool MRT, class T, class R, class RT>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1) k_step_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.ntiles);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.tiles + t);
+    const StepArgs a = flipped(b.lats[tl.x].a, flip);
+    const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    if (x < a.g.nx && y < a.g.ny && z < a.g.nz) step_site<D, S, ISO, MRT, false, T, R, RT>(a, x, y, z);
+  }
+}
+
+// after k_step_tiles at the same flip: the pushed populations are in a.fout
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_density_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.ntiles);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.tiles + t);
+    const StepArgs a = flipped(b.lats[tl.x].a, flip);
+    const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    if (x < a.g.nx && y < a.g.ny && z < a.g.nz) density_site<D, S, T, R, RT>(a, x, y, z, 0);
+  }
+}
+
+// Velocity of every pore site (the common velocity of FlowUpdateUED3/D2,
+// forces included) against the previous probe; one ProbePart per tile,
+// reduced in a fixed order so that the result depends only on the lattice.
+template <int D, int S, int ISO, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
+  __shared__ double red[4][6];
+  const int nt = __ldg(b.ntiles);
+  const int tid = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.tiles + t);
+    const LatDesc& L = b.lats[tl.x];
+    const StepArgs a = flipped(L.a, flip);
+    const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // du, umax, usum x/y/z, npore
+    if (x < a.g.nx && y < a.g.ny && z < a.g.nz) {
+      const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * z);
+      if (__ldg(a.mask + idx) == 0) {
+        const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
+        R fv[S][Lat<D>::Q];
+        load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), a.g.n, (unsigned)idx, R(P.rho0), fv);
+        R rc[S], rf[S], F[S][D], up[D];
+        cell_moments<D, S, ISO, false, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double u = double(up[d]);
+          double* uo = L.uold + (long long)d * a.g.n + idx;
+          v[0] = fmax(v[0], fabs(u - *uo));
+          v[1] = fmax(v[1], fabs(u));
+          v[2 + d] = u;
+          *uo = u;
+        }
+        v[5] = 1.0;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v[0] = fmax(v[0], __shfl_xor_sync(0xffffffffu, v[0], o));
+      v[1] = fmax(v[1], __shfl_xor_sync(0xffffffffu, v[1], o));
+#pragma unroll
+      for (int k = 2; k < 6; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+    if (lane == 0)
+      for (int k = 0; k < 6; ++k) red[warp][k] = v[k];
+    __syncthreads();
+    if (tid == 0) {
+      ProbePart p;
+      p.du = fmax(fmax(red[0][0], red[1][0]), fmax(red[2][0], red[3][0]));
+      p.umax = fmax(fmax(red[0][1], red[1][1]), fmax(red[2][1], red[3][1]));
+      for (int d = 0; d < 3; ++d) p.usum[d] = ((red[0][2 + d] + red[1][2 + d]) + red[2][2 + d]) + red[3][2 + d];
+      p.npore = ((red[0][5] + red[1][5]) + red[2][5]) + red[3][5];
+      b.parts[t] = p;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace tx

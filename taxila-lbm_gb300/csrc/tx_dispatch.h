@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tx_batch.cuh"
 #include "tx_host_params.h"
 #include "tx_kernels.cuh"
 
@@ -16,6 +17,10 @@ struct KernelSet {
   void (*moments)(const StepArgs&, int what, double* out, cudaStream_t);
   void (*to_natural)(const void* f, const uint8_t* mask, long long N, double rho0, double* out, cudaStream_t);
   void (*from_natural)(const double* in, const uint8_t* mask, long long N, double rho0, void* f, cudaStream_t);
+  // batched (persistent, tile-table) kernels; no-ops in the exact FP64 form
+  void (*step_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
+  void (*density_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
+  void (*probe_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   const char* name;
 };
 
@@ -79,6 +84,15 @@ inline Launch3 launch3(const Geo& g, int threads) {
     static void from_nat(const double* i, const uint8_t* m, long long N, double r0, void* f, cudaStream_t s) { \
       k_pops_from_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(i, m, N, r0, reinterpret_cast<T*>(f)); \
     }                                                                                                         \
+    static void step_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {                \
+      if constexpr (!EXACT) k_step_tiles<D, S, ISO, MRT, T, R, RT><<<grid, blk, 0, s>>>(b, flip);             \
+    }                                                                                                         \
+    static void density_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {             \
+      if constexpr (!EXACT) k_density_tiles<D, S, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                    \
+    }                                                                                                         \
+    static void probe_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {               \
+      if constexpr (!EXACT) k_probe_tiles<D, S, ISO, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                 \
+    }                                                                                                         \
   };
 
 #define TX_FORM_CASE(S, ISO, MRT) TX_FORM_CASE_(S, ISO, MRT)
@@ -86,6 +100,8 @@ inline Launch3 launch3(const Geo& g, int threads) {
   if (s == S && iso == ISO && mrt == MRT) {                                                                    \
     *ks = KernelSet{&L_##S##_##ISO##_##MRT::step,   &L_##S##_##ISO##_##MRT::density,                           \
                     &L_##S##_##ISO##_##MRT::init,   &L_##S##_##ISO##_##MRT::moments,                           \
-                    &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat, #S "c iso" #ISO " mrt" #MRT}; \
+                    &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat,                          \
+                    &L_##S##_##ISO##_##MRT::step_tiles, &L_##S##_##ISO##_##MRT::density_tiles,                 \
+                    &L_##S##_##ISO##_##MRT::probe_tiles, #S "c iso" #ISO " mrt" #MRT};                         \
     return true;                                                                                               \
   }

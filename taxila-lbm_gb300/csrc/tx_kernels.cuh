@@ -619,14 +619,11 @@ __device__ __forceinline__ void feq_pf(const PhysT<R>& P, int m, R r, const R u[
 // Each kernel copies its StepArgs parameter into a local before use; the
 // helpers take references to that copy, never to the parameter itself.
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1) k_step(StepArgs a_in) {
+__device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
-  int x, y, z;
-  long long idx;
-  if (!site_of(a.g, x, y, z, idx)) return;
+  const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * (long long)z);
   const unsigned c = (unsigned)idx;  // N < 2^31
   const uint32_t links = __ldg(a.links + c);
   if (!(links & 1u)) return;  // wall site
@@ -864,6 +861,15 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1)
   }
 }
 
+template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1) k_step(StepArgs a_in) {
+  const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
+  step_site<D, S, ISO, MRT, EXACT, T, R, RT>(a, x, y, z);
+}
+
 // Link masks of every site from the wall mask (see link_of).
 template <int D>
 __global__ void __launch_bounds__(256) k_links(const uint8_t* mask, Geo g, uint32_t* links) {
@@ -937,14 +943,11 @@ __device__ __forceinline__ void dirichlet_node(int f, const R pv[S], R fv[S][Lat
 // (BCApplyDirichletToRho, :252-434) on face nodes, sum of populations elsewhere.
 // mode 1 (FlowUpdateMoments at init, lbm_flow.F90:466-478): plain sums.
 template <int D, int S, class T, class R, class RT>
-__global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
+__device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, int z, int mode) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
-  int x, y, z;
-  long long idx;
-  if (!site_of(a.g, x, y, z, idx)) return;
+  const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * (long long)z);
   const unsigned c = (unsigned)idx;  // N < 2^31
   if (__ldg(a.mask + c) != 0) return;
   const long long N = a.g.n;
@@ -995,19 +998,25 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   }
 }
 
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
+  const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
+  density_site<D, S, T, R, RT>(a, x, y, z, mode);
+}
+
 // -------------------------------------------------------------------- init
 // FlowFiInit (lbm_flow.F90:923-934): forces from the initial density, the
 // equilibrium at the initial velocity, f = (1 - P/2) feq (FlowFeqBarD3/D2).
 // uic is [(m*D + d) * N + cell]; rho holds the initial density.
 template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) {
+__device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z, const double* uic) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
-  int x, y, z;
-  long long idx;
-  if (!site_of(a.g, x, y, z, idx)) return;
+  const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * (long long)z);
   if (__ldg(a.mask + idx) != 0) return;
   const long long N = a.g.n;
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
@@ -1039,19 +1048,25 @@ __global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) 
   }
 }
 
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_init(StepArgs a_in, const double* uic) {
+  const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
+  init_site<D, S, ISO, EXACT, T, R, RT>(a, x, y, z, uic);
+}
+
 // -------------------------------------------------------------- downloads
 // Fields of the current state in natural order (component fastest).
 // what: 2 rho, 3 flux (common velocity), 4 forces, 5 prs, 6 velt, 7 rhot
 // (FlowUpdateDiagnosticsD3/D2, lbm_flow.F90:654-758, for psi = rho).
 template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double* out) {
+__device__ __forceinline__ void moments_site(const StepArgs& a, int x, int y, int z, int what, double* out) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const StepArgs a = a_in;  // local copy: helpers below never address the kernel parameter
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
-  int x, y, z;
-  long long idx;
-  if (!site_of(a.g, x, y, z, idx)) return;
+  const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * (long long)z);
   const bool wall = __ldg(a.mask + idx) != 0;
   const int dof = what == 2 ? S : (what == 3 || what == 4) ? S * D : (what == 6 ? D : 1);
   if (wall) {
@@ -1091,6 +1106,15 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
       }
     }
   }
+}
+
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double* out) {
+  const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
+  moments_site<D, S, ISO, EXACT, T, R, RT>(a, x, y, z, what, out);
 }
 
 // Natural-order populations <-> SoA state.

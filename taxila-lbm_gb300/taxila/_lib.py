@@ -16,6 +16,12 @@ LIB_PATH = os.path.join(PKG_ROOT, "libtaxila_gb300.so")
 _lib = None
 
 
+class TxProbe(C.Structure):
+    """tx_probe of include/taxila_gb300.h."""
+    _fields_ = [("id", C.c_int32), ("pad_", C.c_int32), ("du_max", C.c_double), ("u_max", C.c_double),
+                ("u_sum", C.c_double * 3), ("pore_sites", C.c_int64), ("steps", C.c_int64)]
+
+
 class TxError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s: %s" % (P.ERR_NAMES.get(code, "TX_ERR_%d" % code), msg))
@@ -52,6 +58,21 @@ def load():
         "tx_get_stream": ([vp], vp),
         "tx_kernel_name": ([vp], C.c_char_p),
         "tx_step_static": ([C.POINTER(P.TxParams), vp, vp, vp, i32, vp], C.c_int),
+        "tx_batch_create": ([C.POINTER(P.TxParams), i64, C.POINTER(vp)], C.c_int),
+        "tx_batch_destroy": ([vp], C.c_int),
+        "tx_batch_last_error": ([vp], C.c_char_p),
+        "tx_batch_lattice_bytes": ([C.POINTER(P.TxParams)], i64),
+        "tx_batch_bytes_in_use": ([vp], i64),
+        "tx_batch_count": ([vp], i32),
+        "tx_batch_add": ([vp, C.POINTER(P.TxParams), dp, dp, dp, C.POINTER(i32)], C.c_int),
+        "tx_batch_remove": ([vp, i32], C.c_int),
+        "tx_batch_step": ([vp, i32], C.c_int),
+        "tx_batch_probe": ([vp, i32, C.POINTER(TxProbe), C.POINTER(i32)], C.c_int),
+        "tx_batch_download": ([vp, i32, i32, dp], C.c_int),
+        "tx_batch_set_tiles": ([vp, i32, i32, i32, i32], C.c_int),
+        "tx_batch_tune": ([vp, i32, C.POINTER(i32)], C.c_int),
+        "tx_batch_set_graph": ([vp, i32], C.c_int),
+        "tx_batch_stream": ([vp], vp),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -158,3 +179,82 @@ class Handle:
 
     def kernel_name(self):
         return self.L.tx_kernel_name(self.h).decode()
+
+
+class Batch:
+    """One tx_batch: many lattices of one kernel form stepped together."""
+
+    def __init__(self, form, hbm_budget_bytes=0):
+        self.L = load()
+        self.form = P.copy_params(form)
+        b = C.c_void_p()
+        rc = self.L.tx_batch_create(C.byref(self.form), int(hbm_budget_bytes), C.byref(b))
+        if rc:
+            raise TxError(rc, self.L.tx_last_error(None).decode())
+        self.b = b
+
+    def _check(self, rc):
+        if rc:
+            raise TxError(rc, self.L.tx_batch_last_error(self.b).decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.tx_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def lattice_bytes(params):
+        p = P.copy_params(params)
+        return load().tx_batch_lattice_bytes(C.byref(p))
+
+    def bytes_in_use(self):
+        return self.L.tx_batch_bytes_in_use(self.b)
+
+    def count(self):
+        return self.L.tx_batch_count(self.b)
+
+    def add(self, params, walls, rho, u=None):
+        p = P.copy_params(params)
+        w, r, v = f64(walls), f64(rho), f64(u)
+        lid = C.c_int32()
+        self._check(self.L.tx_batch_add(self.b, C.byref(p), dptr(w), dptr(r), dptr(v), C.byref(lid)))
+        return lid.value
+
+    def remove(self, lid):
+        self._check(self.L.tx_batch_remove(self.b, int(lid)))
+
+    def step(self, n=1):
+        self._check(self.L.tx_batch_step(self.b, int(n)))
+
+    def probe(self):
+        """{id: TxProbe} for every lattice in the batch."""
+        cap = max(1, self.count())
+        arr = (TxProbe * cap)()
+        n = C.c_int32()
+        self._check(self.L.tx_batch_probe(self.b, cap, arr, C.byref(n)))
+        return {arr[i].id: arr[i] for i in range(min(n.value, cap))}
+
+    def download(self, lid, field, size):
+        out = np.empty(size, dtype=np.float64)
+        self._check(self.L.tx_batch_download(self.b, int(lid), int(field), dptr(out)))
+        return out
+
+    def set_tiles(self, bx, by, bz, blocks_per_sm):
+        self._check(self.L.tx_batch_set_tiles(self.b, bx, by, bz, blocks_per_sm))
+
+    def tune(self, steps_per_trial=4):
+        ch = (C.c_int32 * 4)()
+        self._check(self.L.tx_batch_tune(self.b, int(steps_per_trial), ch))
+        return tuple(ch)
+
+    def set_graph(self, steps_per_graph):
+        self._check(self.L.tx_batch_set_graph(self.b, int(steps_per_graph)))
+
+    def stream(self):
+        return self.L.tx_batch_stream(self.b)

@@ -103,3 +103,25 @@ PARITY = [
     ("d2_porous_dirichlet", lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), 30),
     ("d3_single_component_porous", lambda: porous_case(P.D3Q19, (10, 12, 14), ncomp=1, body=True), 20),
 ]
+
+
+def permeability_case(shape, seed=11, porosity=0.45, rmin=2.0, rmax=4.0, precision=P.PREC_F64, gz=1e-5):
+    """Single-phase D3Q19 BGK (tau = 1) periodic sphere pack driven by a body
+    force along z: the batched permeability workload at test size."""
+    p = base(P.D3Q19, shape, ncomp=1, mode=P.SRT, iso=4)
+    p.tau[0] = 1.0
+    p.nminerals = 1
+    p.body_forces = 1
+    p.gvt[2] = gz
+    p.precision = precision
+    p.rho0 = 1.0
+    solid = problems.sphere_pack(p.shape, porosity, rmin, rmax, seed, periodic=True)
+    walls = np.where(solid.ravel(), 1.0, 0.0)
+    rho = np.ones(p.nsites)
+    return p, walls, rho
+
+
+def permeability(p, u_sum_z, nsites):
+    """k = nu <u_z> phi / g, with <u_z> phi = sum of u_z over pore sites / all sites."""
+    nu = (p.tau[0] - 0.5) / 3.0
+    return nu * (u_sum_z / nsites) / p.gvt[2]
