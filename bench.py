@@ -64,7 +64,7 @@ def workload_params(precision=P.PREC_F64, n=N_SIDE):
     p.s_nu[0], p.s_nu[1] = 1.0 / 1.0, 1.0 / 0.7
     p.g[0][1] = p.g[1][0] = 0.9 / 6.0
     p.precision = precision
-    p.rho0 = 1.0
+    p.rho0[0] = p.rho0[1] = 0.0  # two phases: plain storage of the populations
     return p
 
 

@@ -63,8 +63,8 @@ extern "C" {
 
 /* storage/arithmetic forms */
 #define TX_PREC_F64 0      /* plain form: FP64 populations and arithmetic */
-#define TX_PREC_F32 1      /* FP32 arithmetic, FP32 populations stored as f - w_n*rho0 */
-#define TX_PREC_F32_F16 2  /* FP32 arithmetic, FP16 populations stored as f - w_n*rho0 */
+#define TX_PREC_F32 1      /* FP32 arithmetic, FP32 populations stored as f - w_n*rho0[m] */
+#define TX_PREC_F32_F16 2  /* FP32 arithmetic, FP16 populations stored as (f - w_n*rho0[m]) * storage_scale */
 
 /* fields for tx_download / tx_delta_norm */
 #define TX_FIELD_FI 1      /* s*Q dof: populations after the step (reference fi)          */
@@ -111,7 +111,11 @@ typedef struct tx_params {
                                single precision, as built without -fdefault-real-8; 8: double */
   int32_t precision;        /* TX_PREC_* */
   int32_t exact;            /* 1: reference operation order, IEEE divides, no FMA (FP64 only) */
-  double rho0;              /* reference density of the shifted storage (precision forms) */
+  double rho0[TX_MAX_COMPONENTS]; /* precision forms: per-component rest density rho0 of the
+                               deviation storage f - w_n*rho0 (0 = plain storage; pick the density
+                               the component mostly has, e.g. 1 for single-phase flow) */
+  double storage_scale;     /* FP16 form: populations stored as (f - w_n*rho0) * storage_scale
+                               (a power of two keeps the scaling exact; 0 = 1) */
 } tx_params;
 
 typedef struct tx_handle tx_handle;

@@ -149,7 +149,7 @@ int sync_stream(tx_handle* h) {
 int stage_field(tx_handle* h, int field) {
   const long long N = h->g.n;
   if (field == TX_FIELD_FI) {
-    h->ks.to_natural(h->f[h->cur], h->mask, N, h->ph.rho0, h->stage, h->stream);
+    h->ks.to_natural(h->f[h->cur], h->mask, N, shift_of(h->ph), h->stage, h->stream);
   } else if (field == TX_FIELD_WALLS) {
     return TX_ERR_ARG;
   } else {
@@ -198,7 +198,8 @@ int tx_params_default(tx_params* p) {
   }
   p->literal_kind = 4;
   p->precision = TX_PREC_F64;
-  p->rho0 = 1.0;
+  for (int m = 0; m < TX_MAX_COMPONENTS; ++m) p->rho0[m] = 0.0;
+  p->storage_scale = 1.0;
   return TX_OK;
 }
 
@@ -324,10 +325,11 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
   if (!h || !rho) return TX_ERR_ARG;
   const long long N = h->g.n;
   const int S = h->S, D = h->D;
-  // rho: natural order (component fastest, the device layout too), zero on walls
+  // rho - rho0: natural order (component fastest, the device layout too), zero on walls
   std::vector<double> rt((size_t)N * S);
   for (long long i = 0; i < N; ++i)
-    for (int m = 0; m < S; ++m) rt[(size_t)(i * S + m)] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] : 0.0;
+    for (int m = 0; m < S; ++m)
+      rt[(size_t)(i * S + m)] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] - h->ph.rho0[m] : 0.0;
   if (h->rho_bytes == 8) {
     TX_CUDA(h, cudaMemcpyAsync(h->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, h->stream));
     TX_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -357,7 +359,7 @@ int tx_upload_fi(tx_handle* h, const double* fi) {
   const long long N = h->g.n;
   const size_t bytes = (size_t)N * h->S * h->Q * sizeof(double);
   TX_CUDA(h, cudaMemcpyAsync(h->stage, fi, bytes, cudaMemcpyHostToDevice, h->stream));
-  h->ks.from_natural(h->stage, h->mask, N, h->ph.rho0, h->f[h->cur], h->stream);
+  h->ks.from_natural(h->stage, h->mask, N, shift_of(h->ph), h->f[h->cur], h->stream);
   int rc = check_launch(h, "k_pops_from_natural");
   if (rc) return rc;
   h->have_fi = true;

@@ -261,7 +261,7 @@ void free_lattice(tx_batch* b, Lattice* L) {
 int stage(tx_batch* b, const Lattice* L, int field, double* out) {
   const long long N = L->g.n;
   if (field == TX_FIELD_FI) {
-    b->ks.to_natural(L->f[b->flip], L->mask, N, L->ph.rho0, out, b->stream);
+    b->ks.to_natural(L->f[b->flip], L->mask, N, shift_of(L->ph), out, b->stream);
   } else {
     const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
                    : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : 7;
@@ -397,7 +397,7 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   }
   std::vector<double> rt((size_t)N * S);
   for (long long i = 0; i < N; ++i)
-    for (int m = 0; m < S; ++m) rt[(size_t)(i * S + m)] = mask[(size_t)i] == 0 ? rho[i * S + m] : 0.0;
+    for (int m = 0; m < S; ++m) rt[(size_t)(i * S + m)] = mask[(size_t)i] == 0 ? rho[i * S + m] - L->ph.rho0[m] : 0.0;
   std::vector<float> rt32;
   if (rho_bytes(p->precision) == 4) rt32.assign(rt.begin(), rt.end());
   std::vector<double> ut;

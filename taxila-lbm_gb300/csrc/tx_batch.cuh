@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
       if (__ldg(a.mask + idx) == 0) {
         const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
         R fv[S][Lat<D>::Q];
-        load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), a.g.n, (unsigned)idx, R(P.rho0), fv);
+        load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), a.g.n, (unsigned)idx, P, fv);
         R rc[S], rf[S], F[S][D], up[D];
         cell_moments<D, S, ISO, false, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
 #pragma unroll

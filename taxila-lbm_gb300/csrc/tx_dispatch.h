@@ -15,8 +15,8 @@ struct KernelSet {
   void (*density)(const StepArgs&, int mode, cudaStream_t);
   void (*init)(const StepArgs&, const double* uic, cudaStream_t);
   void (*moments)(const StepArgs&, int what, double* out, cudaStream_t);
-  void (*to_natural)(const void* f, const uint8_t* mask, long long N, double rho0, double* out, cudaStream_t);
-  void (*from_natural)(const double* in, const uint8_t* mask, long long N, double rho0, void* f, cudaStream_t);
+  void (*to_natural)(const void* f, const uint8_t* mask, long long N, Shift sh, double* out, cudaStream_t);
+  void (*from_natural)(const double* in, const uint8_t* mask, long long N, Shift sh, void* f, cudaStream_t);
   // batched (persistent, tile-table) kernels; no-ops in the exact FP64 form
   void (*step_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   void (*density_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
@@ -78,11 +78,11 @@ inline Launch3 launch3(const Geo& g, int threads) {
     static void moments(const StepArgs& a, int what, double* out, cudaStream_t s) {                           \
       k_moments<D, S, ISO, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, what, out);               \
     }                                                                                                         \
-    static void to_nat(const void* f, const uint8_t* m, long long N, double r0, double* o, cudaStream_t s) {  \
-      k_pops_to_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, r0, o); \
+    static void to_nat(const void* f, const uint8_t* m, long long N, Shift sh, double* o, cudaStream_t s) {   \
+      k_pops_to_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, sh, o); \
     }                                                                                                         \
-    static void from_nat(const double* i, const uint8_t* m, long long N, double r0, void* f, cudaStream_t s) { \
-      k_pops_from_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(i, m, N, r0, reinterpret_cast<T*>(f)); \
+    static void from_nat(const double* i, const uint8_t* m, long long N, Shift sh, void* f, cudaStream_t s) { \
+      k_pops_from_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(i, m, N, sh, reinterpret_cast<T*>(f)); \
     }                                                                                                         \
     static void step_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {                \
       if constexpr (!EXACT) k_step_tiles<D, S, ISO, MRT, T, R, RT><<<grid, blk, 0, s>>>(b, flip);             \

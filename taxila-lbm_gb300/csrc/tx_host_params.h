@@ -36,6 +36,8 @@ inline int validate(const tx_params* p, std::string* why) {
                       : "isotropy_order must be 4, 8 or 10");
   if (p->precision < TX_PREC_F64 || p->precision > TX_PREC_F32_F16) return bad("unknown precision form");
   if (p->exact && p->precision != TX_PREC_F64) return bad("exact operation order exists for the FP64 form only");
+  if (!(p->storage_scale >= 0.0) || !std::isfinite(p->storage_scale) || p->storage_scale > 1e30)
+    return bad("storage_scale must be finite and >= 0");
   for (int a = 0; a < D; ++a) {
     const int lo = p->bc_flags[2 * a], hi = p->bc_flags[2 * a + 1];
     if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
@@ -48,6 +50,7 @@ inline int validate(const tx_params* p, std::string* why) {
     }
   }
   for (int m = 0; m < p->ncomponents; ++m) {
+    if (!std::isfinite(p->rho0[m])) return bad("rho0 must be finite");
     if (p->relaxation_mode == TX_RELAX_SRT && !(p->tau[m] > 0.0)) return bad("tau must be > 0");
     if (!(p->mm[m] > 0.0)) return bad("molecular masses must be > 0");
   }
@@ -135,7 +138,17 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
     for (int m = 0; m < S; ++m)
       if (std::fabs(p.gw[q][m]) > eps15) P.fs_on = 1;
   P.body_on = p.body_forces != 0;
-  P.rho0 = p.precision == TX_PREC_F64 ? 0.0 : p.rho0;
+  for (int m = 0; m < S; ++m) P.rho0[m] = p.precision == TX_PREC_F64 ? 0.0 : p.rho0[m];
+  P.sscale = p.precision == TX_PREC_F32_F16 && p.storage_scale > 0.0 ? p.storage_scale : 1.0;
+  for (int m = 0; m < S; ++m) {
+    const double mm = p.mm[m], rel = (mm - 1.0) / mm;  // 0 for unit mass
+    P.A0[m] = D == 3 ? P.dk[m] : (1.0 + 5.0 * P.dk[m]) / 6.0;
+    P.An[m] = 1.0 / mm;  // 1.5 (1 - dk)
+    P.cA[m][0] = (D == 3 ? 2.0 / 3.0 : 5.0 / 9.0) * rel * P.rho0[m];
+    P.cA[m][1] = -(D == 3 ? 1.0 / 18.0 : 1.0 / 9.0) * rel * P.rho0[m];
+    P.cA[m][2] = -(1.0 / 36.0) * rel * P.rho0[m];
+  }
+  P.inv_sscale = 1.0 / P.sscale;
 }
 
 // Reference wall value (lbm_walls.F90:151-177) -> device mask code:

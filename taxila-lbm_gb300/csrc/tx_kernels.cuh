@@ -22,7 +22,10 @@
 //   ISO    isotropy order 4, 8, 10      MRT  MRT (true) or BGK (false)
 //   EXACT  reference operation order: no FMA (its translation unit is built
 //          with --fmad=false), IEEE divides, the reference's expression shapes
-//   T      population storage type (double; float/half hold f - w_n*rho0)
+//   T      population storage type (double holds f; float holds f - w_n*rho0_m
+//          and half (f - w_n*rho0_m) * storage scale, the deviation from a
+//          per-component rest density, with the forcing density stored as
+//          rho - rho0_m)
 //   R      arithmetic type              RT   storage type of rho
 #pragma once
 #include <cuda_fp16.h>
@@ -61,7 +64,12 @@ struct PhysT {
   R c0, fs_w_axis, fs_w_diag;
   R srate[MAXC][19];       // MRT rate of moment k
   R srate_mmt[MAXC][19];   // rate / diag(M M^T)
-  R rho0;                  // shift of the reduced-precision storage
+  R rho0[MAXC];            // rest density of the deviation storage (0 in the FP64 form)
+  R sscale, inv_sscale;    // FP16 storage scale of the deviations (1 otherwise)
+  // equilibrium constants: feq_n = rho W~_n (A_n + B_n) with A_0 = A0, A_n = An
+  // (= 1/mm), and cA = (W~_n A_n - w_n) rho0 for the rest, axis and diagonal
+  // classes, evaluated exactly on the host (zero for unit molecular mass)
+  R A0[MAXC], An[MAXC], cA[MAXC][3];
   // fast form: relax every moment at s0, then correct the moments whose rate
   // differs (bit k of spec_mask) by dspec = (rate_k - s0) / diag(M M^T)_k
   R s0[MAXC];
@@ -81,7 +89,10 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   cp(a.gvt, b->gvt, 3); cp(a.ffw, b->ffw, 12);
   b->c0 = R(a.c0); b->fs_w_axis = R(a.fs_w_axis); b->fs_w_diag = R(a.fs_w_diag);
   cp(&a.srate[0][0], &b->srate[0][0], MAXC * 19); cp(&a.srate_mmt[0][0], &b->srate_mmt[0][0], MAXC * 19);
-  b->rho0 = R(a.rho0);
+  cp(a.rho0, b->rho0, MAXC);
+  cp(a.A0, b->A0, MAXC); cp(a.An, b->An, MAXC); cp(&a.cA[0][0], &b->cA[0][0], MAXC * 3);
+  b->sscale = R(a.sscale);
+  b->inv_sscale = R(a.inv_sscale);
   cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19); cp(a.inv_ws_full, b->inv_ws_full, 3);
   for (int m = 0; m < MAXC; ++m) b->spec_mask[m] = a.spec_mask[m];
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
@@ -91,6 +102,18 @@ struct Faces {
   int on[6];                // Dirichlet density face flags, XM..ZP
   const double* vals[6];    // [m * area + node], node in natural order of the tangential axes
 };
+
+// The deviation storage of a lattice for the natural-order conversions.
+struct Shift {
+  double rho0[MAXC];
+  double scale;
+};
+inline Shift shift_of(const PhysT<double>& P) {
+  Shift s{};
+  for (int m = 0; m < MAXC; ++m) s.rho0[m] = P.rho0[m];
+  s.scale = P.sscale;
+  return s;
+}
 
 struct StepArgs {
   const void* fin;
@@ -123,6 +146,22 @@ struct St<__half> {
 };
 template <class T>
 constexpr bool kShifted = !std::is_same<T, double>::value;
+
+// Population deviation f - w_n rho0 at p (the FP16 form divides the storage scale out).
+template <class T, class R>
+__device__ __forceinline__ R ld_dev(const T* p, const PhysT<R>& P) {
+  if constexpr (std::is_same<T, __half>::value)
+    return R(St<T>::ld(p)) * P.inv_sscale;
+  else
+    return R(St<T>::ld(p));
+}
+template <class T, class R>
+__device__ __forceinline__ void st_dev(T* p, R v, const PhysT<R>& P) {
+  if constexpr (std::is_same<T, __half>::value)
+    St<T>::st(p, v * P.sscale);
+  else
+    St<T>::st(p, v);
+}
 
 // The forcing density is stored component-fastest, rho[cell * S + m], so that
 // one vector load brings every component of a neighbour.
@@ -324,7 +363,7 @@ inline double full_weight_sum(int iso, const double ffw[12], int d) {
 // fast form counts them per weight class and multiplies once (wc).
 template <int D, int S, int ISO, bool EXACT, int TI, int RCH, class R, class RT>
 __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P, const uint8_t* mask,
-                                        const RT* rho, long long N, const R rf[S], R gr[S][D], R ws[D], int wc[12][D]) {
+                                        const RT* rho, long long N, const R rfd[S], R gr[S][D], R ws[D], int wc[12][D]) {
   constexpr FFTerm T = ffterm<D>(TI);
   if constexpr (T.level <= ISO) {
     constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2];
@@ -343,7 +382,7 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
       R dif[S];
       rho_at<S>(rho, pi, dif);
 #pragma unroll
-      for (int m = 0; m < S; ++m) dif[m] = dif[m] - rf[m];
+      for (int m = 0; m < S; ++m) dif[m] = dif[m] - rfd[m];
       sfor<0, D>([&](auto dd) {
         constexpr int d = decltype(dd)::value;
         constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
@@ -365,10 +404,11 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
 // FlowCalcForces (lbm_flow.F90:760-808) for one pore site: zero, then
 // fluid-solid (lbm_forcing.F90:1326-1421), body (:1440-1496) and the
 // wall-aware Shan-Chen term (:51-958 / :960-1299), in that order.
+// rfd: stored forcing density of the site (rho - rho0); rf: rho itself.
 template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT>
 __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P,
-                                            const uint8_t* mask, const RT* rho, long long N, const R rf[S],
-                                            R F[S][D]) {
+                                            const uint8_t* mask, const RT* rho, long long N, const R rfd[S],
+                                            const R rf[S], R F[S][D]) {
   using L = Lat<D>;
 #pragma unroll
   for (int m = 0; m < S; ++m)
@@ -463,7 +503,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
     }
     constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
     sfor<0, NT>([&](auto tt) {
-      ff_term<D, S, ISO, EXACT, decltype(tt)::value, RCH, R, RT>(h, links, P, mask, rho, N, rf, gr, ws, wc);
+      ff_term<D, S, ISO, EXACT, decltype(tt)::value, RCH, R, RT>(h, links, P, mask, rho, N, rfd, gr, ws, wc);
     });
     if constexpr (!EXACT) {
 #pragma unroll
@@ -496,17 +536,16 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
   }
 }
 
-// Load the site's populations (shifted storage adds w_n * rho0 back).
+// Load the site's population deviations f - w_n rho0 (f itself in the FP64 form).
 template <int D, int S, class T, class R>
-__device__ __forceinline__ void load_pops(const T* f, long long N, unsigned c, R rho0, R fv[S][Lat<D>::Q]) {
+__device__ __forceinline__ void load_pops(const T* f, long long N, unsigned c, const PhysT<R>& P,
+                                          R fv[S][Lat<D>::Q]) {
   using L = Lat<D>;
 #pragma unroll
   for (int m = 0; m < S; ++m)
     sfor<0, L::Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
-      R v = R(St<T>::ld(f + ((long long)(m * L::Q + n)) * N + c));
-      if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
-      fv[m][n] = v;
+      fv[m][n] = ld_dev<T, R>(f + ((long long)(m * L::Q + n)) * N + c, P);
     });
 }
 
@@ -536,19 +575,16 @@ __device__ __forceinline__ R pop_flux(const R fv[S][Lat<D>::Q], int m, int d0) {
   return acc;
 }
 
-// Moments of a pore site from its post-stream populations: the density of the
-// collision (rc: Dirichlet nodes re-summed as in BCUpdateRho, lbm_bc.F90:436-611),
-// forces, and the common velocity of FlowUpdateUED3/D2 (lbm_flow.F90:494-574).
 // Density of the collision (Dirichlet nodes re-summed as in BCUpdateRho,
 // lbm_bc.F90:436-611) and the common velocity of FlowUpdateUED3/D2
-// (lbm_flow.F90:494-574) from the post-stream populations and the forces.
+// (lbm_flow.F90:494-574) from the post-stream population deviations and the forces.
 template <int D, int S, bool EXACT, class R>
 __device__ __forceinline__ void cell_velocity(const StepArgs& a, const PhysT<R>& P, int x, int y, int z,
                                               const R fv[S][Lat<D>::Q], const R rf[S], const R F[S][D], R rc[S],
                                               R up[D]) {
   const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
 #pragma unroll
-  for (int m = 0; m < S; ++m) rc[m] = dn ? pop_sum<D, S, R>(fv, m) : rf[m];
+  for (int m = 0; m < S; ++m) rc[m] = dn ? P.rho0[m] + pop_sum<D, S, R>(fv, m) : rf[m];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     R num = R(0), den = R(0);
@@ -572,9 +608,12 @@ template <int D, int S, int ISO, bool EXACT, class R, class RT>
 __device__ __forceinline__ void cell_moments(const StepArgs& a, const PhysT<R>& P, int x, int y, int z, long long idx,
                                              const R fv[S][Lat<D>::Q], R rc[S], R rf[S], R F[S][D], R up[D]) {
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
-  rho_at<S>(rho, (unsigned)idx, rf);
+  R rfd[S];
+  rho_at<S>(rho, (unsigned)idx, rfd);
+#pragma unroll
+  for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
-  cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, a.g.n, rf, F);
+  cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, a.g.n, rfd, rf, F);
   cell_velocity<D, S, EXACT, R>(a, P, x, y, z, fv, rf, F, rc, up);
 }
 
@@ -616,8 +655,8 @@ __device__ __forceinline__ void feq_pf(const PhysT<R>& P, int m, R r, const R u[
 }
 
 // ------------------------------------------------------------------ step
-// Each kernel copies its StepArgs parameter into a local before use; the
-// helpers take references to that copy, never to the parameter itself.
+// One pore site of the step: forces, moments, collision, push.  The kernels
+// copy their StepArgs parameter into a local and pass references to that copy.
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
 __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z) {
   using L = Lat<D>;
@@ -628,29 +667,31 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   const uint32_t links = __ldg(a.links + c);
   if (!(links & 1u)) return;  // wall site
   const long long N = a.g.n;
-  const R rho0 = R(P.rho0);
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
 
   // forces first (they need only rho and the wall layout)
-  R rf[S], F[S][D];
+  R rfd[S], rf[S], F[S][D];
   {
     const RT* rho = reinterpret_cast<const RT*>(a.rho);
-    rho_at<S>(rho, c, rf);
-    cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, N, rf, F);
+    rho_at<S>(rho, c, rfd);
+#pragma unroll
+    for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
+    cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, N, rfd, rf, F);
   }
   const T* fin = reinterpret_cast<const T*>(a.fin);
-  // moments pass, one component's populations at a time
-  R rc[S], up[D];
+  // moments pass, one component's populations at a time; rcd = rc - rho0
+  R rc[S], rcd[S], up[D];
   {
     const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
     R jm[S][D];
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       R f1[1][Q];
-      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, rho0, f1);
+      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, P, f1);
 #pragma unroll
       for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
-      rc[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rf[m];
+      rcd[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rfd[m];
+      rc[m] = dn ? P.rho0[m] + rcd[m] : rf[m];
     }
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -675,7 +716,6 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   auto push = [&](auto nn, int m, R v) {
     constexpr int n = decltype(nn)::value;
     constexpr int o = opp<D>(n);
-    if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;  // w(opp n) == w(n): same shift
     T* dst;
     if constexpr (n == 0) {
       dst = fout + (long long)(m * Q) * N + c;
@@ -685,7 +725,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       T* const base = fout + (long long)(m * Q + (pore ? n : o)) * N;
       dst = base + (pore ? h.template at<cx, cy, cz>() : c);
     }
-    St<T>::st(dst, v);
+    st_dev<T, R>(dst, v, P);
   };
 
   if constexpr (EXACT) {
@@ -694,7 +734,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       R f[Q];
       {
         R fv1[1][Q];
-        load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, rho0, fv1);
+        load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, P, fv1);
   #pragma unroll
         for (int n = 0; n < Q; ++n) f[n] = fv1[0][n];
       }
@@ -750,9 +790,13 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     // Fast form, with c_s^2 = 1/3 and E_n = W~_n (A_m,n + B_n) (W~_0 = 1):
     //   feq_n   = rho E_n                      (B_n holds the velocity terms)
     //   P feq_n = 3 E_n (F.c_n - F.u)          (He forcing)
-    //   f'_n    = (1 - s0) f_n + E_n (s0 rho - k F.u + k F.c_n),  k = 3 - 1.5 s0
-    // i.e. f - s0 (f - feq + P feq / 2) + P feq, every moment relaxed at s0.
-    // Moments whose MRT rate differs from s0 are corrected afterwards.
+    //   f'_n    = (1 - s0) f_n + s0 feq_n + (3 - 1.5 s0) E_n (F.c_n - F.u),
+    // i.e. f - s0 (f - feq + P feq / 2) + P feq, every moment relaxed at s0;
+    // moments whose MRT rate differs from s0 are corrected afterwards.
+    // Everything is computed on deviations from the rest state, g = f - w rho0
+    // (rho0 = 0 in the FP64 form): g'_n = (1 - s0) g_n + s0 dE_n + k E_n (F.c_n - F.u)
+    // with dE_n = feq_n - w_n rho0 = W~A (rho - rho0) + W~B rho + (W~A - w) rho0,
+    // so that FP32 arithmetic keeps the precision of the small deviations.
     // WB_n = W~_n B_n is shared by the components.
     R WB[Q];
     const R cu_axis = R(1.5 * L::w(1)) * usqr, cu_diag = R(1.5 * L::w(Q - 1)) * usqr;
@@ -774,11 +818,10 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     });
 #pragma unroll
     for (int m = 0; m < S; ++m) {
-      const R r = rc[m];
-      const R dk = P.dk[m];
-      const R A0 = D == 3 ? dk : (R(1) + R(5) * dk) * R(1.0 / 6.0);
-      const R An = R(1.5) * (R(1) - dk);
-      const R WA_axis = R(L::w(1)) * An, WA_diag = R(L::w(Q - 1)) * An;
+      const R r = rc[m], rd = rcd[m];
+      // W~A per direction class (rest, axis, diagonal) and its offset from w
+      const R WA0 = P.A0[m], WA1 = R(L::w(1)) * P.An[m], WA2 = R(L::w(Q - 1)) * P.An[m];
+      const R cA0 = P.cA[m][0], cA1 = P.cA[m][1], cA2 = P.cA[m][2];
       const R s0 = P.s0[m];
       const R k = R(3) - R(1.5) * s0;
       const R keep = R(1) - s0;
@@ -788,19 +831,27 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         Fu = Fu + F[m][d] * up[d];
         kF[d] = k * F[m][d];
       }
-      const R G = s0 * r - k * Fu;
+      const R kFu = k * Fu;
       const unsigned spec = P.spec_mask[m];
       const T* fm = fin + (long long)m * Q * N;
-      auto E_of = [&](auto nn) -> R {
+      auto WA_of = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
-        if constexpr (n == 0) return A0 + WB[0];
-        else return (n <= L::NAXIS ? WA_axis : WA_diag) + WB[n];
+        return n == 0 ? WA0 : (n <= L::NAXIS ? WA1 : WA2);
+      };
+      auto E_of = [&](auto nn) -> R { return WA_of(nn) + WB[decltype(nn)::value]; };
+      // dE_n = feq_n - w_n rho0
+      auto dE_of = [&](auto nn) -> R {
+        constexpr int n = decltype(nn)::value;
+        if constexpr (kShifted<T>) {
+          const R cA = n == 0 ? cA0 : (n <= L::NAXIS ? cA1 : cA2);
+          return WA_of(nn) * rd + WB[n] * r + cA;
+        } else {
+          return E_of(nn) * r;
+        }
       };
       auto pop = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
-        R f = R(St<T>::ld(fm + (long long)n * N + c));
-        if constexpr (kShifted<T>) f = f + R(L::w(n)) * rho0;
-        return f;
+        return ld_dev<T, R>(fm + (long long)n * N + c, P);
       };
       // sum_d c_n,d v_d
       auto cdot = [&](auto nn, const R v[D]) -> R {
@@ -814,25 +865,31 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         });
         return acc;
       };
+      const R G = s0 * r - kFu;
+      auto relax = [&](auto nn, R g) -> R {
+        if constexpr (kShifted<T>)
+          return keep * g + s0 * dE_of(nn) + E_of(nn) * (cdot(nn, kF) - kFu);
+        else
+          return keep * g + E_of(nn) * (G + cdot(nn, kF));
+      };
       if (spec == 0u) {
         // every moment relaxes at s0 (BGK): one direction at a time
-        sfor<0, Q>([&](auto nn) {
-          const R f = pop(nn);
-          push(nn, m, keep * f + E_of(nn) * (G + cdot(nn, kF)));
-        });
+        sfor<0, Q>([&](auto nn) { push(nn, m, relax(nn, pop(nn))); });
       } else {
-        // deviation from the forced equilibrium: f - E_n (rho + 1.5 F.u - 1.5 F.c_n)
-        const R H = r + R(1.5) * Fu;
+        // deviation from the forced equilibrium: g - dE_n + 1.5 E_n (F.c_n - F.u)
         R hF[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
+        const R hFu = R(1.5) * Fu;
         R fo[Q], dfi[Q];
         sfor<0, Q>([&](auto nn) {
           constexpr int n = decltype(nn)::value;
-          const R f = pop(nn);
-          const R E = E_of(nn);
-          fo[n] = keep * f + E * (G + cdot(nn, kF));
-          dfi[n] = f - E * (H - cdot(nn, hF));
+          const R g = pop(nn);
+          fo[n] = relax(nn, g);
+          if constexpr (kShifted<T>)
+            dfi[n] = g - dE_of(nn) + E_of(nn) * (cdot(nn, hF) - hFu);
+          else
+            dfi[n] = g - E_of(nn) * (r + hFu - cdot(nn, hF));
         });
         sfor<0, Q>([&](auto kk) {
           constexpr int k = decltype(kk)::value;
@@ -951,26 +1008,30 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
   const unsigned c = (unsigned)idx;  // N < 2^31
   if (__ldg(a.mask + c) != 0) return;
   const long long N = a.g.n;
-  const R rho0 = R(P.rho0);
   RT* rho = reinterpret_cast<RT*>(a.rho);
   T* fcur = reinterpret_cast<T*>(a.fout);
   const bool dn = mode == 0 && any_dirichlet<D>(a.g, a.faces, x, y, z);
   if (!dn) {
+    // stored as rho - rho0 = sum_n (f_n - w_n rho0)
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       R acc = R(0);
       sfor<0, Q>([&](auto nn) {
         constexpr int n = decltype(nn)::value;
-        R v = R(St<T>::ld(fcur + (long long)(m * Q + n) * N + c));
-        if constexpr (kShifted<T>) v = v + R(L::w(n)) * rho0;
-        acc = acc + v;
+        acc = acc + ld_dev<T, R>(fcur + (long long)(m * Q + n) * N + c, P);
       });
       rho[(size_t)c * S + m] = RT(acc);
     }
     return;
   }
+  // Dirichlet nodes work on the populations themselves
   R fv[S][Q];
-  load_pops<D, S, T, R>(fcur, N, c, rho0, fv);
+  load_pops<D, S, T, R>(fcur, N, c, P, fv);
+  if constexpr (kShifted<T>) {
+#pragma unroll
+    for (int m = 0; m < S; ++m)
+      sfor<0, Q>([&](auto nn) { fv[m][decltype(nn)::value] += R(L::w(decltype(nn)::value)) * P.rho0[m]; });
+  }
   R rf[S];
   const unsigned hit = face_bits(a.faces) & site_faces(a.g, x, y, z);
   sfor<0, 2 * D>([&](auto ff) {
@@ -988,12 +1049,12 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
   });
 #pragma unroll
   for (int m = 0; m < S; ++m) {
-    rho[(size_t)c * S + m] = RT(rf[m]);
+    rho[(size_t)c * S + m] = RT(kShifted<T> ? rf[m] - P.rho0[m] : rf[m]);
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       R v = fv[m][n];
-      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
-      St<T>::st(fcur + (long long)(m * Q + n) * N + c, v);
+      if constexpr (kShifted<T>) v = v - R(L::w(n)) * P.rho0[m];
+      st_dev<T, R>(fcur + (long long)(m * Q + n) * N + c, v, P);
     });
   }
 }
@@ -1020,14 +1081,15 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
   if (__ldg(a.mask + idx) != 0) return;
   const long long N = a.g.n;
   const RT* rho = reinterpret_cast<const RT*>(a.rho);
-  R rf[S], F[S][D];
-  rho_at<S>(rho, (unsigned)idx, rf);
+  R rfd[S], rf[S], F[S][D];
+  rho_at<S>(rho, (unsigned)idx, rfd);
+#pragma unroll
+  for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
   {
     const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
-    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, N, rf, F);
+    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, N, rfd, rf, F);
   }
   T* fout = reinterpret_cast<T*>(a.fout);
-  const R rho0 = R(P.rho0);
 #pragma unroll
   for (int m = 0; m < S; ++m) {
     R u[D];
@@ -1037,14 +1099,50 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
       u[d] = uic ? R(uic[(long long)(m * D + d) * N + idx]) : R(0);
       usqr = usqr + u[d] * u[d];
     }
-    sfor<0, Q>([&](auto nn) {
-      constexpr int n = decltype(nn)::value;
-      R feq, pf;
-      feq_pf<D, n, EXACT, R>(P, m, rf[m], u, usqr, F[m], feq, pf);
-      R v = (R(1.) - R(0.5) * pf) * feq;
-      if constexpr (kShifted<T>) v = v - R(L::w(n)) * rho0;
-      St<T>::st(fout + (long long)(m * Q + n) * N + idx, v);
-    });
+    if constexpr (!kShifted<T>) {
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        R feq, pf;
+        feq_pf<D, n, EXACT, R>(P, m, rf[m], u, usqr, F[m], feq, pf);
+        St<T>::st(fout + (long long)(m * Q + n) * N + idx, (R(1.) - R(0.5) * pf) * feq);
+      });
+    } else {
+      // the deviation (1 - P/2) feq - w rho0 = dE_n - 1.5 E_n (F.c_n - F.u), as in step_site
+      const R A0 = P.A0[m], An = P.An[m];
+      R Fu = R(0);
+#pragma unroll
+      for (int d = 0; d < D; ++d) Fu = Fu + F[m][d] * u[d];
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        constexpr double w = L::w(n);
+        R ud = R(0), Fc = R(0);
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          constexpr int cc = L::c(n, d);
+          if constexpr (cc > 0) {
+            ud = ud + u[d];
+            Fc = Fc + F[m][d];
+          }
+          if constexpr (cc < 0) {
+            ud = ud - u[d];
+            Fc = Fc - F[m][d];
+          }
+        });
+        R WA, WB, cA;
+        if constexpr (n == 0) {
+          WA = A0;
+          WB = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
+          cA = P.cA[m][0];
+        } else {
+          WA = R(w) * An;
+          WB = ud * (R(3 * w) + R(4.5 * w) * ud) - R(1.5 * w) * usqr;
+          cA = P.cA[m][n <= L::NAXIS ? 1 : 2];
+        }
+        const R dE = WA * rfd[m] + WB * rf[m] + cA;
+        const R v = dE - R(1.5) * (WA + WB) * (Fc - Fu);
+        st_dev<T, R>(fout + (long long)(m * Q + n) * N + idx, v, P);
+      });
+    }
   }
 }
 
@@ -1075,11 +1173,20 @@ __device__ __forceinline__ void moments_site(const StepArgs& a, int x, int y, in
   }
   const long long N = a.g.n;
   R fv[S][Q];
-  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, (unsigned)idx, R(P.rho0), fv);
+  load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, (unsigned)idx, P, fv);
   R rc[S], rf[S], F[S][D], up[D];
   cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
   if (what == 2) {
-    for (int m = 0; m < S; ++m) out[idx * S + m] = double(rc[m]);
+    if constexpr (kShifted<T>) {
+      // rho0 + (rho - rho0) in FP64, so that the stored deviation keeps its digits
+      const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
+      R rfd[S];
+      rho_at<S>(reinterpret_cast<const RT*>(a.rho), (unsigned)idx, rfd);
+      for (int m = 0; m < S; ++m)
+        out[idx * S + m] = double(P.rho0[m]) + double(dn ? pop_sum<D, S, R>(fv, m) : rfd[m]);
+    } else {
+      for (int m = 0; m < S; ++m) out[idx * S + m] = double(rc[m]);
+    }
   } else if (what == 3 || what == 4) {
     for (int d = 0; d < D; ++d)
       for (int m = 0; m < S; ++m) out[(idx * D + d) * S + m] = double(what == 3 ? up[d] : F[m][d]);
@@ -1117,9 +1224,10 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
   moments_site<D, S, ISO, EXACT, T, R, RT>(a, x, y, z, what, out);
 }
 
-// Natural-order populations <-> SoA state.
+// Natural-order populations <-> SoA state (the shift and the FP16 scale are
+// applied in FP64).
 template <int D, int S, class T, class R>
-__global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, double rho0, double* out) {
+__global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, Shift sh, double* out) {
   constexpr int Q = Lat<D>::Q;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N) return;
@@ -1129,23 +1237,26 @@ __global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, 
       double v = 0.0;
       if (!wall) {
         v = double(St<T>::ld(f + (long long)(m * Q + n) * N + idx));
-        if constexpr (kShifted<T>) v = double(R(v) + R(Lat<D>::w(n)) * R(rho0));
+        if constexpr (kShifted<T>) v = v / sh.scale + Lat<D>::w(n) * sh.rho0[m];
       }
       out[(idx * Q + n) * S + m] = v;
     }
 }
 
 template <int D, int S, class T, class R>
-__global__ void k_pops_from_natural(const double* in, const uint8_t* mask, long long N, double rho0, T* f) {
+__global__ void k_pops_from_natural(const double* in, const uint8_t* mask, long long N, Shift sh, T* f) {
   constexpr int Q = Lat<D>::Q;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N) return;
   const bool wall = __ldg(mask + idx) != 0;
   for (int n = 0; n < Q; ++n)
     for (int m = 0; m < S; ++m) {
-      R v = wall ? R(0) : R(in[(idx * Q + n) * S + m]);
-      if constexpr (kShifted<T>) v = v - R(Lat<D>::w(n)) * R(rho0);
-      St<T>::st(f + (long long)(m * Q + n) * N + idx, v);
+      double v = wall ? 0.0 : in[(idx * Q + n) * S + m];
+      if constexpr (kShifted<T>) v = wall ? 0.0 : (v - Lat<D>::w(n) * sh.rho0[m]) * sh.scale;
+      if constexpr (std::is_same<T, double>::value)
+        f[(long long)(m * Q + n) * N + idx] = v;
+      else
+        St<T>::st(f + (long long)(m * Q + n) * N + idx, R(v));
     }
 }
 

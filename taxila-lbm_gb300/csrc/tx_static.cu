@@ -201,7 +201,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   a.g = g;
   a.faces = faces;
   // restart from fi_in exactly like tx_upload_fi + tx_init (FlowUpdateMoments: plain sums)
-  ks.from_natural(fi_in, mask, N, 0.0, pa, st);
+  ks.from_natural(fi_in, mask, N, shift_of(ph), pa, st);
   a.fin = pa;
   a.fout = pa;
   ks.density(a, 1, st);
@@ -216,7 +216,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
     cur = nxt;
     nxt = tmp;
   }
-  ks.to_natural(cur, mask, N, 0.0, fi_out, st);
+  ks.to_natural(cur, mask, N, shift_of(ph), fi_out, st);
   TX_SCHK(cudaGetLastError());
   unsigned bad = 0;
   TX_SCHK(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, st));

@@ -35,7 +35,7 @@ class TxParams(C.Structure):
         ("mm", _D * MAXC), ("g", (_D * MAXC) * MAXC), ("gw", (_D * MAXC) * MAXMIN),
         ("body_forces", _I), ("gvt", _D * 3),
         ("bc_density", (_D * MAXC) * 6),
-        ("literal_kind", _I), ("precision", _I), ("exact", _I), ("rho0", _D),
+        ("literal_kind", _I), ("precision", _I), ("exact", _I), ("rho0", _D * MAXC), ("storage_scale", _D),
     ]
 
     @property
@@ -78,7 +78,9 @@ def default_params():
     p.literal_kind = 4
     p.precision = PREC_F64
     p.exact = 0
-    p.rho0 = 1.0
+    for m in range(MAXC):
+        p.rho0[m] = 0.0
+    p.storage_scale = 1.0
     return p
 
 

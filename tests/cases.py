@@ -114,7 +114,7 @@ def permeability_case(shape, seed=11, porosity=0.45, rmin=2.0, rmax=4.0, precisi
     p.body_forces = 1
     p.gvt[2] = gz
     p.precision = precision
-    p.rho0 = 1.0
+    p.rho0[0] = 1.0
     solid = problems.sphere_pack(p.shape, porosity, rmin, rmax, seed, periodic=True)
     walls = np.where(solid.ravel(), 1.0, 0.0)
     rho = np.ones(p.nsites)

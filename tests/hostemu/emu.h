@@ -121,13 +121,13 @@ std::string run(const Case& c, Result& out) {
     a.faces = faces;
     return a;
   };
-  const double rho0 = ph.rho0;
+  const Shift sh = shift_of(ph);
   if (c.from_fi) {
-    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), mask.data(), N, rho0, buf[cur]); });
+    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), mask.data(), N, sh, buf[cur]); });
   } else {
     for (long long i = 0; i < N; ++i)
       for (int m = 0; m < S; ++m)
-        rho[(size_t)(i * S + m)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] : 0.0);
+        rho[(size_t)(i * S + m)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] - ph.rho0[m] : 0.0);
     const StepArgs a = args(cur, cur);
     launch3(g, 128, [&] { k_init<D, S, ISO, EXACT, T, R, RT>(a, nullptr); });
   }
@@ -142,7 +142,7 @@ std::string run(const Case& c, Result& out) {
     cur = 1 - cur;
   }
   out.fi.assign((size_t)N * S * Q, 0.0);
-  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], mask.data(), N, rho0, out.fi.data()); });
+  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], mask.data(), N, sh, out.fi.data()); });
   const StepArgs a = args(cur, cur);
   out.rho.assign((size_t)N * S, 0.0);
   out.flux.assign((size_t)N * S * D, 0.0);

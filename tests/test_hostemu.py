@@ -129,7 +129,26 @@ def test_emulated_reduced_precision_forms(emu_exe, tmp_path, prec):
     ref = oracle_run(p, walls, rho, 20)
     q = P.copy_params(p)
     q.precision = prec
-    q.rho0 = 1.0
+    q.rho0[0] = q.rho0[1] = 0.0  # two phases: no single rest density; plain storage
     got = run_emu(emu_exe, q, walls, rho, 20, False, tmp_path)
     errs = compare(ref, got, p, walls, FORM_TOL[prec])
     print("form %d after 20 steps:" % prec, errs)
+
+
+@pytest.mark.parametrize("prec,scale", [(P.PREC_F32, 1.0), (P.PREC_F32_F16, 4096.0)], ids=["f32", "f32_f16"])
+def test_emulated_permeability_precision(emu_exe, tmp_path, prec, scale):
+    # single-phase body-force flow through a sphere pack, deviations stored
+    # from rho0 = 1: the Darcy velocity (hence the permeability) within 1e-3 of
+    # the FP64 oracle, populations and density far tighter
+    p, walls, rho = cases.permeability_case((14, 12, 16), seed=5)
+    ref = oracle_run(p, walls, rho, 40)
+    q = P.copy_params(p)
+    q.precision = prec
+    q.rho0[0] = 1.0
+    q.storage_scale = scale
+    got = run_emu(emu_exe, q, walls, rho, 40, False, tmp_path)
+    compare(ref, got, p, walls, {"fi": 1e-6, "rho": 1e-6, "flux": 1e-3, "forces": 1e-6})
+    pore = walls == 0
+    k_ref = cases.permeability(p, ref["flux"].reshape(-1, 3)[pore, 2].sum(), p.nsites)
+    k_got = cases.permeability(p, got["flux"].reshape(-1, 3)[pore, 2].sum(), p.nsites)
+    assert abs(k_got / k_ref - 1.0) < 1e-3
