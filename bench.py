@@ -272,6 +272,113 @@ def traffic_from_profile():
         return None
 
 
+def batched_run(n_lat=96, steps=40, seed=4, compare=8):
+    """Many uneven single-phase permeability lattices (D3Q19 BGK tau = 1, sides
+    uniform in 48..192 per axis, seeded sphere packs with radii 4..10 and
+    porosity 0.25..0.5, periodic, body force 1e-6 along z) in one batch of the
+    FP32 form: tile shape from the autotuner, steps replayed as a CUDA graph.
+    The first ``compare`` lattices are also stepped one by one in tx_handles."""
+    import torch
+    from taxila import serve
+    from taxila._lib import Batch, Handle
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n_lat):
+        sides = [int(v) for v in rng.integers(48, 193, size=3)]
+        reqs.append(serve.perm_request(i, 0.0, sides, int(rng.integers(0, 1 << 30)), 1e-7, 10 ** 9, gz=1e-6,
+                                       radii=(4.0, 10.0)))
+    form = P.copy_params(reqs[0].params)
+    form.precision = P.PREC_F32
+
+    def params_of(r):
+        q = P.copy_params(r.params)
+        q.precision = P.PREC_F32
+        return q
+
+    def timed(b, k):
+        stream = torch.cuda.ExternalStream(b.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.launch(k)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    b = Batch(form)
+    for r in reqs:
+        b.add(params_of(r), r.walls, r.rho)
+    sites = sum(r.params.nsites for r in reqs)
+    tiles = b.tune(2)
+    b.set_graph(20)
+    b.step(20)
+    ms = timed(b, steps)
+    probes = b.probe()
+    finite = all(np.isfinite(pr.u_sum[2]) for pr in probes.values())
+    b.close()
+    # the first lattices batched and one by one
+    sub = reqs[:compare]
+    sub_sites = sum(r.params.nsites for r in sub)
+    bs = Batch(form)
+    for r in sub:
+        bs.add(params_of(r), r.walls, r.rho)
+    bs.set_tiles(*tiles)
+    bs.set_graph(20)
+    bs.step(20)
+    ms_sub = timed(bs, steps)
+    bs.close()
+    ms_one = 0.0
+    for r in sub:
+        h = Handle(params_of(r))
+        h.upload_walls(r.walls)
+        h.upload_state(r.rho)
+        h.init()
+        h.step(5)
+        h.sync()
+        stream = torch.cuda.ExternalStream(h.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms_one += e0.elapsed_time(e1)
+        h.close()
+    mlups = sites * steps / (ms * 1e-3) / 1e6
+    bpl = 2 * 19 * 4 + 1 + 19 * 4 + 4  # collide-push read+write, mask; density read + write
+    return {"workload": "%d single-phase D3Q19 BGK sphere packs, sides 48-192 per axis (%d sites), FP32 form, "
+                        "body force 1e-6, periodic" % (n_lat, sites),
+            "steps": steps, "ms_per_step": round(ms / steps, 4), "mlups": round(mlups, 1),
+            "gbs_algorithmic": round(mlups * 1e6 * bpl / 1e9, 1), "bytes_per_lup": bpl,
+            "tiles": {"bx": tiles[0], "by": tiles[1], "bz": tiles[2], "blocks_per_sm": tiles[3]},
+            "graph_steps": 20, "finite": finite,
+            "first_%d_batched_mlups" % compare: round(sub_sites * steps / (ms_sub * 1e-3) / 1e6, 1),
+            "first_%d_one_by_one_mlups" % compare: round(sub_sites * steps / (ms_one * 1e-3) / 1e6, 1)}
+
+
+def serving_run(n=30, rate=30.0, seed=1):
+    """The request mix of the server (70% permeability solves, sides 32-64,
+    stop at 1e-5 relative change of the mean flow; 30% drainage, D3Q19
+    32-48 / D2Q9 96-192, 1500 steps) at ``rate`` Poisson arrivals per second,
+    served by the FP16-storage and FP32 forms and, one request at a time, by
+    the plain FP64 form."""
+    from taxila import serve
+    reqs = serve.make_mix(seed=seed, n=n, rate=rate)
+    out = {"mix": "%d requests, Poisson %.0f/s, seed %d: 70%% permeability (D3Q19 sides 32-64, tol 1e-5 on the "
+                  "mean flow), 30%% drainage (D3Q19 32-48 or D2Q9 96-192, 1500 steps)" % (n, rate, seed)}
+    for name, prec, maxa in (("fp32_fp16_storage", P.PREC_F32_F16, None), ("fp32", P.PREC_F32, None),
+                             ("fp64_sequential", P.PREC_F64, 1)):
+        for mode, realtime in (("", True), ("_saturated", False)):
+            srv = serve.Server(precision=prec, max_active=maxa, chunk=100)
+            res = srv.run(reqs, realtime=realtime)
+            srv.close()
+            out[name + mode] = serve.summary(res)
+    for mode in ("", "_saturated"):
+        f, s = out["fp32_fp16_storage" + mode], out["fp64_sequential" + mode]
+        if f and s:
+            out["fp16_storage_vs_fp64_sequential_solves" + mode] = round(f["solves_per_s"] / s["solves_per_s"], 2)
+    out["saturated"] = "the same requests all queued at once: solves/s is the server's capacity"
+    return out
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -364,6 +471,11 @@ def run_gpu(args):
             except Exception as ex:
                 forms[name] = {"error": str(ex)}
         line["precision_forms"] = forms
+        for key, fn in (("batched", batched_run), ("serving", serving_run)):
+            try:
+                line[key] = fn()
+            except Exception as ex:  # report, do not hide
+                line[key] = {"error": str(ex)}
         try:
             threads = os.cpu_count() or 1
             v, dt = cpu_oracle_mlups(p, walls, rho, 3, threads)
@@ -386,7 +498,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form and CPU legs")
+    ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form, batched, serving and CPU legs")
     ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling runs use a smaller case)")
     ap.add_argument("--form", default="f64", choices=sorted(FORMS), help="storage/arithmetic form of the timed run")
     args = ap.parse_args()

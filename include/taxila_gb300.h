@@ -242,6 +242,11 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
 int tx_batch_remove(tx_batch* b, int32_t id);
 /* nsteps flow steps of every lattice in the batch */
 int tx_batch_step(tx_batch* b, int32_t nsteps);
+/* tx_batch_step without waiting: the steps are queued on the batch's stream,
+ * so that the work of several batches overlaps on the device; tx_batch_sync
+ * waits for them.  The other calls order themselves after queued steps. */
+int tx_batch_launch(tx_batch* b, int32_t nsteps);
+int tx_batch_sync(tx_batch* b);
 /* Probes every lattice; writes up to cap records, *n = lattices probed. */
 int tx_batch_probe(tx_batch* b, int32_t cap, tx_probe* out, int32_t* n);
 /* a field of one lattice, as tx_download */

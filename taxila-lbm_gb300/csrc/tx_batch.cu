@@ -496,7 +496,18 @@ int tx_batch_remove(tx_batch* b, int32_t id) {
   return bfail(b, TX_ERR_ARG, "no lattice with id " + std::to_string(id));
 }
 
+int tx_batch_sync(tx_batch* b) {
+  if (!b) return TX_ERR_ARG;
+  TX_BCUDA(b, cudaStreamSynchronize(b->stream));
+  return TX_OK;
+}
+
 int tx_batch_step(tx_batch* b, int32_t nsteps) {
+  const int rc = tx_batch_launch(b, nsteps);
+  return rc ? rc : tx_batch_sync(b);
+}
+
+int tx_batch_launch(tx_batch* b, int32_t nsteps) {
   if (!b) return TX_ERR_ARG;
   if (nsteps < 0) return bfail(b, TX_ERR_ARG, "nsteps must be >= 0");
   if (b->slots.empty() || nsteps == 0) return TX_OK;
@@ -517,7 +528,6 @@ int tx_batch_step(tx_batch* b, int32_t nsteps) {
     }
   }
   for (Lattice* L : b->slots) L->steps += nsteps;
-  TX_BCUDA(b, cudaStreamSynchronize(b->stream));
   return TX_OK;
 }
 

@@ -67,6 +67,8 @@ def load():
         "tx_batch_add": ([vp, C.POINTER(P.TxParams), dp, dp, dp, C.POINTER(i32)], C.c_int),
         "tx_batch_remove": ([vp, i32], C.c_int),
         "tx_batch_step": ([vp, i32], C.c_int),
+        "tx_batch_launch": ([vp, i32], C.c_int),
+        "tx_batch_sync": ([vp], C.c_int),
         "tx_batch_probe": ([vp, i32, C.POINTER(TxProbe), C.POINTER(i32)], C.c_int),
         "tx_batch_download": ([vp, i32, i32, dp], C.c_int),
         "tx_batch_set_tiles": ([vp, i32, i32, i32, i32], C.c_int),
@@ -231,6 +233,13 @@ class Batch:
 
     def step(self, n=1):
         self._check(self.L.tx_batch_step(self.b, int(n)))
+
+    def launch(self, n=1):
+        """Queue n steps on the batch's stream without waiting."""
+        self._check(self.L.tx_batch_launch(self.b, int(n)))
+
+    def sync(self):
+        self._check(self.L.tx_batch_sync(self.b))
 
     def probe(self):
         """{id: TxProbe} for every lattice in the batch."""

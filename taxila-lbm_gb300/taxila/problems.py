@@ -45,28 +45,41 @@ def bubble_ball_state(nx, ny, nz, radius, rho_in, rho_out):
 def sphere_pack(shape, porosity, rmin, rmax, seed, periodic=True, max_spheres=1_000_000):
     """Seeded random overlapping spheres added until the pore fraction drops
     to ``porosity``.  shape = (nz, ny, nx); radii uniform in [rmin, rmax];
-    centres uniform in the box; periodic images wrap when ``periodic``.
-    Returns a bool array (True = solid), natural order."""
+    centres uniform in the box; periodic images wrap (nearest image) when
+    ``periodic``.  Returns a bool array (True = solid), natural order.
+    Each sphere touches only its bounding box."""
     nz, ny, nx = shape
+    dims = (nz, ny, nx)
     rng = np.random.default_rng(seed)
     solid = np.zeros(shape, dtype=bool)
     target = (1.0 - porosity) * solid.size
+    nsolid = 0
     count = 0
-    zz = np.arange(nz)[:, None, None]
-    yy = np.arange(ny)[None, :, None]
-    xx = np.arange(nx)[None, None, :]
-    while solid.sum() < target and count < max_spheres:
+
+    def axis(cc, r, n):
+        if periodic:
+            if 2 * r + 2 >= n:
+                idx = np.arange(n)
+            else:
+                idx = np.arange(int(np.floor(cc - r)), int(np.ceil(cc + r)) + 1) % n
+            d = (idx - cc + n / 2.0) % n - n / 2.0
+        else:
+            idx = np.arange(max(0, int(np.floor(cc - r))), min(n - 1, int(np.ceil(cc + r))) + 1)
+            d = idx - cc
+        return idx, d
+
+    while nsolid < target and count < max_spheres:
         r = rng.uniform(rmin, rmax)
         c = rng.uniform(0, 1, 3) * np.array([nz, ny, nx])
-        dz = zz - c[0]
-        dy = yy - c[1]
-        dx = xx - c[2]
-        if periodic:
-            dz = (dz + nz / 2.0) % nz - nz / 2.0
-            dy = (dy + ny / 2.0) % ny - ny / 2.0
-            dx = (dx + nx / 2.0) % nx - nx / 2.0
-        solid |= (dz * dz + dy * dy + dx * dx) <= r * r
+        (iz, dz), (iy, dy), (ix, dx) = (axis(c[k], r, dims[k]) for k in range(3))
         count += 1
+        if not (len(iz) and len(iy) and len(ix)):
+            continue
+        ball = (dz[:, None, None] ** 2 + dy[None, :, None] ** 2 + dx[None, None, :] ** 2) <= r * r
+        box = np.ix_(iz, iy, ix)
+        sub = solid[box]
+        nsolid += int(np.count_nonzero(ball & ~sub))
+        solid[box] = sub | ball
     return solid
 
 
