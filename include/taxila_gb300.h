@@ -75,6 +75,9 @@ extern "C" {
 #define TX_FIELD_VELT 6    /* ndims dof: total velocity diagnostic                        */
 #define TX_FIELD_RHOT 7    /* 1 dof: total mass density diagnostic                        */
 #define TX_FIELD_WALLS 8   /* 1 dof: wall codes as uploaded                               */
+#define TX_FIELD_SPECIES_FI 9    /* ns*Q dof: transported species populations (reference gi) */
+#define TX_FIELD_SPECIES_RHO 10  /* ns dof: species concentrations (reference psi)           */
+#define TX_FIELD_SPECIES_FLUX 11 /* ns*ndims dof: species flux sum_n g_n c_n                 */
 
 /* error codes */
 #define TX_OK 0
@@ -116,6 +119,14 @@ typedef struct tx_params {
                                the component mostly has, e.g. 1 for single-phase flow) */
   double storage_scale;     /* FP16 form: populations stored as (f - w_n*rho0) * storage_scale
                                (a power of two keeps the scaling exact; 0 = 1) */
+  /* passive species (LBM_Transport_module, src/lbm/lbm_transport.F90): the
+   * -nspecies / -transport_relaxation_mode / -tau_<specie> / -s_*_<specie>
+   * options.  The transport lattice is the flow's (same discretization and
+   * faces); species feel no force and no boundary condition. */
+  int32_t nspecies;                        /* 0 = no transport */
+  int32_t species_relaxation_mode;         /* TX_RELAX_SRT or TX_RELAX_MRT */
+  double species_tau[TX_MAX_COMPONENTS];   /* SRT relaxation time */
+  double species_rates[TX_MAX_COMPONENTS][7]; /* MRT s_c, s_e, s_e2, s_q, s_nu, s_pi, s_m */
 } tx_params;
 
 typedef struct tx_handle tx_handle;
@@ -154,11 +165,19 @@ int tx_upload_fi(tx_handle* h, const double* fi);
  * tangential axes.  Optional: tx_create fills faces from bc_density. */
 int tx_upload_bc_values(tx_handle* h, int32_t face, const double* vals);
 
+/* Species concentrations [N*ns] and fluxes [N*ndims*ns] (NULL = 0), natural
+ * order with the species fastest: the initial state of the transported
+ * species (LBMInitializeState_FlowTransport, src/lbm/lbm.F90:455-480).
+ * tx_init then sets gi = geq (TransportFiInit, lbm_transport.F90:320-334). */
+int tx_upload_species(tx_handle* h, const double* conc, const double* flux);
+
 /* LBMInit2 for istep = 0 (src/lbm/lbm.F90:183-253): FlowFiInit (unless
- * populations were uploaded) then FlowUpdateMoments. */
+ * populations were uploaded) then FlowUpdateMoments; with species,
+ * TransportFiInit and TransportUpdateMoments. */
 int tx_init(tx_handle* h);
 
-/* nsteps iterations of the flow part of LBMRun2's loop body (lbm.F90:283-363). */
+/* nsteps iterations of the flow part of LBMRun2's loop body (lbm.F90:283-363),
+ * and of its transport part when the handle has species. */
 int tx_step(tx_handle* h, int32_t nsteps);
 
 /* DistributionCalcDeltaNorm (lbm_distribution_function.F90:809-833):

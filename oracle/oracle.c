@@ -51,6 +51,11 @@ struct orc {
   double *bcv[6];            /* nbcs * face area per Dirichlet face */
   double *old_rho, *old_fi;
   int have_fi, have_state, inited;
+  /* passive species: a second distribution over the same lattice, kept as
+   * an orc of its own with transport = 1 (LBM_Transport_module) */
+  int transport;
+  struct orc* tr;
+  int have_species;
 };
 
 /* ---------------------------------------------------------------- indexing */
@@ -172,6 +177,8 @@ static void setup_lattice(orc* o) {
 }
 
 /* ---------------------------------------------------------------- creation */
+static orc* orc_create_transport(const tx_params* p);
+
 orc* orc_create(const tx_params* p) {
   orc* o = (orc*)calloc(1, sizeof(orc));
   if (!o) return NULL;
@@ -242,11 +249,48 @@ orc* orc_create(const tx_params* p) {
     for (long q = 0; q < area; ++q)
       for (int m = 0; m < o->s; ++m) o->bcv[f][q * nbcs + m] = p->bc_density[f][m];
   }
+  if (p->nspecies > 0) o->tr = orc_create_transport(p);
   return o;
+}
+
+/* TransportSetFromOptions / TransportSetUp (lbm_transport.F90:130-286) and
+ * SpecieSetFromOptions (lbm_species.F90:111-133): nspecies "components" on the
+ * flow's lattice with the species' relaxation (RelaxationCreate leaves d_k =
+ * 0 for species, lbm_relaxation.F90:80), no forces, and no boundary
+ * condition but the periodic faces (TransportApplyBCs is not called by
+ * LBMRun2, lbm.F90:348-352). */
+static orc* orc_create_transport(const tx_params* p) {
+  tx_params q = *p;
+  q.ncomponents = p->nspecies;
+  q.relaxation_mode = p->species_relaxation_mode;
+  q.nspecies = 0;
+  q.body_forces = 0;
+  for (int m = 0; m < TX_MAX_COMPONENTS; ++m) {
+    q.tau[m] = p->species_tau[m];
+    q.s_c[m] = p->species_rates[m][0];
+    q.s_e[m] = p->species_rates[m][1];
+    q.s_e2[m] = p->species_rates[m][2];
+    q.s_q[m] = p->species_rates[m][3];
+    q.s_nu[m] = p->species_rates[m][4];
+    q.s_pi[m] = p->species_rates[m][5];
+    q.s_m[m] = p->species_rates[m][6];
+    q.mm[m] = 1.0;
+    for (int n = 0; n < TX_MAX_COMPONENTS; ++n) q.g[m][n] = 0.0;
+  }
+  for (int w = 0; w < TX_MAX_MINERALS; ++w)
+    for (int m = 0; m < TX_MAX_COMPONENTS; ++m) q.gw[w][m] = 0.0;
+  for (int f = 0; f < 6; ++f)
+    if (q.bc_flags[f] != TX_BC_PERIODIC) q.bc_flags[f] = TX_BC_NULL;
+  orc* t = orc_create(&q);
+  if (!t) return NULL;
+  t->transport = 1;
+  for (int m = 0; m < t->s; ++m) t->dk[m] = 0.0;
+  return t;
 }
 
 void orc_destroy(orc* o) {
   if (!o) return;
+  orc_destroy(o->tr);
   free(o->fi); free(o->tmp); free(o->fieq); free(o->flux); free(o->forces);
   free(o->rho); free(o->walls); free(o->old_rho); free(o->old_fi);
   for (int f = 0; f < 6; ++f) free(o->bcv[f]);
@@ -318,6 +362,7 @@ int orc_set_walls(orc* o, const double* walls) {
           if (v < 1 || v > o->N[a]) WALL(o, i, j, k) = 999.0;
         }
   }
+  if (o->tr) orc_set_walls(o->tr, walls);
   return 0;
 }
 
@@ -727,6 +772,72 @@ static void bc_update_rho(orc* o) {
   }
 }
 
+/* ------------------------------------------------------------- transport */
+/* TransportCollisionD3 (lbm_transport.F90:403-431) collides pore cells
+ * (walls == 0); TransportCollisionD2 (:433-458) collides cells with walls > 0,
+ * which the reference does as written: in 2D the species are only streamed
+ * and bounced back.  RelaxationCollideSRT/MRT (lbm_relaxation.F90:171-200)
+ * toward fi_eq, no forcing. */
+static void transport_collision(orc* o) {
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= o->N[2]; ++k)
+    for (int j = 1; j <= o->N[1]; ++j)
+      for (int i = 1; i <= o->N[0]; ++i) {
+        const int on = o->nd == 3 ? WALL(o, i, j, k) == 0 : WALL(o, i, j, k) > 0;
+        if (!on) continue;
+        for (int m = 0; m < o->s; ++m) {
+          if (o->mode == TX_RELAX_SRT) {
+            for (int n = 0; n < o->Q; ++n)
+              FI(o, m, n, i, j, k) = FI(o, m, n, i, j, k) - (FI(o, m, n, i, j, k) - FEQ(o, m, n, i, j, k)) / o->tau[m];
+          } else {
+            double dfi[MAXQ];
+            for (int n = 0; n < o->Q; ++n) dfi[n] = FI(o, m, n, i, j, k) - FEQ(o, m, n, i, j, k);
+            for (int q = 0; q < o->Q; ++q) {
+              double mdiff = 0.0;
+              for (int n = 0; n < o->Q; ++n) mdiff = mdiff + o->mt[n][q] * dfi[n];
+              const double coef = o->tau_mrt[m][q] * mdiff / o->mmt[q];
+              for (int n = 0; n < o->Q; ++n) FI(o, m, n, i, j, k) = FI(o, m, n, i, j, k) - coef * o->mt[n][q];
+            }
+          }
+        }
+      }
+}
+
+/* TransportFiInit (lbm_transport.F90:320-334): fi_eq from the initial
+ * concentration and flux, fi = fi_eq over the whole local array, then
+ * TransportUpdateMoments (:312-318). */
+static void transport_init(orc* t) {
+  halo_rho_like(t, t->walls, 1);
+  update_feq(t);
+  long ntot = (long)t->gl[0] * t->gl[1] * t->gl[2] * t->Q * t->s;
+  memcpy(t->fi, t->fieq, sizeof(double) * (size_t)ntot);
+  calc_density(t);
+  calc_flux(t, t->flux);
+  t->inited = 1;
+}
+
+/* The transport part of LBMRun2's loop body (lbm.F90:290-370): collision with
+ * the equilibrium of the species' own density and flux (TransportUpdateFeq,
+ * lbm_transport.F90:363-378, passes the flux array as the velocity), halo,
+ * stream, bounceback (TransportReactWithWalls without a reactive matrix),
+ * moments. */
+static void transport_step(orc* t) {
+  update_feq(t);
+  transport_collision(t);
+  halo_fi(t);
+  stream(t);
+  bounceback(t);
+  calc_density(t);
+  calc_flux(t, t->flux);
+}
+
+int orc_set_species(orc* o, const double* conc, const double* flux) {
+  if (!o->tr) return TX_ERR_STATE;
+  orc_set_state(o->tr, conc, flux);
+  o->have_species = 1;
+  return 0;
+}
+
 /* ------------------------------------------------------------ step drivers */
 /* FlowUpdateMoments (lbm_flow.F90:466-478) */
 static void update_moments(orc* o) {
@@ -780,6 +891,7 @@ int orc_init(orc* o) {
     fibar_init(o);
   }
   update_moments(o);
+  if (o->tr && o->have_species) transport_init(o->tr);
   o->inited = 1;
   return 0;
 }
@@ -803,7 +915,11 @@ static void one_step(orc* o) {
 
 int orc_step(orc* o, int nsteps) {
   if (!o->inited) return TX_ERR_STATE;
-  for (int t = 0; t < nsteps; ++t) one_step(o);
+  const int species = o->tr && o->have_species;
+  for (int t = 0; t < nsteps; ++t) {
+    one_step(o);
+    if (species) transport_step(o->tr);
+  }
   return 0;
 }
 
@@ -819,6 +935,9 @@ long orc_field_size(const orc* o, int field) {
     case TX_FIELD_RHOT:
     case TX_FIELD_WALLS: return n;
     case TX_FIELD_VELT: return n * o->nd;
+    case TX_FIELD_SPECIES_FI: return o->tr ? n * o->tr->s * o->Q : -1;
+    case TX_FIELD_SPECIES_RHO: return o->tr ? n * o->tr->s : -1;
+    case TX_FIELD_SPECIES_FLUX: return o->tr ? n * o->tr->s * o->nd : -1;
   }
   return -1;
 }
@@ -894,6 +1013,9 @@ int orc_get(orc* o, int field, double* out) {
     case TX_FIELD_PRS: diagnostics(o, NULL, out, NULL); return 0;
     case TX_FIELD_RHOT: diagnostics(o, out, NULL, NULL); return 0;
     case TX_FIELD_VELT: diagnostics(o, NULL, NULL, out); return 0;
+    case TX_FIELD_SPECIES_FI: return o->tr ? orc_get(o->tr, TX_FIELD_FI, out) : TX_ERR_ARG;
+    case TX_FIELD_SPECIES_RHO: return o->tr ? orc_get(o->tr, TX_FIELD_RHO, out) : TX_ERR_ARG;
+    case TX_FIELD_SPECIES_FLUX: return o->tr ? orc_get(o->tr, TX_FIELD_FLUX, out) : TX_ERR_ARG;
   }
   return TX_ERR_ARG;
 }

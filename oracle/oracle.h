@@ -29,6 +29,7 @@ double orc_delta_norm(orc* o, int field);
 int orc_get(orc* o, int field, double* out);
 long orc_field_size(const orc* o, int field);
 int orc_set_threads(int n);
+int orc_set_species(orc* o, const double* conc, const double* flux);
 
 #ifdef __cplusplus
 }

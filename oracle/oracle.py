@@ -37,6 +37,7 @@ def lib():
         for fn in ("orc_set_walls", "orc_set_fi"):
             getattr(L, fn).argtypes = [C.c_void_p, C.c_void_p]
         L.orc_set_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_set_species.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_set_bc_values.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_init.argtypes = [C.c_void_p]
         L.orc_step.argtypes = [C.c_void_p, C.c_int]
@@ -87,6 +88,12 @@ class Oracle:
     def set_fi(self, fi):
         fi = np.ascontiguousarray(fi, dtype=np.float64).ravel()
         self.L.orc_set_fi(self.h, _ptr(fi))
+
+    def set_species(self, conc, flux=None):
+        conc = np.ascontiguousarray(conc, dtype=np.float64).ravel()
+        flux = None if flux is None else np.ascontiguousarray(flux, dtype=np.float64).ravel()
+        if self.L.orc_set_species(self.h, _ptr(conc), _ptr(flux)):
+            raise ValueError("the parameters declare no species")
 
     def set_bc_values(self, face, vals):
         vals = np.ascontiguousarray(vals, dtype=np.float64).ravel()

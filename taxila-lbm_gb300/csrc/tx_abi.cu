@@ -40,6 +40,15 @@ struct tx_handle {
   double* uic = nullptr;
   unsigned long long* red = nullptr;  // [0] max bits, [1] non-finite count
   std::vector<uint8_t> host_mask;
+  // passive species (transport): populations, parameters, initial state
+  int NS = 0;
+  SpeciesSet ss{};
+  void* sg[2] = {nullptr, nullptr};  // species populations (ping-pong)
+  int gcur = 0;
+  void* d_sphys = nullptr;    // SpeciesPhysT of the arithmetic type
+  double* sconc = nullptr;    // uploaded initial concentration and flux
+  double* sflux = nullptr;
+  bool have_species = false;
   bool have_walls = false, have_state = false, have_fi = false, inited = false;
   bool timing = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -94,7 +103,11 @@ StepArgs args(tx_handle* h, int in, int out) {
 }
 
 long long field_dof(const tx_handle* h, int field) {
+  if (h->NS == 0 && field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) return -1;
   switch (field) {
+    case TX_FIELD_SPECIES_FI: return (long long)h->NS * h->Q;
+    case TX_FIELD_SPECIES_RHO: return h->NS;
+    case TX_FIELD_SPECIES_FLUX: return (long long)h->NS * h->D;
     case TX_FIELD_FI: return (long long)h->S * h->Q;
     case TX_FIELD_RHO: return h->S;
     case TX_FIELD_FLUX:
@@ -110,6 +123,7 @@ long long field_dof(const tx_handle* h, int field) {
 }  // namespace
 
 namespace tx {
+bool select_species(const tx_params* p, SpeciesSet* ss);
 int validate_params(const tx_params* p, std::string* why);
 void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out);
 bool select_kernels(const tx_params* p, KernelSet* ks);
@@ -146,9 +160,23 @@ int sync_stream(tx_handle* h) {
 }
 
 // populations of state cur -> natural order staging
+SpeciesArgs species_args(tx_handle* h, int in, int out) {
+  SpeciesArgs a{};
+  a.gin = h->sg[in];
+  a.gout = h->sg[out];
+  a.links = h->links;
+  a.mask = h->mask;
+  a.phys = h->d_sphys;
+  a.g = h->g;
+  a.ns = h->NS;
+  return a;
+}
+
 int stage_field(tx_handle* h, int field) {
   const long long N = h->g.n;
-  if (field == TX_FIELD_FI) {
+  if (field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) {
+    h->ss.fields(species_args(h, h->gcur, h->gcur), field, h->stage, h->stream);
+  } else if (field == TX_FIELD_FI) {
     h->ks.to_natural(h->f[h->cur], h->mask, N, shift_of(h->ph), h->stage, h->stream);
   } else if (field == TX_FIELD_WALLS) {
     return TX_ERR_ARG;
@@ -165,6 +193,14 @@ int stage_field(tx_handle* h, int field) {
 namespace tx {
 int validate_params(const tx_params* p, std::string* why) { return validate(p, why); }
 void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out) { fill_phys_impl(p, D, S, Q, *out); }
+bool select_species(const tx_params* p, SpeciesSet* ss) {
+  using Fn = bool (*)(bool, SpeciesSet*);
+  static const Fn table[4][2] = {{species_d3_exact, species_d2_exact}, {species_d3_f64, species_d2_f64},
+                                 {species_d3_f32, species_d2_f32}, {species_d3_f16, species_d2_f16}};
+  const int form = p->precision == TX_PREC_F64 ? (p->exact ? 0 : 1) : (p->precision == TX_PREC_F32 ? 2 : 3);
+  return table[form][p->discretization == TX_D3Q19 ? 0 : 1](p->species_relaxation_mode == TX_RELAX_MRT, ss);
+}
+
 bool select_kernels(const tx_params* p, KernelSet* ks) {
   const bool mrt = p->relaxation_mode == TX_RELAX_MRT;
   using Fn = bool (*)(int, int, bool, KernelSet*);
@@ -200,6 +236,12 @@ int tx_params_default(tx_params* p) {
   p->precision = TX_PREC_F64;
   for (int m = 0; m < TX_MAX_COMPONENTS; ++m) p->rho0[m] = 0.0;
   p->storage_scale = 1.0;
+  p->nspecies = 0;
+  p->species_relaxation_mode = TX_RELAX_SRT;
+  for (int m = 0; m < TX_MAX_COMPONENTS; ++m) {
+    p->species_tau[m] = 1.0;
+    for (int k = 0; k < 7; ++k) p->species_rates[m][k] = 1.0;
+  }
   return TX_OK;
 }
 
@@ -239,7 +281,8 @@ int tx_create(const tx_params* p, tx_handle** out) {
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup("cudaStreamCreate failed", TX_ERR_CUDA);
   const size_t popb = (size_t)N * h->S * h->Q * h->pop_bytes;
-  const size_t stageb = (size_t)N * h->S * h->Q * sizeof(double);
+  h->NS = p->nspecies;
+  const size_t stageb = (size_t)N * (h->S > h->NS ? h->S : h->NS) * h->Q * sizeof(double);
   if (cudaMalloc(&h->f[0], popb) != cudaSuccess || cudaMalloc(&h->f[1], popb) != cudaSuccess ||
       cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
       cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->links, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
@@ -255,6 +298,23 @@ int tx_create(const tx_params* p, tx_handle** out) {
     return cleanup("parameter upload failed", TX_ERR_CUDA);
   cudaMemsetAsync(h->f[0], 0, popb, h->stream);
   cudaMemsetAsync(h->f[1], 0, popb, h->stream);
+  if (h->NS > 0) {
+    if (!select_species(p, &h->ss)) return cleanup("no species kernel built for this form", TX_ERR_ARG);
+    const size_t gb = (size_t)N * h->NS * h->Q * h->pop_bytes;
+    SpeciesPhysT<double> sp{};
+    fill_species_phys(*p, h->D, sp);
+    SpeciesPhysT<float> sp32{};
+    convert_species(sp, &sp32);
+    const bool f64 = p->precision == TX_PREC_F64;
+    const size_t spb = f64 ? sizeof(sp) : sizeof(sp32);
+    if (cudaMalloc(&h->sg[0], gb) != cudaSuccess || cudaMalloc(&h->sg[1], gb) != cudaSuccess ||
+        cudaMalloc(&h->d_sphys, spb) != cudaSuccess)
+      return cleanup("device allocation failed", TX_ERR_NOMEM);
+    if (cudaMemcpy(h->d_sphys, f64 ? (const void*)&sp : (const void*)&sp32, spb, cudaMemcpyHostToDevice) != cudaSuccess)
+      return cleanup("species parameter upload failed", TX_ERR_CUDA);
+    cudaMemsetAsync(h->sg[0], 0, gb, h->stream);
+    cudaMemsetAsync(h->sg[1], 0, gb, h->stream);
+  }
   cudaMemsetAsync(h->rho, 0, (size_t)N * h->S * h->rho_bytes, h->stream);
   cudaMemsetAsync(h->mask, 0, (size_t)N, h->stream);
   h->host_mask.assign((size_t)N, 0);
@@ -293,6 +353,11 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->mask);
   cudaFree(h->links);
   cudaFree(h->stage);
+  cudaFree(h->sg[0]);
+  cudaFree(h->sg[1]);
+  cudaFree(h->d_sphys);
+  cudaFree(h->sconc);
+  cudaFree(h->sflux);
   cudaFree(h->old_rho);
   cudaFree(h->old_fi);
   cudaFree(h->uic);
@@ -354,6 +419,24 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
   return TX_OK;
 }
 
+int tx_upload_species(tx_handle* h, const double* conc, const double* flux) {
+  if (!h || !conc) return TX_ERR_ARG;
+  if (h->NS == 0) return fail(h, TX_ERR_STATE, "the handle was created with nspecies = 0");
+  const long long N = h->g.n;
+  const size_t cb = (size_t)N * h->NS * sizeof(double), fb = cb * h->D;
+  if (!h->sconc) TX_CUDA(h, cudaMalloc(&h->sconc, cb));
+  TX_CUDA(h, cudaMemcpyAsync(h->sconc, conc, cb, cudaMemcpyHostToDevice, h->stream));
+  cudaFree(h->sflux);
+  h->sflux = nullptr;
+  if (flux) {
+    TX_CUDA(h, cudaMalloc(&h->sflux, fb));
+    TX_CUDA(h, cudaMemcpyAsync(h->sflux, flux, fb, cudaMemcpyHostToDevice, h->stream));
+  }
+  h->have_species = true;
+  h->inited = false;
+  return sync_stream(h);
+}
+
 int tx_upload_fi(tx_handle* h, const double* fi) {
   if (!h || !fi) return TX_ERR_ARG;
   const long long N = h->g.n;
@@ -395,6 +478,12 @@ int tx_init(tx_handle* h) {
   h->ks.density(args(h, h->cur, h->cur), 1, h->stream);
   int rc = check_launch(h, "k_density");
   if (rc) return rc;
+  if (h->NS > 0 && h->have_species) {
+    // TransportFiInit; TransportUpdateMoments happens in the next collision
+    h->ss.init(species_args(h, h->gcur, h->gcur), h->sconc, h->sflux, h->stream);
+    rc = check_launch(h, "k_species_init");
+    if (rc) return rc;
+  }
   rc = sync_stream(h);
   if (rc) return rc;
   cudaFree(h->uic);
@@ -415,6 +504,10 @@ int tx_step(tx_handle* h, int32_t nsteps) {
     if (h->timing) cudaEventRecord(h->ev[1], h->stream);
     h->ks.density(a, 0, h->stream);
     if (h->timing) cudaEventRecord(h->ev[2], h->stream);
+    if (h->NS > 0 && h->have_species) {
+      h->ss.step(species_args(h, h->gcur, 1 - h->gcur), h->stream);
+      h->gcur = 1 - h->gcur;
+    }
     int rc = check_launch(h, "k_step/k_density");
     if (rc) return rc;
     h->cur = nxt;

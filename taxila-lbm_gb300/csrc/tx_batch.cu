@@ -292,8 +292,8 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   if (!form || !out) return TX_ERR_ARG;
   *out = nullptr;
   tx_params f = *form;
-  if (f.exact) {
-    tx::set_global_error("batches run the fast forms only (exact must be 0)");
+  if (f.exact || f.nspecies) {
+    tx::set_global_error("batches run the fast forms of the flow only (exact and nspecies must be 0)");
     return TX_ERR_ARG;
   }
   // the geometry of the form is irrelevant: validate it on a small lattice
@@ -366,7 +366,7 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   const tx_params& f = b->form;
   if (p->discretization != f.discretization || p->ncomponents != f.ncomponents ||
       p->relaxation_mode != f.relaxation_mode || p->isotropy_order != f.isotropy_order ||
-      p->precision != f.precision || p->exact)
+      p->precision != f.precision || p->exact || p->nspecies)
     return bfail(b, TX_ERR_ARG, "lattice parameters do not match the batch's kernel form");
   const long long bytes = lattice_bytes(*p);
   if (b->budget && b->in_use + bytes > b->budget)

@@ -7,6 +7,7 @@
 #include "tx_batch.cuh"
 #include "tx_host_params.h"
 #include "tx_kernels.cuh"
+#include "tx_species.cuh"
 
 namespace tx {
 
@@ -23,6 +24,21 @@ struct KernelSet {
   void (*probe_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   const char* name;
 };
+
+// Passive-species kernels of one (dimension, form); built by the s1 units.
+struct SpeciesSet {
+  void (*step)(const SpeciesArgs&, cudaStream_t);
+  void (*init)(const SpeciesArgs&, const double* conc, const double* flux, cudaStream_t);
+  void (*fields)(const SpeciesArgs&, int what, double* out, cudaStream_t);
+};
+bool species_d3_exact(bool mrt, SpeciesSet* ss);
+bool species_d2_exact(bool mrt, SpeciesSet* ss);
+bool species_d3_f64(bool mrt, SpeciesSet* ss);
+bool species_d2_f64(bool mrt, SpeciesSet* ss);
+bool species_d3_f32(bool mrt, SpeciesSet* ss);
+bool species_d2_f32(bool mrt, SpeciesSet* ss);
+bool species_d3_f16(bool mrt, SpeciesSet* ss);
+bool species_d2_f16(bool mrt, SpeciesSet* ss);
 
 bool kernels_d3_exact_s1(int S, int ISO, bool MRT, KernelSet* ks);
 bool kernels_d3_exact_s2(int S, int ISO, bool MRT, KernelSet* ks);

@@ -9,6 +9,7 @@
 
 #include "../../include/taxila_gb300.h"
 #include "tx_kernels.cuh"
+#include "tx_species.cuh"
 
 namespace tx {
 
@@ -48,6 +49,13 @@ inline int validate(const tx_params* p, std::string* why) {
       if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
         return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
     }
+  }
+  if (p->nspecies < 0 || p->nspecies > TX_MAX_COMPONENTS) return bad("nspecies out of range");
+  if (p->nspecies > 0) {
+    if (p->species_relaxation_mode != TX_RELAX_SRT && p->species_relaxation_mode != TX_RELAX_MRT)
+      return bad("species_relaxation_mode must be 0 or 1");
+    for (int s = 0; s < p->nspecies; ++s)
+      if (p->species_relaxation_mode == TX_RELAX_SRT && !(p->species_tau[s] > 0.0)) return bad("species tau must be > 0");
   }
   for (int m = 0; m < p->ncomponents; ++m) {
     if (!std::isfinite(p->rho0[m])) return bad("rho0 must be finite");
@@ -149,6 +157,53 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
     P.cA[m][2] = -(1.0 / 36.0) * rel * P.rho0[m];
   }
   P.inv_sscale = 1.0 / P.sscale;
+}
+
+// Species relaxation (SpecieSetFromOptions, lbm_species.F90:111-133; the
+// MRT rate map of DiscretizationSetupRelax) and the fast form's base rate.
+inline void fill_species_phys(const tx_params& p, int D, SpeciesPhysT<double>& P) {
+  std::memset(&P, 0, sizeof(P));
+  const int Q = D == 3 ? 19 : 9;
+  P.sscale = p.precision == TX_PREC_F32_F16 && p.storage_scale > 0.0 ? p.storage_scale : 1.0;
+  P.inv_sscale = 1.0 / P.sscale;
+  for (int s = 0; s < p.nspecies; ++s) {
+    SpecieRelax<double>& r = P.sp[s];
+    r.tau = p.species_tau[s];
+    r.inv_tau = 1.0 / p.species_tau[s];
+    for (int k = 0; k < Q; ++k) r.srate[k] = p.species_rates[s][D == 3 ? rate_of<3>(k) : rate_of<2>(k)];
+    if (p.species_relaxation_mode == TX_RELAX_SRT) {
+      r.s0 = 1.0 / p.species_tau[s];
+    } else {
+      int best = 0, best_count = -1;
+      for (int k = 0; k < Q; ++k) {
+        int c = 0;
+        for (int j = 0; j < Q; ++j) c += r.srate[j] == r.srate[k];
+        if (c > best_count) { best_count = c; best = k; }
+      }
+      r.s0 = r.srate[best];
+      for (int k = 0; k < Q; ++k) {
+        if (r.srate[k] == r.s0) continue;
+        r.spec_mask |= 1u << k;
+        r.dspec[k] = (r.srate[k] - r.s0) / (D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k));
+      }
+    }
+  }
+}
+
+template <class R>
+inline void convert_species(const SpeciesPhysT<double>& a, SpeciesPhysT<R>* b) {
+  for (int s = 0; s < MAXC; ++s) {
+    b->sp[s].tau = R(a.sp[s].tau);
+    b->sp[s].inv_tau = R(a.sp[s].inv_tau);
+    b->sp[s].s0 = R(a.sp[s].s0);
+    b->sp[s].spec_mask = a.sp[s].spec_mask;
+    for (int k = 0; k < 19; ++k) {
+      b->sp[s].srate[k] = R(a.sp[s].srate[k]);
+      b->sp[s].dspec[k] = R(a.sp[s].dspec[k]);
+    }
+  }
+  b->sscale = R(a.sscale);
+  b->inv_sscale = R(a.inv_sscale);
 }
 
 // Reference wall value (lbm_walls.F90:151-177) -> device mask code:

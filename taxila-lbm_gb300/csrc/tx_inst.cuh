@@ -17,6 +17,31 @@ TX_L(10, true)
 #undef TX_L
 }  // namespace
 
+#ifdef TX_SPECIES_FN
+namespace {
+template <bool MRT>
+struct SpeciesLaunch {
+  static void step(const SpeciesArgs& a, cudaStream_t s) {
+    k_species<TX_D, MRT, TX_EXACT, TX_T, TX_R><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a);
+  }
+  static void init(const SpeciesArgs& a, const double* conc, const double* flux, cudaStream_t s) {
+    k_species_init<TX_D, TX_T, TX_R><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, conc, flux);
+  }
+  static void fields(const SpeciesArgs& a, int what, double* out, cudaStream_t s) {
+    k_species_fields<TX_D, TX_T, TX_R><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, what, out);
+  }
+};
+}  // namespace
+
+bool TX_SPECIES_FN(bool mrt, SpeciesSet* ss) {
+  if (mrt)
+    *ss = SpeciesSet{&SpeciesLaunch<true>::step, &SpeciesLaunch<true>::init, &SpeciesLaunch<true>::fields};
+  else
+    *ss = SpeciesSet{&SpeciesLaunch<false>::step, &SpeciesLaunch<false>::init, &SpeciesLaunch<false>::fields};
+  return true;
+}
+#endif
+
 bool TX_FN(int s, int iso, bool mrt, KernelSet* ks) {
   TX_FORM_CASE(TX_S, 4, false)
   TX_FORM_CASE(TX_S, 4, true)

@@ -6,4 +6,5 @@
 #define TX_R float
 #define TX_RT float
 #define TX_FN kernels_d2_f32_s1
+#define TX_SPECIES_FN species_d2_f32
 #include "tx_inst.cuh"

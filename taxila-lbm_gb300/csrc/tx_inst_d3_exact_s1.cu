@@ -6,4 +6,5 @@
 #define TX_R double
 #define TX_RT double
 #define TX_FN kernels_d3_exact_s1
+#define TX_SPECIES_FN species_d3_exact
 #include "tx_inst.cuh"

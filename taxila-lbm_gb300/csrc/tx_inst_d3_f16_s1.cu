@@ -6,4 +6,5 @@
 #define TX_R float
 #define TX_RT float
 #define TX_FN kernels_d3_f16_s1
+#define TX_SPECIES_FN species_d3_f16
 #include "tx_inst.cuh"

@@ -6,4 +6,5 @@
 #define TX_R double
 #define TX_RT double
 #define TX_FN kernels_d3_f64_s1
+#define TX_SPECIES_FN species_d3_f64
 #include "tx_inst.cuh"

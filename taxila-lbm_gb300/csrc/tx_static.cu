@@ -90,6 +90,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   int rc = validate_params(p, &why);
   if (rc) return static_fail(rc, why);
   if (p->precision != TX_PREC_F64) return static_fail(TX_ERR_ARG, "tx_step_static runs the FP64 form only");
+  if (p->nspecies != 0) return static_fail(TX_ERR_ARG, "tx_step_static runs the flow only (nspecies must be 0)");
   KernelSet ks{};
   if (!select_kernels(p, &ks)) return static_fail(TX_ERR_ARG, "no kernel built for this parameter combination");
 

@@ -46,6 +46,7 @@ def load():
         "tx_upload_walls": ([vp, dp], C.c_int),
         "tx_upload_state": ([vp, dp, dp], C.c_int),
         "tx_upload_fi": ([vp, dp], C.c_int),
+        "tx_upload_species": ([vp, dp, dp], C.c_int),
         "tx_upload_bc_values": ([vp, i32, dp], C.c_int),
         "tx_init": ([vp], C.c_int),
         "tx_step": ([vp, i32], C.c_int),
@@ -137,6 +138,10 @@ class Handle:
     def upload_state(self, rho, u=None):
         r, v = f64(rho), f64(u)
         self._check(self.L.tx_upload_state(self.h, dptr(r), dptr(v)))
+
+    def upload_species(self, conc, flux=None):
+        c, f = f64(conc), f64(flux)
+        self._check(self.L.tx_upload_species(self.h, dptr(c), dptr(f)))
 
     def upload_fi(self, fi):
         f = f64(fi)

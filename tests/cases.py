@@ -125,3 +125,40 @@ def permeability(p, u_sum_z, nsites):
     """k = nu <u_z> phi / g, with <u_z> phi = sum of u_z over pore sites / all sites."""
     nu = (p.tau[0] - 0.5) / 3.0
     return nu * (u_sum_z / nsites) / p.gvt[2]
+
+
+def with_species(p, walls, mode=P.SRT, tau=0.8, ns=1, front=4):
+    """Adds ns passive species to p (in place): concentration 1 in the first
+    ``front`` slices along the last axis of the lattice (z in 3D, y in 2D) on
+    pore sites, 0 elsewhere; species s has tau + 0.1 s (MRT: s_nu = 1/tau,
+    s_e = 1.1, other rates 1).  Returns the concentration array [N*ns]."""
+    p.nspecies = ns
+    p.species_relaxation_mode = mode
+    axis = 0 if p.ndims == 3 else 1
+    first = np.indices(p.shape)[axis].ravel() < front
+    pore = np.asarray(walls).ravel() == 0
+    conc = np.zeros((p.nsites, ns))
+    for s in range(ns):
+        p.species_tau[s] = tau + 0.1 * s
+        for k in range(7):
+            p.species_rates[s][k] = 1.0
+        if mode == P.MRT:
+            p.species_rates[s][4] = 1.0 / (tau + 0.1 * s)
+            p.species_rates[s][1] = 1.1
+        conc[:, s] = np.where(first & pore, 1.0 - 0.2 * s, 0.0)
+    return conc.ravel()
+
+
+# (name, case factory returning (p, walls, rho, conc), steps): species parity matrix
+def _sp(make, mode, ns=1):
+    def f():
+        p, w, r = make()
+        return p, w, r, with_species(p, w, mode=mode, ns=ns)
+    return f
+
+
+SPECIES = [
+    ("d3_srt_species", _sp(lambda: porous_case(P.D3Q19, (12, 10, 14), body=True), P.SRT), 20),
+    ("d3_mrt_two_species", _sp(lambda: sc_bubble(P.D3Q19, (12, 12, 10), P.MRT, 4), P.MRT, ns=2), 20),
+    ("d2_species_streaming", _sp(lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), P.SRT), 30),
+]

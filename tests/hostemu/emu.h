@@ -21,10 +21,12 @@ struct Case {
   int from_fi = 0;            // 0: tx_upload_state + tx_init, 1: tx_upload_fi + tx_init
   std::vector<double> walls;  // [N]
   std::vector<double> init;   // rho [N*S] or fi [N*S*Q], natural order
+  std::vector<double> conc;   // species concentrations [N*ns] (empty: no species)
 };
 
 struct Result {
   std::vector<double> fi, rho, flux, forces;  // natural order, as tx_download
+  std::vector<double> sfi, srho, sflux;       // species fields (when the case has species)
 };
 
 // the library's launch3 shape, walked block by block and thread by thread
@@ -135,11 +137,57 @@ std::string run(const Case& c, Result& out) {
     const StepArgs a = args(cur, cur);
     launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 1); });
   }
+  // species: as tx_create / tx_upload_species / tx_init / tx_step
+  const int NS = c.conc.empty() ? 0 : p.nspecies;
+  SpeciesPhysT<double> sp{};
+  fill_species_phys(p, D, sp);
+  SpeciesPhysT<R> spR{};
+  if constexpr (std::is_same<R, double>::value)
+    spR = sp;
+  else
+    convert_species(sp, &spR);
+  std::vector<T> g0((size_t)N * (NS ? NS : 1) * Q), g1(g0.size());
+  std::memset(g0.data(), 0, g0.size() * sizeof(T));
+  std::memset(g1.data(), 0, g1.size() * sizeof(T));
+  T* gbuf[2] = {g0.data(), g1.data()};
+  int gcur = 0;
+  auto sargs = [&](int in, int o) {
+    SpeciesArgs a{};
+    a.gin = gbuf[in];
+    a.gout = gbuf[o];
+    a.links = links.data();
+    a.mask = mask.data();
+    a.phys = &spR;
+    a.g = g;
+    a.ns = NS;
+    return a;
+  };
+  if (NS) {
+    const SpeciesArgs a = sargs(gcur, gcur);
+    launch3(g, 128, [&] { k_species_init<D, T, R>(a, c.conc.data(), nullptr); });
+  }
   for (int t = 0; t < c.nsteps; ++t) {
     const StepArgs a = args(cur, 1 - cur);
     launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 0); });
     cur = 1 - cur;
+    if (NS) {
+      const SpeciesArgs sa = sargs(gcur, 1 - gcur);
+      if (p.species_relaxation_mode == TX_RELAX_MRT)
+        launch3(g, 128, [&] { k_species<D, true, EXACT, T, R>(sa); });
+      else
+        launch3(g, 128, [&] { k_species<D, false, EXACT, T, R>(sa); });
+      gcur = 1 - gcur;
+    }
+  }
+  if (NS) {
+    const SpeciesArgs sa = sargs(gcur, gcur);
+    out.sfi.assign((size_t)N * NS * Q, 0.0);
+    out.srho.assign((size_t)N * NS, 0.0);
+    out.sflux.assign((size_t)N * NS * D, 0.0);
+    launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 9, out.sfi.data()); });
+    launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 10, out.srho.data()); });
+    launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 11, out.sflux.data()); });
   }
   out.fi.assign((size_t)N * S * Q, 0.0);
   launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], mask.data(), N, sh, out.fi.data()); });

@@ -1,8 +1,10 @@
 // emu <case.bin> <result.bin>: one flow run of the host emulation.
 //
 // case.bin:   tx_params (raw struct) | int32 nsteps | int32 from_fi |
-//             walls [N] f64 | rho [N*S] or fi [N*S*Q] f64 (natural order)
-// result.bin: fi [N*S*Q] | rho [N*S] | flux [N*D*S] | forces [N*D*S], f64
+//             walls [N] f64 | rho [N*S] or fi [N*S*Q] f64 (natural order) |
+//             species concentrations [N*ns] f64 when params.nspecies > 0
+// result.bin: fi [N*S*Q] | rho [N*S] | flux [N*D*S] | forces [N*D*S], then
+//             species gi [N*ns*Q] | concentration [N*ns] | flux [N*D*ns], f64
 // Exit status 0 on success, 2 for parameters the library rejects (message on
 // stderr), 3 when the combination is not compiled into the emulation.
 #include <cstdio>
@@ -36,6 +38,10 @@ int main(int argc, char** argv) {
   c.walls.resize((size_t)N);
   c.init.resize((size_t)(N * S * (c.from_fi ? Q : 1)));
   if (!read_all(f, c.walls.data(), c.walls.size() * 8) || !read_all(f, c.init.data(), c.init.size() * 8)) return 1;
+  if (c.p.nspecies > 0) {
+    c.conc.resize((size_t)(N * c.p.nspecies));
+    if (!read_all(f, c.conc.data(), c.conc.size() * 8)) return 1;
+  }
   fclose(f);
 
   Result r;
@@ -52,7 +58,8 @@ int main(int argc, char** argv) {
   }
   FILE* o = fopen(argv[2], "wb");
   if (!o) return 1;
-  for (const std::vector<double>* v : {&r.fi, &r.rho, &r.flux, &r.forces}) fwrite(v->data(), 8, v->size(), o);
+  for (const std::vector<double>* v : {&r.fi, &r.rho, &r.flux, &r.forces, &r.sfi, &r.srho, &r.sflux})
+    if (!v->empty()) fwrite(v->data(), 8, v->size(), o);
   fclose(o);
   return 0;
 }

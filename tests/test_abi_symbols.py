@@ -36,7 +36,7 @@ def test_library_exports_all_declared():
 def test_params_struct_layout():
     # ctypes mirror matches the C struct (offset of the last field + its size)
     from taxila import params as P
-    assert ctypes.sizeof(P.TxParams) == P.TxParams.storage_scale.offset + 8
+    assert ctypes.sizeof(P.TxParams) == P.TxParams.species_rates.offset + 8 * 7 * P.MAXC
 
 
 def test_params_default_matches_c():

@@ -45,7 +45,10 @@ def emu_exe():
     return build_emu.build()
 
 
-def run_emu(exe, p, walls, init, steps, from_fi, tmp_path):
+SPECIES_FIELDS = ("sfi", "srho", "sflux")
+
+
+def run_emu(exe, p, walls, init, steps, from_fi, tmp_path, conc=None):
     case = os.path.join(str(tmp_path), "case.bin")
     res = os.path.join(str(tmp_path), "result.bin")
     with open(case, "wb") as f:
@@ -53,13 +56,16 @@ def run_emu(exe, p, walls, init, steps, from_fi, tmp_path):
         f.write(np.array([steps, 1 if from_fi else 0], dtype=np.int32).tobytes())
         f.write(np.ascontiguousarray(walls, dtype=np.float64).tobytes())
         f.write(np.ascontiguousarray(init, dtype=np.float64).tobytes())
+        if p.nspecies > 0:
+            f.write(np.ascontiguousarray(conc, dtype=np.float64).tobytes())
     r = subprocess.run([exe, case, res], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, "emu exit %d: %s" % (r.returncode, r.stderr[-3000:])
     raw = np.fromfile(res, dtype=np.float64)
-    n, s, d, q = p.nsites, p.ncomponents, p.ndims, p.Q
-    sizes = {"fi": n * s * q, "rho": n * s, "flux": n * s * d, "forces": n * s * d}
+    n, s, d, q, ns = p.nsites, p.ncomponents, p.ndims, p.Q, p.nspecies
+    sizes = {"fi": n * s * q, "rho": n * s, "flux": n * s * d, "forces": n * s * d,
+             "sfi": n * ns * q, "srho": n * ns, "sflux": n * ns * d}
     out, o = {}, 0
-    for k in FIELDS:
+    for k in FIELDS + (SPECIES_FIELDS if ns else ()):
         out[k] = raw[o:o + sizes[k]]
         o += sizes[k]
     assert o == raw.size
@@ -79,10 +85,10 @@ def oracle_run(p, walls, rho, steps, fi=None):
     return {k: o.get(v) for k, v in ORACLE_FIELDS.items()}
 
 
-def compare(ref, got, p, walls, tol):
+def compare(ref, got, p, walls, tol, fields=FIELDS):
     pore = np.asarray(walls).ravel() == 0
     errs = {}
-    for k in FIELDS:
+    for k in fields:
         a, b = ref[k], got[k]
         t = tol[k] if isinstance(tol, dict) else tol
         m = np.repeat(pore, a.size // p.nsites)
@@ -152,3 +158,24 @@ def test_emulated_permeability_precision(emu_exe, tmp_path, prec, scale):
     k_ref = cases.permeability(p, ref["flux"].reshape(-1, 3)[pore, 2].sum(), p.nsites)
     k_got = cases.permeability(p, got["flux"].reshape(-1, 3)[pore, 2].sum(), p.nsites)
     assert abs(k_got / k_ref - 1.0) < 1e-3
+
+
+@pytest.mark.parametrize("name,make,steps", cases.SPECIES, ids=[c[0] for c in cases.SPECIES])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_emulated_species_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
+    p, walls, rho, conc = make()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.set_species(conc)
+    o.init()
+    o.step(steps)
+    ref = {"sfi": o.get(P.FIELD_SPECIES_FI), "srho": o.get(P.FIELD_SPECIES_RHO),
+           "sflux": o.get(P.FIELD_SPECIES_FLUX), "fi": o.get(P.FIELD_FI)}
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path, conc=conc)
+    compare(ref, got, p, walls, 0.0 if exact else 1e-12, fields=("fi",) + SPECIES_FIELDS)
+    pore = walls == 0
+    mass0 = np.asarray(conc).reshape(p.nsites, -1)[pore].sum(axis=0)
+    assert np.allclose(got["srho"].reshape(p.nsites, -1)[pore].sum(axis=0), mass0, rtol=1e-12)
