@@ -363,7 +363,8 @@ def serving_run(n=30, rate=30.0, seed=1):
     from taxila import serve
     reqs = serve.make_mix(seed=seed, n=n, rate=rate)
     out = {"mix": "%d requests, Poisson %.0f/s, seed %d: 70%% permeability (D3Q19 sides 32-64, tol 1e-5 on the "
-                  "mean flow), 30%% drainage (D3Q19 32-48 or D2Q9 96-192, 1500 steps)" % (n, rate, seed)}
+                  "mean flow), 30%% drainage with one passive tracer (D3Q19 32-48 or D2Q9 96-192, 1500 steps)"
+                  % (n, rate, seed)}
     for name, prec, maxa in (("fp32_fp16_storage", P.PREC_F32_F16, None), ("fp32", P.PREC_F32, None),
                              ("fp64_sequential", P.PREC_F64, 1)):
         for mode, realtime in (("", True), ("_saturated", False)):

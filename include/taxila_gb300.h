@@ -242,8 +242,9 @@ typedef struct {
   int64_t steps;
 } tx_probe;
 
-/* form: discretization, ncomponents, relaxation_mode, isotropy_order and
- * precision shared by every lattice of the batch (exact must be 0).
+/* form: discretization, ncomponents, relaxation_mode, isotropy_order,
+ * precision, nspecies and species_relaxation_mode shared by every lattice of
+ * the batch (exact must be 0).
  * hbm_budget_bytes > 0 caps the device memory of all lattices together;
  * tx_batch_add fails with TX_ERR_NOMEM above it. */
 int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** out);
@@ -254,10 +255,12 @@ int64_t tx_batch_lattice_bytes(const tx_params* p);
 int64_t tx_batch_bytes_in_use(const tx_batch* b);
 int32_t tx_batch_count(const tx_batch* b);
 
-/* Adds a lattice (walls and initial state as tx_upload_walls + tx_upload_state,
- * then tx_init) and returns its id.  It joins the next step of the batch. */
+/* Adds a lattice (walls and initial state as tx_upload_walls + tx_upload_state
+ * [+ tx_upload_species(conc, NULL)], then tx_init) and returns its id.  It
+ * joins the next step of the batch.  conc is required when the batch form has
+ * species and ignored otherwise. */
 int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const double* rho, const double* u,
-                 int32_t* id);
+                 const double* conc, int32_t* id);
 int tx_batch_remove(tx_batch* b, int32_t id);
 /* nsteps flow steps of every lattice in the batch */
 int tx_batch_step(tx_batch* b, int32_t nsteps);

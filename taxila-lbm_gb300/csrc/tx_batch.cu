@@ -24,6 +24,7 @@ using namespace tx;
 
 namespace tx {
 bool select_kernels(const tx_params* p, KernelSet* ks);
+bool select_species(const tx_params* p, SpeciesSet* ss);
 void set_global_error(const std::string& msg);
 }
 
@@ -43,6 +44,9 @@ struct Lattice {
   double* faceval[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* phys = nullptr;       // PhysT<R> of the batch's arithmetic type
   Faces faces{};
+  void* sg[2] = {nullptr, nullptr};  // species populations
+  void* sphys = nullptr;             // SpeciesPhysT<R>
+  int NS = 0;
   long long bytes = 0;
   long long steps = 0;
 };
@@ -63,6 +67,7 @@ long long lattice_bytes(const tx_params& p) {
                 4 * N + 8LL * D * N + (long long)sizeof(Phys);
   for (int f = 0; f < 2 * D; ++f)
     if (p.bc_flags[f] == TX_BC_DENSITY) b += face_area(p, D, f) * S * 8;
+  if (p.nspecies > 0) b += 2 * N * p.nspecies * Q * (long long)pop_bytes(p.precision) + (long long)sizeof(SpeciesPhysT<double>);
   return b;
 }
 
@@ -71,6 +76,7 @@ long long lattice_bytes(const tx_params& p) {
 struct tx_batch {
   tx_params form{};
   KernelSet ks{};
+  SpeciesSet ss{};
   int D = 3, S = 1, Q = 19;
   cudaStream_t stream = nullptr;
   int sm_count = 1;
@@ -183,6 +189,10 @@ int rebuild_tables(tx_batch* b) {
     LatDesc d{};
     d.a = lattice_args(b, L, 0, 1);
     d.uold = L->uold;
+    d.sg0 = L->sg[0];
+    d.sg1 = L->sg[1];
+    d.sphys = L->sphys;
+    d.ns = L->NS;
     d.tile_begin = (int)tiles.size();
     for (int z = 0; z < L->g.nz; z += b->bz)
       for (int y = 0; y < L->g.ny; y += b->by)
@@ -223,6 +233,7 @@ int launch_step(tx_batch* b, int flip) {
   const BatchArgs a = bargs(b);
   b->ks.step_tiles(a, flip, grid_of(b), blk, b->stream);
   b->ks.density_tiles(a, flip, grid_of(b), blk, b->stream);
+  if (b->form.nspecies > 0) b->ss.step_tiles(a, flip, grid_of(b), blk, b->stream);
   TX_BCUDA(b, cudaGetLastError());
   return TX_OK;
 }
@@ -250,7 +261,8 @@ int capture_graph(tx_batch* b) {
 
 void free_lattice(tx_batch* b, Lattice* L) {
   cudaStream_t s = b->stream;
-  for (void* p : {(void*)L->f[0], (void*)L->f[1], L->rho, (void*)L->mask, (void*)L->links, (void*)L->uold, L->phys})
+  for (void* p : {(void*)L->f[0], (void*)L->f[1], L->rho, (void*)L->mask, (void*)L->links, (void*)L->uold, L->phys,
+                  L->sg[0], L->sg[1], L->sphys})
     if (p) cudaFreeAsync(p, s);
   for (int f = 0; f < 6; ++f)
     if (L->faceval[f]) cudaFreeAsync(L->faceval[f], s);
@@ -260,7 +272,17 @@ void free_lattice(tx_batch* b, Lattice* L) {
 
 int stage(tx_batch* b, const Lattice* L, int field, double* out) {
   const long long N = L->g.n;
-  if (field == TX_FIELD_FI) {
+  if (field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) {
+    SpeciesArgs a{};
+    a.gin = L->sg[b->flip];
+    a.gout = L->sg[b->flip];
+    a.links = L->links;
+    a.mask = L->mask;
+    a.phys = L->sphys;
+    a.g = L->g;
+    a.ns = L->NS;
+    b->ss.fields(a, field, out, b->stream);
+  } else if (field == TX_FIELD_FI) {
     b->ks.to_natural(L->f[b->flip], L->mask, N, shift_of(L->ph), out, b->stream);
   } else {
     const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
@@ -272,7 +294,11 @@ int stage(tx_batch* b, const Lattice* L, int field, double* out) {
 }
 
 long long field_dof(const Lattice* L, int field) {
+  if (L->NS == 0 && field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) return -1;
   switch (field) {
+    case TX_FIELD_SPECIES_FI: return (long long)L->NS * L->Q;
+    case TX_FIELD_SPECIES_RHO: return L->NS;
+    case TX_FIELD_SPECIES_FLUX: return (long long)L->NS * L->D;
     case TX_FIELD_FI: return (long long)L->S * L->Q;
     case TX_FIELD_RHO: return L->S;
     case TX_FIELD_FLUX:
@@ -292,8 +318,8 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   if (!form || !out) return TX_ERR_ARG;
   *out = nullptr;
   tx_params f = *form;
-  if (f.exact || f.nspecies) {
-    tx::set_global_error("batches run the fast forms of the flow only (exact and nspecies must be 0)");
+  if (f.exact) {
+    tx::set_global_error("batches run the fast forms only (exact must be 0)");
     return TX_ERR_ARG;
   }
   // the geometry of the form is irrelevant: validate it on a small lattice
@@ -311,7 +337,7 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   b->S = f.ncomponents;
   b->Q = b->D == 3 ? 19 : 9;
   b->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : 0;
-  if (!select_kernels(&f, &b->ks)) {
+  if (!select_kernels(&f, &b->ks) || (f.nspecies > 0 && !select_species(&f, &b->ss))) {
     delete b;
     tx::set_global_error("no kernel built for this parameter combination");
     return TX_ERR_ARG;
@@ -358,15 +384,17 @@ int32_t tx_batch_count(const tx_batch* b) { return b ? (int32_t)b->slots.size() 
 void* tx_batch_stream(tx_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const double* rho, const double* u,
-                 int32_t* id) {
+                 const double* conc, int32_t* id) {
   if (!b || !p || !walls || !rho || !id) return TX_ERR_ARG;
+  if (p->nspecies > 0 && !conc) return bfail(b, TX_ERR_ARG, "the lattice has species: conc is required");
   std::string why;
   int rc = tx::validate(p, &why);
   if (rc) return bfail(b, rc, why);
   const tx_params& f = b->form;
   if (p->discretization != f.discretization || p->ncomponents != f.ncomponents ||
       p->relaxation_mode != f.relaxation_mode || p->isotropy_order != f.isotropy_order ||
-      p->precision != f.precision || p->exact || p->nspecies)
+      p->precision != f.precision || p->exact || p->nspecies != f.nspecies ||
+      (p->nspecies > 0 && p->species_relaxation_mode != f.species_relaxation_mode))
     return bfail(b, TX_ERR_ARG, "lattice parameters do not match the batch's kernel form");
   const long long bytes = lattice_bytes(*p);
   if (b->budget && b->in_use + bytes > b->budget)
@@ -446,6 +474,21 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
     L->faces.vals[fc] = L->faceval[fc];
   }
   if (u) TX_BALLOC(uic, ut.size() * sizeof(double));
+  // species: populations, parameters and the initial concentration
+  double* sconc = nullptr;
+  SpeciesPhysT<double> sp{};
+  SpeciesPhysT<float> sp32{};
+  const size_t spb = p->precision == TX_PREC_F64 ? sizeof(sp) : sizeof(sp32);
+  const size_t gb = (size_t)N * p->nspecies * Q * pop_bytes(p->precision);
+  if (p->nspecies > 0) {
+    L->NS = p->nspecies;
+    fill_species_phys(*p, D, sp);
+    convert_species(sp, &sp32);
+    TX_BALLOC(L->sg[0], gb);
+    TX_BALLOC(L->sg[1], gb);
+    TX_BALLOC(L->sphys, spb);
+    TX_BALLOC(sconc, (size_t)N * p->nspecies * sizeof(double));
+  }
 #undef TX_BALLOC
   const void* phsrc = p->precision == TX_PREC_F64 ? (const void*)&L->ph : (const void*)&ph32;
   bool ok = cudaMemcpyAsync(L->phys, phsrc, physb, cudaMemcpyHostToDevice, st) == cudaSuccess &&
@@ -456,7 +499,15 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
     ok = rt32.empty() ? cudaMemcpyAsync(L->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, st) == cudaSuccess
                       : cudaMemcpyAsync(L->rho, rt32.data(), rt32.size() * 4, cudaMemcpyHostToDevice, st) == cudaSuccess;
   if (ok && uic) ok = cudaMemcpyAsync(uic, ut.data(), ut.size() * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess;
-  if (!ok) return undo("state upload failed", TX_ERR_CUDA);
+  if (ok && L->NS > 0)
+    ok = cudaMemcpyAsync(L->sphys, p->precision == TX_PREC_F64 ? (const void*)&sp : (const void*)&sp32, spb,
+                         cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaMemsetAsync(L->sg[0], 0, gb, st) == cudaSuccess && cudaMemsetAsync(L->sg[1], 0, gb, st) == cudaSuccess &&
+         cudaMemcpyAsync(sconc, conc, (size_t)N * L->NS * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess;
+  if (!ok) {
+    if (sconc) cudaFreeAsync(sconc, st);
+    return undo("state upload failed", TX_ERR_CUDA);
+  }
   {
     const Launch3 l = launch3(L->g, 256);
     if (D == 3)
@@ -468,11 +519,24 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   const StepArgs a = lattice_args(b, L, b->flip, b->flip);
   b->ks.init(a, uic, st);
   b->ks.density(a, 1, st);
+  if (L->NS > 0) {
+    // TransportFiInit into the species buffer of the batch's flip
+    SpeciesArgs sa{};
+    sa.gin = L->sg[b->flip];
+    sa.gout = L->sg[b->flip];
+    sa.links = L->links;
+    sa.mask = L->mask;
+    sa.phys = L->sphys;
+    sa.g = L->g;
+    sa.ns = L->NS;
+    b->ss.init(sa, sconc, nullptr, st);
+  }
   const cudaError_t e = cudaGetLastError();
   const cudaError_t es = cudaStreamSynchronize(st);  // the host staging vectors die with this call
   if (e != cudaSuccess || es != cudaSuccess)
     return undo(std::string("lattice init: ") + cudaGetErrorString(e != cudaSuccess ? e : es), TX_ERR_CUDA);
   if (uic) cudaFreeAsync(uic, st);
+  if (sconc) cudaFreeAsync(sconc, st);
   L->bytes = bytes;
   b->in_use += bytes;
   L->id = b->next_id++;

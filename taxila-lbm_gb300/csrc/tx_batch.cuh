@@ -20,6 +20,7 @@
 // LatDesc::a.fout.
 #pragma once
 #include "tx_kernels.cuh"
+#include "tx_species.cuh"
 
 namespace tx {
 
@@ -28,6 +29,11 @@ struct LatDesc {
   double* uold;       // velocity at the previous probe, [d * N + cell]
   int tile_begin;     // this lattice's tiles in the table
   int tile_count;
+  // passive species: populations at flip 0 / the other buffer, parameters
+  const void* sg0;
+  void* sg1;
+  const void* sphys;
+  int ns;
 };
 
 // per-tile partial of a probe: velocity change and velocity statistics over pore sites
@@ -74,6 +80,26 @@ __global__ void __launch_bounds__(128) k_density_tiles(BatchArgs b, int flip) {
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
     if (x < a.g.nx && y < a.g.ny && z < a.g.nz) density_site<D, S, T, R, RT>(a, x, y, z, 0);
+  }
+}
+
+// species step of every lattice after the flow step at the same flip
+template <int D, bool MRT, class T, class R>
+__global__ void __launch_bounds__(128) k_species_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.ntiles);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.tiles + t);
+    const LatDesc& L = b.lats[tl.x];
+    SpeciesArgs a{};
+    a.gin = flip ? L.sg1 : L.sg0;
+    a.gout = flip ? const_cast<void*>(L.sg0) : L.sg1;
+    a.links = L.a.links;
+    a.mask = L.a.mask;
+    a.phys = L.sphys;
+    a.g = L.a.g;
+    a.ns = L.ns;
+    const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    if (a.ns > 0 && x < a.g.nx && y < a.g.ny && z < a.g.nz) species_site<D, MRT, false, T, R>(a, x, y, z);
   }
 }
 

@@ -30,6 +30,7 @@ struct SpeciesSet {
   void (*step)(const SpeciesArgs&, cudaStream_t);
   void (*init)(const SpeciesArgs&, const double* conc, const double* flux, cudaStream_t);
   void (*fields)(const SpeciesArgs&, int what, double* out, cudaStream_t);
+  void (*step_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);  // no-op in the exact form
 };
 bool species_d3_exact(bool mrt, SpeciesSet* ss);
 bool species_d2_exact(bool mrt, SpeciesSet* ss);

@@ -65,7 +65,7 @@ def load():
         "tx_batch_lattice_bytes": ([C.POINTER(P.TxParams)], i64),
         "tx_batch_bytes_in_use": ([vp], i64),
         "tx_batch_count": ([vp], i32),
-        "tx_batch_add": ([vp, C.POINTER(P.TxParams), dp, dp, dp, C.POINTER(i32)], C.c_int),
+        "tx_batch_add": ([vp, C.POINTER(P.TxParams), dp, dp, dp, dp, C.POINTER(i32)], C.c_int),
         "tx_batch_remove": ([vp, i32], C.c_int),
         "tx_batch_step": ([vp, i32], C.c_int),
         "tx_batch_launch": ([vp, i32], C.c_int),
@@ -226,11 +226,11 @@ class Batch:
     def count(self):
         return self.L.tx_batch_count(self.b)
 
-    def add(self, params, walls, rho, u=None):
+    def add(self, params, walls, rho, u=None, conc=None):
         p = P.copy_params(params)
-        w, r, v = f64(walls), f64(rho), f64(u)
+        w, r, v, c = f64(walls), f64(rho), f64(u), f64(conc)
         lid = C.c_int32()
-        self._check(self.L.tx_batch_add(self.b, C.byref(p), dptr(w), dptr(r), dptr(v), C.byref(lid)))
+        self._check(self.L.tx_batch_add(self.b, C.byref(p), dptr(w), dptr(r), dptr(v), dptr(c), C.byref(lid)))
         return lid.value
 
     def remove(self, lid):

@@ -59,6 +59,11 @@ class LBM:
         self.handle.upload_state(rho, u)
 
     # LBMInitializeStateFromFile (lbm.F90:482-517)
+    # LBMInitializeState_FlowTransport (lbm.F90:455-480): the transport plugin's
+    # concentrations [N*ns] and, optionally, fluxes [N*ndims*ns]
+    def initialize_species(self, conc, flux=None):
+        self.handle.upload_species(conc, flux)
+
     def initialize_state_from_file(self):
         n, s, q = self.params.nsites, self.params.ncomponents, self.params.Q
         if self.run_opts.ic_file:
@@ -93,6 +98,11 @@ class LBM:
         self._write("rho", h.download(P.FIELD_RHO), self.params.ncomponents)
         self._write("u", h.download(P.FIELD_VELT), self.nd)
         self._write("prs", h.download(P.FIELD_PRS), 1)
+        if self.params.nspecies > 0:
+            # TransportOutputDiagnostics (lbm_transport.F90:342-356): gi and psi
+            ns = self.params.nspecies
+            self._write("gi", h.download(P.FIELD_SPECIES_FI), ns * self.params.Q)
+            self._write("psi", h.download(P.FIELD_SPECIES_RHO), ns)
         self.counter += 1
 
     def _write(self, name, arr, dof):

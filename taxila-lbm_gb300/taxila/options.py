@@ -66,6 +66,7 @@ class RunOptions:
     ic_file: str = ""
     ic_file_rho: str = ""
     component_names: list = field(default_factory=list)
+    species_names: list = field(default_factory=list)
     mineral_names: list = field(default_factory=list)
     extra: dict = field(default_factory=dict)
 
@@ -180,6 +181,39 @@ def params_from_options(opts):
                 raise DeckError("-bc_%s_%s: only periodic and density faces are on this path" % (other, fname))
 
     _physical_scales(p, viscosity, density)
+
+    # transport (lbm_options.F90:326-361, TransportSetFromOptions lbm_transport.F90:130-245,
+    # SpecieSetFromOptions lbm_species.F90:111-133)
+    if has("transport_discretization"):
+        tname = get("transport_discretization").strip().lower()
+        if tname.startswith("d3q19"):
+            tdims = 3
+        elif tname.startswith("d2q9"):
+            tdims = 2
+        else:
+            raise DeckError("Invalid Discretization")
+        if tdims != nd:
+            raise DeckError("Flow and transport discretization dimensions don't match")
+        p.nspecies = int(get("nspecies", 1))
+        if not 1 <= p.nspecies <= P.MAXC:
+            raise DeckError("nspecies must be 1..%d" % P.MAXC)
+        p.species_relaxation_mode = int(get("transport_relaxation_mode", 0))
+        if _bool(get("reactive_matrix", "0")):
+            raise DeckError("-reactive_matrix: dissolution/precipitation is not on this path")
+        snames = []
+        rate_keys = ("s_c", "s_e", "s_e2", "s_q", "s_nu", "s_pi", "s_m")
+        for sp in range(p.nspecies):
+            nm = "specie%d" % (sp + 1)
+            nm = (get(nm + "_name") or nm).strip()
+            snames.append(nm)
+            if p.species_relaxation_mode == P.SRT:
+                if has("tau_" + nm):
+                    p.species_tau[sp] = float(get("tau_" + nm))
+            else:
+                for k, key in enumerate(rate_keys):
+                    if has(key + "_" + nm):
+                        p.species_rates[sp][k] = float(get(key + "_" + nm))
+        run.species_names = snames
 
     # driver options (lbm_options.F90:184-262)
     run.npasses = int(get("npasses", 1))

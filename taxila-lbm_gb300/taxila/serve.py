@@ -49,6 +49,7 @@ class Request:
     invader: int = 0
     lo: float = 0.06
     hi: float = 2.0
+    conc: object = None    # passive-species concentrations [N*ns] (drainage tracer)
 
 
 @dataclasses.dataclass
@@ -62,6 +63,7 @@ class Result:
     finished: float
     value: float           # permeability (perm) or saturation of the invader (drain)
     front: float = 0.0     # drainage: mean front position (lattice units)
+    tracer: float = 0.0    # drainage: mean position of the tracer along the flow axis
 
     @property
     def latency(self):
@@ -69,7 +71,8 @@ class Result:
 
 
 def form_key(p):
-    return (p.discretization, p.ncomponents, p.relaxation_mode, p.isotropy_order, p.precision)
+    return (p.discretization, p.ncomponents, p.relaxation_mode, p.isotropy_order, p.precision, p.nspecies,
+            p.species_relaxation_mode)
 
 
 def _random_sides(rng, lo, hi, n):
@@ -112,7 +115,9 @@ def drain_request(rid, arrival, sides, seed, steps, dims=3):
     (bulk density 1, the other 0.03); the non-wetting component 0 enters
     through a density face at the low end of the flow axis (rho 1.05, first
     three slices pre-filled) against the wetting phase at the high end (rho
-    0.95); walls on the other axes.  g_12 = 0.06 and a = 0.05: with the
+    0.95); walls on the other axes.  One passive tracer species (tau_s =
+    0.8) starts at concentration 1 where the injected phase is.  g_12 = 0.06
+    and a = 0.05: with the
     stronger coupling g_12 = 0.15, adhesion 0.3 and densities 2.1 / 1.9 the
     reference algorithm (the FP64 oracle) diverges within 50 steps on these
     small packs, so the requests use the strongest values found stable."""
@@ -156,7 +161,12 @@ def drain_request(rid, arrival, sides, seed, steps, dims=3):
     rho = np.empty((p.nsites, 2))
     rho[:, 0] = np.where(pore, np.where(inlet, 1.05, 0.03), 0.0)
     rho[:, 1] = np.where(pore, np.where(inlet, 0.03, 1.0), 0.0)
-    return Request(rid, "drain", arrival, p, walls, rho.ravel(), max_steps=steps, invader=0, lo=0.03, hi=1.05)
+    p.nspecies = 1
+    p.species_relaxation_mode = P.SRT
+    p.species_tau[0] = 0.8
+    conc = np.where(pore & inlet, 1.0, 0.0)
+    return Request(rid, "drain", arrival, p, walls, rho.ravel(), max_steps=steps, invader=0, lo=0.03, hi=1.05,
+                   conc=conc)
 
 
 def make_mix(seed=1, n=40, rate=30.0, perm_sides=(32, 64), drain3_sides=(32, 48), drain2_sides=(96, 192),
@@ -252,7 +262,7 @@ class Server:
                 if self.in_use() + need > self.budget:
                     continue
                 key, b = self._batch(q)
-                lid = b.add(q, req.walls, req.rho)
+                lid = b.add(q, req.walls, req.rho, conc=req.conc)
                 active[(key, lid)] = [req, q, now(), None]
                 pending.remove(req)
             if not active:
@@ -279,10 +289,16 @@ class Server:
                             done = done or abs(pr.u_sum[2] - prev) <= req.tol * abs(pr.u_sum[2])
                     if not done:
                         continue
+                    tracer = 0.0
                     if req.kind == "perm":
                         value = (q.tau[0] - 0.5) / 3.0 * (pr.u_sum[2] / q.nsites) / q.gvt[2]
                         front = 0.0
                     else:
+                        if q.nspecies > 0:
+                            c = b.download(lid, P.FIELD_SPECIES_RHO, q.nsites * q.nspecies)[::q.nspecies]
+                            axis = 0 if q.discretization == P.D3Q19 else 1
+                            pos = np.indices(q.shape)[axis].ravel()
+                            tracer = float((c * pos).sum() / max(c.sum(), 1e-300))
                         rho = b.download(lid, P.FIELD_RHO, q.nsites * q.ncomponents)
                         value = metrics.saturation(rho, 2, req.invader, req.lo, req.hi, req.walls)
                         shape = q.shape
@@ -291,7 +307,7 @@ class Server:
                     b.remove(lid)
                     del active[(key, lid)]
                     results.append(Result(req.rid, req.kind, q.nsites, int(pr.steps), req.arrival, admitted, now(),
-                                          float(value), float(front)))
+                                          float(value), float(front), tracer))
         return results
 
     def close(self):

@@ -135,3 +135,24 @@ def test_form_mismatch_is_rejected():
     q.precision = P.PREC_F32
     with pytest.raises(TxError):
         b.add(q, w, r)
+
+
+def test_batch_with_species_equals_alone():
+    mk = [cases.porous_case(P.D3Q19, (12, 10, 14), body=True), cases.porous_case(P.D3Q19, (10, 12, 9), body=True, seed=8)]
+    items = []
+    for p, w, r in mk:
+        conc = cases.with_species(p, w, mode=P.SRT, tau=0.8)
+        items.append((p, w, r, conc))
+    b = Batch(form_of(items[0][0]))
+    ids = [b.add(form_of(p), w, r, conc=c) for p, w, r, c in items]
+    b.step(23)
+    for (p, w, r, c), lid in zip(items, ids):
+        q = form_of(p)
+        h = Handle(q)
+        h.upload_walls(w)
+        h.upload_state(r)
+        h.upload_species(c)
+        h.init()
+        h.step(23)
+        for f in (P.FIELD_FI, P.FIELD_SPECIES_FI, P.FIELD_SPECIES_RHO):
+            assert np.array_equal(b.download(lid, f, h.L.tx_field_size(h.h, f)), h.download(f)), f

@@ -93,3 +93,26 @@ def test_viscosity_consistency():
     # time scale = (tau1 - 0.5)/(3 nu1); tau2 = 3 ts nu2 + 0.5
     ts = (1.0 - 0.5) / (0.1 * 3.0)
     assert abs(p.tau[1] - (3 * ts * 0.05 + 0.5)) < 1e-15
+
+
+def test_transport_options():
+    from taxila import options
+    deck = """
+-flow_discretization d3q19
+-NX 8
+-NY 8
+-NZ 8
+-transport_discretization d3q19
+-nspecies 2
+-specie2_name salt
+-tau_specie1 0.8
+-tau_salt 1.2
+"""
+    p, run = options.params_from_options(options.parse_deck_text(deck))
+    assert p.nspecies == 2 and p.species_relaxation_mode == 0
+    assert p.species_tau[0] == 0.8 and p.species_tau[1] == 1.2
+    assert run.species_names == ["specie1", "salt"]
+    bad = deck.replace("-transport_discretization d3q19", "-transport_discretization d2q9")
+    import pytest
+    with pytest.raises(options.DeckError):
+        options.params_from_options(options.parse_deck_text(bad))

@@ -52,7 +52,10 @@ def test_same_result_alone_and_in_mix(prec):
         (res,) = one.run([req], realtime=False)
         one.close()
         m = mix[req.rid]
-        assert (res.steps, res.value, res.front) == (m.steps, m.value, m.front), (req.rid, req.kind, res, m)
+        assert (res.steps, res.value, res.front, res.tracer) == (m.steps, m.value, m.front, m.tracer), \
+            (req.rid, req.kind, res, m)
+        if req.kind == "drain":
+            assert m.tracer > 0.0
 
 
 def test_budget_admission_waits_for_memory():
