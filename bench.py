@@ -506,11 +506,20 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form, batched, serving and CPU legs")
     ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling runs use a smaller case)")
     ap.add_argument("--form", default="f64", choices=sorted(FORMS), help="storage/arithmetic form of the timed run")
+    ap.add_argument("--leg", default="all", choices=["all", "batched", "serving"],
+                    help="run one extra leg alone and print its JSON (profiling)")
+    ap.add_argument("--lattices", type=int, default=96, help="lattices of the batched leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.leg == "batched":
+        print(json.dumps(batched_run(n_lat=args.lattices, steps=args.steps, compare=min(8, args.lattices))))
+        return 0
+    if args.leg == "serving":
+        print(json.dumps(serving_run()))
+        return 0
     return run_gpu(args)
 
 

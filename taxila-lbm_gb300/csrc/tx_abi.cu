@@ -28,6 +28,7 @@ struct tx_handle {
   size_t pop_bytes = 0;       // bytes of one population element
   void* f[2] = {nullptr, nullptr};
   int cur = 0;                // f[cur] holds the current state
+  unsigned steps_done = 0;    // steps since tx_init (seeds FP16 stochastic rounding)
   void* rho = nullptr;        // forcing density
   size_t rho_bytes = 0;
   uint8_t* mask = nullptr;
@@ -99,6 +100,7 @@ StepArgs args(tx_handle* h, int in, int out) {
   a.phys = h->p.precision == TX_PREC_F64 ? (const void*)h->d_phys : (const void*)h->d_phys32;
   a.g = h->g;
   a.faces = h->faces;
+  a.step = h->steps_done;
   return a;
 }
 
@@ -488,6 +490,7 @@ int tx_init(tx_handle* h) {
   if (rc) return rc;
   cudaFree(h->uic);
   h->uic = nullptr;
+  h->steps_done = 0;
   h->inited = true;
   return TX_OK;
 }
@@ -511,6 +514,7 @@ int tx_step(tx_handle* h, int32_t nsteps) {
     int rc = check_launch(h, "k_step/k_density");
     if (rc) return rc;
     h->cur = nxt;
+    h->steps_done++;
     h->n_step_launch++;
     h->n_density_launch++;
     if (h->timing) {

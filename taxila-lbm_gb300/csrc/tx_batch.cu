@@ -41,6 +41,7 @@ struct Lattice {
   uint8_t* mask = nullptr;
   uint32_t* links = nullptr;
   double* uold = nullptr;
+  unsigned* steps_dev = nullptr;  // device step counter (FP16 stochastic-rounding seed)
   double* faceval[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* phys = nullptr;       // PhysT<R> of the batch's arithmetic type
   Faces faces{};
@@ -176,6 +177,7 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
   a.phys = L->phys;
   a.g = L->g;
   a.faces = L->faces;
+  a.steps_ptr = L->steps_dev;
   (void)b;
   return a;
 }
@@ -262,7 +264,7 @@ int capture_graph(tx_batch* b) {
 void free_lattice(tx_batch* b, Lattice* L) {
   cudaStream_t s = b->stream;
   for (void* p : {(void*)L->f[0], (void*)L->f[1], L->rho, (void*)L->mask, (void*)L->links, (void*)L->uold, L->phys,
-                  L->sg[0], L->sg[1], L->sphys})
+                  L->sg[0], L->sg[1], L->sphys, (void*)L->steps_dev})
     if (p) cudaFreeAsync(p, s);
   for (int f = 0; f < 6; ++f)
     if (L->faceval[f]) cudaFreeAsync(L->faceval[f], s);
@@ -459,6 +461,7 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   TX_BALLOC(L->mask, (size_t)N);
   TX_BALLOC(L->links, (size_t)N * sizeof(uint32_t));
   TX_BALLOC(L->uold, (size_t)N * D * sizeof(double));
+  TX_BALLOC(L->steps_dev, sizeof(unsigned));
   TX_BALLOC(L->phys, physb);
   for (int fc = 0; fc < 2 * D; ++fc) {
     if (p->bc_flags[fc] != TX_BC_DENSITY) continue;
@@ -494,7 +497,8 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   bool ok = cudaMemcpyAsync(L->phys, phsrc, physb, cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemcpyAsync(L->mask, mask.data(), (size_t)N, cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemsetAsync(L->f[0], 0, popb, st) == cudaSuccess && cudaMemsetAsync(L->f[1], 0, popb, st) == cudaSuccess &&
-            cudaMemsetAsync(L->uold, 0, (size_t)N * D * sizeof(double), st) == cudaSuccess;
+            cudaMemsetAsync(L->uold, 0, (size_t)N * D * sizeof(double), st) == cudaSuccess &&
+            cudaMemsetAsync(L->steps_dev, 0, sizeof(unsigned), st) == cudaSuccess;
   if (ok)
     ok = rt32.empty() ? cudaMemcpyAsync(L->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, st) == cudaSuccess
                       : cudaMemcpyAsync(L->rho, rt32.data(), rt32.size() * 4, cudaMemcpyHostToDevice, st) == cudaSuccess;

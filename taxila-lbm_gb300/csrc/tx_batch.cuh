@@ -80,6 +80,10 @@ __global__ void __launch_bounds__(128) k_density_tiles(BatchArgs b, int flip) {
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
     if (x < a.g.nx && y < a.g.ny && z < a.g.nz) density_site<D, S, T, R, RT>(a, x, y, z, 0);
+    // the lattice's step counter advances once per step (the step kernel of
+    // this step has finished reading it; the next one reads the new value)
+    if (t == b.lats[tl.x].tile_begin && threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0 && a.steps_ptr)
+      atomicAdd(const_cast<unsigned*>(a.steps_ptr), 1u);
   }
 }
 

@@ -124,6 +124,11 @@ struct StepArgs {
   const void* phys;         // device PhysT<R> of the kernels' arithmetic type
   Geo g;
   Faces faces;
+  // step count of this lattice: seeds the stochastic rounding of FP16 stores.
+  // Handles pass it by value; batches pass steps_ptr, a per-lattice device
+  // counter that the density pass advances (so replayed graphs see it move).
+  unsigned step;
+  const unsigned* steps_ptr;
 };
 
 // ----------------------------------------------------------------- storage
@@ -161,6 +166,34 @@ __device__ __forceinline__ void st_dev(T* p, R v, const PhysT<R>& P) {
     St<T>::st(p, v * P.sscale);
   else
     St<T>::st(p, v);
+}
+
+// 32-bit integer finaliser (the "lowbias32" constants of C. Wellons' hash
+// prospector): a well-mixed hash of the site, direction and step.
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7feb352dU;
+  h ^= h >> 15;
+  h *= 0x846ca68bU;
+  h ^= h >> 16;
+  return h;
+}
+
+// FP16 store with stochastic rounding: the 13 FP32 mantissa bits that FP16
+// drops are rounded up with probability equal to their value (a hashed
+// 13-bit dither added to the bit pattern, then truncation toward zero).
+// Round-to-nearest of slowly varying fields makes the same error every step
+// and biases steady states; a dither that changes with the step does not.
+// Other storage types store as st_dev.
+template <class T, class R>
+__device__ __forceinline__ void st_dev_sr(T* p, R v, const PhysT<R>& P, uint32_t key) {
+  if constexpr (std::is_same<T, __half>::value) {
+    const float x = float(v * P.sscale);
+    const uint32_t b = __float_as_uint(x) + (mix32(key) & 0x1FFFu);
+    *p = __float2half_rz(__uint_as_float(b));
+  } else {
+    st_dev<T, R>(p, v, P);
+  }
 }
 
 // The forcing density is stored component-fastest, rho[cell * S + m], so that
@@ -668,6 +701,10 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   if (!(links & 1u)) return;  // wall site
   const long long N = a.g.n;
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
+  // stochastic-rounding seed of this site and step (FP16 storage only)
+  uint32_t sr_seed = 0;
+  if constexpr (std::is_same<T, __half>::value)
+    sr_seed = mix32(c ^ (0x9E3779B9u * ((a.steps_ptr ? __ldg(a.steps_ptr) : a.step) + 1u)));
 
   // forces first (they need only rho and the wall layout)
   R rfd[S], rf[S], F[S][D];
@@ -725,7 +762,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       T* const base = fout + (long long)(m * Q + (pore ? n : o)) * N;
       dst = base + (pore ? h.template at<cx, cy, cz>() : c);
     }
-    st_dev<T, R>(dst, v, P);
+    st_dev_sr<T, R>(dst, v, P, sr_seed + 0x85EBCA6Bu * (uint32_t)(m * Q + n + 1));
   };
 
   if constexpr (EXACT) {

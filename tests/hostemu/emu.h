@@ -111,6 +111,7 @@ std::string run(const Case& c, Result& out) {
 
   T* buf[2] = {f0.data(), f1.data()};
   int cur = 0;
+  unsigned step = 0;
   auto args = [&](int in, int o) {
     StepArgs a{};
     a.fin = buf[in];
@@ -121,6 +122,7 @@ std::string run(const Case& c, Result& out) {
     a.phys = &P;
     a.g = g;
     a.faces = faces;
+    a.step = step;
     return a;
   };
   const Shift sh = shift_of(ph);
@@ -171,6 +173,7 @@ std::string run(const Case& c, Result& out) {
     launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 0); });
     cur = 1 - cur;
+    ++step;
     if (NS) {
       const SpeciesArgs sa = sargs(gcur, 1 - gcur);
       if (p.species_relaxation_mode == TX_RELAX_MRT)

@@ -30,3 +30,14 @@ inline T __ldg(const T* p) {
 }
 
 typedef void* cudaStream_t;
+
+inline unsigned __float_as_uint(float f) {
+  unsigned u;
+  __builtin_memcpy(&u, &f, 4);
+  return u;
+}
+inline float __uint_as_float(unsigned u) {
+  float f;
+  __builtin_memcpy(&f, &u, 4);
+  return f;
+}
