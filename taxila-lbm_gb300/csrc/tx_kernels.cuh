@@ -32,11 +32,16 @@
 #include <stdint.h>
 
 // Resident 128-thread blocks per SM that ptxas must make room for in the
-// float-arithmetic k_step (4 caps it at 128 registers a thread; the FP64 form
-// is bound by the FP64 pipe and keeps its full register budget).
+// float-arithmetic k_step: 4 (128 registers a thread) for two components, 6
+// (80 registers, no spills) for one.  The FP64 form is bound by the FP64 pipe
+// and keeps its full register budget.
 #ifndef TX_FLOAT_MIN_BLOCKS
 #define TX_FLOAT_MIN_BLOCKS 4
 #endif
+#ifndef TX_FLOAT_MIN_BLOCKS_S1
+#define TX_FLOAT_MIN_BLOCKS_S1 6
+#endif
+#define TX_STEP_MIN_BLOCKS(S, R) (sizeof(R) == 4 ? ((S) == 1 ? TX_FLOAT_MIN_BLOCKS_S1 : TX_FLOAT_MIN_BLOCKS) : 1)
 
 #include "tx_ff_stencil.cuh"
 #include "tx_lattice.cuh"
@@ -956,7 +961,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
 }
 
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TX_FLOAT_MIN_BLOCKS : 1) k_step(StepArgs a_in) {
+__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R)) k_step(StepArgs a_in) {
   const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
   int x, y, z;
   long long idx;
