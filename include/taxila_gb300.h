@@ -75,12 +75,18 @@ extern "C" {
 #define TX_FIELD_VELT 6    /* ndims dof: total velocity diagnostic                        */
 #define TX_FIELD_RHOT 7    /* 1 dof: total mass density diagnostic                        */
 #define TX_FIELD_WALLS 8   /* 1 dof: wall codes as uploaded                               */
+#define TX_FIELD_PSI 12    /* s dof: Shan-Chen potential psi(rho) (= rho without an EOS)  */
 #define TX_FIELD_SPECIES_FI 9    /* ns*Q dof: transported species populations (reference gi) */
 #define TX_FIELD_SPECIES_RHO 10  /* ns dof: species concentrations (reference psi)           */
 #define TX_FIELD_SPECIES_FLUX 11 /* ns*ndims dof: species flux sum_n g_n c_n                 */
 
 /* error codes */
 #define TX_OK 0
+#define TX_EOS_RHO 0        /* psi = rho */
+#define TX_EOS_SC 1         /* psi = rho0 (1 - exp(-rho / rho0))       (Shan & Chen 1993) */
+#define TX_EOS_THERMO 2     /* psi = psi0 exp(-rho0 / rho)             (Shan & Chen 1994) */
+#define TX_EOS_PR 3         /* Peng-Robinson: psi = sqrt(2 (p(rho) - rho/3) / (c0 g_mm)) */
+
 #define TX_ERR_ARG 1       /* invalid argument / unsupported parameter combination */
 #define TX_ERR_STATE 2     /* call out of order (e.g. tx_step before tx_init) */
 #define TX_ERR_CUDA 3      /* CUDA runtime error (message has the CUDA string) */
@@ -123,6 +129,13 @@ typedef struct tx_params {
    * -nspecies / -transport_relaxation_mode / -tau_<specie> / -s_*_<specie>
    * options.  The transport lattice is the flow's (same discretization and
    * faces); species feel no force and no boundary condition. */
+  /* non-ideal equation of state psi(rho) per component: -flow_use_nonideal_eos
+   * with -eos_<component> {rho,sc,thermo,pr} (LBM_EOS_module,
+   * src/lbm/lbm_eos.F90:183-350).  psi replaces rho in the fluid-fluid force
+   * and the pressure diagnostic (FlowCalcForces, lbm_flow.F90:790-806). */
+  int32_t use_nonideal_eos;
+  int32_t eos[TX_MAX_COMPONENTS];          /* TX_EOS_RHO, TX_EOS_SC, TX_EOS_THERMO, TX_EOS_PR */
+  double eos_coef[TX_MAX_COMPONENTS][4];   /* SC: rho0 | thermo: psi0, rho0 | PR: a, b, T, omega */
   int32_t nspecies;                        /* 0 = no transport */
   int32_t species_relaxation_mode;         /* TX_RELAX_SRT or TX_RELAX_MRT */
   double species_tau[TX_MAX_COMPONENTS];   /* SRT relaxation time */

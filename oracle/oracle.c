@@ -48,6 +48,8 @@ struct orc {
   int ff_on, fs_on, body_on;
   double fs_w_axis, fs_w_diag;
   double *fi, *tmp, *rho, *walls, *flux, *forces, *fieq;
+  double *psi;               /* psi_of_rho (rho layout) when use_nonideal_eos */
+  double eos_alpha[MAXC];    /* Peng-Robinson alpha(T) */
   double *bcv[6];            /* nbcs * face area per Dirichlet face */
   double *old_rho, *old_fi;
   int have_fi, have_state, inited;
@@ -236,6 +238,16 @@ orc* orc_create(const tx_params* p) {
   o->forces = (double*)calloc((size_t)ncell * o->nd * o->s, sizeof(double));
   o->rho = (double*)calloc((size_t)nrc * o->s, sizeof(double));
   o->walls = (double*)calloc((size_t)nrc, sizeof(double));
+  o->psi = (double*)calloc((size_t)nrc * o->s, sizeof(double));
+  /* EOSSetFromOptions_PR (lbm_eos.F90:253-300): T_c from a and b with R = 1 */
+  for (int m = 0; m < o->s; ++m) {
+    if (p->eos[m] != TX_EOS_PR) continue;
+    const double a = p->eos_coef[m][0], b = p->eos_coef[m][1], T = p->eos_coef[m][2], om = p->eos_coef[m][3];
+    /* single-precision literals in the Fortran source (lbm_eos.F90:296,336) */
+    const double Tc = a / b * (double)0.0778f / (double)0.45724f / 1.;
+    const double t = 1. + ((double)0.37464f + (double)1.54226f * om - (double)0.26992f * (om * om)) * (1. - sqrt(T / Tc));
+    o->eos_alpha[m] = t * t;
+  }
   long nown = (long)o->N[0] * o->N[1] * o->N[2];
   o->old_rho = (double*)calloc((size_t)nown * o->s, sizeof(double));
   o->old_fi = (double*)calloc((size_t)nown * o->s * o->Q, sizeof(double));
@@ -292,7 +304,7 @@ void orc_destroy(orc* o) {
   if (!o) return;
   orc_destroy(o->tr);
   free(o->fi); free(o->tmp); free(o->fieq); free(o->flux); free(o->forces);
-  free(o->rho); free(o->walls); free(o->old_rho); free(o->old_fi);
+  free(o->rho); free(o->walls); free(o->old_rho); free(o->old_fi); free(o->psi);
   for (int f = 0; f < 6; ++f) free(o->bcv[f]);
   free(o);
 }
@@ -463,7 +475,31 @@ static void add_body(orc* o) {
 }
 
 /* LBMAddFluidFluidForcesD3/D2 (lbm_forcing.F90:51-958, :960-1299) */
+/* EOSApply_Rho/_SC/_Thermo/_PR (lbm_eos.F90:183-350) with R = 1 */
+static double eos_psi(const orc* o, int m, double rho) {
+  const int t = o->p.eos[m];
+  const double* c = o->p.eos_coef[m];
+  if (t == TX_EOS_SC) return c[0] * (1. - exp(-rho / c[0]));
+  if (t == TX_EOS_THERMO) return c[0] * exp(-c[1] / rho);
+  if (t == TX_EOS_PR) {
+    const double a = c[0], b = c[1], T = c[2], alpha = o->eos_alpha[m];
+    const double tmp = 2. * (rho * 1. * T / (1. - b * rho) - (a * alpha) * (rho * rho) / (1. + 2. * b * rho - (b * rho) * (b * rho)) -
+                             rho / 3.) / (o->c0 * o->p.g[m][m]);
+    return sqrt(tmp);
+  }
+  return rho;
+}
+
+/* FlowCalcForces with use_nonideal_eos (lbm_flow.F90:795-805): psi over the
+ * whole rho-ghosted box */
+static void apply_eos(orc* o) {
+  const long nrc = (long)o->rl[0] * o->rl[1] * o->rl[2];
+  for (long q = 0; q < nrc; ++q)
+    for (int m = 0; m < o->s; ++m) o->psi[q * o->s + m] = eos_psi(o, m, o->rho[q * o->s + m]);
+}
+
 static void add_fluid_fluid(orc* o) {
+  const double* fld = o->p.use_nonideal_eos ? o->psi : o->rho;
   const double eps = (double)1.e-12f;
   const int ISO = o->iso;
   const int NS = o->s;
@@ -476,7 +512,7 @@ static void add_fluid_fluid(orc* o) {
         double gr[MAXC][3] = {{0}};
         double ws[3] = {0., 0., 0.};
 #define O_WALL(dx, dy, dz) (WALL(o, i + (dx), j + (dy), k + (dz)) == 0)
-#define O_RHO(m, dx, dy, dz) RHO(o, m, i + (dx), j + (dy), k + (dz))
+#define O_RHO(m, dx, dy, dz) fld[(ridx(o, i + (dx), j + (dy), k + (dz))) * o->s + (m)]
 #define O_GR(m, a) gr[m][a]
         if (o->nd == 3) {
           ORC_FF_GRADIENT_D3(O_WALL, O_RHO, O_GR, ws, FFW, NS);
@@ -491,7 +527,7 @@ static void add_fluid_fluid(orc* o) {
             if (ws[d] > eps) {
               double acc = 0.0;
               for (int q = 0; q < o->s; ++q) acc = acc + o->p.g[m][q] * (gr[q][d] / ws[d]);
-              FRC(o, m, d, i, j, k) = FRC(o, m, d, i, j, k) - o->c0 * RHO(o, m, i, j, k) * acc;
+              FRC(o, m, d, i, j, k) = FRC(o, m, d, i, j, k) - o->c0 * fld[ridx(o, i, j, k) * o->s + m] * acc;
             }
           }
       }
@@ -505,6 +541,7 @@ static void calc_forces(orc* o) {
   if (o->body_on) add_body(o);
   if (o->ff_on) {
     halo_rho(o);
+    if (o->p.use_nonideal_eos) apply_eos(o);
     add_fluid_fluid(o);
   }
 }
@@ -938,6 +975,7 @@ long orc_field_size(const orc* o, int field) {
     case TX_FIELD_SPECIES_FI: return o->tr ? n * o->tr->s * o->Q : -1;
     case TX_FIELD_SPECIES_RHO: return o->tr ? n * o->tr->s : -1;
     case TX_FIELD_SPECIES_FLUX: return o->tr ? n * o->tr->s * o->nd : -1;
+    case TX_FIELD_PSI: return n * o->s;
   }
   return -1;
 }
@@ -954,11 +992,14 @@ static void diagnostics(orc* o, double* rhot, double* prs, double* velt) {
       double rt = 0.0;
       for (int m = 0; m < o->s; ++m) rt = rt + RHO(o, m, i, j, k) * o->mm[m];
       double pr = rt / 3.;
-      if (o->s > 1) {
+      if (o->s > 1 || o->p.use_nonideal_eos) {
+        double ps[MAXC];
+        for (int m = 0; m < o->s; ++m)
+          ps[m] = o->p.use_nonideal_eos ? eos_psi(o, m, RHO(o, m, i, j, k)) : RHO(o, m, i, j, k);
         for (int m = 0; m < o->s; ++m) {
           double acc = 0.0;
-          for (int n = 0; n < o->s; ++n) acc = acc + o->p.g[m][n] * RHO(o, n, i, j, k);
-          pr = pr + o->c0 / 2. * RHO(o, m, i, j, k) * acc;
+          for (int n = 0; n < o->s; ++n) acc = acc + o->p.g[m][n] * ps[n];
+          pr = pr + o->c0 / 2. * ps[m] * acc;
         }
       }
       for (int m = 0; m < o->s; ++m)
@@ -1013,6 +1054,14 @@ int orc_get(orc* o, int field, double* out) {
     case TX_FIELD_PRS: diagnostics(o, NULL, out, NULL); return 0;
     case TX_FIELD_RHOT: diagnostics(o, out, NULL, NULL); return 0;
     case TX_FIELD_VELT: diagnostics(o, NULL, NULL, out); return 0;
+    case TX_FIELD_PSI:
+      OWNED_LOOP(o) {
+        for (int m = 0; m < o->s; ++m)
+          out[q * o->s + m] = WALL(o, i, j, k) == 0 ? (o->p.use_nonideal_eos ? eos_psi(o, m, RHO(o, m, i, j, k))
+                                                                              : RHO(o, m, i, j, k)) : 0.0;
+        ++q;
+      }
+      return 0;
     case TX_FIELD_SPECIES_FI: return o->tr ? orc_get(o->tr, TX_FIELD_FI, out) : TX_ERR_ARG;
     case TX_FIELD_SPECIES_RHO: return o->tr ? orc_get(o->tr, TX_FIELD_RHO, out) : TX_ERR_ARG;
     case TX_FIELD_SPECIES_FLUX: return o->tr ? orc_get(o->tr, TX_FIELD_FLUX, out) : TX_ERR_ARG;

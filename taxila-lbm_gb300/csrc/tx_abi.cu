@@ -30,6 +30,7 @@ struct tx_handle {
   int cur = 0;                // f[cur] holds the current state
   unsigned steps_done = 0;    // steps since tx_init (seeds FP16 stochastic rounding)
   void* rho = nullptr;        // forcing density
+  void* psi = nullptr;        // psi(rho) when the EOS is on
   size_t rho_bytes = 0;
   uint8_t* mask = nullptr;
   uint32_t* links = nullptr;  // link masks (k_links), rebuilt with every wall upload
@@ -95,6 +96,7 @@ StepArgs args(tx_handle* h, int in, int out) {
   a.fin = h->f[in];
   a.fout = h->f[out];
   a.rho = h->rho;
+  a.psi = h->psi;
   a.mask = h->mask;
   a.links = h->links;
   a.phys = h->p.precision == TX_PREC_F64 ? (const void*)h->d_phys : (const void*)h->d_phys32;
@@ -111,7 +113,8 @@ long long field_dof(const tx_handle* h, int field) {
     case TX_FIELD_SPECIES_RHO: return h->NS;
     case TX_FIELD_SPECIES_FLUX: return (long long)h->NS * h->D;
     case TX_FIELD_FI: return (long long)h->S * h->Q;
-    case TX_FIELD_RHO: return h->S;
+    case TX_FIELD_RHO:
+    case TX_FIELD_PSI: return h->S;
     case TX_FIELD_FLUX:
     case TX_FIELD_FORCES: return (long long)h->S * h->D;
     case TX_FIELD_PRS:
@@ -184,7 +187,7 @@ int stage_field(tx_handle* h, int field) {
     return TX_ERR_ARG;
   } else {
     const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
-                   : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : 7;
+                   : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : field == TX_FIELD_PSI ? 12 : 7;
     h->ks.moments(args(h, h->cur, h->cur), what, h->stage, h->stream);
   }
   return check_launch(h, "download kernel");
@@ -287,6 +290,7 @@ int tx_create(const tx_params* p, tx_handle** out) {
   const size_t stageb = (size_t)N * (h->S > h->NS ? h->S : h->NS) * h->Q * sizeof(double);
   if (cudaMalloc(&h->f[0], popb) != cudaSuccess || cudaMalloc(&h->f[1], popb) != cudaSuccess ||
       cudaMalloc(&h->rho, (size_t)N * h->S * h->rho_bytes) != cudaSuccess ||
+      (p->use_nonideal_eos && cudaMalloc(&h->psi, (size_t)N * h->S * h->rho_bytes) != cudaSuccess) ||
       cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->links, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&h->stage, stageb) != cudaSuccess ||
       cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess ||
@@ -352,6 +356,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->f[0]);
   cudaFree(h->f[1]);
   cudaFree(h->rho);
+  cudaFree(h->psi);
   cudaFree(h->mask);
   cudaFree(h->links);
   cudaFree(h->stage);
@@ -404,6 +409,22 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
     std::vector<float> rf(rt.begin(), rt.end());
     TX_CUDA(h, cudaMemcpyAsync(h->rho, rf.data(), rf.size() * 4, cudaMemcpyHostToDevice, h->stream));
     TX_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  if (h->psi) {
+    // psi(rho) of the initial density, for the forces of FlowFiInit
+    std::vector<double> ps((size_t)N * S, 0.0);
+    for (long long i = 0; i < N; ++i)
+      if (h->host_mask[(size_t)i] == 0)
+        for (int m = 0; m < S; ++m)
+          ps[(size_t)(i * S + m)] = eos_psi<double>(h->ph.eos[m], h->ph.eos_c[m], h->ph.g[m][m], h->ph.c0, rho[i * S + m]);
+    if (h->rho_bytes == 8) {
+      TX_CUDA(h, cudaMemcpyAsync(h->psi, ps.data(), ps.size() * 8, cudaMemcpyHostToDevice, h->stream));
+      TX_CUDA(h, cudaStreamSynchronize(h->stream));
+    } else {
+      std::vector<float> pf(ps.begin(), ps.end());
+      TX_CUDA(h, cudaMemcpyAsync(h->psi, pf.data(), pf.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      TX_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
   }
   cudaFree(h->uic);
   h->uic = nullptr;

@@ -38,6 +38,7 @@ struct Lattice {
   Phys ph{};
   void* f[2] = {nullptr, nullptr};
   void* rho = nullptr;
+  void* psi = nullptr;        // psi(rho) when the EOS is on
   uint8_t* mask = nullptr;
   uint32_t* links = nullptr;
   double* uold = nullptr;
@@ -64,7 +65,8 @@ long long face_area(const tx_params& p, int D, int f) {
 long long lattice_bytes(const tx_params& p) {
   const int D = p.discretization == TX_D3Q19 ? 3 : 2, Q = D == 3 ? 19 : 9, S = p.ncomponents;
   const long long N = (long long)p.nx * p.ny * (D == 3 ? p.nz : 1);
-  long long b = 2 * N * S * Q * (long long)pop_bytes(p.precision) + N * S * (long long)rho_bytes(p.precision) + N +
+  long long b = 2 * N * S * Q * (long long)pop_bytes(p.precision) +
+                N * S * (long long)rho_bytes(p.precision) * (p.use_nonideal_eos ? 2 : 1) + N +
                 4 * N + 8LL * D * N + (long long)sizeof(Phys);
   for (int f = 0; f < 2 * D; ++f)
     if (p.bc_flags[f] == TX_BC_DENSITY) b += face_area(p, D, f) * S * 8;
@@ -172,6 +174,7 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
   a.fin = L->f[in];
   a.fout = L->f[out];
   a.rho = L->rho;
+  a.psi = L->psi;
   a.mask = L->mask;
   a.links = L->links;
   a.phys = L->phys;
@@ -263,7 +266,7 @@ int capture_graph(tx_batch* b) {
 
 void free_lattice(tx_batch* b, Lattice* L) {
   cudaStream_t s = b->stream;
-  for (void* p : {(void*)L->f[0], (void*)L->f[1], L->rho, (void*)L->mask, (void*)L->links, (void*)L->uold, L->phys,
+  for (void* p : {(void*)L->f[0], (void*)L->f[1], L->rho, L->psi, (void*)L->mask, (void*)L->links, (void*)L->uold, L->phys,
                   L->sg[0], L->sg[1], L->sphys, (void*)L->steps_dev})
     if (p) cudaFreeAsync(p, s);
   for (int f = 0; f < 6; ++f)
@@ -288,7 +291,7 @@ int stage(tx_batch* b, const Lattice* L, int field, double* out) {
     b->ks.to_natural(L->f[b->flip], L->mask, N, shift_of(L->ph), out, b->stream);
   } else {
     const int what = field == TX_FIELD_RHO ? 2 : field == TX_FIELD_FLUX ? 3 : field == TX_FIELD_FORCES ? 4
-                   : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : 7;
+                   : field == TX_FIELD_PRS ? 5 : field == TX_FIELD_VELT ? 6 : field == TX_FIELD_PSI ? 12 : 7;
     b->ks.moments(lattice_args(b, L, b->flip, b->flip), what, out, b->stream);
   }
   TX_BCUDA(b, cudaGetLastError());
@@ -302,7 +305,8 @@ long long field_dof(const Lattice* L, int field) {
     case TX_FIELD_SPECIES_RHO: return L->NS;
     case TX_FIELD_SPECIES_FLUX: return (long long)L->NS * L->D;
     case TX_FIELD_FI: return (long long)L->S * L->Q;
-    case TX_FIELD_RHO: return L->S;
+    case TX_FIELD_RHO:
+    case TX_FIELD_PSI: return L->S;
     case TX_FIELD_FLUX:
     case TX_FIELD_FORCES: return (long long)L->S * L->D;
     case TX_FIELD_PRS:
@@ -430,6 +434,17 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
     for (int m = 0; m < S; ++m) rt[(size_t)(i * S + m)] = mask[(size_t)i] == 0 ? rho[i * S + m] - L->ph.rho0[m] : 0.0;
   std::vector<float> rt32;
   if (rho_bytes(p->precision) == 4) rt32.assign(rt.begin(), rt.end());
+  // psi(rho) of the initial density for the forces of FlowFiInit
+  std::vector<double> ps;
+  std::vector<float> ps32;
+  if (p->use_nonideal_eos) {
+    ps.assign((size_t)N * S, 0.0);
+    for (long long i = 0; i < N; ++i)
+      if (mask[(size_t)i] == 0)
+        for (int m = 0; m < S; ++m)
+          ps[(size_t)(i * S + m)] = eos_psi<double>(L->ph.eos[m], L->ph.eos_c[m], L->ph.g[m][m], L->ph.c0, rho[i * S + m]);
+    if (rho_bytes(p->precision) == 4) ps32.assign(ps.begin(), ps.end());
+  }
   std::vector<double> ut;
   if (u) {
     ut.resize((size_t)N * S * D);
@@ -458,6 +473,7 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   TX_BALLOC(L->f[0], popb);
   TX_BALLOC(L->f[1], popb);
   TX_BALLOC(L->rho, (size_t)N * S * rho_bytes(p->precision));
+  if (p->use_nonideal_eos) TX_BALLOC(L->psi, (size_t)N * S * rho_bytes(p->precision));
   TX_BALLOC(L->mask, (size_t)N);
   TX_BALLOC(L->links, (size_t)N * sizeof(uint32_t));
   TX_BALLOC(L->uold, (size_t)N * D * sizeof(double));
@@ -503,6 +519,9 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
     ok = rt32.empty() ? cudaMemcpyAsync(L->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, st) == cudaSuccess
                       : cudaMemcpyAsync(L->rho, rt32.data(), rt32.size() * 4, cudaMemcpyHostToDevice, st) == cudaSuccess;
   if (ok && uic) ok = cudaMemcpyAsync(uic, ut.data(), ut.size() * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess;
+  if (ok && L->psi)
+    ok = ps32.empty() ? cudaMemcpyAsync(L->psi, ps.data(), ps.size() * 8, cudaMemcpyHostToDevice, st) == cudaSuccess
+                      : cudaMemcpyAsync(L->psi, ps32.data(), ps32.size() * 4, cudaMemcpyHostToDevice, st) == cudaSuccess;
   if (ok && L->NS > 0)
     ok = cudaMemcpyAsync(L->sphys, p->precision == TX_PREC_F64 ? (const void*)&sp : (const void*)&sp32, spb,
                          cudaMemcpyHostToDevice, st) == cudaSuccess &&

@@ -50,6 +50,16 @@ inline int validate(const tx_params* p, std::string* why) {
         return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
     }
   }
+  if (p->use_nonideal_eos) {
+    for (int m = 0; m < p->ncomponents; ++m) {
+      const int t = p->eos[m];
+      if (t < TX_EOS_RHO || t > TX_EOS_PR) return bad("Invalid EOS type");
+      if (t == TX_EOS_SC && !(p->eos_coef[m][0] != 0.0)) return bad("EOS sc: rho0 must be nonzero");
+      if (t == TX_EOS_PR && (!(p->eos_coef[m][0] > 0.0) || !(p->eos_coef[m][1] > 0.0) || !(p->eos_coef[m][2] > 0.0) ||
+                             p->g[m][m] == 0.0))
+        return bad("EOS pr: a, b and T must be > 0 and the self coupling g_mm nonzero");
+    }
+  }
   if (p->nspecies < 0 || p->nspecies > TX_MAX_COMPONENTS) return bad("nspecies out of range");
   if (p->nspecies > 0) {
     if (p->species_relaxation_mode != TX_RELAX_SRT && p->species_relaxation_mode != TX_RELAX_MRT)
@@ -148,6 +158,21 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
   P.body_on = p.body_forces != 0;
   for (int m = 0; m < S; ++m) P.rho0[m] = p.precision == TX_PREC_F64 ? 0.0 : p.rho0[m];
   P.sscale = p.precision == TX_PREC_F32_F16 && p.storage_scale > 0.0 ? p.storage_scale : 1.0;
+  // non-ideal EOS (EOSSetFromOptions_*, lbm_eos.F90:90-300); PR keeps a, b, T, alpha(T)
+  P.eos_on = p.use_nonideal_eos ? 1 : 0;
+  for (int m = 0; m < S; ++m) {
+    P.eos[m] = p.use_nonideal_eos ? p.eos[m] : TX_EOS_RHO;
+    for (int k = 0; k < 4; ++k) P.eos_c[m][k] = p.eos_coef[m][k];
+    if (P.eos[m] == TX_EOS_PR) {
+      const double a = p.eos_coef[m][0], b = p.eos_coef[m][1], T = p.eos_coef[m][2], om = p.eos_coef[m][3];
+      // the Fortran source spells these constants as default-kind (single
+      // precision) literals: they enter the double expressions rounded to float
+      const double Tc = a / b * double(0.0778f) / double(0.45724f) / 1.;
+      const double t =
+          1. + (double(0.37464f) + double(1.54226f) * om - double(0.26992f) * (om * om)) * (1. - std::sqrt(T / Tc));
+      P.eos_c[m][3] = t * t;
+    }
+  }
   for (int m = 0; m < S; ++m) {
     const double mm = p.mm[m], rel = (mm - 1.0) / mm;  // 0 for unit mass
     P.A0[m] = D == 3 ? P.dk[m] : (1.0 + 5.0 * P.dk[m]) / 6.0;

@@ -31,6 +31,10 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <cmath>
+
+#include "../../include/taxila_gb300.h"
+
 // Resident 128-thread blocks per SM that ptxas must make room for in the
 // float-arithmetic k_step: 4 (128 registers a thread) for two components, 6
 // (80 registers, no spills) for one.  The FP64 form is bound by the FP64 pipe
@@ -75,6 +79,11 @@ struct PhysT {
   // (= 1/mm), and cA = (W~_n A_n - w_n) rho0 for the rest, axis and diagonal
   // classes, evaluated exactly on the host (zero for unit molecular mass)
   R A0[MAXC], An[MAXC], cA[MAXC][3];
+  // non-ideal EOS: psi(rho) replaces rho in the fluid-fluid force when eos_on
+  // (coefficients: SC rho0 | thermo psi0, rho0 | PR a, b, T, alpha)
+  int eos_on;
+  int eos[MAXC];
+  R eos_c[MAXC][4];
   // fast form: relax every moment at s0, then correct the moments whose rate
   // differs (bit k of spec_mask) by dspec = (rate_k - s0) / diag(M M^T)_k
   R s0[MAXC];
@@ -96,6 +105,9 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   cp(&a.srate[0][0], &b->srate[0][0], MAXC * 19); cp(&a.srate_mmt[0][0], &b->srate_mmt[0][0], MAXC * 19);
   cp(a.rho0, b->rho0, MAXC);
   cp(a.A0, b->A0, MAXC); cp(a.An, b->An, MAXC); cp(&a.cA[0][0], &b->cA[0][0], MAXC * 3);
+  b->eos_on = a.eos_on;
+  for (int m = 0; m < MAXC; ++m) b->eos[m] = a.eos[m];
+  cp(&a.eos_c[0][0], &b->eos_c[0][0], MAXC * 4);
   b->sscale = R(a.sscale);
   b->inv_sscale = R(a.inv_sscale);
   cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19); cp(a.inv_ws_full, b->inv_ws_full, 3);
@@ -129,12 +141,30 @@ struct StepArgs {
   const void* phys;         // device PhysT<R> of the kernels' arithmetic type
   Geo g;
   Faces faces;
+  void* psi;                // RT [cell * S + m]: psi(rho) when the EOS is on, else unused
   // step count of this lattice: seeds the stochastic rounding of FP16 stores.
   // Handles pass it by value; batches pass steps_ptr, a per-lattice device
   // counter that the density pass advances (so replayed graphs see it move).
   unsigned step;
   const unsigned* steps_ptr;
 };
+
+// psi(rho) of one component: EOSApply_Rho / _SC / _Thermo / _PR
+// (lbm_eos.F90:183-350) in the reference's expression shapes; R = 1 in PR.
+// A negative PR radicand gives NaN here (the reference stops with an error).
+template <class R>
+__host__ __device__ __forceinline__ R eos_psi(int type, const R c[4], R gmm, R c0, R rho) {
+  if (type == TX_EOS_SC) return c[0] * (R(1.) - exp(-rho / c[0]));
+  if (type == TX_EOS_THERMO) return c[0] * exp(-c[1] / rho);
+  if (type == TX_EOS_PR) {
+    const R a = c[0], b = c[1], T = c[2], alpha = c[3];
+    const R br = b * rho;
+    const R tmp = R(2.) * (rho * T / (R(1.) - br) - (a * alpha) * (rho * rho) / (R(1.) + R(2.) * b * rho - br * br) - rho / R(3.)) /
+                  (c0 * gmm);
+    return sqrt(tmp);
+  }
+  return rho;
+}
 
 // ----------------------------------------------------------------- storage
 template <class T>
@@ -442,11 +472,13 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
 // FlowCalcForces (lbm_flow.F90:760-808) for one pore site: zero, then
 // fluid-solid (lbm_forcing.F90:1326-1421), body (:1440-1496) and the
 // wall-aware Shan-Chen term (:51-958 / :960-1299), in that order.
-// rfd: stored forcing density of the site (rho - rho0); rf: rho itself.
+// rfd: stored forcing density of the site (rho - rho0); rf: rho itself;
+// psi: the psi(rho) field when the EOS is on (then the fluid-fluid force
+// differentiates psi and scales by psi(x), FlowCalcForces lbm_flow.F90:790-806).
 template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT>
 __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P,
-                                            const uint8_t* mask, const RT* rho, long long N, const R rfd[S],
-                                            const R rf[S], R F[S][D]) {
+                                            const uint8_t* mask, const RT* rho, const RT* psi, long long N,
+                                            const R rfd[S], const R rf[S], R F[S][D]) {
   using L = Lat<D>;
 #pragma unroll
   for (int m = 0; m < S; ++m)
@@ -484,10 +516,25 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
 #pragma unroll
       for (int d = 0; d < D; ++d) F[m][d] = F[m][d] + R(P.gvt[d]) * R(P.mm[m]) * rf[m];
   }
+  if (!P.ff_on) return;
+  // the differentiated field, its value at x and the force's scale factor
+  const RT* src = P.eos_on ? psi : rho;
+  R selfv[S], mult[S];
+  if (P.eos_on) {
+    rho_at<S>(psi, h.template at<0, 0, 0>(), selfv);
+#pragma unroll
+    for (int m = 0; m < S; ++m) mult[m] = selfv[m];
+  } else {
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      selfv[m] = rfd[m];
+      mult[m] = rf[m];
+    }
+  }
   if constexpr (!EXACT && stencil_is_links<D, ISO>()) {
     // every stencil neighbour pore: the weight sums are constant and the
     // psi(x) terms cancel, so grad = sum_k w_k e_k psi(x + e_k)
-    if (P.ff_on && (links | 1u) == (all_links<D>() | 1u)) {
+    if ((links | 1u) == (all_links<D>() | 1u)) {
       R gr[S][D];
 #pragma unroll
       for (int d = 0; d < D; ++d)
@@ -499,7 +546,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
         if constexpr (T.level <= ISO) {
           constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2], tw = T.w;
           R v[S];
-          rho_at<S>(rho, h.template at<ex, ey, ez>(), v);
+          rho_at<S>(src, h.template at<ex, ey, ez>(), v);
           sfor<0, D>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
             constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
@@ -521,13 +568,13 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
           R acc = R(0);
 #pragma unroll
           for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * q[k];
-          F[m][d] = F[m][d] - R(P.c0) * rf[m] * acc;
+          F[m][d] = F[m][d] - R(P.c0) * mult[m] * acc;
         }
       }
       return;
     }
   }
-  if (P.ff_on) {
+  {
     R gr[S][D];
     R ws[D];
     int wc[12][D];
@@ -541,7 +588,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
     }
     constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
     sfor<0, NT>([&](auto tt) {
-      ff_term<D, S, ISO, EXACT, decltype(tt)::value, RCH, R, RT>(h, links, P, mask, rho, N, rfd, gr, ws, wc);
+      ff_term<D, S, ISO, EXACT, decltype(tt)::value, RCH, R, RT>(h, links, P, mask, src, N, selfv, gr, ws, wc);
     });
     if constexpr (!EXACT) {
 #pragma unroll
@@ -567,7 +614,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
           R acc = R(0);
 #pragma unroll
           for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * q[k];
-          F[m][d] = F[m][d] - R(P.c0) * rf[m] * acc;
+          F[m][d] = F[m][d] - R(P.c0) * mult[m] * acc;
         }
       }
     }
@@ -651,7 +698,8 @@ __device__ __forceinline__ void cell_moments(const StepArgs& a, const PhysT<R>& 
 #pragma unroll
   for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
-  cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, a.g.n, rfd, rf, F);
+  cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, reinterpret_cast<const RT*>(a.psi), a.g.n,
+                                rfd, rf, F);
   cell_velocity<D, S, EXACT, R>(a, P, x, y, z, fv, rf, F, rc, up);
 }
 
@@ -718,7 +766,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     rho_at<S>(rho, c, rfd);
 #pragma unroll
     for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
-    cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, N, rfd, rf, F);
+    cell_forces<D, S, ISO, EXACT>(h, links, P, a.mask, rho, reinterpret_cast<const RT*>(a.psi), N, rfd, rf, F);
   }
   const T* fin = reinterpret_cast<const T*>(a.fin);
   // moments pass, one component's populations at a time; rcd = rc - rho0
@@ -1063,6 +1111,9 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
         acc = acc + ld_dev<T, R>(fcur + (long long)(m * Q + n) * N + c, P);
       });
       rho[(size_t)c * S + m] = RT(acc);
+      if (P.eos_on)
+        reinterpret_cast<RT*>(a.psi)[(size_t)c * S + m] =
+            RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, P.rho0[m] + acc));
     }
     return;
   }
@@ -1092,6 +1143,8 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
 #pragma unroll
   for (int m = 0; m < S; ++m) {
     rho[(size_t)c * S + m] = RT(kShifted<T> ? rf[m] - P.rho0[m] : rf[m]);
+    if (P.eos_on)
+      reinterpret_cast<RT*>(a.psi)[(size_t)c * S + m] = RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, rf[m]));
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       R v = fv[m][n];
@@ -1129,7 +1182,8 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
   for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
   {
     const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
-    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, N, rfd, rf, F);
+    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + idx), P, a.mask, rho, reinterpret_cast<const RT*>(a.psi), N,
+                                  rfd, rf, F);
   }
   T* fout = reinterpret_cast<T*>(a.fout);
 #pragma unroll
@@ -1208,7 +1262,7 @@ __device__ __forceinline__ void moments_site(const StepArgs& a, int x, int y, in
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * (long long)z);
   const bool wall = __ldg(a.mask + idx) != 0;
-  const int dof = what == 2 ? S : (what == 3 || what == 4) ? S * D : (what == 6 ? D : 1);
+  const int dof = (what == 2 || what == 12) ? S : (what == 3 || what == 4) ? S * D : (what == 6 ? D : 1);
   if (wall) {
     for (int q = 0; q < dof; ++q) out[idx * dof + q] = 0.0;
     return;
@@ -1237,13 +1291,20 @@ __device__ __forceinline__ void moments_site(const StepArgs& a, int x, int y, in
     for (int m = 0; m < S; ++m) rt = rt + rc[m] * R(P.mm[m]);
     if (what == 7) {
       out[idx] = double(rt);
-    } else if (what == 5) {
+    } else if (what == 5 || what == 12) {
+      // FlowUpdateDiagnosticsD3/D2: psi = EOS(rho) when the EOS is on
+      R ps[S];
+      for (int m = 0; m < S; ++m) ps[m] = P.eos_on ? eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, rc[m]) : rc[m];
+      if (what == 12) {
+        for (int m = 0; m < S; ++m) out[idx * S + m] = double(ps[m]);
+        return;
+      }
       R pr = rt / R(3.);
-      if (S > 1) {
+      if (S > 1 || P.eos_on) {
         for (int m = 0; m < S; ++m) {
           R acc = R(0);
-          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * rc[k];
-          pr = pr + R(P.c0) / R(2.) * rc[m] * acc;
+          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * ps[k];
+          pr = pr + R(P.c0) / R(2.) * ps[m] * acc;
         }
       }
       out[idx] = double(pr);

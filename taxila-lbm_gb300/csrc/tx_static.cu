@@ -121,6 +121,8 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   off = align256(off + (size_t)N * sizeof(uint32_t));
   const size_t o_rho = off;
   off = align256(off + (size_t)N * S * sizeof(double));
+  const size_t o_psi = off;
+  if (p->use_nonideal_eos) off = align256(off + (size_t)N * S * sizeof(double));
   size_t o_face[6];
   for (int f = 0; f < 6; ++f) {
     o_face[f] = off;
@@ -196,6 +198,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
 
   StepArgs a{};
   a.rho = rho;
+  a.psi = p->use_nonideal_eos ? (void*)(base + o_psi) : nullptr;
   a.mask = mask;
   a.links = links;
   a.phys = d_phys;

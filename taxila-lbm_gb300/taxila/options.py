@@ -6,9 +6,10 @@ density faces, ComponentSetFromOptions (lbm_component.F90:131-176),
 RelaxationSetFromOptions (lbm_relaxation.F90:117-151), MineralSetFromOptions
 (lbm_mineral.F90:103-134), GridSetFromOptions/InfoSetFromOptions
 (lbm_grid.F90:97-132, lbm_info.F90:116-238) and FlowSetPhysicalScales
-(lbm_flow.F90:295-376).  Option names and defaults are the reference's, so an
+(lbm_flow.F90:295-376) and EOSSetFromOptions (lbm_eos.F90:90-300).  Option names and defaults are the reference's, so an
 unchanged deck drives this library.
 """
+import struct
 from dataclasses import dataclass, field
 
 from . import params as P
@@ -31,6 +32,11 @@ def parse_deck_text(text):
             raise DeckError("option must start with '-': %r" % raw)
         opts[key[1:]] = parts[1].strip() if len(parts) > 1 else None
     return opts
+
+
+def _f32(v):
+    """A Fortran default-kind real literal: the value rounded to single precision."""
+    return struct.unpack("f", struct.pack("f", v))[0]
 
 
 def _bool(v):
@@ -117,8 +123,6 @@ def params_from_options(opts):
         p.isotropy_order = int(get("isotropy_order"))
     elif has("derivative_order"):
         p.isotropy_order = int(get("derivative_order"))
-    if _bool(get("flow_use_nonideal_eos", "0")):
-        raise DeckError("-flow_use_nonideal_eos: only psi = rho is on this path")
 
     # components (lbm_component.F90:82-176, lbm_relaxation.F90:117-151)
     s = p.ncomponents
@@ -147,6 +151,35 @@ def params_from_options(opts):
             key = "g_%d%d" % (m + 1, q + 1)
             if has(key):
                 p.g[m][q] = float(get(key))
+
+    # non-ideal EOS per component (EOSSetFromOptions, lbm_eos.F90:90-300)
+    if _bool(get("flow_use_nonideal_eos", "0")):
+        p.use_nonideal_eos = 1
+        for m, nm in enumerate(names):
+            kind = (get("eos_" + nm) or "").strip().lower()
+            if kind.startswith("rho"):
+                p.eos[m] = P.EOS_RHO
+            elif kind.startswith("sc"):
+                p.eos[m] = P.EOS_SC
+                p.eos_coef[m][0] = float(get("eos_sc_rho0_" + nm, 1.0))
+            elif kind.startswith("thermo"):
+                p.eos[m] = P.EOS_THERMO
+                p.eos_coef[m][0] = float(get("eos_thermo_psi0_" + nm, 1.0))
+                p.eos_coef[m][1] = float(get("eos_thermo_rho0_" + nm, 1.0))
+            elif kind.startswith("pr"):
+                p.eos[m] = P.EOS_PR
+                a = float(get("eos_pr_a_" + nm, 2.0 / 49.0))
+                b = float(get("eos_pr_b_" + nm, 2.0 / 21.0))
+                # lbm_eos.F90:296 and the 0.9 / 0.344 defaults are single-precision literals
+                tc = a / b * _f32(0.0778) / _f32(0.45724) / 1.0
+                if has("eos_pr_T_" + nm):
+                    t = float(get("eos_pr_T_" + nm))
+                else:
+                    t = (float(get("eos_pr_reduced_T_" + nm)) if has("eos_pr_reduced_T_" + nm) else _f32(0.9)) * tc
+                p.eos_coef[m][0], p.eos_coef[m][1], p.eos_coef[m][2] = a, b, t
+                p.eos_coef[m][3] = float(get("eos_pr_omega_" + nm)) if has("eos_pr_omega_" + nm) else _f32(0.344)
+            else:
+                raise DeckError("Invalid EOS type")
 
     # minerals (lbm_mineral.F90:64-134)
     mnames = []

@@ -18,6 +18,8 @@ PREC_F64, PREC_F32, PREC_F32_F16 = 0, 1, 2
 FIELD_FI, FIELD_RHO, FIELD_FLUX, FIELD_FORCES = 1, 2, 3, 4
 FIELD_PRS, FIELD_VELT, FIELD_RHOT, FIELD_WALLS = 5, 6, 7, 8
 FIELD_SPECIES_FI, FIELD_SPECIES_RHO, FIELD_SPECIES_FLUX = 9, 10, 11
+FIELD_PSI = 12
+EOS_RHO, EOS_SC, EOS_THERMO, EOS_PR = 0, 1, 2, 3
 
 ERR_NAMES = {0: "TX_OK", 1: "TX_ERR_ARG", 2: "TX_ERR_STATE", 3: "TX_ERR_CUDA",
              4: "TX_ERR_NOMEM", 5: "TX_ERR_NONFINITE", 6: "TX_ERR_NODEVICE"}
@@ -37,6 +39,7 @@ class TxParams(C.Structure):
         ("body_forces", _I), ("gvt", _D * 3),
         ("bc_density", (_D * MAXC) * 6),
         ("literal_kind", _I), ("precision", _I), ("exact", _I), ("rho0", _D * MAXC), ("storage_scale", _D),
+        ("use_nonideal_eos", _I), ("eos", _I * MAXC), ("eos_coef", (_D * 4) * MAXC),
         ("nspecies", _I), ("species_relaxation_mode", _I), ("species_tau", _D * MAXC),
         ("species_rates", (_D * 7) * MAXC),
     ]

@@ -162,3 +162,36 @@ SPECIES = [
     ("d3_mrt_two_species", _sp(lambda: sc_bubble(P.D3Q19, (12, 12, 10), P.MRT, 4), P.MRT, ns=2), 20),
     ("d2_species_streaming", _sp(lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), P.SRT), 30),
 ]
+
+
+def eos_drop(disc, shape, eos, coef, g11, mode=P.SRT, r=None, rho_in=2.0, rho_out=0.2):
+    """Single-component Shan-Chen with a non-ideal EOS psi(rho): a drop of
+    rho_in in rho_out, self coupling g11, periodic."""
+    p = base(disc, shape, ncomp=1, mode=mode, iso=4)
+    p.tau[0] = 1.0
+    p.g[0][0] = g11
+    p.use_nonideal_eos = 1
+    p.eos[0] = eos
+    for k, v in enumerate(coef):
+        p.eos_coef[0][k] = v
+    z, y, x = p.shape
+    r = r if r is not None else max(2.0, min(x, y) / 5.0)
+    rho = problems.bubble_ball_state(x, y, z, r, [rho_in], [rho_out])
+    return p, np.zeros(p.nsites), rho
+
+
+def _pr_coef():
+    a, b = 2.0 / 49.0, 2.0 / 21.0
+    f = lambda v: float(np.float32(v))  # single-precision literals of lbm_eos.F90
+    tc = a / b * f(0.0778) / f(0.45724)
+    return (a, b, f(0.9) * tc, f(0.344))
+
+
+# (name, case factory, steps): EOS parity cases
+EOS = [
+    ("d2_eos_sc", lambda: eos_drop(P.D2Q9, (1, 36, 40), P.EOS_SC, (1.0,), -0.28), 40),
+    ("d2_eos_thermo", lambda: eos_drop(P.D2Q9, (1, 32, 32), P.EOS_THERMO, (1.0, 1.0), -0.5), 40),
+    ("d3_eos_pr", lambda: eos_drop(P.D3Q19, (14, 12, 16), P.EOS_PR, _pr_coef(), -1.0 / 6.0,
+                                   rho_in=6.5, rho_out=0.4), 20),
+    ("d3_eos_sc_mrt", lambda: eos_drop(P.D3Q19, (12, 14, 12), P.EOS_SC, (1.0,), -0.28, mode=P.MRT), 20),
+]

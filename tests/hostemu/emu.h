@@ -94,6 +94,7 @@ std::string run(const Case& c, Result& out) {
   std::memset(f0.data(), 0, f0.size() * sizeof(T));
   std::memset(f1.data(), 0, f1.size() * sizeof(T));
   std::vector<RT> rho((size_t)N * S, RT(0));
+  std::vector<RT> psi(p.use_nonideal_eos ? (size_t)N * S : 0, RT(0));
   std::vector<double> facevals[6];
   Faces faces{};
   for (int f = 0; f < 2 * D; ++f) {
@@ -117,6 +118,7 @@ std::string run(const Case& c, Result& out) {
     a.fin = buf[in];
     a.fout = buf[o];
     a.rho = rho.data();
+    a.psi = psi.empty() ? nullptr : psi.data();
     a.mask = mask.data();
     a.links = links.data();
     a.phys = &P;
@@ -132,6 +134,12 @@ std::string run(const Case& c, Result& out) {
     for (long long i = 0; i < N; ++i)
       for (int m = 0; m < S; ++m)
         rho[(size_t)(i * S + m)] = RT(mask[(size_t)i] == 0 ? c.init[(size_t)(i * S + m)] - ph.rho0[m] : 0.0);
+    if (!psi.empty())
+      for (long long i = 0; i < N; ++i)
+        if (mask[(size_t)i] == 0)
+          for (int m = 0; m < S; ++m)
+            psi[(size_t)(i * S + m)] =
+                RT(eos_psi<double>(ph.eos[m], ph.eos_c[m], ph.g[m][m], ph.c0, c.init[(size_t)(i * S + m)]));
     const StepArgs a = args(cur, cur);
     launch3(g, 128, [&] { k_init<D, S, ISO, EXACT, T, R, RT>(a, nullptr); });
   }

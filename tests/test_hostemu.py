@@ -179,3 +179,15 @@ def test_emulated_species_match_oracle(emu_exe, tmp_path, name, make, steps, exa
     pore = walls == 0
     mass0 = np.asarray(conc).reshape(p.nsites, -1)[pore].sum(axis=0)
     assert np.allclose(got["srho"].reshape(p.nsites, -1)[pore].sum(axis=0), mass0, rtol=1e-12)
+
+
+@pytest.mark.parametrize("name,make,steps", cases.EOS, ids=[c[0] for c in cases.EOS])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_emulated_eos_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
+    # psi(rho) from the EOS in the fluid-fluid force; the host's exp is the oracle's
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    compare(ref, got, p, walls, 0.0 if exact else 1e-12)

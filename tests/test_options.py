@@ -116,3 +116,28 @@ def test_transport_options():
     import pytest
     with pytest.raises(options.DeckError):
         options.params_from_options(options.parse_deck_text(bad))
+
+
+
+def test_eos_options():
+    from taxila import options
+    from taxila import params as P
+    deck = """
+-flow_discretization d2q9
+-NX 8
+-NY 8
+-ncomponents 2
+-flow_use_nonideal_eos true
+-eos_component1 sc
+-eos_sc_rho0_component1 2.0
+-eos_component2 pr
+-eos_pr_reduced_T_component2 0.8
+"""
+    p, _ = options.params_from_options(options.parse_deck_text(deck))
+    assert p.use_nonideal_eos == 1
+    assert p.eos[0] == P.EOS_SC and p.eos_coef[0][0] == 2.0
+    a, b = 2.0 / 49.0, 2.0 / 21.0
+    assert p.eos[1] == P.EOS_PR and abs(p.eos_coef[1][2] - 0.8 * a / b * 0.0778 / 0.45724) < 1e-8
+    import pytest
+    with pytest.raises(options.DeckError):
+        options.params_from_options(options.parse_deck_text(deck.replace("-eos_component1 sc", "-eos_component1 vdw")))
