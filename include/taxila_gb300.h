@@ -48,10 +48,23 @@ extern "C" {
 #define TX_RELAX_SRT 0
 #define TX_RELAX_MRT 1
 
-/* per-face flow BC kinds, include/lbm_definitions.h:31-44 (subset on this path) */
-#define TX_BC_NULL 0     /* non-periodic face closed by ghost walls (bounceback) */
+/* per-face flow BC kinds (flow%bc_flags), include/lbm_definitions.h:30-43, and
+ * what tx_params.bc_data[face] holds for each (flow%bc_data(:, face),
+ * FlowParseBC, src/lbm/lbm_flow.F90:1031-1309).  Node values per kind are set
+ * up as FlowSetUpBCsD3/D2 do (lbm_flow.F90:1311-1956). */
+#define TX_BC_NULL 0            /* non-periodic face closed by ghost walls (bounceback) */
 #define TX_BC_PERIODIC 1
-#define TX_BC_DENSITY 6  /* Dirichlet density face (BC_DIRICHLET + BC_DENSITY) */
+#define TX_BC_REFLECTING 2      /* -bc_reflecting_<face>: mirror the incoming populations */
+#define TX_BC_VELOCITY 5        /* -bc_velocity_<face>_values: bc_data[0..ndims-1] = u */
+#define TX_BC_DENSITY 6         /* -bc_density_<face>_<c>: bc_data[m] = rho_m */
+#define TX_BC_MOMENTUM 7        /* -bc_momentum_<face>_<c>: bc_data[m*ndims + d] = (rho u)_m,d */
+#define TX_BC_PRESSURE 8        /* one component: bc_data[0] = p, rho = 3 p */
+#define TX_BC_PRESSURE_INLET 9  /* bc_data[0] = p, bc_data[1] = rho_1 / sum(rho) */
+#define TX_BC_PRESSURE_OUTLET 10 /* bc_data[0] = p; two components: rho_1 / sum(rho) from the
+                                   neighbour inside, every step */
+#define TX_BC_FLUX 11           /* one component: bc_data[0] = inward flux */
+#define TX_BC_FLUX_INLET 12     /* bc_data[0] = flux, bc_data[1] = rho_1 / sum(rho) */
+#define TX_BC_FLUX_OUTLET 13    /* bc_data[0] = flux */
 
 /* faces, include/lbm_definitions.h:47-52 (index = value - 1 in arrays below) */
 #define TX_XM 1
@@ -115,7 +128,7 @@ typedef struct tx_params {
   double gw[TX_MAX_MINERALS][TX_MAX_COMPONENTS];      /* -gw_<mineral>_<c> */
   int32_t body_forces;      /* 1 when -gvt was given */
   double gvt[3];            /* -gvt */
-  double bc_density[6][TX_MAX_COMPONENTS];  /* -bc_density_<face>_<c> for TX_BC_DENSITY faces */
+  double bc_data[6][3 * TX_MAX_COMPONENTS];  /* per face: the kind's values (see TX_BC_*) */
   int32_t literal_kind;     /* 4: the reference's default-REAL literals (1./6. etc.) are
                                single precision, as built without -fdefault-real-8; 8: double */
   int32_t precision;        /* TX_PREC_* */
@@ -173,9 +186,12 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u);
 int tx_upload_fi(tx_handle* h, const double* fi);
 
 /* The initialize_bcs plugin's face arrays (src/lbm/lbm_bc.F90:215-228):
- * vals has nbcs = s*ndims values per face node (component fastest, only the
- * first s used for density faces), face nodes in natural order of the two
- * tangential axes.  Optional: tx_create fills faces from bc_density. */
+ * vals has nbcs = s*ndims values per face node, the reference's (s, ndims)
+ * block with the component fastest (densities in the first s for Dirichlet
+ * faces, momenta for Neumann faces, the velocity in entries 0, s, 2s for
+ * velocity faces), face nodes in natural order of the two tangential axes.
+ * Optional: tx_create fills the faces from bc_data.  Faces without values
+ * (periodic, closed, reflecting) return TX_ERR_ARG. */
 int tx_upload_bc_values(tx_handle* h, int32_t face, const double* vals);
 
 /* Species concentrations [N*ns] and fluxes [N*ndims*ns] (NULL = 0), natural

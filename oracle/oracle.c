@@ -50,7 +50,7 @@ struct orc {
   double *fi, *tmp, *rho, *walls, *flux, *forces, *fieq;
   double *psi;               /* psi_of_rho (rho layout) when use_nonideal_eos */
   double eos_alpha[MAXC];    /* Peng-Robinson alpha(T) */
-  double *bcv[6];            /* nbcs * face area per Dirichlet face */
+  double *bcv[6];            /* nbcs * face area per face with values (Dirichlet, Neumann, velocity) */
   double *old_rho, *old_fi;
   int have_fi, have_state, inited;
   /* passive species: a second distribution over the same lattice, kept as
@@ -181,6 +181,103 @@ static void setup_lattice(orc* o) {
 /* ---------------------------------------------------------------- creation */
 static orc* orc_create_transport(const tx_params* p);
 
+/* ------------------------------------------------------------ exterior BCs */
+/* bc%flags classes next to flow%bc_flags (FlowParseBC, lbm_flow.F90:1031-1309;
+ * include/lbm_definitions.h:30-43) */
+enum { CLS_NONE = 0, CLS_REFL = 2, CLS_DIR = 3, CLS_NEU = 4, CLS_VEL = 5 };
+static int face_class(const orc* o, int f) {
+  if (f >= 2 * o->nd) return CLS_NONE;
+  switch (o->p.bc_flags[f]) {
+    case TX_BC_REFLECTING: return CLS_REFL;
+    case TX_BC_DENSITY: case TX_BC_PRESSURE: case TX_BC_PRESSURE_INLET: case TX_BC_PRESSURE_OUTLET: return CLS_DIR;
+    case TX_BC_FLUX: case TX_BC_MOMENTUM: case TX_BC_FLUX_INLET: case TX_BC_FLUX_OUTLET: return CLS_NEU;
+    case TX_BC_VELOCITY: return CLS_VEL;
+  }
+  return CLS_NONE;
+}
+static int has_values(const orc* o, int f) {
+  const int c = face_class(o, f);
+  return c == CLS_DIR || c == CLS_NEU || c == CLS_VEL;
+}
+static long face_area(const orc* o, int f) {
+  const int a = f / 2, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+  return (long)o->N[t1] * (o->nd == 3 ? o->N[t2] : 1);
+}
+
+/* FlowUpdateDensityFromPressure (lbm_flow.F90:2235-2263) */
+static void density_from_pressure(const orc* o, double pressure, double rho1frac, double* rho) {
+  const double eps = 1.e-10;
+  if (o->s == 1) {
+    rho[0] = pressure * 3.0;
+  } else {
+    if (rho1frac < eps) {
+      rho[0] = 0.0;
+      rho[1] = pressure * 3.0;
+    } else if (rho1frac > 1 - eps) {
+      rho[0] = pressure * 3.0;
+      rho[1] = 0.0;
+    } else {
+      const double alpha = 1.0 / (1.0 / rho1frac - 1.0);
+      const double g21 = o->p.g[1][0]; /* components(2)%gf(1) */
+      rho[0] = (-((1.0 + alpha) / 3.0) + sqrt((1.0 + alpha) / 3.0 * (1.0 + alpha) / 3.0 + 4. * o->c0 * g21 * alpha * pressure)) /
+               (2 * o->c0 * g21);
+      rho[1] = rho[0] / alpha;
+    }
+  }
+}
+
+/* FlowSetUpBCsD3/D2 (lbm_flow.F90:1311-1956): node values per face, the same
+ * at every node, in the (s, ndims) block xm_vals(m, d) = v[d * s + m] */
+static void setup_bc_values(orc* o) {
+  const tx_params* p = &o->p;
+  const int s = o->s, nd = o->nd, nbcs = s * nd;
+  for (int f = 0; f < 2 * nd; ++f) {
+    if (!has_values(o, f)) continue;
+    const int a = f / 2, plus = f % 2;
+    const double* bd = p->bc_data[f];
+    double v[3 * MAXC];
+    for (int k = 0; k < nbcs; ++k) v[k] = 0.0;
+    switch (p->bc_flags[f]) {
+      case TX_BC_DENSITY:
+        for (int m = 0; m < s; ++m) v[m] = bd[m];
+        break;
+      case TX_BC_PRESSURE_INLET:
+      case TX_BC_PRESSURE: {
+        double density[MAXC] = {0.0};
+        density_from_pressure(o, bd[0], bd[1], density);
+        for (int m = 0; m < s; ++m) v[m] = density[m];
+        break;
+      }
+      case TX_BC_PRESSURE_OUTLET:
+        v[0] = bd[0];
+        break;
+      case TX_BC_MOMENTUM:
+        for (int m = 0; m < s; ++m)
+          for (int d = 0; d < nd; ++d) v[d * s + m] = bd[m * nd + d];
+        break;
+      case TX_BC_FLUX_INLET:
+      case TX_BC_FLUX:
+        if (s == 1) {
+          v[a * s] = plus ? -bd[0] : bd[0];
+        } else {
+          v[a * s] = bd[0] * bd[1];
+          v[a * s + 1] = bd[0] * (1.0 - bd[1]);
+        }
+        break;
+      case TX_BC_FLUX_OUTLET:
+        v[a * s] = plus ? -bd[0] : bd[0];
+        break;
+      case TX_BC_VELOCITY:
+        for (int d = 0; d < nd; ++d) v[d * s] = bd[d];
+        break;
+    }
+    const long area = face_area(o, f);
+    o->bcv[f] = (double*)calloc((size_t)area * nbcs, sizeof(double));
+    for (long q = 0; q < area; ++q)
+      for (int k = 0; k < nbcs; ++k) o->bcv[f][q * nbcs + k] = v[k];
+  }
+}
+
 orc* orc_create(const tx_params* p) {
   orc* o = (orc*)calloc(1, sizeof(orc));
   if (!o) return NULL;
@@ -251,16 +348,7 @@ orc* orc_create(const tx_params* p) {
   long nown = (long)o->N[0] * o->N[1] * o->N[2];
   o->old_rho = (double*)calloc((size_t)nown * o->s, sizeof(double));
   o->old_fi = (double*)calloc((size_t)nown * o->s * o->Q, sizeof(double));
-  /* FlowSetUpBCsD3/D2 (lbm_flow.F90:1311-1956): uniform density per face */
-  for (int f = 0; f < 2 * o->nd; ++f) {
-    if (p->bc_flags[f] != TX_BC_DENSITY) continue;
-    int a = f / 2, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-    long area = (long)o->N[t1] * (o->nd == 3 ? o->N[t2] : 1);
-    int nbcs = o->s * o->nd;
-    o->bcv[f] = (double*)calloc((size_t)area * nbcs, sizeof(double));
-    for (long q = 0; q < area; ++q)
-      for (int m = 0; m < o->s; ++m) o->bcv[f][q * nbcs + m] = p->bc_density[f][m];
-  }
+  setup_bc_values(o);
   if (p->nspecies > 0) o->tr = orc_create_transport(p);
   return o;
 }
@@ -634,12 +722,12 @@ static void fibar_init(orc* o) {
 }
 
 /* --------------------------------------------------------- stream/bounceback */
-static int is_dirichlet(const orc* o, int f) { return f < 2 * o->nd && o->p.bc_flags[f] == TX_BC_DENSITY; }
+static int is_dirichlet(const orc* o, int f) { return face_class(o, f) == CLS_DIR; }
 
-/* BCPreStream_D3/D2 (lbm_bc.F90:613-779) */
+/* BCPreStream_D3/D2 (lbm_bc.F90:613-779): Dirichlet, Neumann and velocity faces */
 static void bc_prestream(orc* o) {
   for (int f = 0; f < 2 * o->nd; ++f) {
-    if (!is_dirichlet(o, f)) continue;
+    if (!has_values(o, f)) continue;
     const int a = f / 2, minus = (f % 2) == 0;
     const int face = minus ? 1 : o->N[a];
     for (int n = 1; n <= o->b; ++n) {
@@ -778,24 +866,128 @@ static void dirichlet_node(orc* o, int f, int i, int j, int k, const double* pv)
   }
 }
 
-/* BCApplyDirichletD3/D2 (lbm_bc.F90:1091-1271): faces XM, XP, YM, YP, ZM, ZP */
-static void bc_apply(orc* o) {
-  const int nbcs = o->s * o->nd;
-  for (int f = 0; f < 2 * o->nd; ++f) {
-    if (!is_dirichlet(o, f)) continue;
-    const int a = f / 2, face = (f % 2) == 0 ? 1 : o->N[a];
-    OWNED_LOOP(o) {
-      int x[3] = {i, j, k};
-      if (x[a] != face || WALL(o, i, j, k) != 0) continue;
-      dirichlet_node(o, f, i, j, k, &o->bcv[f][face_node(o, f, i, j, k) * nbcs]);
+/* BCApplyNeumannNode (lbm_bc.F90:1533-1593): mv = the node's (s, ndims) block */
+static void neumann_node(orc* o, int f, int i, int j, int k, const double* mv) {
+  const int a = f / 2;
+  const int sg = (f % 2) == 0 ? 1 : -1;
+  for (int m = 0; m < o->s; ++m) {
+    double ws[3] = {0.0, 0.0, 0.0}, mom[3] = {0.0, 0.0, 0.0}, Q[3] = {0.0, 0.0, 0.0};
+    for (int p = 0; p < o->nd; ++p) {
+      for (int n = 1; n <= o->b; ++n) {
+        mom[p] = mom[p] + FI(o, m, n, i, j, k) * (double)o->ci[n][p];
+        if (sg * o->ci[n][a] == 1 && o->ci[n][p] != 0) ws[p] = ws[p] + o->w[n];
+      }
+      Q[p] = (mv[p * o->s + m] - FRC(o, m, p, i, j, k) / 2.0 - mom[p]) / ws[p];
+    }
+    for (int n = 1; n <= o->b; ++n) {
+      if (sg * o->ci[n][a] != 1) continue;
+      double cq = 0.0;
+      for (int d = 0; d < o->nd; ++d) cq = cq + (double)o->ci[n][d] * Q[d];
+      FI(o, m, n, i, j, k) = FI(o, m, n, i, j, k) + o->w[n] * cq;
     }
   }
 }
 
-/* BCUpdateRho_D3/D2 (lbm_bc.F90:436-611) */
+/* BCApplyVelocityNode (lbm_bc.F90:1793-1865): uvals(1, :) = uv[d * s] */
+static void velocity_node(orc* o, int f, int i, int j, int k, const double* uv) {
+  const int a = f / 2;
+  const int sg = (f % 2) == 0 ? 1 : -1;
+  int tang[2], nt = 0;
+  if (o->nd == 3) {
+    if (a == 0) { tang[0] = 1; tang[1] = 2; }
+    else if (a == 1) { tang[0] = 2; tang[1] = 0; }
+    else { tang[0] = 0; tang[1] = 1; }
+    nt = 2;
+  } else {
+    tang[0] = a == 0 ? 1 : 0;
+    nt = 1;
+  }
+  for (int m = 0; m < o->s; ++m) {
+    double ws[3] = {0.0, 0.0, 0.0}, mom[3] = {0.0, 0.0, 0.0}, Q[3] = {0.0, 0.0, 0.0};
+    for (int n = 1; n <= o->b; ++n) {
+      mom[a] = mom[a] + FI(o, m, n, i, j, k) * (double)o->ci[n][a];
+      if (sg * o->ci[n][a] == 1) ws[a] = ws[a] + o->w[n];
+    }
+    double sum = 0.0;
+    for (int n = 0; n < o->Q; ++n) sum = sum + FI(o, m, n, i, j, k);
+    Q[a] = (sum * uv[a * o->s] - mom[a] - FRC(o, m, a, i, j, k) / 2.0) / (1.0 - (double)sg * uv[a * o->s]) / ws[a];
+    const double rho = sum + ws[a] * Q[a] * (double)sg;
+    for (int p = 0; p < nt; ++p) {
+      const int t = tang[p];
+      for (int n = 1; n <= o->b; ++n) {
+        mom[t] = mom[t] + FI(o, m, n, i, j, k) * (double)o->ci[n][t];
+        if (sg * o->ci[n][a] == 1 && o->ci[n][t] != 0) ws[t] = ws[t] + o->w[n];
+      }
+      Q[t] = (rho * uv[t * o->s] - FRC(o, m, t, i, j, k) / 2.0 - mom[t]) / ws[t];
+    }
+    for (int n = 1; n <= o->b; ++n) {
+      if (sg * o->ci[n][a] != 1) continue;
+      double cq = 0.0;
+      for (int d = 0; d < o->nd; ++d) cq = cq + (double)o->ci[n][d] * Q[d];
+      FI(o, m, n, i, j, k) = FI(o, m, n, i, j, k) + o->w[n] * cq;
+    }
+  }
+}
+
+/* BCApplyReflectingD3/D2 (lbm_bc.F90:825-1073) at one node, as written: on
+ * the XM face in 3D the normal component of n is compared with the z
+ * component of p (:851).  (The 2D XM face compares with ci(p, Z), past the
+ * D2Q9 table; the library rejects that face.) */
+static void reflect_node(orc* o, int f, int i, int j, int k) {
+  const int a = f / 2;
+  const int sg = (f % 2) == 0 ? 1 : -1;
+  const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+  const int b3 = (o->nd == 3 && f == 0) ? 2 : a;
+  for (int n = 1; n <= o->b; ++n) {
+    if (!(sg * o->ci[n][a] > 0)) continue;
+    for (int q = 1; q <= o->b; ++q) {
+      if (o->ci[n][t1] != o->ci[q][t1]) continue;
+      if (o->nd == 3 && o->ci[n][t2] != o->ci[q][t2]) continue;
+      if (o->ci[n][a] != -o->ci[q][b3]) continue;
+      for (int m = 0; m < o->s; ++m) FI(o, m, n, i, j, k) = FI(o, m, q, i, j, k);
+    }
+  }
+}
+
+/* BCApplyReflecting / BCApplyDirichlet / BCApplyNeumann / BCApplyVelocity
+ * D3/D2 (lbm_bc.F90:809-1865) for one class: its faces in XM..ZP order, pore
+ * nodes of each face */
+static void apply_class(orc* o, int cls) {
+  const int nbcs = o->s * o->nd;
+  for (int f = 0; f < 2 * o->nd; ++f) {
+    if (face_class(o, f) != cls) continue;
+    const int a = f / 2, face = (f % 2) == 0 ? 1 : o->N[a];
+    OWNED_LOOP(o) {
+      int x[3] = {i, j, k};
+      if (x[a] != face || WALL(o, i, j, k) != 0) continue;
+      if (cls == CLS_REFL) {
+        reflect_node(o, f, i, j, k);
+        continue;
+      }
+      const double* v = &o->bcv[f][face_node(o, f, i, j, k) * nbcs];
+      if (cls == CLS_DIR) dirichlet_node(o, f, i, j, k, v);
+      else if (cls == CLS_NEU) neumann_node(o, f, i, j, k, v);
+      else velocity_node(o, f, i, j, k, v);
+    }
+  }
+}
+
+/* BCApply (lbm_bc.F90:781-807): each class once, in order of first appearance
+ * over the six sides (periodic and closed sides apply nothing) */
+static void bc_apply(orc* o) {
+  int done[8] = {0};
+  for (int side = 0; side < 6; ++side) {
+    const int cls = face_class(o, side);
+    if (cls == CLS_NONE || done[cls]) continue;
+    apply_class(o, cls);
+    done[cls] = 1;
+  }
+}
+
+/* BCUpdateRho_D3/D2 (lbm_bc.F90:436-611): Dirichlet, Neumann and velocity faces */
 static void bc_update_rho(orc* o) {
   for (int f = 0; f < 2 * o->nd; ++f) {
-    if (!is_dirichlet(o, f)) continue;
+    if (!has_values(o, f)) continue;
     const int a = f / 2, face = (f % 2) == 0 ? 1 : o->N[a];
     OWNED_LOOP(o) {
       int x[3] = {i, j, k};
@@ -805,6 +997,29 @@ static void bc_update_rho(orc* o) {
         for (int n = 0; n < o->Q; ++n) acc = acc + FI(o, m, n, i, j, k);
         RHO(o, m, i, j, k) = acc;
       }
+    }
+  }
+}
+
+/* FlowUpdateBCPressureOutletD3/D2 (lbm_flow.F90:2020-2233), two components:
+ * the mass fraction of the neighbour inside (of the node when that neighbour
+ * is a wall) at the start of FlowApplyBCs */
+static void update_pressure_outlets(orc* o) {
+  const int nbcs = o->s * o->nd;
+  for (int f = 0; f < 2 * o->nd; ++f) {
+    if (o->p.bc_flags[f] != TX_BC_PRESSURE_OUTLET) continue;
+    const int a = f / 2, minus = (f % 2) == 0;
+    const int face = minus ? 1 : o->N[a];
+    OWNED_LOOP(o) {
+      int x[3] = {i, j, k};
+      if (x[a] != face || WALL(o, i, j, k) != 0) continue;
+      int q[3] = {i, j, k};
+      q[a] += minus ? 1 : -1;
+      if (WALL(o, q[0], q[1], q[2]) != 0) { q[0] = i; q[1] = j; q[2] = k; }
+      double tot = 0.0;
+      for (int m = 0; m < o->s; ++m) tot = tot + RHO(o, m, q[0], q[1], q[2]);
+      const double rho1frac = RHO(o, 0, q[0], q[1], q[2]) / tot;
+      density_from_pressure(o, o->p.bc_data[f][0], rho1frac, &o->bcv[f][face_node(o, f, i, j, k) * nbcs]);
     }
   }
 }
@@ -941,7 +1156,16 @@ static void one_step(orc* o) {
   bc_prestream(o);        /* FlowStream: BCPreStream */
   stream(o);              /*             DistributionStream */
   bounceback(o);          /* FlowBounceback */
-  calc_density(o);        /* FlowApplyBCs -> FlowCalcRhoForces */
+  /* FlowApplyBCs (lbm_flow.F90:1958-1991): two-component pressure outlets first;
+   * the flux-outlet update acts on pressure-outlet faces only (:2282-2497)
+   * and the library rejects the two outlets together */
+  if (o->s != 1)
+    for (int f = 0; f < 2 * o->nd; ++f)
+      if (o->p.bc_flags[f] == TX_BC_PRESSURE_OUTLET) {
+        update_pressure_outlets(o);
+        break;
+      }
+  calc_density(o);        /*              -> FlowCalcRhoForces */
   bc_dirichlet_to_rho(o);
   calc_forces(o);
   bc_apply(o);            /*              -> BCApply */

@@ -23,6 +23,8 @@ struct tx_handle {
   Phys* d_phys = nullptr;     // device copy of ph
   PhysT<float>* d_phys32 = nullptr;  // FP32 copy for the reduced-precision forms
   Faces faces{};
+  FaceShell shell{};          // face nodes of the face pass (faces.post)
+  bool outlet = false;        // two-component pressure outlets refresh every step
   KernelSet ks{};
   cudaStream_t stream = nullptr;
   size_t pop_bytes = 0;       // bytes of one population element
@@ -55,7 +57,7 @@ struct tx_handle {
   bool timing = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double t_step_ms = 0.0, t_density_ms = 0.0;
-  long long n_step_launch = 0, n_density_launch = 0;
+  long long n_step_launch = 0, n_density_launch = 0, n_face_launch = 0;
   std::string err;
 };
 
@@ -328,20 +330,24 @@ int tx_create(const tx_params* p, tx_handle** out) {
     const std::string why = h->err;
     return cleanup(why, TX_ERR_CUDA);
   }
-  // Dirichlet density faces (FlowSetUpBCsD3/D2, lbm_flow.F90:1311-1956): uniform values
+  // exterior faces (FlowSetUpBCsD3/D2, lbm_flow.F90:1311-1956): the same values at
+  // every node of a face, the reference's (s, ndims) block per node
+  setup_faces(*p, h->D, &h->faces);
+  h->shell = face_shell(*p, h->D, h->g.nx, h->g.ny, h->g.nz);
+  h->outlet = has_outlet_update(*p, h->D);
+  const int nbcs = h->S * h->D;
   for (int f = 0; f < 2 * h->D; ++f) {
-    if (p->bc_flags[f] != TX_BC_DENSITY) continue;
-    const int a = f / 2;
-    long long area = h->D == 2 ? (a == 0 ? h->g.ny : h->g.nx)
-                               : (a == 0 ? (long long)h->g.ny * h->g.nz : a == 1 ? (long long)h->g.nx * h->g.nz
-                                                                                 : (long long)h->g.nx * h->g.ny);
+    if (!face_has_values(*p, h->D, f)) continue;
+    const long long area = face_area_of(h->D, h->g.nx, h->g.ny, h->g.nz, f);
     h->face_n[f] = area;
-    std::vector<double> v((size_t)area * h->S);
-    for (int m = 0; m < h->S; ++m)
-      for (long long q = 0; q < area; ++q) v[(size_t)m * area + q] = p->bc_density[f][m];
+    double nv[3 * TX_MAX_COMPONENTS];
+    face_node_values(*p, h->D, f, h->ph.c0, nv);
+    std::vector<double> v((size_t)area * nbcs);
+    for (int k = 0; k < nbcs; ++k)
+      for (long long q = 0; q < area; ++q) v[(size_t)k * area + q] = nv[k];
     if (cudaMalloc(&h->faceval[f], v.size() * sizeof(double)) != cudaSuccess) return cleanup("device allocation failed", TX_ERR_NOMEM);
-    cudaMemcpy(h->faceval[f], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
-    h->faces.on[f] = 1;
+    if (cudaMemcpy(h->faceval[f], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      return cleanup("face value upload failed", TX_ERR_CUDA);
     h->faces.vals[f] = h->faceval[f];
   }
   for (int i = 0; i < 4; ++i) cudaEventCreate(&h->ev[i]);
@@ -477,12 +483,12 @@ int tx_upload_fi(tx_handle* h, const double* fi) {
 int tx_upload_bc_values(tx_handle* h, int32_t face, const double* vals) {
   if (!h || !vals) return TX_ERR_ARG;
   const int f = face - 1;
-  if (f < 0 || f >= 2 * h->D || !h->faceval[f]) return fail(h, TX_ERR_ARG, "face is not a density face");
+  if (f < 0 || f >= 2 * h->D || !h->faceval[f]) return fail(h, TX_ERR_ARG, "face carries no boundary values");
   const long long area = h->face_n[f];
   const int nbcs = h->S * h->D;
-  std::vector<double> v((size_t)area * h->S);
+  std::vector<double> v((size_t)area * nbcs);
   for (long long q = 0; q < area; ++q)
-    for (int m = 0; m < h->S; ++m) v[(size_t)m * area + q] = vals[q * nbcs + m];
+    for (int k = 0; k < nbcs; ++k) v[(size_t)k * area + q] = vals[q * nbcs + k];
   TX_CUDA(h, cudaMemcpy(h->faceval[f], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
   return TX_OK;
 }
@@ -523,10 +529,22 @@ int tx_step(tx_handle* h, int32_t nsteps) {
   for (int t = 0; t < nsteps; ++t) {
     const int nxt = 1 - h->cur;
     StepArgs a = args(h, h->cur, nxt);
+    if (h->outlet) {
+      // FlowApplyBCs' pressure-outlet refresh (lbm_flow.F90:1964-1978), from the state
+      for (int f = 0; f < 2 * h->D; ++f)
+        if (h->p.bc_flags[f] == TX_BC_PRESSURE_OUTLET) {
+          h->ks.outlet(a, f, h->faceval[f], h->p.bc_data[f][0], h->ph.c0, h->p.g[1][0], h->stream);
+          ++h->n_face_launch;
+        }
+    }
     if (h->timing) cudaEventRecord(h->ev[0], h->stream);
     h->ks.step(a, h->stream);
     if (h->timing) cudaEventRecord(h->ev[1], h->stream);
     h->ks.density(a, 0, h->stream);
+    if (h->faces.post) {
+      h->ks.faces(a, h->shell, h->stream);
+      ++h->n_face_launch;
+    }
     if (h->timing) cudaEventRecord(h->ev[2], h->stream);
     if (h->NS > 0 && h->have_species) {
       h->ss.step(species_args(h, h->gcur, 1 - h->gcur), h->stream);
@@ -613,7 +631,7 @@ int tx_set_timing(tx_handle* h, int32_t on) {
   if (!h) return TX_ERR_ARG;
   h->timing = on != 0;
   h->t_step_ms = h->t_density_ms = 0.0;
-  h->n_step_launch = h->n_density_launch = 0;
+  h->n_step_launch = h->n_density_launch = h->n_face_launch = 0;
   return TX_OK;
 }
 
@@ -621,7 +639,7 @@ int tx_get_timing(tx_handle* h, double* ms_step, double* ms_density, int64_t* la
   if (!h) return TX_ERR_ARG;
   if (ms_step) *ms_step = h->t_step_ms;
   if (ms_density) *ms_density = h->t_density_ms;
-  if (launches) *launches = h->n_step_launch + h->n_density_launch;
+  if (launches) *launches = h->n_step_launch + h->n_density_launch + h->n_face_launch;
   return TX_OK;
 }
 

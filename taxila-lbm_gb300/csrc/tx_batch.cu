@@ -396,6 +396,8 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   std::string why;
   int rc = tx::validate(p, &why);
   if (rc) return bfail(b, rc, why);
+  if (!faces_plain(*p, p->discretization == TX_D3Q19 ? 3 : 2))
+    return bfail(b, TX_ERR_ARG, "batched lattices run periodic, closed and density faces; other BCs run on handles");
   const tx_params& f = b->form;
   if (p->discretization != f.discretization || p->ncomponents != f.ncomponents ||
       p->relaxation_mode != f.relaxation_mode || p->isotropy_order != f.isotropy_order ||
@@ -479,17 +481,17 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   TX_BALLOC(L->uold, (size_t)N * D * sizeof(double));
   TX_BALLOC(L->steps_dev, sizeof(unsigned));
   TX_BALLOC(L->phys, physb);
+  setup_faces(*p, D, &L->faces);
   for (int fc = 0; fc < 2 * D; ++fc) {
     if (p->bc_flags[fc] != TX_BC_DENSITY) continue;
     const long long area = face_area(*p, D, fc);
     std::vector<double> v((size_t)area * S);
     for (int m = 0; m < S; ++m)
-      for (long long q = 0; q < area; ++q) v[(size_t)(m * area + q)] = p->bc_density[fc][m];
+      for (long long q = 0; q < area; ++q) v[(size_t)(m * area + q)] = p->bc_data[fc][m];
     TX_BALLOC(L->faceval[fc], v.size() * sizeof(double));
     if (cudaMemcpyAsync(L->faceval[fc], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return undo("face upload failed", TX_ERR_CUDA);
-    L->faces.on[fc] = 1;
     L->faces.vals[fc] = L->faceval[fc];
   }
   if (u) TX_BALLOC(uic, ut.size() * sizeof(double));

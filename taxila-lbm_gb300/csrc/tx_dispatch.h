@@ -22,6 +22,10 @@ struct KernelSet {
   void (*step_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   void (*density_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   void (*probe_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
+  // exterior BCs beyond Dirichlet faces: the face pass after k_density, and the
+  // per-step refresh of one two-component pressure-outlet face before k_step
+  void (*faces)(const StepArgs&, const FaceShell&, cudaStream_t);
+  void (*outlet)(const StepArgs&, int face, double* vals, double pressure, double c0, double g21, cudaStream_t);
   const char* name;
 };
 
@@ -110,6 +114,14 @@ inline Launch3 launch3(const Geo& g, int threads) {
     static void probe_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {               \
       if constexpr (!EXACT) k_probe_tiles<D, S, ISO, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                 \
     }                                                                                                         \
+    static void faces(const StepArgs& a, const FaceShell& sh, cudaStream_t s) {                               \
+      const long long n = sh.start[sh.nf];                                                                    \
+      if (n > 0) k_faces<D, S, ISO, EXACT, T, R, RT><<<grid_for(n, 128), 128, 0, s>>>(a, sh);                 \
+    }                                                                                                         \
+    static void outlet(const StepArgs& a, int f, double* v, double p, double c0, double g21, cudaStream_t s) { \
+      const long long n = face_area_of(D, a.g.nx, a.g.ny, a.g.nz, f);                                         \
+      k_outlet<D, S, T, R, RT><<<grid_for(n, 128), 128, 0, s>>>(a, f, v, p, c0, g21);                         \
+    }                                                                                                         \
   };
 
 #define TX_FORM_CASE(S, ISO, MRT) TX_FORM_CASE_(S, ISO, MRT)
@@ -119,6 +131,7 @@ inline Launch3 launch3(const Geo& g, int threads) {
                     &L_##S##_##ISO##_##MRT::init,   &L_##S##_##ISO##_##MRT::moments,                           \
                     &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat,                          \
                     &L_##S##_##ISO##_##MRT::step_tiles, &L_##S##_##ISO##_##MRT::density_tiles,                 \
-                    &L_##S##_##ISO##_##MRT::probe_tiles, #S "c iso" #ISO " mrt" #MRT};                         \
+                    &L_##S##_##ISO##_##MRT::probe_tiles, &L_##S##_##ISO##_##MRT::faces,                        \
+                    &L_##S##_##ISO##_##MRT::outlet, #S "c iso" #ISO " mrt" #MRT};                              \
     return true;                                                                                               \
   }

@@ -44,12 +44,31 @@ inline int validate(const tx_params* p, std::string* why) {
     if ((lo == TX_BC_PERIODIC) != (hi == TX_BC_PERIODIC)) return bad("periodic faces must come in pairs");
     const int ext = a == 0 ? p->nx : (a == 1 ? p->ny : p->nz);
     if (lo == TX_BC_PERIODIC && ext < 3) return bad("periodic axes need at least 3 sites");
-    for (int f : {2 * a, 2 * a + 1}) {
-      const int v = p->bc_flags[f];
-      if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY)
-        return bad("face BC " + std::to_string(f + 1) + ": only periodic, density or wall faces are supported");
-    }
   }
+  // exterior BCs with the reference's own restrictions (FlowParseBC, FlowSetUpBCs,
+  // FlowApplyBCs, FlowUpdateDensityFromPressure in lbm_flow.F90)
+  bool has_po = false, has_fo = false;
+  for (int f = 0; f < 2 * D; ++f) {
+    const int v = p->bc_flags[f], S = p->ncomponents;
+    const std::string face = "face " + std::to_string(f + 1) + ": ";
+    if (v != TX_BC_NULL && v != TX_BC_PERIODIC && bc_class(v) == kClsNone) return bad(face + "unknown BC kind");
+    if ((v == TX_BC_PRESSURE || v == TX_BC_FLUX) && S != 1)
+      return bad(face + "pressure and flux BCs are single-component BCs (use the _inlet forms)");
+    if ((v == TX_BC_PRESSURE_INLET || v == TX_BC_PRESSURE_OUTLET) && S > 2)
+      return bad(face + "Invalid number of components for flow");
+    if (v == TX_BC_FLUX_INLET && S > 2) return bad(face + "BC flux inlet only implemented for 1 or 2 components.");
+    if (v == TX_BC_REFLECTING && D == 2 && f == 0)
+      return bad(face + "reflecting XM face of D2Q9: the reference reads ci(p, Z) past its direction table there");
+    for (int k = 0; k < 3 * TX_MAX_COMPONENTS; ++k)
+      if (!std::isfinite(p->bc_data[f][k])) return bad(face + "bc_data must be finite");
+    has_po |= v == TX_BC_PRESSURE_OUTLET;
+    has_fo |= v == TX_BC_FLUX_OUTLET;
+  }
+  if (has_po && p->ncomponents != 1 && (std::fabs(p->g[0][0]) > 1e-10 || p->use_nonideal_eos))
+    return bad("Pressure outlet not implemented for non-ideal EOS or g11 or g22 /= 0");
+  if (has_po && has_fo)
+    return bad("pressure and flux outlets together: the reference's flux-outlet update writes its values into the "
+               "pressure-outlet faces");
   if (p->use_nonideal_eos) {
     for (int m = 0; m < p->ncomponents; ++m) {
       const int t = p->eos[m];
@@ -182,6 +201,112 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
     P.cA[m][2] = -(1.0 / 36.0) * rel * P.rho0[m];
   }
   P.inv_sscale = 1.0 / P.sscale;
+}
+
+// ------------------------------------------------------------ exterior BCs
+inline long long face_area_of(int D, int nx, int ny, int nz, int f) {
+  const int a = f / 2;
+  if (D == 2) return a == 0 ? ny : nx;
+  return a == 0 ? (long long)ny * nz : (a == 1 ? (long long)nx * nz : (long long)nx * ny);
+}
+
+// FlowSetUpBCsD3/D2 (lbm_flow.F90:1311-1956): the values of every node of
+// face f, in the reference's (s, ndims) block v[d * S + m] (zero elsewhere).
+inline void face_node_values(const tx_params& p, int D, int f, double c0, double* v) {
+  const int S = p.ncomponents, a = f / 2;
+  const bool plus = (f % 2) == 1;
+  const double* bd = p.bc_data[f];
+  for (int k = 0; k < S * D; ++k) v[k] = 0.0;
+  switch (p.bc_flags[f]) {
+    case TX_BC_DENSITY:
+      for (int m = 0; m < S; ++m) v[m] = bd[m];
+      break;
+    case TX_BC_PRESSURE:
+    case TX_BC_PRESSURE_INLET: {
+      double dens[2] = {0.0, 0.0};
+      density_from_pressure(S, c0, S > 1 ? p.g[1][0] : 0.0, bd[0], bd[1], dens);
+      for (int m = 0; m < S; ++m) v[m] = dens[m];
+      break;
+    }
+    case TX_BC_PRESSURE_OUTLET:
+      v[0] = bd[0];
+      break;
+    case TX_BC_MOMENTUM:
+      for (int m = 0; m < S; ++m)
+        for (int d = 0; d < D; ++d) v[d * S + m] = bd[m * D + d];
+      break;
+    case TX_BC_FLUX:
+    case TX_BC_FLUX_INLET:
+      if (S == 1) {
+        v[a * S] = plus ? -bd[0] : bd[0];
+      } else {  // two components: no sign change on the plus faces, as written
+        v[a * S] = bd[0] * bd[1];
+        v[a * S + 1] = bd[0] * (1.0 - bd[1]);
+      }
+      break;
+    case TX_BC_FLUX_OUTLET:
+      v[a * S] = plus ? -bd[0] : bd[0];
+      break;
+    case TX_BC_VELOCITY:
+      for (int d = 0; d < D; ++d) v[d * S] = bd[d];
+      break;
+  }
+}
+
+// Face flags, classes and BCApply's class order (lbm_bc.F90:781-807); vals
+// pointers are left to the caller.
+inline void setup_faces(const tx_params& p, int D, Faces* fc) {
+  std::memset(fc, 0, sizeof(*fc));
+  bool seen[8] = {false};
+  for (int f = 0; f < 6; ++f) {
+    const int cls = f < 2 * D ? bc_class(p.bc_flags[f]) : kClsNone;
+    fc->cls[f] = cls;
+    fc->on[f] = cls == kClsDir || cls == kClsNeu || cls == kClsVel;
+    fc->dir[f] = cls == kClsDir;
+    if (cls != kClsDir && cls != kClsNone) fc->post = 1;
+    if (cls != kClsNone && !seen[cls]) {
+      seen[cls] = true;
+      fc->order[fc->norder++] = cls;
+    }
+  }
+}
+
+// Whether a face needs node values on the device.
+inline bool face_has_values(const tx_params& p, int D, int f) {
+  if (f >= 2 * D) return false;
+  const int cls = bc_class(p.bc_flags[f]);
+  return cls == kClsDir || cls == kClsNeu || cls == kClsVel;
+}
+
+// Two-component pressure outlets refresh their values every step.
+inline bool has_outlet_update(const tx_params& p, int D) {
+  if (p.ncomponents == 1) return false;
+  for (int f = 0; f < 2 * D; ++f)
+    if (p.bc_flags[f] == TX_BC_PRESSURE_OUTLET) return true;
+  return false;
+}
+
+// The face-pass grid: faces with a node correction, in XM..ZP order.
+inline FaceShell face_shell(const tx_params& p, int D, int nx, int ny, int nz) {
+  FaceShell sh{};
+  sh.start[0] = 0;
+  for (int f = 0; f < 2 * D; ++f) {
+    if (bc_class(p.bc_flags[f]) == kClsNone) continue;
+    sh.face[sh.nf] = f;
+    sh.start[sh.nf + 1] = sh.start[sh.nf] + face_area_of(D, nx, ny, nz, f);
+    ++sh.nf;
+  }
+  return sh;
+}
+
+// Only periodic, closed and density faces (what batches and the
+// allocation-free step run).
+inline bool faces_plain(const tx_params& p, int D) {
+  for (int f = 0; f < 2 * D; ++f) {
+    const int v = p.bc_flags[f];
+    if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY) return false;
+  }
+  return true;
 }
 
 // Species relaxation (SpecieSetFromOptions, lbm_species.F90:111-133; the

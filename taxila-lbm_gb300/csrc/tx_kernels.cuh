@@ -115,10 +115,54 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
 }
 
+// Classes of the exterior BC kinds, as bc%flags holds them next to
+// flow%bc_flags (FlowParseBC, lbm_flow.F90:1031-1309; include/lbm_definitions.h:30-35).
+enum : int { kClsNone = 0, kClsRefl = 2, kClsDir = 3, kClsNeu = 4, kClsVel = 5 };
+__host__ __device__ constexpr int bc_class(int kind) {
+  return kind == TX_BC_REFLECTING ? kClsRefl
+         : (kind == TX_BC_DENSITY || kind == TX_BC_PRESSURE || kind == TX_BC_PRESSURE_INLET ||
+            kind == TX_BC_PRESSURE_OUTLET)
+             ? kClsDir
+         : (kind == TX_BC_FLUX || kind == TX_BC_MOMENTUM || kind == TX_BC_FLUX_INLET || kind == TX_BC_FLUX_OUTLET)
+             ? kClsNeu
+         : kind == TX_BC_VELOCITY ? kClsVel
+                                  : kClsNone;
+}
+
 struct Faces {
-  int on[6];                // Dirichlet density face flags, XM..ZP
-  const double* vals[6];    // [m * area + node], node in natural order of the tangential axes
+  int on[6];              // Dirichlet, Neumann or velocity class: the node density is re-summed
+                          // after the corrections (BCUpdateRho, lbm_bc.F90:436-611)
+  int dir[6];             // Dirichlet class: the face value is the forcing density of the node
+                          // (BCApplyDirichletToRho, lbm_bc.F90:252-434)
+  int cls[6];             // kCls* per face XM..ZP
+  const double* vals[6];  // [k * area + node], k = d * S + m: the reference's (s, ndims) block
+                          // per node; nodes in natural order of the tangential axes
+  int order[4];           // BCApply's class sequence (first appearance over XM..ZP, lbm_bc.F90:781-807)
+  int norder;
+  int post;               // 1: every node correction runs in k_faces (some face is not Dirichlet)
 };
+
+// FlowUpdateDensityFromPressure (lbm_flow.F90:2235-2263): component densities
+// of pressure p at mass fraction rho1frac (one or two components), in the
+// reference's operation order.  g21 = components(2)%gf(1).
+__host__ __device__ inline void density_from_pressure(int S, double c0, double g21, double pressure, double rho1frac,
+                                                      double* rho) {
+  const double eps = 1.e-10;
+  if (S == 1) {
+    rho[0] = pressure * 3.0;
+  } else if (rho1frac < eps) {
+    rho[0] = 0.0;
+    rho[1] = pressure * 3.0;
+  } else if (rho1frac > 1 - eps) {
+    rho[0] = pressure * 3.0;
+    rho[1] = 0.0;
+  } else {
+    const double alpha = 1.0 / (1.0 / rho1frac - 1.0);
+    rho[0] = (-((1.0 + alpha) / 3.0) + sqrt((1.0 + alpha) / 3.0 * (1.0 + alpha) / 3.0 + 4. * c0 * g21 * alpha * pressure)) /
+             (2 * c0 * g21);
+    rho[1] = rho[0] / alpha;
+  }
+}
 
 // The deviation storage of a lattice for the natural-order conversions.
 struct Shift {
@@ -339,10 +383,22 @@ __device__ __forceinline__ bool on_face(const Geo& g, int f, int x, int y, int z
   return (f & 1) ? c == n - 1 : c == 0;
 }
 
-// bit f set <=> face f is a Dirichlet density face (constant-index reads only)
+// bit f set <=> face f re-sums its node densities (constant-index reads only)
 __device__ __forceinline__ unsigned face_bits(const Faces& fc) {
   return (fc.on[0] ? 1u : 0u) | (fc.on[1] ? 2u : 0u) | (fc.on[2] ? 4u : 0u) | (fc.on[3] ? 8u : 0u) |
          (fc.on[4] ? 16u : 0u) | (fc.on[5] ? 32u : 0u);
+}
+// bit f set <=> face f is of the Dirichlet class
+__device__ __forceinline__ unsigned dir_bits(const Faces& fc) {
+  return (fc.dir[0] ? 1u : 0u) | (fc.dir[1] ? 2u : 0u) | (fc.dir[2] ? 4u : 0u) | (fc.dir[3] ? 8u : 0u) |
+         (fc.dir[4] ? 16u : 0u) | (fc.dir[5] ? 32u : 0u);
+}
+// bit f set <=> face f carries a node correction of some class
+__device__ __forceinline__ unsigned active_bits(const Faces& fc) {
+  unsigned b = 0u;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) b |= fc.cls[f] != kClsNone ? (1u << f) : 0u;
+  return b;
 }
 
 // bit f set <=> (x, y, z) lies on face f
@@ -1085,9 +1141,11 @@ __device__ __forceinline__ void dirichlet_node(int f, const R pv[S], R fv[S][Lat
 }
 
 // -------------------------------------------------------------- density
-// mode 0 (after a step): Dirichlet faces in XM..ZP order (BCApplyDirichletD3/D2,
-// lbm_bc.F90:1091-1271), forcing density = the face value
-// (BCApplyDirichletToRho, :252-434) on face nodes, sum of populations elsewhere.
+// mode 0 (after a step): forcing density = the face value on Dirichlet-class
+// face nodes (BCApplyDirichletToRho, lbm_bc.F90:252-434; the last such face in
+// XM..ZP order wins), the sum of populations elsewhere.  With only Dirichlet
+// faces the node corrections run here too (BCApplyDirichletD3/D2,
+// lbm_bc.F90:1091-1271); otherwise k_faces applies every class in order.
 // mode 1 (FlowUpdateMoments at init, lbm_flow.F90:466-478): plain sums.
 template <int D, int S, class T, class R, class RT>
 __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, int z, int mode) {
@@ -1100,8 +1158,28 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
   const long long N = a.g.n;
   RT* rho = reinterpret_cast<RT*>(a.rho);
   T* fcur = reinterpret_cast<T*>(a.fout);
-  const bool dn = mode == 0 && any_dirichlet<D>(a.g, a.faces, x, y, z);
-  if (!dn) {
+  const unsigned keep = D == 3 ? 63u : 15u;
+  const unsigned dhit = mode == 0 ? dir_bits(a.faces) & site_faces(a.g, x, y, z) & keep : 0u;
+  if (dhit && a.faces.post) {
+    // corrections follow in k_faces: here only the face value as forcing density
+    R rf[S];
+    sfor<0, 2 * D>([&](auto ff) {
+      constexpr int f = decltype(ff)::value;
+      if (dhit & (1u << f)) {
+        const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
+#pragma unroll
+        for (int m = 0; m < S; ++m) rf[m] = R(a.faces.vals[f][(long long)m * area + node]);
+      }
+    });
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      rho[(size_t)c * S + m] = RT(kShifted<T> ? rf[m] - P.rho0[m] : rf[m]);
+      if (P.eos_on)
+        reinterpret_cast<RT*>(a.psi)[(size_t)c * S + m] = RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, rf[m]));
+    }
+    return;
+  }
+  if (!dhit) {
     // stored as rho - rho0 = sum_n (f_n - w_n rho0)
 #pragma unroll
     for (int m = 0; m < S; ++m) {
@@ -1126,10 +1204,9 @@ __device__ __forceinline__ void density_site(const StepArgs& a, int x, int y, in
       sfor<0, Q>([&](auto nn) { fv[m][decltype(nn)::value] += R(L::w(decltype(nn)::value)) * P.rho0[m]; });
   }
   R rf[S];
-  const unsigned hit = face_bits(a.faces) & site_faces(a.g, x, y, z);
   sfor<0, 2 * D>([&](auto ff) {
     constexpr int f = decltype(ff)::value;
-    if (hit & (1u << f)) {
+    if (dhit & (1u << f)) {
       const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
       const double* vals = a.faces.vals[f];
       R pv[S];
@@ -1161,6 +1238,306 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
   density_site<D, S, T, R, RT>(a, x, y, z, mode);
+}
+
+// ------------------------------------------------ Neumann and velocity nodes
+// BCApplyNeumannNode (lbm_bc.F90:1533-1593): v is the node's (s, ndims)
+// momentum block, F the node's forces (FlowCalcRhoForces of this step).
+template <int D, int S, class R>
+__device__ __forceinline__ void neumann_node(int f, const R v[S * D], const R F[S][D], R fv[S][Lat<D>::Q]) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const int a = f >> 1;
+  const int sg = (f & 1) == 0 ? 1 : -1;
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R Qv[3] = {R(0), R(0), R(0)};
+#pragma unroll
+    for (int p = 0; p < D; ++p) {
+      R mom = R(0), ws = R(0);
+#pragma unroll
+      for (int n = 1; n < Q; ++n) {
+        const int cp = L::c(n, p);
+        if (cp > 0) mom = mom + fv[m][n];
+        if (cp < 0) mom = mom - fv[m][n];
+        if (sg * L::c(n, a) == 1 && cp != 0) ws = ws + R(L::w(n));
+      }
+      Qv[p] = (v[p * S + m] - F[m][p] / R(2) - mom) / ws;
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+      if (sg * L::c(n, a) != 1) continue;
+      R cq = R(0);
+      for (int d = 0; d < D; ++d) cq = cq + R(L::c(n, d)) * Qv[d];
+      fv[m][n] = fv[m][n] + R(L::w(n)) * cq;
+    }
+  }
+}
+
+// BCApplyVelocityNode (lbm_bc.F90:1793-1865): every component is driven to
+// the velocity in v's first row (entries d * S); tangential axes in CARDINAL order.
+template <int D, int S, class R>
+__device__ __forceinline__ void velocity_node(int f, const R v[S * D], const R F[S][D], R fv[S][Lat<D>::Q]) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const int a = f >> 1;
+  const int sg = (f & 1) == 0 ? 1 : -1;
+  int tang[2];
+  int nt;
+  if (D == 3) {
+    tang[0] = a == 0 ? 1 : (a == 1 ? 2 : 0);
+    tang[1] = a == 0 ? 2 : (a == 1 ? 0 : 1);
+    nt = 2;
+  } else {
+    tang[0] = a == 0 ? 1 : 0;
+    tang[1] = 0;
+    nt = 1;
+  }
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R Qv[3] = {R(0), R(0), R(0)};
+    R momn = R(0), wsn = R(0);
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+      const int ca = L::c(n, a);
+      if (ca > 0) momn = momn + fv[m][n];
+      if (ca < 0) momn = momn - fv[m][n];
+      if (sg * ca == 1) wsn = wsn + R(L::w(n));
+    }
+    R sum = R(0);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) sum = sum + fv[m][n];
+    const R un = v[a * S];
+    Qv[a] = (sum * un - momn - F[m][a] / R(2)) / (R(1) - R(sg) * un) / wsn;
+    const R rh = sum + wsn * Qv[a] * R(sg);
+    for (int p = 0; p < nt; ++p) {
+      const int t = tang[p];
+      R mom = R(0), ws = R(0);
+#pragma unroll
+      for (int n = 1; n < Q; ++n) {
+        const int ct = L::c(n, t);
+        if (ct > 0) mom = mom + fv[m][n];
+        if (ct < 0) mom = mom - fv[m][n];
+        if (sg * L::c(n, a) == 1 && ct != 0) ws = ws + R(L::w(n));
+      }
+      Qv[t] = (rh * v[t * S] - F[m][t] / R(2) - mom) / ws;
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+      if (sg * L::c(n, a) != 1) continue;
+      R cq = R(0);
+      for (int d = 0; d < D; ++d) cq = cq + R(L::c(n, d)) * Qv[d];
+      fv[m][n] = fv[m][n] + R(L::w(n)) * cq;
+    }
+  }
+}
+
+// BCApplyReflectingD3/D2 (lbm_bc.F90:825-1073) at a node of face FC, as
+// written: each incoming population n takes, in p order, the value of every p
+// with the same tangential components and the opposite normal one.  On the
+// XM face in 3D the reference compares n's x component with p's z component
+// (lbm_bc.F90:851); that comparison is kept.
+template <int D, int S, int FC, class R>
+__device__ __forceinline__ void reflect_node(R fv[S][Lat<D>::Q]) {
+  using L = Lat<D>;
+  constexpr int a = FC >> 1, sg = (FC & 1) == 0 ? 1 : -1;
+  constexpr int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+  constexpr int b3 = (D == 3 && FC == 0) ? 2 : a;
+  sfor<1, L::Q>([&](auto nn) {
+    constexpr int n = decltype(nn)::value;
+    if constexpr (sg * L::c(n, a) > 0) {
+      sfor<1, L::Q>([&](auto pp) {
+        constexpr int q = decltype(pp)::value;
+        constexpr bool same2 = D == 2 ? true : L::c(n, t2) == L::c(q, t2);
+        if constexpr (L::c(n, t1) == L::c(q, t1) && same2 && L::c(n, a) == -L::c(q, b3)) {
+#pragma unroll
+          for (int m = 0; m < S; ++m) fv[m][n] = fv[m][q];
+        }
+      });
+    }
+  });
+}
+
+// -------------------------------------------------------------- face pass
+// BCApply (lbm_bc.F90:781-807) after the density pass, for lattices with a
+// face that is not of the Dirichlet class: at each pore face node, the
+// classes in BCApply's order, each over the node's faces in XM..ZP order.
+// The forces of Neumann and velocity nodes are the ones FlowCalcRhoForces
+// computes from this step's forcing density (the next collision's forces).
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__device__ __forceinline__ void face_site(const StepArgs& a, int x, int y, int z) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
+  const unsigned c = (unsigned)x + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  if (__ldg(a.mask + c) != 0) return;
+  const unsigned keep = D == 3 ? 63u : 15u;
+  const unsigned hit = active_bits(a.faces) & site_faces(a.g, x, y, z) & keep;
+  if (!hit) return;
+  const long long N = a.g.n;
+  T* fcur = reinterpret_cast<T*>(a.fout);
+  R fv[S][Q];
+  load_pops<D, S, T, R>(fcur, N, c, P, fv);
+  if constexpr (kShifted<T>) {
+#pragma unroll
+    for (int m = 0; m < S; ++m)
+      sfor<0, Q>([&](auto nn) { fv[m][decltype(nn)::value] += R(L::w(decltype(nn)::value)) * P.rho0[m]; });
+  }
+  R F[S][D];
+  bool need_f = false;
+#pragma unroll
+  for (int f = 0; f < 2 * D; ++f)
+    need_f |= ((hit >> f) & 1u) && (a.faces.cls[f] == kClsNeu || a.faces.cls[f] == kClsVel);
+  if (need_f) {
+    const RT* rho = reinterpret_cast<const RT*>(a.rho);
+    const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
+    R rfd[S], rf[S];
+    rho_at<S>(rho, c, rfd);
+#pragma unroll
+    for (int m = 0; m < S; ++m) rf[m] = P.rho0[m] + rfd[m];
+    cell_forces<D, S, ISO, EXACT>(h, __ldg(a.links + c), P, a.mask, rho, reinterpret_cast<const RT*>(a.psi), N, rfd,
+                                  rf, F);
+  } else {
+#pragma unroll
+    for (int m = 0; m < S; ++m)
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[m][d] = R(0);
+  }
+  for (int i = 0; i < a.faces.norder; ++i) {
+    const int cls = a.faces.order[i];
+    sfor<0, 2 * D>([&](auto ff) {
+      constexpr int f = decltype(ff)::value;
+      if (!((hit >> f) & 1u) || a.faces.cls[f] != cls) return;
+      if (cls == kClsRefl) {
+        reflect_node<D, S, f, R>(fv);
+        return;
+      }
+      const long long area = face_area<D>(a.g, f), node = face_node<D>(a.g, f, x, y, z);
+      R v[S * D];
+#pragma unroll
+      for (int k = 0; k < S * D; ++k) v[k] = R(a.faces.vals[f][(long long)k * area + node]);
+      if (cls == kClsDir)
+        dirichlet_node<D, S, R>(f, v, fv);
+      else if (cls == kClsNeu)
+        neumann_node<D, S, R>(f, v, F, fv);
+      else
+        velocity_node<D, S, R>(f, v, F, fv);
+    });
+  }
+#pragma unroll
+  for (int m = 0; m < S; ++m)
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      R w = fv[m][n];
+      if constexpr (kShifted<T>) w = w - R(L::w(n)) * P.rho0[m];
+      st_dev<T, R>(fcur + (long long)(m * Q + n) * N + c, w, P);
+    });
+}
+
+// The face nodes of a lattice: faces with a node correction, each node once
+// (by the first of its faces in XM..ZP order).
+struct FaceShell {
+  int nf;
+  int face[6];
+  long long start[7];
+};
+
+template <int D>
+__device__ __forceinline__ bool shell_site(const Geo& g, const FaceShell& sh, long long t, int& x, int& y, int& z) {
+  if (t >= sh.start[sh.nf]) return false;
+  int i = 0;
+  while (i + 1 < sh.nf && t >= sh.start[i + 1]) ++i;
+  const int f = sh.face[i];
+  const long long q = t - sh.start[i];
+  const int a = f >> 1;
+  const int fixed = (f & 1) ? (a == 0 ? g.nx : (a == 1 ? g.ny : g.nz)) - 1 : 0;
+  if (D == 2) {
+    x = a == 0 ? fixed : (int)q;
+    y = a == 0 ? (int)q : fixed;
+    z = 0;
+  } else if (a == 0) {
+    x = fixed; y = (int)(q % g.ny); z = (int)(q / g.ny);
+  } else if (a == 1) {
+    y = fixed; x = (int)(q % g.nx); z = (int)(q / g.nx);
+  } else {
+    z = fixed; x = (int)(q % g.nx); y = (int)(q / g.nx);
+  }
+  for (int j = 0; j < i; ++j)
+    if (on_face(g, sh.face[j], x, y, z)) return false;
+  return true;
+}
+
+template <int D, int S, int ISO, bool EXACT, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_faces(StepArgs a_in, FaceShell sh) {
+  const StepArgs a = a_in;
+  int x, y, z;
+  if (!shell_site<D>(a.g, sh, (long long)blockIdx.x * blockDim.x + threadIdx.x, x, y, z)) return;
+  face_site<D, S, ISO, EXACT, T, R, RT>(a, x, y, z);
+}
+
+// ------------------------------------------------------- pressure outlets
+// FlowUpdateBCPressureOutletD3/D2 (lbm_flow.F90:2020-2233), two components:
+// before a step's boundary pass, the outlet face values become the densities
+// of the face pressure at the mass fraction of the neighbour inside (of the
+// node itself when that neighbour is a wall).  rho_a there is the previous
+// step's: the population sum on re-summed face nodes, the forcing density
+// elsewhere.  Reads the state (fin) and the forcing density; writes face f.
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_outlet(StepArgs a_in, int f, double* vals, double pressure, double c0,
+                                                double g21) {
+  const StepArgs a = a_in;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
+  const long long area = face_area<D>(a.g, f);
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= area) return;
+  const int ax = f >> 1;
+  const int ext = ax == 0 ? a.g.nx : (ax == 1 ? a.g.ny : a.g.nz);
+  const int fixed = (f & 1) ? ext - 1 : 0;
+  int x, y, z;
+  if (D == 2) {
+    x = ax == 0 ? fixed : (int)q;
+    y = ax == 0 ? (int)q : fixed;
+    z = 0;
+  } else if (ax == 0) {
+    x = fixed; y = (int)(q % a.g.ny); z = (int)(q / a.g.ny);
+  } else if (ax == 1) {
+    y = fixed; x = (int)(q % a.g.nx); z = (int)(q / a.g.nx);
+  } else {
+    z = fixed; x = (int)(q % a.g.nx); y = (int)(q / a.g.nx);
+  }
+  const unsigned c = (unsigned)x + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  if (__ldg(a.mask + c) != 0) return;
+  int nb[3] = {x, y, z};
+  nb[ax] += (f & 1) ? -1 : 1;
+  unsigned src = c;
+  int sx = x, sy = y, sz = z;
+  if (nb[ax] >= 0 && nb[ax] < ext) {
+    const unsigned cn = (unsigned)nb[0] + (unsigned)a.g.nx * ((unsigned)nb[1] + (unsigned)a.g.ny * (unsigned)nb[2]);
+    if (__ldg(a.mask + cn) == 0) {
+      src = cn;
+      sx = nb[0]; sy = nb[1]; sz = nb[2];
+    }
+  }
+  double r[S];
+  const unsigned keep = D == 3 ? 63u : 15u;
+  if (face_bits(a.faces) & site_faces(a.g, sx, sy, sz) & keep) {
+    R fv[S][Lat<D>::Q];
+    load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), a.g.n, src, P, fv);
+#pragma unroll
+    for (int m = 0; m < S; ++m) r[m] = double(P.rho0[m]) + double(pop_sum<D, S, R>(fv, m));
+  } else {
+    R rfd[S];
+    rho_at<S>(reinterpret_cast<const RT*>(a.rho), src, rfd);
+#pragma unroll
+    for (int m = 0; m < S; ++m) r[m] = double(P.rho0[m]) + double(rfd[m]);
+  }
+  double tot = 0.0;
+#pragma unroll
+  for (int m = 0; m < S; ++m) tot = tot + r[m];
+  double out[2] = {0.0, 0.0};
+  density_from_pressure(S, c0, g21, pressure, r[0] / tot, out);
+  vals[q] = out[0];
+  if (S > 1) vals[area + q] = out[1];
 }
 
 // -------------------------------------------------------------------- init

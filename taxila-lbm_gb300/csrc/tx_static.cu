@@ -91,6 +91,8 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   if (rc) return static_fail(rc, why);
   if (p->precision != TX_PREC_F64) return static_fail(TX_ERR_ARG, "tx_step_static runs the FP64 form only");
   if (p->nspecies != 0) return static_fail(TX_ERR_ARG, "tx_step_static runs the flow only (nspecies must be 0)");
+  if (!faces_plain(*p, p->discretization == TX_D3Q19 ? 3 : 2))
+    return static_fail(TX_ERR_ARG, "tx_step_static runs periodic, closed and density faces only");
   KernelSet ks{};
   if (!select_kernels(p, &ks)) return static_fail(TX_ERR_ARG, "no kernel built for this parameter combination");
 
@@ -187,11 +189,11 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
       k_links<2><<<l.grid, l.block, 0, st>>>(mask, g, links);
   }
   Faces faces{};
+  setup_faces(*p, D, &faces);
   for (int f = 0; f < 2 * D; ++f) {
     if (!area[f]) continue;
     double* v = (double*)(base + o_face[f]);
-    for (int m = 0; m < S; ++m) k_static_fill<<<grid_for(area[f], 256), 256, 0, st>>>(v + (long long)m * area[f], area[f], p->bc_density[f][m]);
-    faces.on[f] = 1;
+    for (int m = 0; m < S; ++m) k_static_fill<<<grid_for(area[f], 256), 256, 0, st>>>(v + (long long)m * area[f], area[f], p->bc_data[f][m]);
     faces.vals[f] = v;
   }
   TX_SCHK(cudaGetLastError());

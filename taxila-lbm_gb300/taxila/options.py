@@ -1,13 +1,13 @@
 """The reference's input deck (a PETSc options file) mapped onto tx_params.
 
 Mirrors OptionsSetUp (lbm_options.F90:163-365), FlowSetFromOptions
-(lbm_flow.F90:188-284), FlowParseBC (lbm_flow.F90:1031-1309) for periodic and
-density faces, ComponentSetFromOptions (lbm_component.F90:131-176),
-RelaxationSetFromOptions (lbm_relaxation.F90:117-151), MineralSetFromOptions
-(lbm_mineral.F90:103-134), GridSetFromOptions/InfoSetFromOptions
-(lbm_grid.F90:97-132, lbm_info.F90:116-238) and FlowSetPhysicalScales
-(lbm_flow.F90:295-376) and EOSSetFromOptions (lbm_eos.F90:90-300).  Option names and defaults are the reference's, so an
-unchanged deck drives this library.
+(lbm_flow.F90:188-284), FlowParseBC (lbm_flow.F90:1031-1309),
+ComponentSetFromOptions (lbm_component.F90:131-176), RelaxationSetFromOptions
+(lbm_relaxation.F90:117-151), MineralSetFromOptions (lbm_mineral.F90:103-134),
+GridSetFromOptions/InfoSetFromOptions (lbm_grid.F90:97-132,
+lbm_info.F90:116-238), FlowSetPhysicalScales (lbm_flow.F90:295-376) and
+EOSSetFromOptions (lbm_eos.F90:90-300).  Option names and defaults are the
+reference's, so an unchanged deck drives this library.
 """
 import struct
 from dataclasses import dataclass, field
@@ -37,6 +37,79 @@ def parse_deck_text(text):
 def _f32(v):
     """A Fortran default-kind real literal: the value rounded to single precision."""
     return struct.unpack("f", struct.pack("f", v))[0]
+
+
+def _parse_face_bc(p, f, fname, s, nd, names, has, get):
+    """FlowParseBC (lbm_flow.F90:1031-1309) for one face: the kind, then its
+    values in flow%bc_data(:, face) order; -1 where the deck gives none (0
+    for -bc_flux).  A second kind on one face is an error, as in the
+    reference; a periodic axis takes no other kind here."""
+    nbcs = s * nd
+    done = p.bc_flags[f] == P.BC_PERIODIC
+
+    def on(name):
+        return has(name) and _bool(get(name))
+
+    def claim(kind, fill):
+        nonlocal done
+        if done:
+            raise DeckError("Multiple BCs provided for boundary " + fname)
+        done = True
+        p.bc_flags[f] = kind
+        for k in range(nbcs):
+            p.bc_data[f][k] = fill
+
+    def real(key, k):
+        if has(key):
+            p.bc_data[f][k] = float(get(key))
+
+    def reals(key, k0):
+        if has(key):
+            vals = _reals(get(key))
+            if len(vals) != nd:
+                raise DeckError("%s was provided the wrong number of components." % key)
+            for d, v in enumerate(vals):
+                p.bc_data[f][k0 + d] = v
+
+    if on("bc_reflecting_" + fname):
+        claim(P.BC_REFLECTING, 0.0)
+    if on("bc_density_" + fname):
+        claim(P.BC_DENSITY, -1.0)
+        for m in range(s):
+            real(("bc_density_%s_value" % fname) if s == 1 else ("bc_density_%s_%s" % (fname, names[m])), m)
+    if s == 1:
+        if on("bc_pressure_" + fname):
+            claim(P.BC_PRESSURE, -1.0)
+            real("bc_pressure_%s_value" % fname, 0)
+        if on("bc_flux_" + fname):
+            claim(P.BC_FLUX, 0.0)
+            real("bc_flux_%s_value" % fname, 0)
+    if on("bc_pressure_inlet_" + fname):
+        claim(P.BC_PRESSURE_INLET, -1.0)
+        real("bc_pressure_%s_value" % fname, 0)
+        if s > 1:
+            real("bc_rho1_fraction_%s_value" % fname, 1)
+    if on("bc_pressure_outlet_" + fname):
+        claim(P.BC_PRESSURE_OUTLET, -1.0)
+        real("bc_pressure_%s_value" % fname, 0)
+    if on("bc_momentum_" + fname):
+        claim(P.BC_MOMENTUM, -1.0)
+        if s == 1:
+            reals("bc_momentum_%s_value" % fname, 0)
+        else:
+            for m in range(s):
+                reals("bc_momentum_%s_%s" % (fname, names[m]), m * nd)
+    if on("bc_flux_inlet_" + fname):
+        claim(P.BC_FLUX_INLET, -1.0)
+        real("bc_flux_inlet_%s_value" % fname, 0)
+        if s > 1:
+            real("bc_rho1_fraction_%s_value" % fname, 1)
+    if on("bc_flux_outlet_" + fname):
+        claim(P.BC_FLUX_OUTLET, -1.0)
+        real("bc_flux_outlet_%s_value" % fname, 0)
+    if on("bc_velocity_" + fname):
+        claim(P.BC_VELOCITY, -1.0)
+        reals("bc_velocity_%s_values" % fname, 0)
 
 
 def _bool(v):
@@ -199,19 +272,9 @@ def params_from_options(opts):
         for d in range(min(nd, len(g))):
             p.gvt[d] = g[d]
 
-    # boundary conditions (lbm_flow.F90:1031-1309): periodic and density
+    # boundary conditions (FlowParseBC, lbm_flow.F90:1031-1309)
     for f, fname in enumerate(P.FACE_NAMES[: 2 * nd]):
-        if has("bc_density_" + fname) and _bool(get("bc_density_" + fname)):
-            if p.bc_flags[f] == P.BC_PERIODIC:
-                raise DeckError("Multiple BCs provided for boundary " + fname)
-            p.bc_flags[f] = P.BC_DENSITY
-            for m in range(s):
-                key = ("bc_density_%s_value" % fname) if s == 1 else ("bc_density_%s_%s" % (fname, names[m]))
-                p.bc_density[f][m] = float(get(key, -1.0))
-        for other in ("reflecting", "pressure", "pressure_inlet", "pressure_outlet", "flux",
-                      "flux_inlet", "flux_outlet", "momentum", "velocity"):
-            if has("bc_%s_%s" % (other, fname)) and _bool(get("bc_%s_%s" % (other, fname))):
-                raise DeckError("-bc_%s_%s: only periodic and density faces are on this path" % (other, fname))
+        _parse_face_bc(p, f, fname, s, nd, names, has, get)
 
     _physical_scales(p, viscosity, density)
 

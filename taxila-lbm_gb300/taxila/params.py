@@ -10,7 +10,16 @@ SRT = 0
 MRT = 1
 BC_NULL = 0
 BC_PERIODIC = 1
+BC_REFLECTING = 2
+BC_VELOCITY = 5
 BC_DENSITY = 6
+BC_MOMENTUM = 7
+BC_PRESSURE = 8
+BC_PRESSURE_INLET = 9
+BC_PRESSURE_OUTLET = 10
+BC_FLUX = 11
+BC_FLUX_INLET = 12
+BC_FLUX_OUTLET = 13
 XM, XP, YM, YP, ZM, ZP = 1, 2, 3, 4, 5, 6
 FACE_NAMES = ("xm", "xp", "ym", "yp", "zm", "zp")
 PREC_F64, PREC_F32, PREC_F32_F16 = 0, 1, 2
@@ -37,7 +46,7 @@ class TxParams(C.Structure):
         ("s_q", _D * MAXC), ("s_nu", _D * MAXC), ("s_pi", _D * MAXC), ("s_m", _D * MAXC),
         ("mm", _D * MAXC), ("g", (_D * MAXC) * MAXC), ("gw", (_D * MAXC) * MAXMIN),
         ("body_forces", _I), ("gvt", _D * 3),
-        ("bc_density", (_D * MAXC) * 6),
+        ("bc_data", (_D * (3 * MAXC)) * 6),
         ("literal_kind", _I), ("precision", _I), ("exact", _I), ("rho0", _D * MAXC), ("storage_scale", _D),
         ("use_nonideal_eos", _I), ("eos", _I * MAXC), ("eos_coef", (_D * 4) * MAXC),
         ("nspecies", _I), ("species_relaxation_mode", _I), ("species_tau", _D * MAXC),

@@ -143,8 +143,8 @@ def drain_request(rid, arrival, sides, seed, steps, dims=3):
     p.gw[1][0], p.gw[1][1] = -0.03, 0.03
     p.bc_flags[2 * axis] = P.BC_DENSITY
     p.bc_flags[2 * axis + 1] = P.BC_DENSITY
-    p.bc_density[2 * axis][0], p.bc_density[2 * axis][1] = 1.05, 0.03
-    p.bc_density[2 * axis + 1][0], p.bc_density[2 * axis + 1][1] = 0.03, 0.95
+    p.bc_data[2 * axis][0], p.bc_data[2 * axis][1] = 1.05, 0.03
+    p.bc_data[2 * axis + 1][0], p.bc_data[2 * axis + 1][1] = 0.03, 0.95
     rmin, rmax = max(2.0, min(sides) / 12.0), max(3.0, min(sides) / 6.0)
     if dims == 3:
         solid = problems.sphere_pack(shape, 0.35, rmin, rmax, seed, periodic=False)
@@ -307,7 +307,9 @@ class Server:
                             if q.discretization == P.D3Q19 else 0.0
                     b.remove(lid)
                     del active[(key, lid)]
-                    results.append(Result(req.rid, req.kind, q.nsites, int(pr.steps), req.arrival, admitted, now(),
+                    # without real-time arrivals every request is queued at t = 0
+                    results.append(Result(req.rid, req.kind, q.nsites, int(pr.steps),
+                                          req.arrival if realtime else 0.0, admitted, now(),
                                           float(value), float(front), tracer))
         return results
 

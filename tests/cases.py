@@ -78,9 +78,9 @@ def porous_case(disc, shape, mode=P.SRT, iso=4, seed=3, dirichlet=True, body=Fal
         a = 2 if disc == P.D3Q19 else 1
         p.bc_flags[2 * a] = P.BC_DENSITY
         p.bc_flags[2 * a + 1] = P.BC_DENSITY
-        p.bc_density[2 * a][0], p.bc_density[2 * a + 1][0] = 1.03, 0.97
+        p.bc_data[2 * a][0], p.bc_data[2 * a + 1][0] = 1.03, 0.97
         if s == 2:
-            p.bc_density[2 * a][1], p.bc_density[2 * a + 1][1] = 0.07, 0.05
+            p.bc_data[2 * a][1], p.bc_data[2 * a + 1][1] = 0.07, 0.05
     if body:
         p.body_forces = 1
         p.gvt[0], p.gvt[1] = 1e-5, -2e-5
@@ -102,6 +102,99 @@ PARITY = [
     ("d3_porous_periodic_iso8", lambda: porous_case(P.D3Q19, (12, 12, 12), iso=8, dirichlet=False), 15),
     ("d2_porous_dirichlet", lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), 30),
     ("d3_single_component_porous", lambda: porous_case(P.D3Q19, (10, 12, 14), ncomp=1, body=True), 20),
+]
+
+
+def bc_case(disc, shape, faces, ncomp=1, mode=P.SRT, iso=4, periodic=(0, 0, 0), seed=5, body=False,
+            porosity=0.8, rho_init=(1.0, 0.05), g12=0.0, eos=None):
+    """A channel with exterior BCs: ``faces`` maps face index (0..5) to
+    (kind, bc_data values); a sparse seeded sphere pack with two minerals
+    (some grains cut by the faces), fluid-solid adhesion, optional body force
+    and component coupling.  The initial density is rho_init per component
+    with 1% noise."""
+    p = base(disc, shape, ncomp=ncomp, mode=mode, iso=iso, periodic=periodic)
+    p.nminerals = 2
+    p.tau[0], p.tau[1] = 1.0, 0.9
+    if mode == P.MRT:
+        p.s_nu[0], p.s_nu[1] = 1.0, 1.0 / 0.9
+        p.s_e[0], p.s_q[1] = 1.2, 1.1
+    if ncomp == 2:
+        p.g[0][1] = p.g[1][0] = g12
+        p.gw[0][0], p.gw[0][1] = 0.1, -0.1
+        p.gw[1][0], p.gw[1][1] = -0.1, 0.1
+    else:
+        p.gw[0][0], p.gw[1][0] = 0.05, -0.05
+    for f, (kind, vals) in faces.items():
+        p.bc_flags[f] = kind
+        for k, v in enumerate(vals):
+            p.bc_data[f][k] = v
+    if body:
+        p.body_forces = 1
+        p.gvt[0], p.gvt[1] = 2e-6, -1e-6
+        if disc == P.D3Q19:
+            p.gvt[2] = 3e-6
+    if eos is not None:
+        p.use_nonideal_eos = 1
+        for m in range(ncomp):
+            p.eos[m] = eos[0]
+            for k, v in enumerate(eos[1]):
+                p.eos_coef[m][k] = v
+    z, y, x = p.shape
+    solid = problems.sphere_pack((z, y, x), porosity, 1.0, 2.0, seed, periodic=True)
+    walls = problems.mineral_walls(solid, seed)
+    rng = np.random.default_rng(seed)
+    rho = np.empty((p.nsites, ncomp))
+    for m in range(ncomp):
+        rho[:, m] = rho_init[m] * (1.0 + 0.01 * rng.standard_normal(p.nsites))
+    return p, walls, rho.ravel()
+
+
+# (name, case factory, steps): exterior boundary conditions.  Face index:
+# 0 XM, 1 XP, 2 YM, 3 YP, 4 ZM, 5 ZP.
+BCS = [
+    # one component: pressure inlet, pressure outlet (its value is the density itself)
+    ("d3_pressure_s1", lambda: bc_case(P.D3Q19, (12, 8, 10), {4: (P.BC_PRESSURE, (0.345,)),
+                                                                5: (P.BC_PRESSURE_OUTLET, (0.99,))},
+                                        periodic=(1, 1, 0), body=True), 20),
+    # flux inlet, velocity outlet, a reflecting and a closed side; MRT
+    ("d3_flux_velocity_mrt", lambda: bc_case(P.D3Q19, (12, 10, 8), {2: (P.BC_REFLECTING, ()),
+                                                                     4: (P.BC_FLUX, (0.002,)),
+                                                                     5: (P.BC_VELOCITY, (0.0, 0.0, 0.0021))},
+                                              mode=P.MRT, periodic=(1, 0, 0)), 20),
+    # reflecting x faces (XM with the reference's z comparison), momentum and flux outlet on y
+    ("d3_reflect_momentum", lambda: bc_case(P.D3Q19, (8, 12, 10), {0: (P.BC_REFLECTING, ()),
+                                                                    1: (P.BC_REFLECTING, ()),
+                                                                    2: (P.BC_MOMENTUM, (0.0, 0.0015, 0.0002)),
+                                                                    3: (P.BC_FLUX_OUTLET, (0.0015,))},
+                                             periodic=(0, 0, 1), body=True), 20),
+    # Neumann class before Dirichlet at the shared edge (BCApply's order of first appearance)
+    ("d3_neumann_then_dirichlet", lambda: bc_case(P.D3Q19, (8, 10, 10), {0: (P.BC_FLUX, (0.001,)),
+                                                                          2: (P.BC_DENSITY, (1.01,)),
+                                                                          3: (P.BC_PRESSURE, (0.33,))},
+                                                   periodic=(0, 0, 1)), 20),
+    # two components: pressure inlet with a mass fraction, pressure outlet refreshed every step
+    ("d3_two_phase_pressure", lambda: bc_case(P.D3Q19, (12, 8, 8), {4: (P.BC_PRESSURE_INLET, (0.35, 0.95)),
+                                                                     5: (P.BC_PRESSURE_OUTLET, (0.33,))},
+                                               ncomp=2, g12=0.1, rho_init=(0.9, 0.05), periodic=(1, 0, 0)), 20),
+    # two components: flux inlet, per-component momentum outlet, density and velocity sides; MRT iso 8
+    ("d3_two_phase_flux_mrt_iso8", lambda: bc_case(P.D3Q19, (12, 10, 8), {
+        2: (P.BC_DENSITY, (0.92, 0.05)), 3: (P.BC_VELOCITY, (0.0, 0.0, 0.0)),
+        4: (P.BC_FLUX_INLET, (0.003, 0.9)), 5: (P.BC_MOMENTUM, (0.0, 0.0, 0.0027, 0.0, 0.0, 0.0003))},
+        ncomp=2, mode=P.MRT, iso=8, g12=0.1, rho_init=(0.9, 0.05), periodic=(1, 0, 0)), 15),
+    # 2D: velocity inlet, pressure outlet, reflecting y faces
+    ("d2_velocity_outlet", lambda: bc_case(P.D2Q9, (1, 20, 28), {0: (P.BC_VELOCITY, (0.004, 0.0)),
+                                                                  1: (P.BC_PRESSURE_OUTLET, (1.0,)),
+                                                                  2: (P.BC_REFLECTING, ()),
+                                                                  3: (P.BC_REFLECTING, ())}, body=True), 30),
+    # 2D two components: pressure inlet / outlet on y, MRT iso 10
+    ("d2_two_phase_pressure_iso10", lambda: bc_case(P.D2Q9, (1, 30, 24), {
+        2: (P.BC_PRESSURE_INLET, (0.35, 0.9)), 3: (P.BC_PRESSURE_OUTLET, (0.34,))},
+        ncomp=2, mode=P.MRT, iso=10, g12=0.1, rho_init=(0.9, 0.05), periodic=(1, 0, 0)), 30),
+    # 2D two components with a Shan-Chen EOS: momentum inlet, flux outlet, flux inlet sides
+    ("d2_momentum_flux_eos", lambda: bc_case(P.D2Q9, (1, 24, 26), {
+        0: (P.BC_MOMENTUM, (0.002, 0.0, 0.0002, 0.0)), 1: (P.BC_FLUX_OUTLET, (0.0022,)),
+        2: (P.BC_FLUX_INLET, (0.0, 0.5))},
+        ncomp=2, g12=0.1, rho_init=(0.9, 0.05), eos=(P.EOS_SC, (1.0,))), 30),
 ]
 
 

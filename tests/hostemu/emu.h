@@ -97,16 +97,16 @@ std::string run(const Case& c, Result& out) {
   std::vector<RT> psi(p.use_nonideal_eos ? (size_t)N * S : 0, RT(0));
   std::vector<double> facevals[6];
   Faces faces{};
+  setup_faces(p, D, &faces);
+  const FaceShell shell = face_shell(p, D, g.nx, g.ny, g.nz);
   for (int f = 0; f < 2 * D; ++f) {
-    if (p.bc_flags[f] != TX_BC_DENSITY) continue;
-    const int a = f / 2;
-    const long long area = D == 2 ? (a == 0 ? g.ny : g.nx)
-                                  : (a == 0 ? (long long)g.ny * g.nz : a == 1 ? (long long)g.nx * g.nz
-                                                                              : (long long)g.nx * g.ny);
-    facevals[f].resize((size_t)area * S);
-    for (int m = 0; m < S; ++m)
-      for (long long q = 0; q < area; ++q) facevals[f][(size_t)(m * area + q)] = p.bc_density[f][m];
-    faces.on[f] = 1;
+    if (!face_has_values(p, D, f)) continue;
+    const long long area = face_area_of(D, g.nx, g.ny, g.nz, f);
+    double nv[3 * TX_MAX_COMPONENTS];
+    face_node_values(p, D, f, ph.c0, nv);
+    facevals[f].resize((size_t)area * S * D);
+    for (int k = 0; k < S * D; ++k)
+      for (long long q = 0; q < area; ++q) facevals[f][(size_t)(k * area + q)] = nv[k];
     faces.vals[f] = facevals[f].data();
   }
 
@@ -178,8 +178,15 @@ std::string run(const Case& c, Result& out) {
   }
   for (int t = 0; t < c.nsteps; ++t) {
     const StepArgs a = args(cur, 1 - cur);
+    if (has_outlet_update(p, D))
+      for (int f = 0; f < 2 * D; ++f)
+        if (p.bc_flags[f] == TX_BC_PRESSURE_OUTLET)
+          launch1(face_area_of(D, g.nx, g.ny, g.nz, f), 128, [&] {
+            k_outlet<D, S, T, R, RT>(a, f, facevals[f].data(), p.bc_data[f][0], ph.c0, p.g[1][0]);
+          });
     launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     launch3(g, 256, [&] { k_density<D, S, T, R, RT>(a, 0); });
+    if (faces.post) launch1(shell.start[shell.nf], 128, [&] { k_faces<D, S, ISO, EXACT, T, R, RT>(a, shell); });
     cur = 1 - cur;
     ++step;
     if (NS) {

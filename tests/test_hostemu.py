@@ -191,3 +191,15 @@ def test_emulated_eos_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
     q.exact = 1 if exact else 0
     got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
     compare(ref, got, p, walls, 0.0 if exact else 1e-12)
+
+
+@pytest.mark.parametrize("name,make,steps", cases.BCS, ids=[c[0] for c in cases.BCS])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_emulated_exterior_bcs_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
+    # pressure, flux, momentum, velocity and reflecting faces, outlets, BCApply's class order
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    compare(ref, got, p, walls, 0.0 if exact else 1e-12)

@@ -70,7 +70,7 @@ def test_density_faces_and_minerals():
 """
     p, _ = O.params_from_options(O.parse_deck_text(deck))
     assert p.bc_flags[4] == P.BC_DENSITY and p.bc_flags[5] == P.BC_DENSITY and p.bc_flags[0] == P.BC_NULL
-    assert p.bc_density[4][0] == 2.1 and p.bc_density[5][1] == 0.06
+    assert p.bc_data[4][0] == 2.1 and p.bc_data[5][1] == 0.06
     assert p.gw[0][0] == 0.3 and p.gw[1][1] == -0.3 and p.gw[0][1] == 0.0
     assert p.body_forces == 1 and p.gvt[2] == 1e-6
 
@@ -81,10 +81,55 @@ def test_conflicting_bcs_rejected():
         O.params_from_options(O.parse_deck_text(deck))
 
 
-def test_unsupported_bc_rejected():
-    deck = "-NX 4\n-NY 4\n-NZ 4\n-bc_velocity_zm\n"
+def test_exterior_bcs_parsed():
+    deck = """
+-NX 4
+-NY 4
+-NZ 6
+-bc_periodic_x
+-bc_velocity_ym
+-bc_velocity_ym_values 0.0,0.01,0.0
+-bc_reflecting_yp
+-bc_pressure_zm
+-bc_pressure_zm_value 0.34
+-bc_flux_outlet_zp
+-bc_flux_outlet_zp_value 0.002
+"""
+    p, _ = O.params_from_options(O.parse_deck_text(deck))
+    assert list(p.bc_flags) == [P.BC_PERIODIC, P.BC_PERIODIC, P.BC_VELOCITY, P.BC_REFLECTING,
+                                P.BC_PRESSURE, P.BC_FLUX_OUTLET]
+    assert list(p.bc_data[2][:3]) == [0.0, 0.01, 0.0]
+    assert p.bc_data[4][0] == 0.34 and p.bc_data[4][1] == -1.0
+    assert p.bc_data[5][0] == 0.002
+    # velocity with the wrong number of components, two kinds on one face
     with pytest.raises(O.DeckError):
-        O.params_from_options(O.parse_deck_text(deck))
+        O.params_from_options(O.parse_deck_text(deck.replace("0.0,0.01,0.0", "0.0,0.01")))
+    with pytest.raises(O.DeckError):
+        O.params_from_options(O.parse_deck_text(deck + "-bc_density_zm\n"))
+
+
+def test_two_component_exterior_bcs():
+    deck = """
+-NX 4
+-NY 4
+-NZ 6
+-ncomponents 2
+-bc_pressure_inlet_zm
+-bc_pressure_zm_value 0.35
+-bc_rho1_fraction_zm_value 0.9
+-bc_momentum_zp
+-bc_momentum_zp_component1 0.0,0.0,-0.01
+-bc_momentum_zp_component2 0.0,0.0,-0.002
+-bc_flux_inlet_xm
+-bc_flux_inlet_xm_value 0.01
+"""
+    p, _ = O.params_from_options(O.parse_deck_text(deck))
+    assert p.bc_flags[4] == P.BC_PRESSURE_INLET and list(p.bc_data[4][:2]) == [0.35, 0.9]
+    assert p.bc_flags[5] == P.BC_MOMENTUM and list(p.bc_data[5][:6]) == [0.0, 0.0, -0.01, 0.0, 0.0, -0.002]
+    assert p.bc_flags[0] == P.BC_FLUX_INLET and p.bc_data[0][0] == 0.01 and p.bc_data[0][1] == -1.0
+    # -bc_pressure / -bc_flux are read for one component only
+    p2, _ = O.params_from_options(O.parse_deck_text(deck + "-bc_pressure_ym\n"))
+    assert p2.bc_flags[2] == P.BC_NULL
 
 
 def test_viscosity_consistency():
