@@ -199,7 +199,15 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
     P.cA[m][0] = (D == 3 ? 2.0 / 3.0 : 5.0 / 9.0) * rel * P.rho0[m];
     P.cA[m][1] = -(D == 3 ? 1.0 / 18.0 : 1.0 / 9.0) * rel * P.rho0[m];
     P.cA[m][2] = -(1.0 / 36.0) * rel * P.rho0[m];
+    P.WAc[m][0] = P.A0[m];
+    P.WAc[m][1] = (D == 3 ? Lat<3>::w(1) : Lat<2>::w(1)) * P.An[m];
+    P.WAc[m][2] = (D == 3 ? Lat<3>::w(18) : Lat<2>::w(8)) * P.An[m];
+    P.keep[m] = 1.0 - P.s0[m];
+    P.kfac[m] = 3.0 - 1.5 * P.s0[m];
+    for (int k = 0; k < S; ++k) P.c0g[m][k] = P.c0 * P.g[m][k];
   }
+  for (int d = 0; d < D; ++d)
+    for (int w = 0; w < 12; ++w) P.ffwq[d][w] = P.ffw[w] * P.inv_ws_full[d];
   P.inv_sscale = 1.0 / P.sscale;
 }
 

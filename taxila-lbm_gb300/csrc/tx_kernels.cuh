@@ -90,6 +90,11 @@ struct PhysT {
   R dspec[MAXC][19];
   R inv_ws_full[3];        // 1 / weight sum of a gradient stencil with every neighbour pore
   unsigned spec_mask[MAXC];
+  // fast-form constants folded on the host: W~A per direction class (rest,
+  // axis, diagonal), 1 - s0, 3 - 1.5 s0, c0 g[m][k], ffw[w] / ws_full[d]
+  R WAc[MAXC][3], keep[MAXC], kfac[MAXC];
+  R c0g[MAXC][MAXC];
+  R ffwq[3][12];
   int ff_on, fs_on, body_on;
 };
 using Phys = PhysT<double>;
@@ -112,6 +117,8 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   b->inv_sscale = R(a.inv_sscale);
   cp(a.s0, b->s0, MAXC); cp(&a.dspec[0][0], &b->dspec[0][0], MAXC * 19); cp(a.inv_ws_full, b->inv_ws_full, 3);
   for (int m = 0; m < MAXC; ++m) b->spec_mask[m] = a.spec_mask[m];
+  cp(&a.WAc[0][0], &b->WAc[0][0], MAXC * 3); cp(a.keep, b->keep, MAXC); cp(a.kfac, b->kfac, MAXC);
+  cp(&a.c0g[0][0], &b->c0g[0][0], MAXC * MAXC); cp(&a.ffwq[0][0], &b->ffwq[0][0], 36);
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
 }
 
@@ -436,6 +443,26 @@ __host__ __device__ constexpr FFTerm ffterm(int t) {
   return D == 3 ? ff_d3(t) : ff_d2(t);
 }
 
+// the stencil term with the opposite offset, weight and level (-1: none)
+template <int D>
+__host__ __device__ constexpr int ff_opp(int t) {
+  const FFTerm a = ffterm<D>(t);
+  const int nt = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  for (int u = 0; u < nt; ++u) {
+    const FFTerm b = ffterm<D>(u);
+    if (b.e[0] == -a.e[0] && b.e[1] == -a.e[1] && b.e[2] == -a.e[2] && b.w == a.w && b.level == a.level) return u;
+  }
+  return -1;
+}
+
+template <int D, int ISO>
+__host__ __device__ constexpr bool stencil_symmetric() {
+  const int nt = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  for (int t = 0; t < nt; ++t)
+    if (ffterm<D>(t).level <= ISO && ff_opp<D>(t) < 0) return false;
+  return true;
+}
+
 // Reach of the isotropy-ISO gradient stencil (at least one lattice link).
 template <int D, int ISO>
 __host__ __device__ constexpr int stencil_reach() {
@@ -539,7 +566,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
 #pragma unroll
   for (int m = 0; m < S; ++m)
 #pragma unroll
-    for (int d = 0; d < D; ++d) F[m][d] = R(0);
+    for (int d = 0; d < D; ++d) F[m][d] = EXACT ? R(0) : R(-0.0);
 
   // only links that end on a wall can carry a fluid-solid force
   const uint32_t walled = ~links & all_links<D>();
@@ -591,42 +618,46 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
     // every stencil neighbour pore: the weight sums are constant and the
     // psi(x) terms cancel, so grad = sum_k w_k e_k psi(x + e_k)
     if ((links | 1u) == (all_links<D>() | 1u)) {
+      // opposite stencil terms pair up: w e (psi(x + e) - psi(x - e))
+      static_assert(stencil_symmetric<D, ISO>(), "every stencil term needs its opposite");
       R gr[S][D];
 #pragma unroll
       for (int d = 0; d < D; ++d)
 #pragma unroll
-        for (int m = 0; m < S; ++m) gr[m][d] = R(0);
+        for (int m = 0; m < S; ++m) gr[m][d] = R(-0.0);
       constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
       sfor<0, NT>([&](auto tt) {
-        constexpr FFTerm T = ffterm<D>(decltype(tt)::value);
-        if constexpr (T.level <= ISO) {
+        constexpr int t = decltype(tt)::value;
+        constexpr FFTerm T = ffterm<D>(t);
+        if constexpr (T.level <= ISO && t < ff_opp<D>(t)) {
           constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2], tw = T.w;
-          R v[S];
-          rho_at<S>(src, h.template at<ex, ey, ez>(), v);
+          R vp[S], vm[S];
+          rho_at<S>(src, h.template at<ex, ey, ez>(), vp);
+          rho_at<S>(src, h.template at<-ex, -ey, -ez>(), vm);
+          R dv[S];
+#pragma unroll
+          for (int m = 0; m < S; ++m) dv[m] = vp[m] - vm[m];
           sfor<0, D>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
             constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
             if constexpr (e != 0) {
-              const R coef = R(e) * P.ffw[tw];
+              const R coef = R(e) * P.ffwq[d][tw];
 #pragma unroll
-              for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * v[m];
+              for (int m = 0; m < S; ++m) gr[m][d] = gr[m][d] + coef * dv[m];
             }
           });
         }
       });
+      // F -= psi(x) c0 sum_k g_mk grad_k (the weight sum is folded into ffwq)
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
-        R q[S];
-#pragma unroll
-        for (int m = 0; m < S; ++m) q[m] = gr[m][d] * P.inv_ws_full[d];
+      for (int d = 0; d < D; ++d)
 #pragma unroll
         for (int m = 0; m < S; ++m) {
-          R acc = R(0);
+          R acc = R(-0.0);
 #pragma unroll
-          for (int k = 0; k < S; ++k) acc = acc + R(P.g[m][k]) * q[k];
-          F[m][d] = F[m][d] - R(P.c0) * mult[m] * acc;
+          for (int k = 0; k < S; ++k) acc = acc + P.c0g[m][k] * gr[k][d];
+          F[m][d] = F[m][d] - mult[m] * acc;
         }
-      }
       return;
     }
   }
@@ -714,6 +745,38 @@ __device__ __forceinline__ R pop_flux(const R fv[S][Lat<D>::Q], int m, int d0) {
     }
   });
   return acc;
+}
+
+// c_n . v over the nonzero components of c_n.  Sums start from -0.0, which
+// x + -0.0 = x for every x lets the compiler drop: the fast forms use these.
+template <int D, int n, class R>
+__device__ __forceinline__ R cdot_z(const R v[D]) {
+  R acc = R(-0.0);
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    constexpr int c = Lat<D>::c(n, d);
+    if constexpr (c > 0) acc = acc + v[d];
+    if constexpr (c < 0) acc = acc - v[d];
+  });
+  return acc;
+}
+
+// Fast-form flux of one component from pair differences f_n - f_opp(n).
+template <int D, class R>
+__device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) j[d] = R(-0.0);
+  sfor<0, npairs<D>()>([&](auto pp) {
+    constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+    const R dlt = f[n] - f[nb];
+    sfor<0, D>([&](auto dd) {
+      constexpr int d = decltype(dd)::value;
+      constexpr int c = Lat<D>::c(n, d);
+      if constexpr (c == 1) j[d] = j[d] + dlt;
+      if constexpr (c == -1) j[d] = j[d] - dlt;
+      if constexpr (c > 1 || c < -1) j[d] = j[d] + R(c) * dlt;
+    });
+  });
 }
 
 // Density of the collision (Dirichlet nodes re-summed as in BCUpdateRho,
@@ -834,14 +897,18 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     for (int m = 0; m < S; ++m) {
       R f1[1][Q];
       load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, P, f1);
+      if constexpr (EXACT) {
 #pragma unroll
-      for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
+        for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
+      } else {
+        pop_flux_pairs<D, R>(f1[0], jm[m]);
+      }
       rcd[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rfd[m];
       rc[m] = dn ? P.rho0[m] + rcd[m] : rf[m];
     }
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      R num = R(0), den = R(0);
+      R num = EXACT ? R(0) : R(-0.0), den = EXACT ? R(0) : R(-0.0);
 #pragma unroll
       for (int m = 0; m < S; ++m) num = num + (jm[m][d] + R(.5) * F[m][d]) * R(P.mmot[m]);
 #pragma unroll
@@ -852,7 +919,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         up[d] = num * (R(1) / den);
     }
   }
-  R usqr = R(0);
+  R usqr = EXACT ? R(0) : R(-0.0);
 #pragma unroll
   for (int d = 0; d < D; ++d) usqr = usqr + up[d] * up[d];
 
@@ -944,114 +1011,203 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     // with dE_n = feq_n - w_n rho0 = W~A (rho - rho0) + W~B rho + (W~A - w) rho0,
     // so that FP32 arithmetic keeps the precision of the small deviations.
     // WB_n = W~_n B_n is shared by the components.
-    R WB[Q];
+    //
+    // Directions come in pairs (n, n~ = opp(n)).  With ud = c_n.u, the velocity
+    // terms split into an even and an odd part, WB_n = WBe + Bo and
+    // WB_n~ = WBe - Bo (WBe = 4.5 w ud^2 - 1.5 w u^2, Bo = 3 w ud), and with
+    // h = c_n.kF the relaxed pair is
+    //   g'_n = keep g_n + Pe + Po,   g'_n~ = keep g_n~ + Pe - Po,
+    //   Pe = s0 De + Bo h - Ae kFu,  Po = Bo G + Ae h,  G = s0 rho - kFu,
+    // where Ae = W~A + WBe and De = W~A (rho - rho0) + WBe rho + cA (in the
+    // FP64 form Pe = Ae G + Bo h).  Moments relaxed at s_nu != s0 (the
+    // traceless second moments, even in c) correct Pe through the pair sums of
+    // the non-equilibrium part, S_p = dfi_n + dfi_n~.  Other rate patterns take
+    // the general path below.
+    constexpr int NP = npairs<D>();
     const R cu_axis = R(1.5 * L::w(1)) * usqr, cu_diag = R(1.5 * L::w(Q - 1)) * usqr;
-    sfor<0, Q>([&](auto nn) {
-      constexpr int n = decltype(nn)::value;
-      if constexpr (n == 0) {
-        WB[0] = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
-      } else {
-        R ud = R(0);
-        sfor<0, D>([&](auto dd) {
-          constexpr int d = decltype(dd)::value;
-          constexpr int c = L::c(n, d);
-          if constexpr (c > 0) ud = ud + up[d];
-          if constexpr (c < 0) ud = ud - up[d];
-        });
-        constexpr double w = L::w(n);
-        WB[n] = ud * (R(3 * w) + R(4.5 * w) * ud) - (n <= L::NAXIS ? cu_axis : cu_diag);
-      }
+    R Bo[NP], WBe[NP];
+    sfor<0, NP>([&](auto pp) {
+      constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+      constexpr double w = L::w(n);
+      const R ud = cdot_z<D, n>(up);
+      Bo[p] = R(3 * w) * ud;
+      WBe[p] = R(4.5 * w) * ud * ud - (n <= L::NAXIS ? cu_axis : cu_diag);
     });
+    const R WB0 = D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr;
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       const R r = rc[m], rd = rcd[m];
       // W~A per direction class (rest, axis, diagonal) and its offset from w
-      const R WA0 = P.A0[m], WA1 = R(L::w(1)) * P.An[m], WA2 = R(L::w(Q - 1)) * P.An[m];
+      const R WA0 = P.WAc[m][0], WA1 = P.WAc[m][1], WA2 = P.WAc[m][2];
       const R cA0 = P.cA[m][0], cA1 = P.cA[m][1], cA2 = P.cA[m][2];
       const R s0 = P.s0[m];
-      const R k = R(3) - R(1.5) * s0;
-      const R keep = R(1) - s0;
-      R Fu = R(0), kF[D];
+      const R k = P.kfac[m];
+      const R keep = P.keep[m];
+      R Fu = R(-0.0), kF[D];
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         Fu = Fu + F[m][d] * up[d];
         kF[d] = k * F[m][d];
       }
       const R kFu = k * Fu;
+      const R G = s0 * r - kFu;
       const unsigned spec = P.spec_mask[m];
       const T* fm = fin + (long long)m * Q * N;
-      auto WA_of = [&](auto nn) -> R {
-        constexpr int n = decltype(nn)::value;
-        return n == 0 ? WA0 : (n <= L::NAXIS ? WA1 : WA2);
-      };
-      auto E_of = [&](auto nn) -> R { return WA_of(nn) + WB[decltype(nn)::value]; };
-      // dE_n = feq_n - w_n rho0
-      auto dE_of = [&](auto nn) -> R {
-        constexpr int n = decltype(nn)::value;
-        if constexpr (kShifted<T>) {
-          const R cA = n == 0 ? cA0 : (n <= L::NAXIS ? cA1 : cA2);
-          return WA_of(nn) * rd + WB[n] * r + cA;
-        } else {
-          return E_of(nn) * r;
-        }
-      };
       auto pop = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
         return ld_dev<T, R>(fm + (long long)n * N + c, P);
       };
-      // sum_d c_n,d v_d
-      auto cdot = [&](auto nn, const R v[D]) -> R {
-        constexpr int n = decltype(nn)::value;
-        R acc = R(0);
-        sfor<0, D>([&](auto dd) {
-          constexpr int d = decltype(dd)::value;
-          constexpr int c = L::c(n, d);
-          if constexpr (c > 0) acc = acc + v[d];
-          if constexpr (c < 0) acc = acc - v[d];
+      const R E0 = WA0 + WB0;
+      // rest direction: g'_0 = keep g_0 + X0
+      R X0;
+      if constexpr (kShifted<T>)
+        X0 = s0 * (WA0 * rd + (WB0 * r + cA0)) - E0 * kFu;
+      else
+        X0 = E0 * G;
+      // the even and odd parts of pair p
+      auto pair_terms = [&](auto pp, R& pe, R& po) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+        const R WA = n <= L::NAXIS ? WA1 : WA2;
+        const R Ae = WA + WBe[p];
+        const R h = cdot_z<D, n>(kF);
+        if constexpr (kShifted<T>) {
+          const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+          pe = s0 * De + (Bo[p] * h - Ae * kFu);
+        } else {
+          pe = Ae * G + Bo[p] * h;
+        }
+        po = Bo[p] * G + Ae * h;
+      };
+      if (spec == 0u && keep == R(0)) {
+        // s0 = 1 (tau = 1): the relaxed populations are the forced equilibrium
+        push(std::integral_constant<int, 0>{}, m, X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+          R pe, po;
+          pair_terms(pp, pe, po);
+          push(std::integral_constant<int, n>{}, m, pe + po);
+          push(std::integral_constant<int, nb>{}, m, pe - po);
         });
-        return acc;
-      };
-      const R G = s0 * r - kFu;
-      auto relax = [&](auto nn, R g) -> R {
-        if constexpr (kShifted<T>)
-          return keep * g + s0 * dE_of(nn) + E_of(nn) * (cdot(nn, kF) - kFu);
-        else
-          return keep * g + E_of(nn) * (G + cdot(nn, kF));
-      };
-      if (spec == 0u) {
-        // every moment relaxes at s0 (BGK): one direction at a time
-        sfor<0, Q>([&](auto nn) { push(nn, m, relax(nn, pop(nn))); });
+      } else if (spec == 0u) {
+        // every moment relaxes at s0 (BGK): one pair at a time
+        push(std::integral_constant<int, 0>{}, m, keep * pop(std::integral_constant<int, 0>{}) + X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+          R pe, po;
+          pair_terms(pp, pe, po);
+          push(std::integral_constant<int, n>{}, m, keep * pop(std::integral_constant<int, n>{}) + (pe + po));
+          push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + (pe - po));
+        });
+      } else if (spec == stress_mask<D>()) {
+        // s_nu != s0, every other rate s0
+        R g[Q], Pe[NP], Po[NP], Sp[NP];
+        sfor<0, Q>([&](auto nn) { g[decltype(nn)::value] = pop(nn); });
+        R F3[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) F3[d] = R(3) * F[m][d];
+        const R hFu2 = R(3) * Fu;
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          pair_terms(pp, Pe[p], Po[p]);
+          // S_p = g_n + g_n~ - 2 De - Ae (3 F.u) + Bo c_n.(3 F)
+          const R WA = n <= L::NAXIS ? WA1 : WA2;
+          const R Ae = WA + WBe[p];
+          const R t2 = cdot_z<D, n>(F3);
+          const R gs = g[n] + g[nb];
+          if constexpr (kShifted<T>) {
+            const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+            Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
+          } else {
+            Sp[p] = gs - Ae * (R(2) * r + hFu2) + Bo[p] * t2;
+          }
+        });
+        sfor<0, Q>([&](auto kk) {
+          constexpr int kq = decltype(kk)::value;
+          if constexpr (rate_of<D>(kq) == R_NU) {
+            R md = R(-0.0);
+            sfor<0, NP>([&](auto pp) {
+              constexpr int p = decltype(pp)::value;
+              constexpr int v = L::mt(pair_n<D>(p), kq);
+              if constexpr (v == 1) md = md + Sp[p];
+              else if constexpr (v == -1) md = md - Sp[p];
+              else if constexpr (v != 0) md = md + R(v) * Sp[p];
+            });
+            const R ck = P.dspec[m][kq] * md;
+            sfor<0, NP>([&](auto pp) {
+              constexpr int p = decltype(pp)::value;
+              constexpr int v = L::mt(pair_n<D>(p), kq);
+              if constexpr (v == 1) Pe[p] = Pe[p] - ck;
+              else if constexpr (v == -1) Pe[p] = Pe[p] + ck;
+              else if constexpr (v != 0) Pe[p] = Pe[p] - R(v) * ck;
+            });
+          }
+        });
+        if (keep == R(0)) {
+          push(std::integral_constant<int, 0>{}, m, X0);
+          sfor<0, NP>([&](auto pp) {
+            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+            push(std::integral_constant<int, n>{}, m, Pe[p] + Po[p]);
+            push(std::integral_constant<int, nb>{}, m, Pe[p] - Po[p]);
+          });
+        } else {
+          push(std::integral_constant<int, 0>{}, m, keep * g[0] + X0);
+          sfor<0, NP>([&](auto pp) {
+            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+            push(std::integral_constant<int, n>{}, m, keep * g[n] + (Pe[p] + Po[p]));
+            push(std::integral_constant<int, nb>{}, m, keep * g[nb] + (Pe[p] - Po[p]));
+          });
+        }
       } else {
-        // deviation from the forced equilibrium: g - dE_n + 1.5 E_n (F.c_n - F.u)
+        // general rate pattern: relax every moment at s0, then correct each
+        // moment k whose rate differs by dspec_k times its projection of the
+        // deviation from the forced equilibrium, g - dE_n + 1.5 E_n (F.c_n - F.u)
+        R fo[Q], dfi[Q];
+        fo[0] = keep * pop(std::integral_constant<int, 0>{}) + X0;
+        const R hFu = R(1.5) * Fu;
         R hF[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
-        const R hFu = R(1.5) * Fu;
-        R fo[Q], dfi[Q];
-        sfor<0, Q>([&](auto nn) {
-          constexpr int n = decltype(nn)::value;
-          const R g = pop(nn);
-          fo[n] = relax(nn, g);
+        {
+          const R g0 = pop(std::integral_constant<int, 0>{});
           if constexpr (kShifted<T>)
-            dfi[n] = g - dE_of(nn) + E_of(nn) * (cdot(nn, hF) - hFu);
+            dfi[0] = g0 - (WA0 * rd + (WB0 * r + cA0)) - E0 * hFu;
           else
-            dfi[n] = g - E_of(nn) * (r + hFu - cdot(nn, hF));
+            dfi[0] = g0 - E0 * (r + hFu);
+        }
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          R pe, po;
+          pair_terms(pp, pe, po);
+          const R gn = pop(std::integral_constant<int, n>{}), gb = pop(std::integral_constant<int, nb>{});
+          fo[n] = keep * gn + (pe + po);
+          fo[nb] = keep * gb + (pe - po);
+          const R WA = n <= L::NAXIS ? WA1 : WA2;
+          const R t = cdot_z<D, n>(hF);
+          const R En = WA + WBe[p] + Bo[p], Eb = WA + WBe[p] - Bo[p];
+          if constexpr (kShifted<T>) {
+            const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+            dfi[n] = gn - (De + Bo[p] * r) + En * (t - hFu);
+            dfi[nb] = gb - (De - Bo[p] * r) - Eb * (t + hFu);
+          } else {
+            dfi[n] = gn - En * (r + hFu - t);
+            dfi[nb] = gb - Eb * (r + hFu + t);
+          }
         });
         sfor<0, Q>([&](auto kk) {
-          constexpr int k = decltype(kk)::value;
-          if (spec & (1u << k)) {
-            R md = R(0);
+          constexpr int kq = decltype(kk)::value;
+          if (spec & (1u << kq)) {
+            R md = R(-0.0);
             sfor<0, Q>([&](auto ii) {
               constexpr int i = decltype(ii)::value;
-              constexpr int v = L::mt(i, k);
+              constexpr int v = L::mt(i, kq);
               if constexpr (v == 1) md = md + dfi[i];
               else if constexpr (v == -1) md = md - dfi[i];
               else if constexpr (v != 0) md = md + R(v) * dfi[i];
             });
-            const R ck = P.dspec[m][k] * md;
+            const R ck = P.dspec[m][kq] * md;
             sfor<0, Q>([&](auto ii) {
               constexpr int i = decltype(ii)::value;
-              constexpr int v = L::mt(i, k);
+              constexpr int v = L::mt(i, kq);
               if constexpr (v == 1) fo[i] = fo[i] - ck;
               else if constexpr (v == -1) fo[i] = fo[i] + ck;
               else if constexpr (v != 0) fo[i] = fo[i] - ck * R(v);

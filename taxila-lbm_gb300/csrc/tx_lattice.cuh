@@ -121,4 +121,61 @@ __host__ __device__ constexpr int rate_of(int k) {
   }
 }
 
+// Direction pairs (n, opp(n)) with n < opp(n), in increasing n: pair p's n.
+template <int D>
+__host__ __device__ constexpr int npairs() {
+  return (Lat<D>::Q - 1) / 2;
+}
+template <int D>
+__host__ __device__ constexpr int pair_n(int p) {
+  int k = 0;
+  for (int n = 1; n < Lat<D>::Q; ++n)
+    if (n < opp<D>(n)) {
+      if (k == p) return n;
+      ++k;
+    }
+  return -1;
+}
+
+// Parity of MRT moment k under c -> -c: even (mt(n,k) = mt(opp(n),k)) or odd
+// (mt(n,k) = -mt(opp(n),k), zero at rest).  Every moment of both bases is one
+// or the other.
+template <int D>
+__host__ __device__ constexpr bool moment_even(int k) {
+  for (int n = 1; n < Lat<D>::Q; ++n)
+    if (Lat<D>::mt(n, k) != Lat<D>::mt(opp<D>(n), k)) return false;
+  return true;
+}
+template <int D>
+__host__ __device__ constexpr bool moment_odd(int k) {
+  if (Lat<D>::mt(0, k) != 0) return false;
+  for (int n = 1; n < Lat<D>::Q; ++n)
+    if (Lat<D>::mt(n, k) != -Lat<D>::mt(opp<D>(n), k)) return false;
+  return true;
+}
+
+// The moments relaxed at s_nu (the traceless second moments): even, zero at rest.
+template <int D>
+__host__ __device__ constexpr unsigned stress_mask() {
+  unsigned b = 0u;
+  for (int k = 0; k < Lat<D>::Q; ++k)
+    if (rate_of<D>(k) == R_NU) b |= 1u << k;
+  return b;
+}
+template <int D>
+__host__ __device__ constexpr bool stress_even_traceless() {
+  for (int k = 0; k < Lat<D>::Q; ++k)
+    if (rate_of<D>(k) == R_NU && (!moment_even<D>(k) || Lat<D>::mt(0, k) != 0)) return false;
+  return true;
+}
+template <int D>
+__host__ __device__ constexpr bool moments_have_parity() {
+  for (int k = 0; k < Lat<D>::Q; ++k)
+    if (!moment_even<D>(k) && !moment_odd<D>(k)) return false;
+  return true;
+}
+static_assert(stress_even_traceless<3>() && stress_even_traceless<2>(), "s_nu moments must be even and traceless");
+static_assert(moments_have_parity<3>() && moments_have_parity<2>(), "MRT moments must have a parity");
+static_assert(npairs<3>() == 9 && pair_n<3>(8) > 0 && npairs<2>() == 4 && pair_n<2>(3) > 0, "direction pairs");
+
 }  // namespace tx

@@ -34,12 +34,18 @@ def bubble_2d_reference_state(p):
     return problems.bubble_box_state(p.nx, p.ny, 1, [0.03, 0.97], [0.97, 0.03], 26, np.zeros(p.nsites))
 
 
-def sc_bubble(disc, shape, mode, iso, g=0.12, r=None, ncomp=2):
+def sc_bubble(disc, shape, mode, iso, g=0.12, r=None, ncomp=2, nu_only=False, base_rate=1.0):
+    """Two-component Shan-Chen bubble; MRT rates mixed (s_e, s_q, s_nu differ
+    from 1) or, with nu_only, only s_nu of the second component differs from
+    the others (base_rate; 1 in the bench's viscosity contrast)."""
     p = base(disc, shape, ncomp=ncomp, mode=mode, iso=iso)
     p.tau[0], p.tau[1] = 1.0, 0.8
     if mode == P.MRT:
+        for key in ("s_c", "s_e", "s_e2", "s_q", "s_pi", "s_m"):
+            getattr(p, key)[1] = base_rate
         p.s_nu[0], p.s_nu[1] = 1.0, 1.0 / 0.7
-        p.s_e[0], p.s_q[1] = 1.2, 1.1
+        if not nu_only:
+            p.s_e[0], p.s_q[1] = 1.2, 1.1
     if ncomp == 2:
         p.g[0][1] = p.g[1][0] = g
     z, y, x = p.shape
@@ -97,6 +103,9 @@ PARITY = [
     ("d3_srt_iso4", lambda: sc_bubble(P.D3Q19, (12, 14, 16), P.SRT, 4), 20),
     ("d3_mrt_iso4", lambda: sc_bubble(P.D3Q19, (16, 12, 14), P.MRT, 4), 20),
     ("d3_mrt_iso8", lambda: sc_bubble(P.D3Q19, (14, 16, 12), P.MRT, 8), 20),
+    ("d3_mrt_nu_only", lambda: sc_bubble(P.D3Q19, (12, 14, 12), P.MRT, 4, nu_only=True), 20),
+    ("d2_mrt_nu_only_iso8", lambda: sc_bubble(P.D2Q9, (1, 36, 40), P.MRT, 8, nu_only=True), 30),
+    ("d3_mrt_nu_only_base_rate", lambda: sc_bubble(P.D3Q19, (12, 12, 14), P.MRT, 4, nu_only=True, base_rate=1.2), 20),
     ("d3_porous_dirichlet_srt", lambda: porous_case(P.D3Q19, (14, 12, 10)), 20),
     ("d3_porous_dirichlet_mrt_body", lambda: porous_case(P.D3Q19, (12, 10, 14), mode=P.MRT, body=True), 20),
     ("d3_porous_periodic_iso8", lambda: porous_case(P.D3Q19, (12, 12, 12), iso=8, dirichlet=False), 15),
