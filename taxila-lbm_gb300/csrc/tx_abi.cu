@@ -133,7 +133,7 @@ namespace tx {
 bool select_species(const tx_params* p, SpeciesSet* ss);
 int validate_params(const tx_params* p, std::string* why);
 void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out);
-bool select_kernels(const tx_params* p, KernelSet* ks);
+bool select_kernels(const tx_params* p, KernelSet* ks, bool any_rates = false);
 void set_global_error(const std::string& msg) { g_create_error = msg; }
 }  // namespace tx
 
@@ -208,8 +208,10 @@ bool select_species(const tx_params* p, SpeciesSet* ss) {
   return table[form][p->discretization == TX_D3Q19 ? 0 : 1](p->species_relaxation_mode == TX_RELAX_MRT, ss);
 }
 
-bool select_kernels(const tx_params* p, KernelSet* ks) {
-  const bool mrt = p->relaxation_mode == TX_RELAX_MRT;
+bool select_kernels(const tx_params* p, KernelSet* ks, bool any_rates) {
+  // the fast forms compile the general MRT rate path into the MRT kernels
+  // only; lattices whose rates do not need it run the leaner kernels
+  const bool mrt = p->relaxation_mode == TX_RELAX_MRT && (p->exact || any_rates || needs_general_rates(*p));
   using Fn = bool (*)(int, int, bool, KernelSet*);
   // [form][dimension 3/2][components 1/2]; form 0 exact FP64, 1 FP64, 2 FP32, 3 FP32/FP16
   static const Fn table[4][2][2] = {

@@ -23,7 +23,7 @@
 using namespace tx;
 
 namespace tx {
-bool select_kernels(const tx_params* p, KernelSet* ks);
+bool select_kernels(const tx_params* p, KernelSet* ks, bool any_rates = false);
 bool select_species(const tx_params* p, SpeciesSet* ss);
 void set_global_error(const std::string& msg);
 }
@@ -343,7 +343,8 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   b->S = f.ncomponents;
   b->Q = b->D == 3 ? 19 : 9;
   b->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : 0;
-  if (!select_kernels(&f, &b->ks) || (f.nspecies > 0 && !select_species(&f, &b->ss))) {
+  // lattices added later may carry any MRT rates
+  if (!select_kernels(&f, &b->ks, true) || (f.nspecies > 0 && !select_species(&f, &b->ss))) {
     delete b;
     tx::set_global_error("no kernel built for this parameter combination");
     return TX_ERR_ARG;

@@ -61,7 +61,7 @@ __device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
 }
 
 template <int D, int S, int ISO, bool MRT, class T, class R, class RT>
-__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R)) k_step_tiles(BatchArgs b, int flip) {
+__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT)) k_step_tiles(BatchArgs b, int flip) {
   const int nt = __ldg(b.ntiles);
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const int4 tl = __ldg(b.tiles + t);

@@ -132,6 +132,7 @@ inline Launch3 launch3(const Geo& g, int threads) {
                     &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat,                          \
                     &L_##S##_##ISO##_##MRT::step_tiles, &L_##S##_##ISO##_##MRT::density_tiles,                 \
                     &L_##S##_##ISO##_##MRT::probe_tiles, &L_##S##_##ISO##_##MRT::faces,                        \
-                    &L_##S##_##ISO##_##MRT::outlet, #S "c iso" #ISO " mrt" #MRT};                              \
+                    &L_##S##_##ISO##_##MRT::outlet,                                                               \
+                    MRT ? #S "c iso" #ISO " rates:any" : #S "c iso" #ISO " rates:bgk/s_nu"};                    \
     return true;                                                                                               \
   }

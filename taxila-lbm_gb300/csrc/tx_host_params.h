@@ -211,6 +211,20 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
   P.inv_sscale = 1.0 / P.sscale;
 }
 
+// Whether the fast MRT step needs its general rate path: some component has
+// moments with a rate other than s0 beyond the s_nu set.  Otherwise the
+// kernels compiled without that path run (fewer registers).
+inline bool needs_general_rates(const tx_params& p) {
+  if (p.relaxation_mode != TX_RELAX_MRT) return false;
+  const int D = p.discretization == TX_D3Q19 ? 3 : 2, S = p.ncomponents, Q = D == 3 ? 19 : 9;
+  Phys ph;
+  fill_phys_impl(p, D, S, Q, ph);
+  const unsigned nu = D == 3 ? stress_mask<3>() : stress_mask<2>();
+  for (int m = 0; m < S; ++m)
+    if (ph.spec_mask[m] != 0u && ph.spec_mask[m] != nu) return true;
+  return false;
+}
+
 // ------------------------------------------------------------ exterior BCs
 inline long long face_area_of(int D, int nx, int ny, int nz, int f) {
   const int a = f / 2;

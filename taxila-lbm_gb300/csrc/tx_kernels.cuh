@@ -45,7 +45,13 @@
 #ifndef TX_FLOAT_MIN_BLOCKS_S1
 #define TX_FLOAT_MIN_BLOCKS_S1 6
 #endif
-#define TX_STEP_MIN_BLOCKS(S, R) (sizeof(R) == 4 ? ((S) == 1 ? TX_FLOAT_MIN_BLOCKS_S1 : TX_FLOAT_MIN_BLOCKS) : 1)
+// FP64 step kernels without the general MRT rate path fit 168 registers
+// without spills: 3 blocks of 128 threads per SM
+#ifndef TX_F64_MIN_BLOCKS
+#define TX_F64_MIN_BLOCKS 3
+#endif
+#define TX_STEP_MIN_BLOCKS(S, R, GENERAL) \
+  (sizeof(R) == 4 ? ((S) == 1 ? TX_FLOAT_MIN_BLOCKS_S1 : TX_FLOAT_MIN_BLOCKS) : ((GENERAL) ? 1 : TX_F64_MIN_BLOCKS))
 
 #include "tx_ff_stencil.cuh"
 #include "tx_lattice.cuh"
@@ -1099,21 +1105,21 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
           push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + (pe - po));
         });
       } else if (spec == stress_mask<D>()) {
-        // s_nu != s0, every other rate s0
-        R g[Q], Pe[NP], Po[NP], Sp[NP];
-        sfor<0, Q>([&](auto nn) { g[decltype(nn)::value] = pop(nn); });
+        // s_nu != s0, every other rate s0.  Pass 1: pair sums of the
+        // non-equilibrium part, S_p = g_n + g_n~ - 2 De - Ae (3 F.u) + Bo c_n.(3 F);
+        // then the s_nu moments and their corrections ck; pass 2 relaxes and
+        // pushes each pair with its correction (no per-pair arrays stay live).
         R F3[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) F3[d] = R(3) * F[m][d];
         const R hFu2 = R(3) * Fu;
+        R Sp[NP];
         sfor<0, NP>([&](auto pp) {
           constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-          pair_terms(pp, Pe[p], Po[p]);
-          // S_p = g_n + g_n~ - 2 De - Ae (3 F.u) + Bo c_n.(3 F)
           const R WA = n <= L::NAXIS ? WA1 : WA2;
           const R Ae = WA + WBe[p];
           const R t2 = cdot_z<D, n>(F3);
-          const R gs = g[n] + g[nb];
+          const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
           if constexpr (kShifted<T>) {
             const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
             Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
@@ -1121,6 +1127,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
             Sp[p] = gs - Ae * (R(2) * r + hFu2) + Bo[p] * t2;
           }
         });
+        R ck[Q];
         sfor<0, Q>([&](auto kk) {
           constexpr int kq = decltype(kk)::value;
           if constexpr (rate_of<D>(kq) == R_NU) {
@@ -1132,33 +1139,36 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
               else if constexpr (v == -1) md = md - Sp[p];
               else if constexpr (v != 0) md = md + R(v) * Sp[p];
             });
-            const R ck = P.dspec[m][kq] * md;
-            sfor<0, NP>([&](auto pp) {
-              constexpr int p = decltype(pp)::value;
-              constexpr int v = L::mt(pair_n<D>(p), kq);
-              if constexpr (v == 1) Pe[p] = Pe[p] - ck;
-              else if constexpr (v == -1) Pe[p] = Pe[p] + ck;
-              else if constexpr (v != 0) Pe[p] = Pe[p] - R(v) * ck;
-            });
+            ck[kq] = P.dspec[m][kq] * md;
           }
         });
-        if (keep == R(0)) {
-          push(std::integral_constant<int, 0>{}, m, X0);
-          sfor<0, NP>([&](auto pp) {
-            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-            push(std::integral_constant<int, n>{}, m, Pe[p] + Po[p]);
-            push(std::integral_constant<int, nb>{}, m, Pe[p] - Po[p]);
+        const bool k0 = keep == R(0);
+        push(std::integral_constant<int, 0>{}, m, k0 ? X0 : keep * pop(std::integral_constant<int, 0>{}) + X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          R pe, po;
+          pair_terms(pp, pe, po);
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU) {
+              constexpr int v = L::mt(n, kq);
+              if constexpr (v == 1) pe = pe - ck[kq];
+              else if constexpr (v == -1) pe = pe + ck[kq];
+              else if constexpr (v != 0) pe = pe - R(v) * ck[kq];
+            }
           });
-        } else {
-          push(std::integral_constant<int, 0>{}, m, keep * g[0] + X0);
-          sfor<0, NP>([&](auto pp) {
-            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-            push(std::integral_constant<int, n>{}, m, keep * g[n] + (Pe[p] + Po[p]));
-            push(std::integral_constant<int, nb>{}, m, keep * g[nb] + (Pe[p] - Po[p]));
-          });
-        }
-      } else {
-        // general rate pattern: relax every moment at s0, then correct each
+          if (k0) {
+            push(std::integral_constant<int, n>{}, m, pe + po);
+            push(std::integral_constant<int, nb>{}, m, pe - po);
+          } else {
+            push(std::integral_constant<int, n>{}, m, keep * pop(std::integral_constant<int, n>{}) + (pe + po));
+            push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + (pe - po));
+          }
+        });
+      } else if constexpr (MRT) {
+        // General rate pattern, compiled into the MRT kernels only (the host
+        // runs the others when every component is BGK-like or s_nu-only):
+        // relax every moment at s0, then correct each
         // moment k whose rate differs by dspec_k times its projection of the
         // deviation from the forced equilibrium, g - dE_n + 1.5 E_n (F.c_n - F.u)
         R fo[Q], dfi[Q];
@@ -1221,7 +1231,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
 }
 
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
-__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R)) k_step(StepArgs a_in) {
+__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT || EXACT)) k_step(StepArgs a_in) {
   const StepArgs a = a_in;  // local copy: helpers never address the kernel parameter
   int x, y, z;
   long long idx;

@@ -79,7 +79,7 @@ __global__ void k_static_fill(double* p, long long n, double v) {
 namespace tx {
 int validate_params(const tx_params* p, std::string* why);
 void fill_phys_from(const tx_params& p, int D, int S, int Q, Phys* out);
-bool select_kernels(const tx_params* p, KernelSet* ks);
+bool select_kernels(const tx_params* p, KernelSet* ks, bool any_rates = false);
 }  // namespace tx
 
 extern "C" int tx_step_static(const tx_params* p, const double* walls, const double* fi_in, double* fi_out,
