@@ -91,7 +91,11 @@ inline Launch3 launch3(const Geo& g, int threads) {
       k_step<D, S, ISO, MRT, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a);                        \
     }                                                                                                         \
     static void density(const StepArgs& a, int mode, cudaStream_t s) {                                        \
-      k_density<D, S, T, R, RT><<<launch3(a.g, 256).grid, launch3(a.g, 256).block, 0, s>>>(a, mode);                                \
+      constexpr int VW = 16 / (int)sizeof(T);                                                                 \
+      if (a.g.n % VW == 0)                                                                                    \
+        k_density_vec<D, S, T, R, RT><<<grid_for(a.g.n / VW, 256), 256, 0, s>>>(a, mode);                     \
+      else                                                                                                    \
+        k_density<D, S, T, R, RT><<<launch3(a.g, 256).grid, launch3(a.g, 256).block, 0, s>>>(a, mode);        \
     }                                                                                                         \
     static void init(const StepArgs& a, const double* u, cudaStream_t s) {                                    \
       k_init<D, S, ISO, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, u);                          \

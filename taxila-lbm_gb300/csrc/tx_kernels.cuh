@@ -32,6 +32,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <cstring>
 
 #include "../../include/taxila_gb300.h"
 
@@ -1404,6 +1405,82 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a_in, int mode) {
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
   density_site<D, S, T, R, RT>(a, x, y, z, mode);
+}
+
+// The density pass with 16-byte loads: VW = 16 / sizeof(T) consecutive sites
+// per thread (lattices with N a multiple of VW, so that every load is
+// aligned).  The pass streams every population once; wide loads keep more
+// bytes in flight per instruction.  Groups with a site on a Dirichlet face
+// take density_site, site by site; the sums are density_site's, in the same
+// order.
+template <class T, class R>
+__device__ __forceinline__ R from_dev(T v, const PhysT<R>& P) {
+  if constexpr (std::is_same<T, __half>::value)
+    return R(__half2float(v)) * P.inv_sscale;
+  else
+    return R(v);
+}
+
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
+  constexpr int VW = 16 / (int)sizeof(T);
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const StepArgs a = a_in;
+  const long long N = a.g.n;
+  const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * VW;
+  if (c0 >= N) return;
+  const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
+  const unsigned keep = D == 3 ? 63u : 15u;
+  if (mode == 0 && (dir_bits(a.faces) & keep)) {
+    bool face = false;
+#pragma unroll
+    for (int v = 0; v < VW; ++v) {
+      const long long c = c0 + v;
+      const int x = (int)(c % a.g.nx), y = (int)((c / a.g.nx) % a.g.ny), z = (int)(c / ((long long)a.g.nx * a.g.ny));
+      face |= (dir_bits(a.faces) & site_faces(a.g, x, y, z) & keep) != 0u;
+    }
+    if (face) {
+      for (int v = 0; v < VW; ++v) {
+        const long long c = c0 + v;
+        const int x = (int)(c % a.g.nx), y = (int)((c / a.g.nx) % a.g.ny), z = (int)(c / ((long long)a.g.nx * a.g.ny));
+        density_site<D, S, T, R, RT>(a, x, y, z, mode);
+      }
+      return;
+    }
+  }
+  bool pore[VW];
+  bool any = false;
+#pragma unroll
+  for (int v = 0; v < VW; ++v) {
+    pore[v] = __ldg(a.mask + c0 + v) == 0;
+    any |= pore[v];
+  }
+  if (!any) return;
+  const T* fcur = reinterpret_cast<const T*>(a.fout);
+  RT* rho = reinterpret_cast<RT*>(a.rho);
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R acc[VW];
+#pragma unroll
+    for (int v = 0; v < VW; ++v) acc[v] = R(0);
+    sfor<0, Q>([&](auto nn) {
+      constexpr int n = decltype(nn)::value;
+      const uint4 w = __ldg(reinterpret_cast<const uint4*>(fcur + (long long)(m * Q + n) * N + c0));
+      T vals[VW];
+      memcpy(vals, &w, 16);
+#pragma unroll
+      for (int v = 0; v < VW; ++v) acc[v] = acc[v] + from_dev<T, R>(vals[v], P);
+    });
+#pragma unroll
+    for (int v = 0; v < VW; ++v) {
+      if (!pore[v]) continue;
+      rho[(size_t)(c0 + v) * S + m] = RT(acc[v]);
+      if (P.eos_on)
+        reinterpret_cast<RT*>(a.psi)[(size_t)(c0 + v) * S + m] =
+            RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, P.rho0[m] + acc[v]));
+    }
+  }
 }
 
 // ------------------------------------------------ Neumann and velocity nodes

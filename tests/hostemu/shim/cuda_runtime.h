@@ -23,6 +23,9 @@ struct float2 {
 struct alignas(16) double2 {
   double x, y;
 };
+struct alignas(16) uint4 {
+  unsigned x, y, z, w;
+};
 
 template <class T>
 inline T __ldg(const T* p) {
