@@ -448,15 +448,18 @@ def run_gpu(args):
                      "kernel": "k_step (collide + push, %d B/LUP algorithmic)" % bpl,
                      "ms_per_launch": round(k_ms, 4), "ms_k_density": round(t_dens / nk, 4),
                      "peak_source": peak_kind,
-                     "compute_bound": ({"pipe": "fp64", "active_frac": 0.854, "fp64_instr_per_lup": 583,
-                                        "fp64_flop_per_lup": 872,
-                                        "fp64_tflops": round(value / ws * 872 / 1e6, 3),
+                     "compute_bound": ({"pipe": "fp64", "active_frac": 0.868, "fp64_instr_per_lup": 412,
+                                        "fp64_flop_per_lup": 539,
+                                        "fp64_instr_per_s": round(p.nsites * 412 / (k_ms * 1e-3) / 1e9, 1),
+                                        "fp64_instr_peak_per_s": round(2 * 152 * 2.07, 1),
+                                        "fp64_tflops": round(value / ws * 539 / 1e6, 3),
                                         "source": "ncu sm__pipe_fp64_cycles_active and "
                                                   "smsp__sass_thread_inst_executed_op_d{add,fma,mul} of k_step, 96^3 "
                                                   "capture (profiles/k_step_d3q19_2c_mrt_96.md)"}
                                        if args.form == "f64" else None),
-                     "note": "FP64 is issue-bound on GB300 (FP64 rate ~1/64 of FP32): the HBM fraction of the "
-                             "plain form is low by construction; see the fp32/fp16 forms"},
+                     "note": "the FP64 form is bound by GB300's FP64 pipe (2 lanes per SM per cycle, "
+                             "fp64_instr_* in G instructions/s): its HBM fraction is low by construction; "
+                             "see the fp32/fp16 forms for the HBM-bound ones"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
