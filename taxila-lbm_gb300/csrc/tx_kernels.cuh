@@ -321,22 +321,39 @@ struct Hood {
   int ox[2 * RCH + 1], oy[2 * RCH + 1], oz[2 * RZ + 1];
   unsigned in_x, in_y, in_z;
 
-  __device__ static __forceinline__ int wrap(int c, int n, int per, unsigned& in, int bit) {
-    const bool out = c < 0 || c >= n;
-    in |= (!out || per) ? (1u << bit) : 0u;
-    int w = c < 0 ? c + n : (c >= n ? c - n : c);
-    w = w < 0 ? 0 : (w >= n ? n - 1 : w);
-    return w;
+  // coordinate c + d of a site coordinate c in [0, n): wrapped on a periodic
+  // axis (n >= 3 >= |d| there), clamped into the lattice otherwise (then the
+  // in-bit is clear and the value only keeps addresses valid)
+  template <int d, int B>
+  __device__ static __forceinline__ int wrap(int c, int n, int per, unsigned& in) {
+    constexpr unsigned bit = 1u << B;  // in-bit of offset d
+    if constexpr (d == 0) {
+      in |= bit;
+      return c;
+    } else if constexpr (d > 0) {
+      const int w = c + d;
+      const bool out = w >= n;
+      in |= (!out || per) ? bit : 0u;
+      return out ? (per ? w - n : n - 1) : w;
+    } else {
+      const int w = c + d;
+      const bool out = w < 0;
+      in |= (!out || per) ? bit : 0u;
+      return out ? (per ? w + n : 0) : w;
+    }
+  }
+  template <int i>
+  __device__ __forceinline__ void fill(const Geo& g, int x, int y, int z) {
+    if constexpr (i < 2 * RCH + 1) {
+      ox[i] = wrap<i - RCH, i>(x, g.nx, g.per[0], in_x);
+      oy[i] = g.nx * wrap<i - RCH, i>(y, g.ny, g.per[1], in_y);
+      if constexpr (i < 2 * RZ + 1) oz[i] = g.nx * g.ny * wrap<i - RZ, i>(z, g.nz, g.per[2], in_z);
+      fill<i + 1>(g, x, y, z);
+    }
   }
   __device__ __forceinline__ Hood(const Geo& g, int x, int y, int z) {
     in_x = in_y = in_z = 0u;
-#pragma unroll
-    for (int d = -RCH; d <= RCH; ++d) {
-      ox[d + RCH] = wrap(x + d, g.nx, g.per[0], in_x, d + RCH);
-      oy[d + RCH] = g.nx * wrap(y + d, g.ny, g.per[1], in_y, d + RCH);
-    }
-#pragma unroll
-    for (int d = -RZ; d <= RZ; ++d) oz[d + RZ] = g.nx * g.ny * wrap(z + d, g.nz, g.per[2], in_z, d + RZ);
+    fill<0>(g, x, y, z);
   }
   template <int dx, int dy, int dz>
   __device__ __forceinline__ unsigned at() const {
