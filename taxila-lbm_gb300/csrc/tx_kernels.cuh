@@ -1906,6 +1906,22 @@ __device__ __forceinline__ void moments_site(const StepArgs& a, int x, int y, in
   }
   const long long N = a.g.n;
   R fv[S][Q];
+  if (what == 2) {
+    // the density needs neither forces nor velocity: the forcing density, or
+    // the population sum on re-summed face nodes (as cell_velocity forms rc)
+    const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
+    R rfd[S];
+    rho_at<S>(reinterpret_cast<const RT*>(a.rho), (unsigned)idx, rfd);
+    if (dn) load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, (unsigned)idx, P, fv);
+    for (int m = 0; m < S; ++m) {
+      const R sum = dn ? pop_sum<D, S, R>(fv, m) : rfd[m];
+      if constexpr (kShifted<T>)
+        out[idx * S + m] = double(P.rho0[m]) + double(sum);  // keeps the digits of the deviation
+      else
+        out[idx * S + m] = double(P.rho0[m] + sum);
+    }
+    return;
+  }
   load_pops<D, S, T, R>(reinterpret_cast<const T*>(a.fin), N, (unsigned)idx, P, fv);
   R rc[S], rf[S], F[S][D], up[D];
   cell_moments<D, S, ISO, EXACT, R, RT>(a, P, x, y, z, idx, fv, rc, rf, F, up);
