@@ -138,9 +138,17 @@ def reduce_max(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(ms_local, sites_local, steps, ws):
+    """Replicas: every rank steps its own lattice of sites_local sites.  The job
+    time is the slowest rank's; the value counts the sites of all ranks."""
+    ms = reduce_max(ms_local, ws)
+    return sites_local * ws * steps / (ms * 1e-3) / 1e6, ms
 
 
 def barrier(ws):
@@ -411,7 +419,7 @@ def run_gpu(args):
         e1.synchronize()
     torch.cuda.synchronize()
     barrier(ws)
-    ms = reduce_max(e0.elapsed_time(e1), ws)
+    value, ms = replica_throughput(e0.elapsed_time(e1), p.nsites, args.steps, ws)
     # per-kernel durations (events around each launch)
     h.set_timing(True)
     nk = min(args.steps, 20)
@@ -422,9 +430,10 @@ def run_gpu(args):
     rho_check = h.delta_norm(P.FIELD_RHO)  # non-finite states raise here
     kname = h.kernel_name()
     h.close()
-    sites = p.nsites * ws
-    value = sites * args.steps / (ms * 1e-3) / 1e6
     if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
         return 0
     peak, peak_kind = peaks()
     k_ms = t_step / nk
