@@ -285,7 +285,8 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
     uniform in 48..192 per axis, seeded sphere packs with radii 4..10 and
     porosity 0.25..0.5, periodic, body force 1e-6 along z) in one batch of the
     FP32 form: tile shape from the autotuner, steps replayed as a CUDA graph.
-    The first ``compare`` lattices are also stepped one by one in tx_handles."""
+    Every lattice is also stepped alone in a tx_handle (the first ``compare``
+    reported on their own as well)."""
     import torch
     from taxila import serve
     from taxila._lib import Batch, Handle
@@ -335,7 +336,9 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
     ms_sub = timed(bs, steps)
     bs.close()
     ms_one = 0.0
-    for r in sub:
+    ms_all = 0.0
+    handles = []
+    for i, r in enumerate(reqs):
         h = Handle(params_of(r))
         h.upload_walls(r.walls)
         h.upload_state(r.rho)
@@ -348,7 +351,19 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
         h.step(steps)
         e1.record(stream)
         e1.synchronize()
-        ms_one += e0.elapsed_time(e1)
+        if i < compare:
+            ms_one += e0.elapsed_time(e1)
+        ms_all += e0.elapsed_time(e1)
+        handles.append(h)
+    # a driver stepping every lattice in turn, one step each, waiting for each
+    # (states evicted from L2 between visits, as in the batch)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for h in handles:
+            h.step(1)
+            h.sync()
+    ms_rr = (time.perf_counter() - t0) * 1e3
+    for h in handles:
         h.close()
     mlups = sites * steps / (ms * 1e-3) / 1e6
     bpl = 2 * 19 * 4 + 1 + 19 * 4 + 4  # collide-push read+write, mask; density read + write
@@ -359,7 +374,12 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
             "tiles": {"bx": tiles[0], "by": tiles[1], "bz": tiles[2], "blocks_per_sm": tiles[3]},
             "graph_steps": 20, "finite": finite,
             "first_%d_batched_mlups" % compare: round(sub_sites * steps / (ms_sub * 1e-3) / 1e6, 1),
-            "first_%d_one_by_one_mlups" % compare: round(sub_sites * steps / (ms_one * 1e-3) / 1e6, 1)}
+            "first_%d_one_by_one_mlups" % compare: round(sub_sites * steps / (ms_one * 1e-3) / 1e6, 1),
+            "all_one_by_one_mlups": round(sites * steps / (ms_all * 1e-3) / 1e6, 1),
+            "all_round_robin_mlups": round(sites * steps / (ms_rr * 1e-3) / 1e6, 1),
+            "one_by_one": "each lattice in its own tx_handle: device time of its steps alone (states of lattices "
+                          "under ~80^3 stay in L2; launch gaps not counted), and round robin: wall time of a "
+                          "driver stepping every lattice once per round and waiting for it"}
 
 
 def serving_run(n=30, rate=30.0, seed=1):

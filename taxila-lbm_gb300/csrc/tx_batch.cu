@@ -95,6 +95,9 @@ struct tx_batch {
   int* d_ntiles = nullptr;
   ProbePart* d_res = nullptr;
   int ntiles = 0;
+  int2* d_ltiles = nullptr;  // the density pass's linear tiles
+  int ltile_cap = 0;
+  int* d_nltiles = nullptr;
   // launch shape
   int bx = 32, by = 4, bz = 1, blocks_per_sm = 4;
   // graph
@@ -166,6 +169,8 @@ BatchArgs bargs(const tx_batch* b) {
   a.tiles = b->d_tiles;
   a.ntiles = b->d_ntiles;
   a.parts = b->d_parts;
+  a.ltiles = b->d_ltiles;
+  a.nltiles = b->d_nltiles;
   return a;
 }
 
@@ -189,6 +194,8 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
 int rebuild_tables(tx_batch* b) {
   std::vector<LatDesc> descs;
   std::vector<int4> tiles;
+  std::vector<int2> ltiles;
+  const long long run = 128LL * (long long)(16 / pop_bytes(b->form.precision));  // sites per density tile
   for (size_t s = 0; s < b->slots.size(); ++s) {
     Lattice* L = b->slots[s];
     LatDesc d{};
@@ -203,9 +210,11 @@ int rebuild_tables(tx_batch* b) {
       for (int y = 0; y < L->g.ny; y += b->by)
         for (int x = 0; x < L->g.nx; x += b->bx) tiles.push_back(make_int4((int)s, x, y, z));
     d.tile_count = (int)tiles.size() - d.tile_begin;
+    d.ltile_begin = (int)ltiles.size();
+    for (long long c0 = 0; c0 < L->g.n; c0 += run) ltiles.push_back(make_int2((int)s, (int)c0));
     descs.push_back(d);
   }
-  const int nl = (int)descs.size(), nt = (int)tiles.size();
+  const int nl = (int)descs.size(), nt = (int)tiles.size(), nlt = (int)ltiles.size();
   if (nl > b->lat_cap) {
     const int cap = std::max(nl, 2 * b->lat_cap);
     drop_graph(b);
@@ -224,7 +233,16 @@ int rebuild_tables(tx_batch* b) {
     TX_BCUDA(b, cudaMallocAsync(&b->d_parts, (size_t)cap * sizeof(ProbePart), b->stream));
     b->tile_cap = cap;
   }
+  if (nlt > b->ltile_cap) {
+    const int cap = std::max(nlt, 2 * b->ltile_cap);
+    drop_graph(b);
+    if (b->d_ltiles) cudaFreeAsync(b->d_ltiles, b->stream);
+    TX_BCUDA(b, cudaMallocAsync(&b->d_ltiles, (size_t)cap * sizeof(int2), b->stream));
+    b->ltile_cap = cap;
+  }
   if (nl) TX_BCUDA(b, cudaMemcpyAsync(b->d_lats, descs.data(), (size_t)nl * sizeof(LatDesc), cudaMemcpyHostToDevice, b->stream));
+  if (nlt) TX_BCUDA(b, cudaMemcpyAsync(b->d_ltiles, ltiles.data(), (size_t)nlt * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+  TX_BCUDA(b, cudaMemcpyAsync(b->d_nltiles, &nlt, sizeof(int), cudaMemcpyHostToDevice, b->stream));
   if (nt) TX_BCUDA(b, cudaMemcpyAsync(b->d_tiles, tiles.data(), (size_t)nt * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
   TX_BCUDA(b, cudaMemcpyAsync(b->d_ntiles, &nt, sizeof(int), cudaMemcpyHostToDevice, b->stream));
   // the host vectors die with this call: the copies must have left them
@@ -358,12 +376,13 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&b->d_ntiles, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&b->d_ntiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_nltiles, sizeof(int)) != cudaSuccess) {
     tx::set_global_error("CUDA device setup failed");
     tx_batch_destroy(b);
     return TX_ERR_NODEVICE;
   }
   cudaMemset(b->d_ntiles, 0, sizeof(int));
+  cudaMemset(b->d_nltiles, 0, sizeof(int));
   *out = b;
   return TX_OK;
 }
@@ -374,10 +393,11 @@ int tx_batch_destroy(tx_batch* b) {
   drop_graph(b);
   for (Lattice* L : b->slots) free_lattice(b, L);
   b->slots.clear();
-  for (void* p : {(void*)b->d_lats, (void*)b->d_tiles, (void*)b->d_parts, (void*)b->d_res})
+  for (void* p : {(void*)b->d_lats, (void*)b->d_tiles, (void*)b->d_parts, (void*)b->d_res, (void*)b->d_ltiles})
     if (p) cudaFreeAsync(p, b->stream);
   if (b->stream) cudaStreamSynchronize(b->stream);
   cudaFree(b->d_ntiles);
+  cudaFree(b->d_nltiles);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return TX_OK;

@@ -29,6 +29,7 @@ struct LatDesc {
   double* uold;       // velocity at the previous probe, [d * N + cell]
   int tile_begin;     // this lattice's tiles in the table
   int tile_count;
+  int ltile_begin;    // its first tile of the density pass's linear table
   // passive species: populations at flip 0 / the other buffer, parameters
   const void* sg0;
   void* sg1;
@@ -49,6 +50,8 @@ struct BatchArgs {
   const int4* tiles;  // (lattice slot, x0, y0, z0)
   const int* ntiles;  // table length (device memory: may change between graph replays)
   ProbePart* parts;   // [tile]
+  const int2* ltiles; // density pass: (lattice slot, first site) of runs of 128 x VW sites
+  const int* nltiles;
 };
 
 __device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
@@ -71,19 +74,28 @@ __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT)) k_step_til
   }
 }
 
-// after k_step_tiles at the same flip: the pushed populations are in a.fout
+// after k_step_tiles at the same flip: the pushed populations are in a.fout.
+// The density pass streams each lattice's sites in order: tiles of 128
+// threads x VW consecutive sites, 16-byte loads where the site count allows.
 template <int D, int S, class T, class R, class RT>
 __global__ void __launch_bounds__(128) k_density_tiles(BatchArgs b, int flip) {
-  const int nt = __ldg(b.ntiles);
+  constexpr int VW = 16 / (int)sizeof(T);
+  const int nt = __ldg(b.nltiles);
+  const int lane = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-    const int4 tl = __ldg(b.tiles + t);
+    const int2 tl = __ldg(b.ltiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
-    const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
-    if (x < a.g.nx && y < a.g.ny && z < a.g.nz) density_site<D, S, T, R, RT>(a, x, y, z, 0);
+    const long long N = a.g.n;
+    const long long c0 = (long long)tl.y + (long long)lane * VW;
+    if (c0 < N) {
+      if (N % VW == 0)
+        density_group<D, S, T, R, RT, true>(a, c0, 0);
+      else
+        density_group<D, S, T, R, RT, false>(a, c0, 0, (int)(N - c0 < VW ? N - c0 : VW));
+    }
     // the lattice's step counter advances once per step (the step kernel of
     // this step has finished reading it; the next one reads the new value)
-    if (t == b.lats[tl.x].tile_begin && threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0 && a.steps_ptr)
-      atomicAdd(const_cast<unsigned*>(a.steps_ptr), 1u);
+    if (t == b.lats[tl.x].ltile_begin && lane == 0 && a.steps_ptr) atomicAdd(const_cast<unsigned*>(a.steps_ptr), 1u);
   }
 }
 

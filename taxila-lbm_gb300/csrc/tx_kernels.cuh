@@ -1438,27 +1438,27 @@ __device__ __forceinline__ R from_dev(T v, const PhysT<R>& P) {
     return R(v);
 }
 
-template <int D, int S, class T, class R, class RT>
-__global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
+// the VW sites from c0: with VEC, 16-byte loads (c0 and N multiples of VW);
+// otherwise element loads of the cnt <= VW sites that exist
+template <int D, int S, class T, class R, class RT, bool VEC = true>
+__device__ __forceinline__ void density_group(const StepArgs& a, long long c0, int mode, int cnt = 16 / (int)sizeof(T)) {
   constexpr int VW = 16 / (int)sizeof(T);
   using L = Lat<D>;
   constexpr int Q = L::Q;
-  const StepArgs a = a_in;
   const long long N = a.g.n;
-  const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * VW;
-  if (c0 >= N) return;
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   const unsigned keep = D == 3 ? 63u : 15u;
   if (mode == 0 && (dir_bits(a.faces) & keep)) {
     bool face = false;
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
+      if (v >= cnt) break;
       const long long c = c0 + v;
       const int x = (int)(c % a.g.nx), y = (int)((c / a.g.nx) % a.g.ny), z = (int)(c / ((long long)a.g.nx * a.g.ny));
       face |= (dir_bits(a.faces) & site_faces(a.g, x, y, z) & keep) != 0u;
     }
     if (face) {
-      for (int v = 0; v < VW; ++v) {
+      for (int v = 0; v < cnt; ++v) {
         const long long c = c0 + v;
         const int x = (int)(c % a.g.nx), y = (int)((c / a.g.nx) % a.g.ny), z = (int)(c / ((long long)a.g.nx * a.g.ny));
         density_site<D, S, T, R, RT>(a, x, y, z, mode);
@@ -1470,7 +1470,7 @@ __global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
   bool any = false;
 #pragma unroll
   for (int v = 0; v < VW; ++v) {
-    pore[v] = __ldg(a.mask + c0 + v) == 0;
+    pore[v] = v < cnt && __ldg(a.mask + c0 + (v < cnt ? v : 0)) == 0;
     any |= pore[v];
   }
   if (!any) return;
@@ -1483,11 +1483,18 @@ __global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
     for (int v = 0; v < VW; ++v) acc[v] = R(0);
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
-      const uint4 w = __ldg(reinterpret_cast<const uint4*>(fcur + (long long)(m * Q + n) * N + c0));
-      T vals[VW];
-      memcpy(vals, &w, 16);
+      const T* src = fcur + (long long)(m * Q + n) * N + c0;
+      if constexpr (VEC) {
+        const uint4 w = __ldg(reinterpret_cast<const uint4*>(src));
+        T vals[VW];
+        memcpy(vals, &w, 16);
 #pragma unroll
-      for (int v = 0; v < VW; ++v) acc[v] = acc[v] + from_dev<T, R>(vals[v], P);
+        for (int v = 0; v < VW; ++v) acc[v] = acc[v] + from_dev<T, R>(vals[v], P);
+      } else {
+#pragma unroll
+        for (int v = 0; v < VW; ++v)
+          if (v < cnt) acc[v] = acc[v] + from_dev<T, R>(__ldg(src + v), P);
+      }
     });
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
@@ -1498,6 +1505,14 @@ __global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
             RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, P.rho0[m] + acc[v]));
     }
   }
+}
+
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(256) k_density_vec(StepArgs a_in, int mode) {
+  constexpr int VW = 16 / (int)sizeof(T);
+  const StepArgs a = a_in;
+  const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * VW;
+  if (c0 < a.g.n) density_group<D, S, T, R, RT>(a, c0, mode);
 }
 
 // ------------------------------------------------ Neumann and velocity nodes
