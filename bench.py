@@ -280,7 +280,7 @@ def traffic_from_profile():
         return None
 
 
-def batched_run(n_lat=96, steps=40, seed=4, compare=8):
+def batched_run(n_lat=96, steps=40, seed=4, compare=8, sides=(48, 192)):
     """Many uneven single-phase permeability lattices (D3Q19 BGK tau = 1, sides
     uniform in 48..192 per axis, seeded sphere packs with radii 4..10 and
     porosity 0.25..0.5, periodic, body force 1e-6 along z) in one batch of the
@@ -293,9 +293,9 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
     rng = np.random.default_rng(seed)
     reqs = []
     for i in range(n_lat):
-        sides = [int(v) for v in rng.integers(48, 193, size=3)]
-        reqs.append(serve.perm_request(i, 0.0, sides, int(rng.integers(0, 1 << 30)), 1e-7, 10 ** 9, gz=1e-6,
-                                       radii=(4.0, 10.0)))
+        dims = [int(v) for v in rng.integers(sides[0], sides[1] + 1, size=3)]
+        reqs.append(serve.perm_request(i, 0.0, dims, int(rng.integers(0, 1 << 30)), 1e-7, 10 ** 9, gz=1e-6,
+                                       radii=(4.0, 10.0) if sides[0] >= 48 else (2.0, 5.0)))
     form = P.copy_params(reqs[0].params)
     form.precision = P.PREC_F32
 
@@ -367,8 +367,8 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8):
         h.close()
     mlups = sites * steps / (ms * 1e-3) / 1e6
     bpl = 2 * 19 * 4 + 1 + 19 * 4 + 4  # collide-push read+write, mask; density read + write
-    return {"workload": "%d single-phase D3Q19 BGK sphere packs, sides 48-192 per axis (%d sites), FP32 form, "
-                        "body force 1e-6, periodic" % (n_lat, sites),
+    return {"workload": "%d single-phase D3Q19 BGK sphere packs, sides %d-%d per axis (%d sites), FP32 form, "
+                        "body force 1e-6, periodic" % (n_lat, sides[0], sides[1], sites),
             "steps": steps, "ms_per_step": round(ms / steps, 4), "mlups": round(mlups, 1),
             "gbs_algorithmic": round(mlups * 1e6 * bpl / 1e9, 1), "bytes_per_lup": bpl,
             "tiles": {"bx": tiles[0], "by": tiles[1], "bz": tiles[2], "blocks_per_sm": tiles[3]},
@@ -508,7 +508,10 @@ def run_gpu(args):
             except Exception as ex:
                 forms[name] = {"error": str(ex)}
         line["precision_forms"] = forms
-        for key, fn in (("batched", batched_run), ("serving", serving_run)):
+        legs = (("batched", batched_run),
+                ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
+                ("serving", serving_run))
+        for key, fn in legs:
             try:
                 line[key] = fn()
             except Exception as ex:  # report, do not hide
