@@ -273,16 +273,22 @@ __host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
 }
 
 // FP16 store with stochastic rounding: the 13 FP32 mantissa bits that FP16
-// drops are rounded up with probability equal to their value (a hashed
-// 13-bit dither added to the bit pattern, then truncation toward zero).
+// drops are rounded up with probability equal to their value (a 13-bit
+// dither added to the bit pattern, then truncation toward zero).
 // Round-to-nearest of slowly varying fields makes the same error every step
 // and biases steady states; a dither that changes with the step does not.
+// The dither of population k at a site is the top 13 bits of seed * M_k,
+// where seed is a hash of the site and the step and M_k a fixed odd
+// multiplier per population (multiply-shift hashing: one multiply per store).
 // Other storage types store as st_dev.
+__host__ __device__ __forceinline__ uint32_t sr_dither(uint32_t seed, uint32_t k) {
+  return (seed * (mix32(k + 1u) | 1u)) >> 19;
+}
 template <class T, class R>
-__device__ __forceinline__ void st_dev_sr(T* p, R v, const PhysT<R>& P, uint32_t key) {
+__device__ __forceinline__ void st_dev_sr(T* p, R v, const PhysT<R>& P, uint32_t dither) {
   if constexpr (std::is_same<T, __half>::value) {
     const float x = float(v * P.sscale);
-    const uint32_t b = __float_as_uint(x) + (mix32(key) & 0x1FFFu);
+    const uint32_t b = __float_as_uint(x) + dither;
     *p = __float2half_rz(__uint_as_float(b));
   } else {
     st_dev<T, R>(p, v, P);
@@ -962,7 +968,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       T* const base = fout + (long long)(m * Q + (pore ? n : o)) * N;
       dst = base + (pore ? h.template at<cx, cy, cz>() : c);
     }
-    st_dev_sr<T, R>(dst, v, P, sr_seed + 0x85EBCA6Bu * (uint32_t)(m * Q + n + 1));
+    st_dev_sr<T, R>(dst, v, P, sr_dither(sr_seed, (uint32_t)(m * Q + n)));
   };
 
   if constexpr (EXACT) {
