@@ -203,3 +203,24 @@ def test_emulated_exterior_bcs_match_oracle(emu_exe, tmp_path, name, make, steps
     q.exact = 1 if exact else 0
     got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
     compare(ref, got, p, walls, 0.0 if exact else 1e-12)
+
+
+BC_FORM_CASES = ["d3_pressure_s1", "d3_reflect_momentum", "d3_neumann_then_dirichlet"]
+
+
+@pytest.mark.parametrize("name", BC_FORM_CASES)
+@pytest.mark.parametrize("prec,scale", [(P.PREC_F32, 1.0), (P.PREC_F32_F16, 4096.0)], ids=["f32", "f32_f16"])
+def test_emulated_exterior_bcs_reduced_precision(emu_exe, tmp_path, name, prec, scale):
+    # the face pass in the FP32-arithmetic forms, deviations from rho0 = 1,
+    # against the FP64 oracle
+    make, steps = next((m, s) for n, m, s in cases.BCS if n == name)
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    q = P.copy_params(p)
+    q.precision = prec
+    q.rho0[0] = 1.0
+    q.storage_scale = scale
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    tol = 1e-5 if prec == P.PREC_F32 else 2e-3
+    errs = compare(ref, got, p, walls, {"fi": tol, "rho": tol, "flux": 50 * tol, "forces": 50 * tol})
+    print(name, prec, errs)
