@@ -46,6 +46,7 @@ struct Lattice {
   double* faceval[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* phys = nullptr;       // PhysT<R> of the batch's arithmetic type
   Faces faces{};
+  FaceShell shell{};          // face nodes of the face pass (faces.post)
   void* sg[2] = {nullptr, nullptr};  // species populations
   void* sphys = nullptr;             // SpeciesPhysT<R>
   int NS = 0;
@@ -69,7 +70,7 @@ long long lattice_bytes(const tx_params& p) {
                 N * S * (long long)rho_bytes(p.precision) * (p.use_nonideal_eos ? 2 : 1) + N +
                 4 * N + 8LL * D * N + (long long)sizeof(Phys);
   for (int f = 0; f < 2 * D; ++f)
-    if (p.bc_flags[f] == TX_BC_DENSITY) b += face_area(p, D, f) * S * 8;
+    if (face_has_values(p, D, f)) b += face_area(p, D, f) * S * D * 8;
   if (p.nspecies > 0) b += 2 * N * p.nspecies * Q * (long long)pop_bytes(p.precision) + (long long)sizeof(SpeciesPhysT<double>);
   return b;
 }
@@ -98,6 +99,13 @@ struct tx_batch {
   int2* d_ltiles = nullptr;  // the density pass's linear tiles
   int ltile_cap = 0;
   int* d_nltiles = nullptr;
+  int2* d_ftiles = nullptr;  // face-pass tiles
+  int ftile_cap = 0;
+  int* d_nftiles = nullptr;
+  int4* d_otiles = nullptr;  // outlet-refresh tiles
+  int otile_cap = 0;
+  int* d_notiles = nullptr;
+  bool need_faces = false, need_outlets = false;  // launched once a lattice needs them
   // launch shape
   int bx = 32, by = 4, bz = 1, blocks_per_sm = 4;
   // graph
@@ -171,6 +179,10 @@ BatchArgs bargs(const tx_batch* b) {
   a.parts = b->d_parts;
   a.ltiles = b->d_ltiles;
   a.nltiles = b->d_nltiles;
+  a.ftiles = b->d_ftiles;
+  a.nftiles = b->d_nftiles;
+  a.otiles = b->d_otiles;
+  a.notiles = b->d_notiles;
   return a;
 }
 
@@ -194,7 +206,8 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
 int rebuild_tables(tx_batch* b) {
   std::vector<LatDesc> descs;
   std::vector<int4> tiles;
-  std::vector<int2> ltiles;
+  std::vector<int2> ltiles, ftiles;
+  std::vector<int4> otiles;
   const long long run = 128LL * (long long)(16 / pop_bytes(b->form.precision));  // sites per density tile
   for (size_t s = 0; s < b->slots.size(); ++s) {
     Lattice* L = b->slots[s];
@@ -212,9 +225,20 @@ int rebuild_tables(tx_batch* b) {
     d.tile_count = (int)tiles.size() - d.tile_begin;
     d.ltile_begin = (int)ltiles.size();
     for (long long c0 = 0; c0 < L->g.n; c0 += run) ltiles.push_back(make_int2((int)s, (int)c0));
+    d.shell = L->shell;
+    d.c0 = L->ph.c0;
+    d.g21 = L->S > 1 ? L->p.g[1][0] : 0.0;
+    for (int f = 0; f < 6; ++f) d.outlet_p[f] = L->p.bc_data[f][0];
+    if (L->faces.post)
+      for (long long q0 = 0; q0 < L->shell.start[L->shell.nf]; q0 += 128) ftiles.push_back(make_int2((int)s, (int)q0));
+    if (has_outlet_update(L->p, L->D))
+      for (int f = 0; f < 2 * L->D; ++f)
+        if (L->p.bc_flags[f] == TX_BC_PRESSURE_OUTLET)
+          for (long long q0 = 0; q0 < face_area(L->p, L->D, f); q0 += 128) otiles.push_back(make_int4((int)s, f, (int)q0, 0));
     descs.push_back(d);
   }
   const int nl = (int)descs.size(), nt = (int)tiles.size(), nlt = (int)ltiles.size();
+  const int nft = (int)ftiles.size(), nov = (int)otiles.size();
   if (nl > b->lat_cap) {
     const int cap = std::max(nl, 2 * b->lat_cap);
     drop_graph(b);
@@ -240,6 +264,24 @@ int rebuild_tables(tx_batch* b) {
     TX_BCUDA(b, cudaMallocAsync(&b->d_ltiles, (size_t)cap * sizeof(int2), b->stream));
     b->ltile_cap = cap;
   }
+  if (nft > b->ftile_cap) {
+    const int cap = std::max(nft, 2 * b->ftile_cap);
+    drop_graph(b);
+    if (b->d_ftiles) cudaFreeAsync(b->d_ftiles, b->stream);
+    TX_BCUDA(b, cudaMallocAsync(&b->d_ftiles, (size_t)cap * sizeof(int2), b->stream));
+    b->ftile_cap = cap;
+  }
+  if (nov > b->otile_cap) {
+    const int cap = std::max(nov, 2 * b->otile_cap);
+    drop_graph(b);
+    if (b->d_otiles) cudaFreeAsync(b->d_otiles, b->stream);
+    TX_BCUDA(b, cudaMallocAsync(&b->d_otiles, (size_t)cap * sizeof(int4), b->stream));
+    b->otile_cap = cap;
+  }
+  if (nft) TX_BCUDA(b, cudaMemcpyAsync(b->d_ftiles, ftiles.data(), (size_t)nft * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+  if (nov) TX_BCUDA(b, cudaMemcpyAsync(b->d_otiles, otiles.data(), (size_t)nov * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+  TX_BCUDA(b, cudaMemcpyAsync(b->d_nftiles, &nft, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  TX_BCUDA(b, cudaMemcpyAsync(b->d_notiles, &nov, sizeof(int), cudaMemcpyHostToDevice, b->stream));
   if (nl) TX_BCUDA(b, cudaMemcpyAsync(b->d_lats, descs.data(), (size_t)nl * sizeof(LatDesc), cudaMemcpyHostToDevice, b->stream));
   if (nlt) TX_BCUDA(b, cudaMemcpyAsync(b->d_ltiles, ltiles.data(), (size_t)nlt * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   TX_BCUDA(b, cudaMemcpyAsync(b->d_nltiles, &nlt, sizeof(int), cudaMemcpyHostToDevice, b->stream));
@@ -254,8 +296,10 @@ int rebuild_tables(tx_batch* b) {
 int launch_step(tx_batch* b, int flip) {
   const dim3 blk((unsigned)b->bx, (unsigned)b->by, (unsigned)b->bz);
   const BatchArgs a = bargs(b);
+  if (b->need_outlets) b->ks.outlet_tiles(a, flip, grid_of(b), blk, b->stream);
   b->ks.step_tiles(a, flip, grid_of(b), blk, b->stream);
   b->ks.density_tiles(a, flip, grid_of(b), blk, b->stream);
+  if (b->need_faces) b->ks.faces_tiles(a, flip, grid_of(b), blk, b->stream);
   if (b->form.nspecies > 0) b->ss.step_tiles(a, flip, grid_of(b), blk, b->stream);
   TX_BCUDA(b, cudaGetLastError());
   return TX_OK;
@@ -376,13 +420,16 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&b->d_ntiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_nltiles, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&b->d_ntiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_nltiles, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&b->d_nftiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_notiles, sizeof(int)) != cudaSuccess) {
     tx::set_global_error("CUDA device setup failed");
     tx_batch_destroy(b);
     return TX_ERR_NODEVICE;
   }
   cudaMemset(b->d_ntiles, 0, sizeof(int));
   cudaMemset(b->d_nltiles, 0, sizeof(int));
+  cudaMemset(b->d_nftiles, 0, sizeof(int));
+  cudaMemset(b->d_notiles, 0, sizeof(int));
   *out = b;
   return TX_OK;
 }
@@ -393,11 +440,14 @@ int tx_batch_destroy(tx_batch* b) {
   drop_graph(b);
   for (Lattice* L : b->slots) free_lattice(b, L);
   b->slots.clear();
-  for (void* p : {(void*)b->d_lats, (void*)b->d_tiles, (void*)b->d_parts, (void*)b->d_res, (void*)b->d_ltiles})
+  for (void* p : {(void*)b->d_lats, (void*)b->d_tiles, (void*)b->d_parts, (void*)b->d_res, (void*)b->d_ltiles,
+                 (void*)b->d_ftiles, (void*)b->d_otiles})
     if (p) cudaFreeAsync(p, b->stream);
   if (b->stream) cudaStreamSynchronize(b->stream);
   cudaFree(b->d_ntiles);
   cudaFree(b->d_nltiles);
+  cudaFree(b->d_nftiles);
+  cudaFree(b->d_notiles);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return TX_OK;
@@ -417,8 +467,6 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   std::string why;
   int rc = tx::validate(p, &why);
   if (rc) return bfail(b, rc, why);
-  if (!faces_plain(*p, p->discretization == TX_D3Q19 ? 3 : 2))
-    return bfail(b, TX_ERR_ARG, "batched lattices run periodic, closed and density faces; other BCs run on handles");
   const tx_params& f = b->form;
   if (p->discretization != f.discretization || p->ncomponents != f.ncomponents ||
       p->relaxation_mode != f.relaxation_mode || p->isotropy_order != f.isotropy_order ||
@@ -503,12 +551,15 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   TX_BALLOC(L->steps_dev, sizeof(unsigned));
   TX_BALLOC(L->phys, physb);
   setup_faces(*p, D, &L->faces);
+  L->shell = face_shell(*p, D, L->g.nx, L->g.ny, L->g.nz);
   for (int fc = 0; fc < 2 * D; ++fc) {
-    if (p->bc_flags[fc] != TX_BC_DENSITY) continue;
+    if (!face_has_values(*p, D, fc)) continue;
     const long long area = face_area(*p, D, fc);
-    std::vector<double> v((size_t)area * S);
-    for (int m = 0; m < S; ++m)
-      for (long long q = 0; q < area; ++q) v[(size_t)(m * area + q)] = p->bc_data[fc][m];
+    double nv[3 * TX_MAX_COMPONENTS];
+    face_node_values(*p, D, fc, L->ph.c0, nv);
+    std::vector<double> v((size_t)area * S * D);
+    for (int k = 0; k < S * D; ++k)
+      for (long long q = 0; q < area; ++q) v[(size_t)(k * area + q)] = nv[k];
     TX_BALLOC(L->faceval[fc], v.size() * sizeof(double));
     if (cudaMemcpyAsync(L->faceval[fc], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
@@ -587,6 +638,12 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   b->in_use += bytes;
   L->id = b->next_id++;
   b->slots.push_back(L);
+  // the face pass and the outlet refresh join the step (and its graph) with
+  // the first lattice that needs them, and stay
+  const bool nf = b->need_faces || L->faces.post, no = b->need_outlets || has_outlet_update(*p, D);
+  if (nf != b->need_faces || no != b->need_outlets) drop_graph(b);
+  b->need_faces = nf;
+  b->need_outlets = no;
   rc = rebuild_tables(b);
   if (rc) return rc;
   *id = L->id;

@@ -30,6 +30,11 @@ struct LatDesc {
   int tile_begin;     // this lattice's tiles in the table
   int tile_count;
   int ltile_begin;    // its first tile of the density pass's linear table
+  // exterior faces beyond Dirichlet ones: the face nodes of the face pass, and
+  // the pressure of each two-component pressure outlet (c0, g21 of its update)
+  FaceShell shell;
+  double outlet_p[6];
+  double c0, g21;
   // passive species: populations at flip 0 / the other buffer, parameters
   const void* sg0;
   void* sg1;
@@ -52,6 +57,10 @@ struct BatchArgs {
   ProbePart* parts;   // [tile]
   const int2* ltiles; // density pass: (lattice slot, first site) of runs of 128 x VW sites
   const int* nltiles;
+  const int2* ftiles; // face pass: (lattice slot, first shell node) of runs of 128 face nodes
+  const int* nftiles;
+  const int4* otiles; // outlet refresh: (lattice slot, face, first node, 0) of runs of 128 nodes
+  const int* notiles;
 };
 
 __device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
@@ -96,6 +105,35 @@ __global__ void __launch_bounds__(128) k_density_tiles(BatchArgs b, int flip) {
     // the lattice's step counter advances once per step (the step kernel of
     // this step has finished reading it; the next one reads the new value)
     if (t == b.lats[tl.x].ltile_begin && lane == 0 && a.steps_ptr) atomicAdd(const_cast<unsigned*>(a.steps_ptr), 1u);
+  }
+}
+
+// Face pass after k_density_tiles at the same flip (lattices whose faces are
+// not all of the Dirichlet class): face_site at each face node.
+template <int D, int S, int ISO, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_faces_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.nftiles);
+  const int lane = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int2 tl = __ldg(b.ftiles + t);
+    const LatDesc& L = b.lats[tl.x];
+    const StepArgs a = flipped(L.a, flip);
+    int x, y, z;
+    if (shell_site<D>(a.g, L.shell, (long long)tl.y + lane, x, y, z)) face_site<D, S, ISO, false, T, R, RT>(a, x, y, z);
+  }
+}
+
+// Two-component pressure outlets, before k_step_tiles at the same flip.
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_outlet_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.notiles);
+  const int lane = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.otiles + t);
+    const LatDesc& L = b.lats[tl.x];
+    const StepArgs a = flipped(L.a, flip);
+    outlet_node<D, S, T, R, RT>(a, tl.y, const_cast<double*>(a.faces.vals[tl.y]), L.outlet_p[tl.y], L.c0, L.g21,
+                                (long long)tl.z + lane);
   }
 }
 

@@ -26,6 +26,9 @@ struct KernelSet {
   // per-step refresh of one two-component pressure-outlet face before k_step
   void (*faces)(const StepArgs&, const FaceShell&, cudaStream_t);
   void (*outlet)(const StepArgs&, int face, double* vals, double pressure, double c0, double g21, cudaStream_t);
+  // their batched forms (no-ops in the exact form)
+  void (*faces_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
+  void (*outlet_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   const char* name;
 };
 
@@ -126,6 +129,12 @@ inline Launch3 launch3(const Geo& g, int threads) {
       const long long n = face_area_of(D, a.g.nx, a.g.ny, a.g.nz, f);                                         \
       k_outlet<D, S, T, R, RT><<<grid_for(n, 128), 128, 0, s>>>(a, f, v, p, c0, g21);                         \
     }                                                                                                         \
+    static void faces_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {               \
+      if constexpr (!EXACT) k_faces_tiles<D, S, ISO, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                 \
+    }                                                                                                         \
+    static void outlet_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {              \
+      if constexpr (!EXACT) k_outlet_tiles<D, S, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                     \
+    }                                                                                                         \
   };
 
 #define TX_FORM_CASE(S, ISO, MRT) TX_FORM_CASE_(S, ISO, MRT)
@@ -136,7 +145,8 @@ inline Launch3 launch3(const Geo& g, int threads) {
                     &L_##S##_##ISO##_##MRT::to_nat, &L_##S##_##ISO##_##MRT::from_nat,                          \
                     &L_##S##_##ISO##_##MRT::step_tiles, &L_##S##_##ISO##_##MRT::density_tiles,                 \
                     &L_##S##_##ISO##_##MRT::probe_tiles, &L_##S##_##ISO##_##MRT::faces,                        \
-                    &L_##S##_##ISO##_##MRT::outlet,                                                               \
+                    &L_##S##_##ISO##_##MRT::outlet, &L_##S##_##ISO##_##MRT::faces_tiles,                          \
+                    &L_##S##_##ISO##_##MRT::outlet_tiles,                                                         \
                     MRT ? #S "c iso" #ISO " rates:any" : #S "c iso" #ISO " rates:bgk/s_nu"};                    \
     return true;                                                                                               \
   }

@@ -1764,12 +1764,10 @@ __global__ void __launch_bounds__(128) k_faces(StepArgs a_in, FaceShell sh) {
 // step's: the population sum on re-summed face nodes, the forcing density
 // elsewhere.  Reads the state (fin) and the forcing density; writes face f.
 template <int D, int S, class T, class R, class RT>
-__global__ void __launch_bounds__(128) k_outlet(StepArgs a_in, int f, double* vals, double pressure, double c0,
-                                                double g21) {
-  const StepArgs a = a_in;
+__device__ __forceinline__ void outlet_node(const StepArgs& a, int f, double* vals, double pressure, double c0,
+                                            double g21, long long q) {
   const PhysT<R>& P = *reinterpret_cast<const PhysT<R>*>(a.phys);
   const long long area = face_area<D>(a.g, f);
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= area) return;
   const int ax = f >> 1;
   const int ext = ax == 0 ? a.g.nx : (ax == 1 ? a.g.ny : a.g.nz);
@@ -1819,6 +1817,13 @@ __global__ void __launch_bounds__(128) k_outlet(StepArgs a_in, int f, double* va
   density_from_pressure(S, c0, g21, pressure, r[0] / tot, out);
   vals[q] = out[0];
   if (S > 1) vals[area + q] = out[1];
+}
+
+template <int D, int S, class T, class R, class RT>
+__global__ void __launch_bounds__(128) k_outlet(StepArgs a_in, int f, double* vals, double pressure, double c0,
+                                                double g21) {
+  const StepArgs a = a_in;
+  outlet_node<D, S, T, R, RT>(a, f, vals, pressure, c0, g21, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // -------------------------------------------------------------------- init

@@ -92,9 +92,43 @@ def test_bc_errors_are_status_codes():
     h = Handle(p)
     with pytest.raises(TxError):
         h.upload_bc_values(P.XM, np.zeros(p.ny * p.nz))
-    # batches run plain faces only
-    q = P.copy_params(p)
-    q.precision = P.PREC_F32
-    b = Batch(q)
-    with pytest.raises(TxError):
-        b.add(q, walls, rho)
+
+
+def _alone(p, walls, rho, steps):
+    h = Handle(p)
+    h.upload_walls(walls)
+    h.upload_state(rho)
+    h.init()
+    h.step(steps)
+    return h
+
+
+@pytest.mark.parametrize("names", [["d3_pressure_s1", "d3_reflect_momentum", "d3_neumann_then_dirichlet"],
+                                   ["d3_two_phase_pressure"]], ids=["one_component", "two_component_outlet"])
+@pytest.mark.parametrize("prec", [P.PREC_F64, P.PREC_F32_F16], ids=["f64", "f16"])
+def test_exterior_bcs_in_a_batch_equal_alone(names, prec):
+    # face pass and outlet refresh as batched tile kernels: each lattice as alone,
+    # bit for bit, including one that joins a running batch
+    mk = {n: m for n, m, _ in cases.BCS}
+    lats = []
+    for n in names:
+        p, w, r = mk[n]()
+        q = P.copy_params(p)
+        q.exact = 0
+        q.precision = prec
+        if prec != P.PREC_F64:
+            q.rho0[0] = 1.0
+            q.storage_scale = 4096.0
+        lats.append((q, w, r))
+    b = Batch(lats[0][0])
+    ids = [b.add(q, w, r) for q, w, r in lats]
+    b.step(23)
+    late = mk[names[0]]()
+    ql = P.copy_params(lats[0][0])
+    il = b.add(ql, late[1], late[2])
+    b.step(9)
+    for (q, w, r), lid, steps in list(zip(lats, ids, [32] * len(ids))) + [((ql, late[1], late[2]), il, 9)]:
+        h = _alone(q, w, r, steps)
+        n = q.nsites * q.ncomponents * q.Q
+        assert np.array_equal(b.download(lid, P.FIELD_FI, n), h.download(P.FIELD_FI))
+        assert np.array_equal(b.download(lid, P.FIELD_RHO, q.nsites * q.ncomponents), h.download(P.FIELD_RHO))
