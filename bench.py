@@ -366,10 +366,12 @@ def batched_run(n_lat=96, steps=40, seed=4, compare=8, sides=(48, 192)):
     for h in handles:
         h.close()
     mlups = sites * steps / (ms * 1e-3) / 1e6
+    fluid = sum(int(np.count_nonzero(np.asarray(r.walls) == 0)) for r in reqs)
     bpl = 2 * 19 * 4 + 1 + 19 * 4 + 4  # collide-push read+write, mask; density read + write
     return {"workload": "%d single-phase D3Q19 BGK sphere packs, sides %d-%d per axis (%d sites), FP32 form, "
                         "body force 1e-6, periodic" % (n_lat, sides[0], sides[1], sites),
             "steps": steps, "ms_per_step": round(ms / steps, 4), "mlups": round(mlups, 1),
+            "mflups_fluid_sites": round(fluid * steps / (ms * 1e-3) / 1e6, 1),
             "gbs_algorithmic": round(mlups * 1e6 * bpl / 1e9, 1), "bytes_per_lup": bpl,
             "tiles": {"bx": tiles[0], "by": tiles[1], "bz": tiles[2], "blocks_per_sm": tiles[3]},
             "graph_steps": 20, "finite": finite,
@@ -508,6 +510,14 @@ def run_gpu(args):
             except Exception as ex:
                 forms[name] = {"error": str(ex)}
         line["precision_forms"] = forms
+        try:
+            # the same workload with the isotropy-8 psi gradient (the higher-order variant)
+            q8 = workload_params(P.PREC_F64)
+            q8.isotropy_order = 8
+            r = measure_form(P.PREC_F64, max(20, args.steps // 4), args.warmup, p=q8)
+            line["fp64_iso8"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
+        except Exception as ex:
+            line["fp64_iso8"] = {"error": str(ex)}
         legs = (("batched", batched_run),
                 ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
                 ("serving", serving_run))
