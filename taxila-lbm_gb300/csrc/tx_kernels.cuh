@@ -389,6 +389,12 @@ __host__ __device__ constexpr uint32_t all_links() {
   return ((1u << Lat<D>::Q) - 1u) & ~1u;
 }
 
+// Link-mask bits above the links: every site of the box of reach 2 (3)
+// around the site is pore space inside the lattice or across a periodic face,
+// so that the isotropy-8 (-10) gradient stencil sees only pore neighbours.
+constexpr uint32_t kBoxPore2 = 1u << 31;
+constexpr uint32_t kBoxPore3 = 1u << 30;
+
 // pore test of the site at offset (dx, dy, dz): a link bit for lattice links,
 // the wall mask for the longer stencil offsets
 template <int D, int RCH, int dx, int dy, int dz>
@@ -644,10 +650,14 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
       mult[m] = rf[m];
     }
   }
-  if constexpr (!EXACT && stencil_is_links<D, ISO>()) {
+  if constexpr (!EXACT) {
     // every stencil neighbour pore: the weight sums are constant and the
     // psi(x) terms cancel, so grad = sum_k w_k e_k psi(x + e_k)
-    if ((links | 1u) == (all_links<D>() | 1u)) {
+    constexpr int RB = stencil_reach<D, ISO>();
+    const bool bulk = stencil_is_links<D, ISO>() ? ((links | 1u) & (all_links<D>() | 1u)) == (all_links<D>() | 1u)
+                      : RB == 2                ? (links & kBoxPore2) != 0u
+                                               : (links & kBoxPore3) != 0u;
+    if (bulk) {
       // opposite stencil terms pair up: w e (psi(x + e) - psi(x - e))
       static_assert(stencil_symmetric<D, ISO>(), "every stencil term needs its opposite");
       R gr[S][D];
@@ -1279,6 +1289,24 @@ __global__ void __launch_bounds__(256) k_links(const uint8_t* mask, Geo g, uint3
     const bool pore = __ldg(mask + h.template at<cx, cy, cz>()) == 0;
     b |= (in & pore) ? (1u << n) : 0u;
   });
+  // the whole box of reach 2 (and, in 2D, 3) pore: the bulk gradient of isotropy 8 (10)
+  if (b & 1u) {
+    const Hood<D, 3> h3(g, x, y, z);
+    bool box2 = true, box3 = true;
+    constexpr int RZ = D == 3 ? 2 : 0;
+    for (int dz = -RZ; dz <= RZ; ++dz)
+      for (int dy = -3; dy <= 3; ++dy)
+        for (int dx = -3; dx <= 3; ++dx) {
+          const bool in = ((h3.in_x >> (dx + 3)) & (h3.in_y >> (dy + 3)) & (h3.in_z >> (dz + (D == 3 ? 3 : 0))) & 1u) != 0u;
+          const unsigned off = (unsigned)(h3.ox[dx + 3] + h3.oy[dy + 3] + h3.oz[dz + (D == 3 ? 3 : 0)]);
+          const bool ok = in && __ldg(mask + off) == 0;
+          const bool r2 = dx >= -2 && dx <= 2 && dy >= -2 && dy <= 2;
+          if (r2) box2 = box2 && ok;
+          if (D == 2) box3 = box3 && ok;
+        }
+    if (box2) b |= kBoxPore2;
+    if (D == 2 && box3) b |= kBoxPore3;
+  }
   links[idx] = b;
 }
 
