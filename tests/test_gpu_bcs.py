@@ -132,3 +132,11 @@ def test_exterior_bcs_in_a_batch_equal_alone(names, prec):
         n = q.nsites * q.ncomponents * q.Q
         assert np.array_equal(b.download(lid, P.FIELD_FI, n), h.download(P.FIELD_FI))
         assert np.array_equal(b.download(lid, P.FIELD_RHO, q.nsites * q.ncomponents), h.download(P.FIELD_RHO))
+
+
+@pytest.mark.parametrize("name", ["d3_two_phase_pressure", "d3_flux_velocity_mrt", "d2_velocity_outlet"])
+def test_fast_form_1000_steps_with_exterior_bcs(name):
+    # the stated tolerance (1e-12 relative after 1,000 steps) through driven faces
+    p, walls, rho = next(m for n, m, _ in cases.BCS if n == name)()
+    o, h = run_both(p, walls, rho, 1000, False)
+    check(o, h, walls, False)

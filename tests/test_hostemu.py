@@ -224,3 +224,17 @@ def test_emulated_exterior_bcs_reduced_precision(emu_exe, tmp_path, name, prec, 
     tol = 1e-5 if prec == P.PREC_F32 else 2e-3
     errs = compare(ref, got, p, walls, {"fi": tol, "rho": tol, "flux": 50 * tol, "forces": 50 * tol})
     print(name, prec, errs)
+
+
+@pytest.mark.parametrize("name", ["d3_two_phase_pressure", "d3_flux_velocity_mrt"])
+def test_emulated_exterior_bcs_fast_form_1000_steps(emu_exe, tmp_path, name):
+    # the fast form's tolerance is stated after 1,000 steps; driven flows through
+    # pressure, flux and velocity faces hold it too
+    make = next(m for n, m, _ in cases.BCS if n == name)
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, 1000)
+    q = P.copy_params(p)
+    q.exact = 0
+    got = run_emu(emu_exe, q, walls, rho, 1000, False, tmp_path)
+    errs = compare(ref, got, p, walls, 1e-12)
+    print(name, errs)
