@@ -321,13 +321,6 @@ inline FaceShell face_shell(const tx_params& p, int D, int nx, int ny, int nz) {
   return sh;
 }
 
-// Only periodic, closed and density faces (what batches and the
-// allocation-free step run).
-inline bool faces_plain(const tx_params& p, int D) {
-  for (int f = 0; f < 2 * D; ++f) {
-    const int v = p.bc_flags[f];
-    if (v != TX_BC_NULL && v != TX_BC_PERIODIC && v != TX_BC_DENSITY) return false;
-  }
   return true;
 }
 

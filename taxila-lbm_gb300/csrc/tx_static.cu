@@ -91,8 +91,6 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   if (rc) return static_fail(rc, why);
   if (p->precision != TX_PREC_F64) return static_fail(TX_ERR_ARG, "tx_step_static runs the FP64 form only");
   if (p->nspecies != 0) return static_fail(TX_ERR_ARG, "tx_step_static runs the flow only (nspecies must be 0)");
-  if (!faces_plain(*p, p->discretization == TX_D3Q19 ? 3 : 2))
-    return static_fail(TX_ERR_ARG, "tx_step_static runs periodic, closed and density faces only");
   KernelSet ks{};
   if (!select_kernels(p, &ks)) return static_fail(TX_ERR_ARG, "no kernel built for this parameter combination");
 
@@ -108,12 +106,8 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
 
   // carve the scratch array: parameters | mask | links | rho | face values | populations A | populations B | flag
   long long area[6] = {0, 0, 0, 0, 0, 0};
-  for (int f = 0; f < 2 * D; ++f) {
-    if (p->bc_flags[f] != TX_BC_DENSITY) continue;
-    const int a = f / 2;
-    area[f] = D == 2 ? (a == 0 ? g.ny : g.nx)
-                     : (a == 0 ? (long long)g.ny * g.nz : a == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny);
-  }
+  for (int f = 0; f < 2 * D; ++f)
+    if (face_has_values(*p, D, f)) area[f] = face_area_of(D, g.nx, g.ny, g.nz, f);
   size_t off = 0;
   const size_t o_phys = off;
   off = align256(off + sizeof(Phys));
@@ -128,7 +122,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   size_t o_face[6];
   for (int f = 0; f < 6; ++f) {
     o_face[f] = off;
-    off = align256(off + (size_t)area[f] * S * sizeof(double));
+    off = align256(off + (size_t)area[f] * S * D * sizeof(double));
   }
   const size_t pop_bytes = (size_t)N * S * Q * sizeof(double);
   const size_t o_pa = off;
@@ -193,7 +187,10 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   for (int f = 0; f < 2 * D; ++f) {
     if (!area[f]) continue;
     double* v = (double*)(base + o_face[f]);
-    for (int m = 0; m < S; ++m) k_static_fill<<<grid_for(area[f], 256), 256, 0, st>>>(v + (long long)m * area[f], area[f], p->bc_data[f][m]);
+    double nv[3 * TX_MAX_COMPONENTS];
+    face_node_values(*p, D, f, ph.c0, nv);
+    for (int k = 0; k < S * D; ++k)
+      k_static_fill<<<grid_for(area[f], 256), 256, 0, st>>>(v + (long long)k * area[f], area[f], nv[k]);
     faces.vals[f] = v;
   }
   TX_SCHK(cudaGetLastError());
@@ -213,11 +210,18 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   ks.density(a, 1, st);
   double* cur = pa;
   double* nxt = pb;
+  const FaceShell shell = face_shell(*p, D, g.nx, g.ny, g.nz);
+  const bool outlet = has_outlet_update(*p, D);
   for (int t = 0; t < nsteps; ++t) {
     a.fin = cur;
     a.fout = nxt;
+    if (outlet)
+      for (int f = 0; f < 2 * D; ++f)
+        if (p->bc_flags[f] == TX_BC_PRESSURE_OUTLET)
+          ks.outlet(a, f, (double*)(base + o_face[f]), p->bc_data[f][0], ph.c0, p->g[1][0], st);
     ks.step(a, st);
     ks.density(a, 0, st);
+    if (faces.post) ks.faces(a, shell, st);
     double* tmp = cur;
     cur = nxt;
     nxt = tmp;

@@ -63,6 +63,26 @@ def test_static_step_matches_handle_twice():
     assert np.all(out2[~pore] == 0.0)
 
 
+@pytest.mark.parametrize("name", ["d3_two_phase_pressure", "d3_reflect_momentum", "d2_velocity_outlet"])
+def test_static_step_with_exterior_bcs(name):
+    # outlet refresh and face pass in the allocation-free step
+    import torch
+    p, walls, rho = next(m for n, m, _ in cases.BCS if n == name)()
+    h0 = Handle(p)
+    h0.upload_walls(walls)
+    h0.upload_state(rho)
+    h0.init()
+    h0.step(2)
+    fi0 = h0.download(P.FIELD_FI)
+    h0.close()
+    pore = np.repeat(np.asarray(walls) == 0, p.ncomponents * p.Q)
+    d_walls = torch.tensor(walls, dtype=torch.float64, device="cuda")
+    d_in = torch.tensor(fi0, dtype=torch.float64, device="cuda")
+    d_out = torch.empty_like(d_in)
+    step_static(p, d_walls.data_ptr(), d_in.data_ptr(), d_out.data_ptr(), 6)
+    assert np.array_equal(handle_path(p, walls, fi0, 6)[pore], d_out.cpu().numpy()[pore])
+
+
 def test_static_step_rejects_lattices_beyond_the_static_area():
     import torch
     p = cases.base(P.D3Q19, (64, 64, 64))
