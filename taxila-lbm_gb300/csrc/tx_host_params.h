@@ -321,9 +321,6 @@ inline FaceShell face_shell(const tx_params& p, int D, int nx, int ny, int nz) {
   return sh;
 }
 
-  return true;
-}
-
 // Species relaxation (SpecieSetFromOptions, lbm_species.F90:111-133; the
 // MRT rate map of DiscretizationSetupRelax) and the fast form's base rate.
 inline void fill_species_phys(const tx_params& p, int D, SpeciesPhysT<double>& P) {
