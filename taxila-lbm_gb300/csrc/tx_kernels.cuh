@@ -1886,7 +1886,7 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
       u[d] = uic ? R(uic[(long long)(m * D + d) * N + idx]) : R(0);
       usqr = usqr + u[d] * u[d];
     }
-    if constexpr (!kShifted<T>) {
+    if constexpr (EXACT) {
       sfor<0, Q>([&](auto nn) {
         constexpr int n = decltype(nn)::value;
         R feq, pf;
@@ -1894,7 +1894,8 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
         St<T>::st(fout + (long long)(m * Q + n) * N + idx, (R(1.) - R(0.5) * pf) * feq);
       });
     } else {
-      // the deviation (1 - P/2) feq - w rho0 = dE_n - 1.5 E_n (F.c_n - F.u), as in step_site
+      // the fast forms: the deviation (1 - P/2) feq - w rho0 = dE_n - 1.5 E_n (F.c_n - F.u), as in
+      // step_site (rho0 = 0 and the deviation is f itself in the FP64 form)
       const R A0 = P.A0[m], An = P.An[m];
       R Fu = R(0);
 #pragma unroll
