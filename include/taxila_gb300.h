@@ -215,6 +215,16 @@ int tx_step(tx_handle* h, int32_t nsteps);
  * is 0 contribute 0.  FP64 device reduction. */
 int tx_delta_norm(tx_handle* h, int32_t field, double* norm);
 
+/* No counterpart in the reference, whose step keeps no conservation totals.
+ * Global mass and momentum of the current state, summed over all sites in
+ * FP64 on the device from the populations (the precision forms add their rest
+ * state back first): out[m] = sum of f(m, n) over sites and directions, and
+ * out[s + m*ndims + d] = sum of f(m, n) * c_n[d], for m < s, d < ndims
+ * (s + s*ndims doubles).  The order of summation is fixed, so repeated calls
+ * on the same state return the same bits.  Non-finite totals return
+ * TX_ERR_NONFINITE. */
+int tx_conservation(tx_handle* h, double* out);
+
 /* Copy a field to a host array in natural order (see TX_FIELD_*). */
 int tx_download(tx_handle* h, int32_t field, double* out);
 

@@ -43,6 +43,7 @@ struct tx_handle {
   double* old_fi = nullptr;
   double* uic = nullptr;
   unsigned long long* red = nullptr;  // [0] max bits, [1] non-finite count
+  double* cons = nullptr;     // conservation-sum partials and per-population totals (first tx_conservation)
   std::vector<uint8_t> host_mask;
   // passive species (transport): populations, parameters, initial state
   int NS = 0;
@@ -160,6 +161,34 @@ __global__ void k_delta_norm(const double* cur, double* old, long long n, unsign
     if (bad) atomicAdd(&red[1], bad);
   }
 }
+
+// Conservation sums, first pass.  Thread t < span adds the elements t,
+// t + span, t + 2 span, ... of a natural-order field of n elements in FP64.
+// span is a multiple of the field's dof, so every element a thread visits is
+// the same degree of freedom (t mod dof), and consecutive threads read
+// consecutive elements.
+__global__ void k_dof_partials(const double* x, long long n, long long span, double* part) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= span) return;
+  double s = 0.0;
+  for (long long e = t; e < n; e += span) s += x[e];
+  part[t] = s;
+}
+
+// Second pass: one warp per degree of freedom k sums part[k + dof * j] over
+// j < span / dof, lane l taking j = l, l + 32, ...; the lanes combine by a
+// fixed xor-shuffle tree, so the sum is the same on every run.
+__global__ void k_dof_reduce(const double* part, long long span, int dof, double* sums) {
+  const int k = blockIdx.x, lane = threadIdx.x;
+  const long long per = span / dof;
+  double s = 0.0;
+  for (long long j = lane; j < per; j += 32) s += part[k + (long long)dof * j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) sums[k] = s;
+}
+
+constexpr int kConsBlocks = 304, kConsThreads = 256;
+constexpr long long kConsSpanMax = (long long)kConsBlocks * kConsThreads;
 
 int sync_stream(tx_handle* h) {
   TX_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -377,6 +406,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->old_fi);
   cudaFree(h->uic);
   cudaFree(h->red);
+  cudaFree(h->cons);
   cudaFree(h->d_phys);
   cudaFree(h->d_phys32);
   for (int f = 0; f < 6; ++f) cudaFree(h->faceval[f]);
@@ -625,6 +655,47 @@ int tx_delta_norm(tx_handle* h, int32_t field, double* norm) {
   std::memcpy(&v, &r[0], sizeof(v));
   *norm = v;
   if (r[1]) return fail(h, TX_ERR_NONFINITE, "non-finite values in the field (" + std::to_string(r[1]) + " sites)");
+  return TX_OK;
+}
+
+int tx_conservation(tx_handle* h, double* out) {
+  if (!h || !out) return TX_ERR_ARG;
+  if (!h->inited) return fail(h, TX_ERR_STATE, "tx_init must come before tx_conservation");
+  const int dof = h->S * h->Q;
+  const long long n = h->g.n * dof;
+  const long long span = (kConsSpanMax / dof) * dof;
+  if (!h->cons) TX_CUDA(h, cudaMalloc(&h->cons, (size_t)(kConsSpanMax + 128) * sizeof(double)));
+  int rc = stage_field(h, TX_FIELD_FI);
+  if (rc) return rc;
+  double* sums_d = h->cons + kConsSpanMax;
+  k_dof_partials<<<kConsBlocks, kConsThreads, 0, h->stream>>>(h->stage, n, span, h->cons);
+  rc = check_launch(h, "k_dof_partials");
+  if (rc) return rc;
+  k_dof_reduce<<<dof, 32, 0, h->stream>>>(h->cons, span, dof, sums_d);
+  rc = check_launch(h, "k_dof_reduce");
+  if (rc) return rc;
+  double sums[TX_MAX_COMPONENTS * 19];
+  TX_CUDA(h, cudaMemcpyAsync(sums, sums_d, (size_t)dof * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  rc = sync_stream(h);
+  if (rc) return rc;
+  // natural order: population n of component m is dof n * S + m
+  bool finite = true;
+  for (int m = 0; m < h->S; ++m) {
+    double mass = 0.0;
+    for (int q = 0; q < h->Q; ++q) mass += sums[q * h->S + m];
+    out[m] = mass;
+    finite = finite && std::isfinite(mass);
+    for (int d = 0; d < h->D; ++d) {
+      double mom = 0.0;
+      for (int q = 0; q < h->Q; ++q) {
+        const int c = h->D == 3 ? Lat<3>::c(q, d) : Lat<2>::c(q, d);
+        if (c) mom += c * sums[q * h->S + m];
+      }
+      out[h->S + m * h->D + d] = mom;
+      finite = finite && std::isfinite(mom);
+    }
+  }
+  if (!finite) return fail(h, TX_ERR_NONFINITE, "non-finite populations in the conservation sums");
   return TX_OK;
 }
 

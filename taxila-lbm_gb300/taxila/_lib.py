@@ -52,6 +52,7 @@ def load():
         "tx_step": ([vp, i32], C.c_int),
         "tx_delta_norm": ([vp, i32, dp], C.c_int),
         "tx_download": ([vp, i32, dp], C.c_int),
+        "tx_conservation": ([vp, dp], C.c_int),
         "tx_field_size": ([vp, i32], i64),
         "tx_sync": ([vp], C.c_int),
         "tx_set_timing": ([vp, i32], C.c_int),
@@ -172,6 +173,13 @@ class Handle:
         v = C.c_double()
         self._check(self.L.tx_delta_norm(self.h, int(field), C.byref(v)))
         return v.value
+
+    def conservation(self):
+        """Global (mass[s], momentum[s][ndims]) of the current state, FP64 sums on the device."""
+        s, d = self.p.ncomponents, self.p.ndims
+        out = np.empty(s + s * d, dtype=np.float64)
+        self._check(self.L.tx_conservation(self.h, dptr(out)))
+        return out[:s].copy(), out[s:].reshape(s, d).copy()
 
     def set_timing(self, on=True):
         self._check(self.L.tx_set_timing(self.h, 1 if on else 0))
