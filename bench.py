@@ -410,6 +410,14 @@ def serving_run(n=30, rate=30.0, seed=1):
     return out
 
 
+def conservation_mass(h):
+    """Each component's mass from tx_conservation, or the error text."""
+    try:
+        return [float(v) for v in h.conservation()[0]]
+    except Exception as ex:  # report, do not hide
+        return "tx_conservation: %s" % ex
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -428,6 +436,7 @@ def run_gpu(args):
     h.upload_walls(walls)
     h.upload_state(rho)
     h.init()
+    mass0 = conservation_mass(h)
     h.step(args.warmup)
     h.sync()
     stream = torch.cuda.ExternalStream(h.stream())
@@ -450,6 +459,7 @@ def run_gpu(args):
     t_step, t_dens, _ = h.timing()
     h.set_timing(False)
     rho_check = h.delta_norm(P.FIELD_RHO)  # non-finite states raise here
+    mass1 = conservation_mass(h)
     kname = h.kernel_name()
     h.close()
     if rank != 0:
@@ -535,6 +545,13 @@ def run_gpu(args):
         except Exception as ex:
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": str(ex)}
     line["state_check"] = {"rho_delta_norm_last": rho_check}
+    if isinstance(mass0, list) and isinstance(mass1, list):
+        # each component's mass (FP64 device sums) after init and after every step of this run
+        line["state_check"]["mass_after_init"] = mass0
+        line["state_check"]["mass_at_end"] = mass1
+        line["state_check"]["mass_rel_drift"] = [abs(b / a - 1.0) if a else None for a, b in zip(mass0, mass1)]
+    else:
+        line["state_check"]["mass_error"] = str(mass0 if not isinstance(mass0, list) else mass1)
     print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
