@@ -471,7 +471,9 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
     for (long long i = 0; i < N; ++i)
       for (int d = 0; d < D; ++d)
         for (int m = 0; m < S; ++m) ut[((size_t)(m * D + d)) * N + i] = u[(i * D + d) * S + m];
-    TX_CUDA(h, cudaMalloc(&h->uic, ut.size() * sizeof(double)));
+    double* fresh = nullptr;  // the handle keeps the pointer only once the allocation succeeded
+    TX_CUDA(h, cudaMalloc(&fresh, ut.size() * sizeof(double)));
+    h->uic = fresh;
     TX_CUDA(h, cudaMemcpy(h->uic, ut.data(), ut.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   h->have_state = true;
@@ -485,12 +487,18 @@ int tx_upload_species(tx_handle* h, const double* conc, const double* flux) {
   if (h->NS == 0) return fail(h, TX_ERR_STATE, "the handle was created with nspecies = 0");
   const long long N = h->g.n;
   const size_t cb = (size_t)N * h->NS * sizeof(double), fb = cb * h->D;
-  if (!h->sconc) TX_CUDA(h, cudaMalloc(&h->sconc, cb));
+  if (!h->sconc) {
+    double* fresh = nullptr;  // the handle keeps the pointer only once the allocation succeeded
+    TX_CUDA(h, cudaMalloc(&fresh, cb));
+    h->sconc = fresh;
+  }
   TX_CUDA(h, cudaMemcpyAsync(h->sconc, conc, cb, cudaMemcpyHostToDevice, h->stream));
   cudaFree(h->sflux);
   h->sflux = nullptr;
   if (flux) {
-    TX_CUDA(h, cudaMalloc(&h->sflux, fb));
+    double* fresh = nullptr;
+    TX_CUDA(h, cudaMalloc(&fresh, fb));
+    h->sflux = fresh;
     TX_CUDA(h, cudaMemcpyAsync(h->sflux, flux, fb, cudaMemcpyHostToDevice, h->stream));
   }
   h->have_species = true;
@@ -638,7 +646,9 @@ int tx_delta_norm(tx_handle* h, int32_t field, double* norm) {
   const long long n = tx_field_size(h, field);
   double*& old = field == TX_FIELD_RHO ? h->old_rho : h->old_fi;
   if (!old) {
-    TX_CUDA(h, cudaMalloc(&old, (size_t)n * sizeof(double)));
+    double* fresh = nullptr;  // the handle keeps the pointer only once the allocation succeeded
+    TX_CUDA(h, cudaMalloc(&fresh, (size_t)n * sizeof(double)));
+    old = fresh;
     TX_CUDA(h, cudaMemsetAsync(old, 0, (size_t)n * sizeof(double), h->stream));
   }
   int rc = stage_field(h, field);
@@ -664,7 +674,11 @@ int tx_conservation(tx_handle* h, double* out) {
   const int dof = h->S * h->Q;
   const long long n = h->g.n * dof;
   const long long span = (kConsSpanMax / dof) * dof;
-  if (!h->cons) TX_CUDA(h, cudaMalloc(&h->cons, (size_t)(kConsSpanMax + 128) * sizeof(double)));
+  if (!h->cons) {
+    double* fresh = nullptr;  // the handle keeps the pointer only once the allocation succeeded
+    TX_CUDA(h, cudaMalloc(&fresh, (size_t)(kConsSpanMax + 128) * sizeof(double)));
+    h->cons = fresh;
+  }
   int rc = stage_field(h, TX_FIELD_FI);
   if (rc) return rc;
   double* sums_d = h->cons + kConsSpanMax;

@@ -106,6 +106,7 @@ struct tx_batch {
   int otile_cap = 0;
   int* d_notiles = nullptr;
   bool need_faces = false, need_outlets = false;  // launched once a lattice needs them
+  bool tables_ok = true;  // false after a failed rebuild_tables: launches and probes refuse until one succeeds
   // launch shape
   int bx = 32, by = 4, bz = 1, blocks_per_sm = 4;
   // graph
@@ -204,6 +205,7 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
 
 // Rewrites the descriptors and the tile table of the active lattices.
 int rebuild_tables(tx_batch* b) {
+  b->tables_ok = false;
   std::vector<LatDesc> descs;
   std::vector<int4> tiles;
   std::vector<int2> ltiles, ftiles;
@@ -244,6 +246,9 @@ int rebuild_tables(tx_batch* b) {
     drop_graph(b);
     if (b->d_lats) cudaFreeAsync(b->d_lats, b->stream);
     if (b->d_res) cudaFreeAsync(b->d_res, b->stream);
+    b->d_lats = nullptr;
+    b->d_res = nullptr;
+    b->lat_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_lats, (size_t)cap * sizeof(LatDesc), b->stream));
     TX_BCUDA(b, cudaMallocAsync(&b->d_res, (size_t)cap * sizeof(ProbePart), b->stream));
     b->lat_cap = cap;
@@ -253,6 +258,9 @@ int rebuild_tables(tx_batch* b) {
     drop_graph(b);
     if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
     if (b->d_parts) cudaFreeAsync(b->d_parts, b->stream);
+    b->d_tiles = nullptr;
+    b->d_parts = nullptr;
+    b->tile_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_tiles, (size_t)cap * sizeof(int4), b->stream));
     TX_BCUDA(b, cudaMallocAsync(&b->d_parts, (size_t)cap * sizeof(ProbePart), b->stream));
     b->tile_cap = cap;
@@ -261,6 +269,8 @@ int rebuild_tables(tx_batch* b) {
     const int cap = std::max(nlt, 2 * b->ltile_cap);
     drop_graph(b);
     if (b->d_ltiles) cudaFreeAsync(b->d_ltiles, b->stream);
+    b->d_ltiles = nullptr;
+    b->ltile_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_ltiles, (size_t)cap * sizeof(int2), b->stream));
     b->ltile_cap = cap;
   }
@@ -268,6 +278,8 @@ int rebuild_tables(tx_batch* b) {
     const int cap = std::max(nft, 2 * b->ftile_cap);
     drop_graph(b);
     if (b->d_ftiles) cudaFreeAsync(b->d_ftiles, b->stream);
+    b->d_ftiles = nullptr;
+    b->ftile_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_ftiles, (size_t)cap * sizeof(int2), b->stream));
     b->ftile_cap = cap;
   }
@@ -275,6 +287,8 @@ int rebuild_tables(tx_batch* b) {
     const int cap = std::max(nov, 2 * b->otile_cap);
     drop_graph(b);
     if (b->d_otiles) cudaFreeAsync(b->d_otiles, b->stream);
+    b->d_otiles = nullptr;
+    b->otile_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_otiles, (size_t)cap * sizeof(int4), b->stream));
     b->otile_cap = cap;
   }
@@ -290,6 +304,7 @@ int rebuild_tables(tx_batch* b) {
   // the host vectors die with this call: the copies must have left them
   TX_BCUDA(b, cudaStreamSynchronize(b->stream));
   b->ntiles = nt;
+  b->tables_ok = true;
   return TX_OK;
 }
 
@@ -678,6 +693,7 @@ int tx_batch_launch(tx_batch* b, int32_t nsteps) {
   if (!b) return TX_ERR_ARG;
   if (nsteps < 0) return bfail(b, TX_ERR_ARG, "nsteps must be >= 0");
   if (b->slots.empty() || nsteps == 0) return TX_OK;
+  if (!b->tables_ok) return bfail(b, TX_ERR_STATE, "the batch's device tables were not rebuilt after the last change (see the error it returned)");
   int left = nsteps;
   while (left > 0) {
     if (b->graph_steps > 0 && b->flip == 0 && left >= b->graph_steps) {
@@ -703,6 +719,7 @@ int tx_batch_probe(tx_batch* b, int32_t cap, tx_probe* out, int32_t* n) {
   const int nl = (int)b->slots.size();
   *n = nl;
   if (!nl) return TX_OK;
+  if (!b->tables_ok) return bfail(b, TX_ERR_STATE, "the batch's device tables were not rebuilt after the last change (see the error it returned)");
   const dim3 blk((unsigned)b->bx, (unsigned)b->by, (unsigned)b->bz);
   b->ks.probe_tiles(bargs(b), b->flip, grid_of(b), blk, b->stream);
   k_probe_reduce<<<nl, 256, 0, b->stream>>>(b->d_lats, nl, b->d_parts, b->d_res);
@@ -774,6 +791,7 @@ int tx_batch_set_graph(tx_batch* b, int32_t steps_per_graph) {
 int tx_batch_tune(tx_batch* b, int32_t steps_per_trial, int32_t* chosen) {
   if (!b || steps_per_trial < 1) return TX_ERR_ARG;
   if (b->slots.empty()) return bfail(b, TX_ERR_STATE, "tune needs lattices in the batch");
+  if (!b->tables_ok) return bfail(b, TX_ERR_STATE, "the batch's device tables were not rebuilt after the last change (see the error it returned)");
   struct Cand {
     int bx, by, bz, bps;
   };
