@@ -7,7 +7,7 @@
     lbm.run()                                      # LBMRun    -> tx_step + outputs
     lbm.destroy()                                  # LBMDestroy
 
-The time loop, output cadence (-kwrite, waypoints), steady-state exit and
+The time loop, output cadence (-kwrite, -waypointN, -output_last), steady-state exit and
 PETSc-binary output stay on the host exactly as in LBMRun2 (lbm.F90:262-422);
 each flow step is one tx_step on the GPU.
 """
@@ -30,6 +30,8 @@ class LBM:
         self.walls = None
         self.counter = 0
         self.nd = self.params.ndims
+        self.io_fi = run.output_flow_fi  # flow%io_fi: -output_last_fi turns it on at the last step, for good
+        self.waypoint = 0                # index of the next waypoint (current_waypoint - 1)
 
     # LBMCreate + OptionsSetUp + LBMSetFromOptions
     @classmethod
@@ -80,57 +82,104 @@ class LBM:
         n, s, q = self.params.nsites, self.params.ncomponents, self.params.Q
         self.handle.upload_fi(petsc_io.read_field(name, n, s * q))
 
-    # LBMInit2 (lbm.F90:183-253)
-    def init(self, istep=0, suppress_output=True):
+    # LBMInit2 (lbm.F90:183-253): walls (step 0 only) and the initial fields
+    # unless -supress_ic_output; the output counter advances either way, so
+    # the first output of the run is file 001
+    def init(self, istep=0, suppress_output=None):
+        if suppress_output is None:
+            suppress_output = self.run_opts.supress_ic_output
         self.handle.init()
-        if not suppress_output and istep == 0:
-            self._write("walls", self.walls, 1)
-            self.output(istep)
+        if not suppress_output:
+            if istep == 0:
+                self._write("walls", self.walls, 1)
+            self._write_fields()
+        self.counter += 1
 
     # LBMOutput (lbm.F90:424-442) / FlowOutputDiagnostics (lbm_flow.F90:576-601)
     def output(self, istep, with_fi=None):
-        pre = self.run_opts.output_prefix
+        self._write_fields(with_fi)
+        self.counter += 1
+
+    def _write_fields(self, with_fi=None):
+        ro = self.run_opts
+        pre = ro.output_prefix
         if pre and os.path.dirname(pre):
             os.makedirs(os.path.dirname(pre), exist_ok=True)
         h = self.handle
-        if with_fi if with_fi is not None else self.run_opts.output_flow_fi:
+        if with_fi if with_fi is not None else self.io_fi:
             self._write("fi", h.download(P.FIELD_FI), self.params.ncomponents * self.params.Q)
-        self._write("rho", h.download(P.FIELD_RHO), self.params.ncomponents)
-        self._write("u", h.download(P.FIELD_VELT), self.nd)
-        self._write("prs", h.download(P.FIELD_PRS), 1)
+        if ro.output_rho:
+            rho = h.download(P.FIELD_RHO)
+            if ro.mass_scale != 1.0 or ro.length_scale != 1.0:
+                rho = rho * (ro.mass_scale / ro.length_scale ** 3)
+            self._write("rho", rho, self.params.ncomponents)
+        if ro.output_velocity:
+            u = h.download(P.FIELD_VELT)
+            if ro.velocity_scale != 1.0:
+                u = u * ro.velocity_scale
+            self._write("u", u, self.nd)
+        if ro.output_rhot:
+            self._write("rhot", h.download(P.FIELD_RHOT), 1)
+        if ro.output_pressure:
+            self._write("prs", h.download(P.FIELD_PRS), 1)
         if self.params.nspecies > 0:
             # TransportOutputDiagnostics (lbm_transport.F90:342-356): gi and psi
             ns = self.params.nspecies
             self._write("gi", h.download(P.FIELD_SPECIES_FI), ns * self.params.Q)
             self._write("psi", h.download(P.FIELD_SPECIES_RHO), ns)
-        self.counter += 1
 
     def _write(self, name, arr, dof):
         petsc_io.write_vec(petsc_io.output_name(self.run_opts.output_prefix, name, self.counter), arr, dof)
 
+    # the output check of LBMRun2 (lbm.F90:373-391): the next waypoint, else
+    # the -kwrite cadence; at the last step -output_flow_last_fi adds fi
+    def _output_check(self, step, kstep):
+        ro = self.run_opts
+        wps = ro.waypoints
+        hit = False
+        if self.waypoint < len(wps) and wps[self.waypoint] == step:
+            hit = True
+            self.waypoint += 1
+        elif ro.kwrite > 0 and step % ro.kwrite == 0:
+            hit = True
+        if hit:
+            if step == kstep:
+                self.io_fi = self.io_fi or ro.output_flow_last_fi
+            self.output(step)
+
     # LBMRun2 (lbm.F90:262-422)
     def run(self, istep=None, kstep=None, write_output=True):
-        istep = self.run_opts.istep if istep is None else istep
-        kstep = self.run_opts.nsteps if kstep is None else kstep
-        kw = self.run_opts.kwrite
-        steady = self.run_opts.run_to_steadystate
-        field = P.FIELD_FI if self.run_opts.steadystate_field_fi else P.FIELD_RHO
+        ro = self.run_opts
+        istep = ro.istep if istep is None else istep
+        kstep = ro.nsteps if kstep is None else kstep
+        kw = ro.kwrite
+        steady = ro.run_to_steadystate
+        field = P.FIELD_FI if ro.steadystate_field_fi else P.FIELD_RHO
         step = istep
+        last = kstep + 1  # the loop variable after a loop that ran to the end
         while step < kstep:
             # advance to the next step that needs host work
             nxt = kstep
             if steady:
                 nxt = step + 1
-            elif write_output and kw > 0:
-                nxt = min(kstep, (step // kw + 1) * kw)
+            elif write_output:
+                if kw > 0:
+                    nxt = min(nxt, (step // kw + 1) * kw)
+                if self.waypoint < len(ro.waypoints) and ro.waypoints[self.waypoint] > step:
+                    nxt = min(nxt, ro.waypoints[self.waypoint])
             self.handle.step(nxt - step)
             step = nxt
-            if write_output and kw > 0 and step % kw == 0:
-                self.output(step, with_fi=self.run_opts.output_flow_fi)
+            if write_output:
+                self._output_check(step, kstep)
             if steady:
                 norm = self.handle.delta_norm(field)
-                if norm < self.run_opts.steadystate_tolerance and step > istep + 2:
+                if norm < ro.steadystate_tolerance and step > istep + 2:
+                    last = step
                     break
+        # -output_last: one more output after the loop (lbm.F90:407-416)
+        if write_output and ro.output_last:
+            self.io_fi = self.io_fi or ro.output_flow_last_fi
+            self.output(last)
         return step
 
     def download(self, field):

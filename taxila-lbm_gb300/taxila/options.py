@@ -142,6 +142,20 @@ class RunOptions:
     walls_file: str = "geometry.dat"
     output_prefix: str = ""
     output_flow_fi: bool = False
+    output_flow_last_fi: bool = False  # -output_flow_last_fi: fi also at the last step
+    output_last: bool = False          # -output_last: one more output after the loop
+    supress_ic_output: bool = False    # -supress_ic_output: no output of the initial state
+    # fields of each output (FlowCreate defaults, lbm_flow.F90:137-142)
+    output_rho: bool = True
+    output_velocity: bool = True
+    output_rhot: bool = False
+    output_pressure: bool = True
+    waypoints: list = field(default_factory=list)  # -waypoint1, -waypoint2, ...: extra output steps
+    # physical scales (GridSetPhysicalScales, FlowSetPhysicalScales): outputs of
+    # rho are scaled by mass_scale / length_scale**3, of u by velocity_scale
+    length_scale: float = 1.0
+    mass_scale: float = 1.0
+    velocity_scale: float = 1.0
     ic_file: str = ""
     ic_file_rho: str = ""
     component_names: list = field(default_factory=list)
@@ -276,7 +290,8 @@ def params_from_options(opts):
     for f, fname in enumerate(P.FACE_NAMES[: 2 * nd]):
         _parse_face_bc(p, f, fname, s, nd, names, has, get)
 
-    _physical_scales(p, viscosity, density)
+    run.length_scale = _length_scale(p, get)
+    run.mass_scale, run.velocity_scale = _physical_scales(p, viscosity, density, run.length_scale)
 
     # transport (lbm_options.F90:326-361, TransportSetFromOptions lbm_transport.F90:130-245,
     # SpecieSetFromOptions lbm_species.F90:111-133)
@@ -325,17 +340,49 @@ def params_from_options(opts):
     run.walls_file = (get("walls_file") or "geometry.dat").strip()
     run.output_prefix = (get("output_file_prefix") or "").strip()
     run.output_flow_fi = _bool(get("output_flow_fi", "0"))
+    # output options (lbm_options.F90:240-241, lbm_flow.F90:262-279)
+    run.output_flow_last_fi = _bool(get("output_flow_last_fi", "0"))
+    run.output_last = _bool(get("output_last", "0"))
+    run.supress_ic_output = _bool(get("supress_ic_output", "0"))
+    run.output_rho = _bool(get("output_rho", "1"))
+    run.output_velocity = _bool(get("output_velocity", "1"))
+    run.output_rhot = _bool(get("output_rhot", "0"))
+    run.output_pressure = _bool(get("output_pressure", "1"))
+    # waypoints (lbm_options.F90:243-276): -waypoint1, -waypoint2, ... up to
+    # the first number that is not given
+    wps = []
+    while has("waypoint%d" % (len(wps) + 1)):
+        wps.append(int(get("waypoint%d" % (len(wps) + 1))))
+    run.waypoints = wps
     run.ic_file = (get("ic_file") or "").strip()
     run.ic_file_rho = (get("ic_file_rho") or "").strip()
     run.extra = dict(opts)
     return p, run
 
 
+def _length_scale(p, get):
+    """Lattice spacing (InfoSetFromOptions, lbm_info.F90:164-222, and
+    GridSetPhysicalScales, lbm_grid.F90:80-95): corners default to 0 and N
+    (periodic axis) or N - 1, overridden by -x_start/-x_end etc.; the spacing
+    (end - start) / N (periodic) or / (N - 1) must be the same on every axis."""
+    sizes = []
+    for a, (ax, n) in enumerate(zip("xyz"[:p.ndims], (p.nx, p.ny, p.nz))):
+        per = p.bc_flags[2 * a] == P.BC_PERIODIC
+        start = float(get(ax + "_start", 0.0))
+        end = float(get(ax + "_end", n if per else n - 1))
+        sizes.append((end - start) / (n if per else n - 1) if (per or n > 1) else float("nan"))
+    for h in sizes[1:]:
+        if abs(h - sizes[0]) > 1.e-8:  # as in the reference, a NaN spacing (N = 1, not periodic) passes
+            raise DeckError("Lattice sizes must be equal, check grid parameters.")
+    return sizes[0]
+
+
 def _physical_scales(p, viscosity, density, length_scale=1.0):
     """FlowSetPhysicalScales (lbm_flow.F90:295-376): tau / mm consistency.
 
     Component 1's tau and mm are taken as correct; other components' tau/mm
-    are derived from -viscosity_<c>/-density_<c> when those are given."""
+    are derived from -viscosity_<c>/-density_<c> when those are given.
+    Returns (mass_scale, velocity_scale)."""
     eps = 1.e-8
     if viscosity[0] < -990.0:
         time_scale = 1.0
@@ -357,6 +404,7 @@ def _physical_scales(p, viscosity, density, length_scale=1.0):
                 p.mm[m] = consistent_mm
             elif abs(p.mm[m] - consistent_mm) > eps:
                 raise DeckError("Densities and molecular masses specified for components are not consistent.")
+    return mass_scale, length_scale / time_scale
 
 
 def load_deck(path):

@@ -1,0 +1,164 @@
+"""The host driver's initial output, time loop and outputs follow LBMInit2, LBMRun2 and LBMOutput
+(src/lbm/lbm.F90:183-442) and FlowOutputDiagnostics (src/lbm/lbm_flow.F90:576-601):
+-kwrite cadence, -waypointN, fi at the last step (-output_flow_last_fi),
+-output_last, the steady-state exit, the per-field output flags and the
+physical scales of the written fields.  The device handle is replaced by a
+fake that records the steps it is asked for, so this runs on the CPU.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from taxila import options as O
+from taxila import params as P
+from taxila import petsc_io
+from taxila.lbm import LBM
+
+BASE = """
+-NX 4
+-NY 3
+-discretization d2q9
+-ncomponents 1
+-component1_name water
+-tau_water 1.0
+-bc_periodic_x
+-bc_periodic_y
+-walls_type 2
+"""
+
+
+class FakeHandle:
+    """Counts steps; downloads return the step count plus field / 100 everywhere."""
+
+    def __init__(self, p, norms=()):
+        self.p = p
+        self.t = 0
+        self.calls = []
+        self.norms = list(norms)
+
+    def init(self):
+        self.inited = True
+
+    def step(self, n):
+        assert n > 0
+        self.calls.append(n)
+        self.t += n
+
+    def download(self, field):
+        p = self.p
+        dof = {P.FIELD_FI: p.ncomponents * p.Q, P.FIELD_RHO: p.ncomponents, P.FIELD_VELT: p.ndims,
+               P.FIELD_PRS: 1, P.FIELD_RHOT: 1}[field]
+        return np.full(p.nsites * dof, self.t + field / 100.0)
+
+    def delta_norm(self, field):
+        return self.norms.pop(0)
+
+
+def driver(tmp_path, extra, norms=()):
+    lbm = LBM.from_deck(BASE + extra + "\n-output_file_prefix %s/o_\n" % tmp_path)
+    lbm.handle = FakeHandle(lbm.params, norms)
+    return lbm
+
+
+def written(tmp_path, name, counter):
+    path = petsc_io.output_name(str(tmp_path) + "/o_", name, counter)
+    return petsc_io.read_vec(path) if os.path.exists(path) else None
+
+
+def steps_of(tmp_path, name="rho"):
+    out, c = [], 0
+    while written(tmp_path, name, c) is not None:
+        out.append(int(written(tmp_path, name, c)[0]))
+        c += 1
+    return out
+
+
+def test_kwrite_and_waypoints(tmp_path):
+    lbm = driver(tmp_path, "-npasses 10\n-kwrite 5\n-waypoint1 3\n-waypoint2 7")
+    assert lbm.run_opts.waypoints == [3, 7]
+    assert lbm.run() == 10
+    assert lbm.handle.calls == [3, 2, 2, 3]
+    assert steps_of(tmp_path) == [3, 5, 7, 10]
+    assert steps_of(tmp_path, "u") == [3, 5, 7, 10] and steps_of(tmp_path, "prs") == [3, 5, 7, 10]
+    assert written(tmp_path, "fi", 0) is None and written(tmp_path, "rhot", 0) is None
+
+
+def test_waypoint_on_a_kwrite_step_outputs_once_and_numbering_stops_at_a_gap(tmp_path):
+    lbm = driver(tmp_path, "-npasses 10\n-kwrite 5\n-waypoint1 5\n-waypoint3 8")
+    assert lbm.run_opts.waypoints == [5]
+    lbm.run()
+    assert steps_of(tmp_path) == [5, 10]
+
+
+def test_waypoints_without_kwrite(tmp_path):
+    lbm = driver(tmp_path, "-npasses 9\n-waypoint1 2\n-waypoint2 6")
+    lbm.run()
+    assert lbm.handle.calls == [2, 4, 3]
+    assert steps_of(tmp_path) == [2, 6]
+
+
+def test_last_fi_and_output_last(tmp_path):
+    lbm = driver(tmp_path, "-npasses 6\n-kwrite 3\n-output_flow_last_fi\n-output_last")
+    lbm.run()
+    # outputs at steps 3 and 6, then the one of -output_last (state still at step 6)
+    assert steps_of(tmp_path) == [3, 6, 6]
+    assert written(tmp_path, "fi", 0) is None
+    assert written(tmp_path, "fi", 1) is not None and written(tmp_path, "fi", 2) is not None
+    assert written(tmp_path, "fi", 1).size == lbm.params.nsites * lbm.params.Q
+
+
+def test_steady_state_exit(tmp_path):
+    # the norm is below the tolerance from the start; the loop exits once step > istep + 2
+    lbm = driver(tmp_path, "-npasses 100\n-kwrite 50\n-run_to_steadystate\n-steadystate_tolerance 1e-3\n-output_last",
+                 norms=[1e-4] * 10)
+    assert lbm.run() == 3
+    assert lbm.handle.calls == [1, 1, 1]
+    assert steps_of(tmp_path) == [3]
+
+
+def test_field_flags(tmp_path):
+    lbm = driver(tmp_path, "-npasses 2\n-kwrite 2\n-output_rho 0\n-output_rhot\n-output_pressure 0")
+    lbm.run()
+    assert written(tmp_path, "rho", 0) is None and written(tmp_path, "prs", 0) is None
+    assert written(tmp_path, "rhot", 0) is not None and written(tmp_path, "u", 0) is not None
+
+
+def test_physical_scales_of_the_outputs(tmp_path):
+    # spacing 2 on both axes; mass scale mm * density * L^3, velocity scale
+    # L / time scale with time scale L^2 (tau - 1/2) / (3 viscosity)
+    lbm = driver(tmp_path, "-npasses 2\n-kwrite 2\n-x_end 8\n-y_end 6\n-mm_water 1.5\n-density_water 2.0\n"
+                           "-viscosity_water 0.5")
+    ro = lbm.run_opts
+    assert ro.length_scale == 2.0
+    assert ro.mass_scale == pytest.approx(1.5 * 2.0 * 8.0)
+    assert ro.velocity_scale == pytest.approx(2.0 / (4.0 * 0.5 / 1.5))
+    lbm.run()
+    assert np.allclose(written(tmp_path, "rho", 0), (2 + P.FIELD_RHO / 100.0) * 1.5 * 2.0)
+    assert np.allclose(written(tmp_path, "u", 0), (2 + P.FIELD_VELT / 100.0) * 1.5)
+    assert np.allclose(written(tmp_path, "prs", 0), 2 + P.FIELD_PRS / 100.0)
+
+
+def test_unequal_spacing_is_an_error():
+    with pytest.raises(O.DeckError):
+        LBM.from_deck(BASE + "-x_end 8\n")
+
+
+def test_init_output_and_counter(tmp_path):
+    # LBMInit2 writes the walls and the initial fields to file 000 and
+    # advances the counter: the first output of the run is file 001
+    lbm = driver(tmp_path, "-npasses 4\n-kwrite 4")
+    lbm.walls = np.zeros(lbm.params.nsites)
+    lbm.init()
+    assert written(tmp_path, "walls", 0) is not None
+    lbm.run()
+    assert steps_of(tmp_path) == [0, 4]
+
+
+def test_suppressed_initial_output_still_advances_the_counter(tmp_path):
+    lbm = driver(tmp_path, "-npasses 4\n-kwrite 4\n-supress_ic_output")
+    lbm.walls = np.zeros(lbm.params.nsites)
+    lbm.init()
+    lbm.run()
+    assert written(tmp_path, "walls", 0) is None and written(tmp_path, "rho", 0) is None
+    assert int(written(tmp_path, "rho", 1)[0]) == 4
