@@ -7,6 +7,9 @@
     lbm.run()                                      # LBMRun    -> tx_step + outputs
     lbm.destroy()                                  # LBMDestroy
 
+or, all of it in the order of the reference's main program (restart and
+initial-condition files included): main(deck, initialize_state=..., ...).
+
 The time loop, output cadence (-kwrite, -waypointN, -output_last), steady-state exit and
 PETSc-binary output stay on the host exactly as in LBMRun2 (lbm.F90:262-422);
 each flow step is one tx_step on the GPU.
@@ -43,8 +46,9 @@ class LBM:
         return cls(p, run)
 
     # LBMSetUp (lbm.F90:140-175): device state and walls
-    def setup(self, initialize_walls=None):
-        self.handle = Handle(self.params)
+    def setup(self, initialize_walls=None, handle=None):
+        # handle: an already created device handle for these parameters (default: a new one)
+        self.handle = Handle(self.params) if handle is None else handle
         z, y, x = self.params.shape
         if self.run_opts.walls_type == 2 or initialize_walls is not None:
             w = np.zeros(self.params.nsites) if initialize_walls is None else initialize_walls(self.params, self.run_opts)
@@ -75,8 +79,17 @@ class LBM:
         else:
             raise O.DeckError("-ic_file or -ic_file_rho required")
 
-    # LBMInitializeStateRestarted (lbm.F90:519-544)
-    def initialize_state_restarted(self, counter):
+    # LBMInitializeStateRestarted (lbm.F90:519-544): the file number is
+    # -restart_counter, else istep / kwrite
+    def initialize_state_restarted(self, counter=None):
+        ro = self.run_opts
+        if counter is None:
+            if ro.restart_counter > -1:
+                counter = ro.restart_counter
+            elif ro.kwrite > 0:
+                counter = ro.istep // ro.kwrite
+            else:
+                raise O.DeckError("must set -restart_counter to define which file to restart from")
         self.counter = counter
         name = petsc_io.output_name(self.run_opts.output_prefix, "fi", counter)
         n, s, q = self.params.nsites, self.params.ncomponents, self.params.Q
@@ -189,3 +202,47 @@ class LBM:
         if self.handle is not None:
             self.handle.close()
             self.handle = None
+
+
+def main(deck, initialize_state=None, initialize_walls=None, initialize_bcs=None, initialize_species=None,
+         handle=None):
+    """One run of a deck, in the order of the reference's main program
+    (src/lbm/main.F90:45-104).  The plugins are the reference's link-time
+    externals as callables: initialize_walls(params, run) -> walls (else the
+    walls file), initialize_bcs(params, run) -> {face: values of
+    tx_upload_bc_values} (else the deck's constant face values),
+    initialize_state(params, run, walls) -> rho or (rho, u), and
+    initialize_species(params, run, walls) -> conc or (conc, flux).  A restart
+    (-restart) reads fi from the output file of -restart_counter (else
+    istep / kwrite); -ic_file / -ic_file_rho read the initial state from
+    PETSc-binary files.  Returns the LBM object after its last step, with the
+    device handle released."""
+    lbm = LBM.from_deck(deck)
+    ro = lbm.run_opts
+    try:
+        lbm.setup(initialize_walls, handle=handle)
+        if initialize_bcs is not None:
+            for face, vals in initialize_bcs(lbm.params, ro).items():
+                lbm.handle.upload_bc_values(face, vals)
+        if ro.restart:
+            lbm.initialize_state_restarted()
+            istep = ro.istep
+        elif ro.ic_file or ro.ic_file_rho:
+            lbm.initialize_state_from_file()
+            istep = 0
+        else:
+            if initialize_state is None:
+                raise O.DeckError("an initialize_state plugin, -ic_file/-ic_file_rho or -restart is required")
+            lbm.initialize_state(initialize_state)
+            istep = 0
+        if lbm.params.nspecies > 0 and not ro.restart:
+            if initialize_species is None:
+                raise O.DeckError("a deck with species needs an initialize_species plugin")
+            res = initialize_species(lbm.params, ro, lbm.walls)
+            conc, flux = res if isinstance(res, tuple) else (res, None)
+            lbm.initialize_species(conc, flux)
+        lbm.init(istep)
+        lbm.run(istep, ro.nsteps)
+    finally:
+        lbm.destroy()
+    return lbm

@@ -145,6 +145,8 @@ class RunOptions:
     output_flow_last_fi: bool = False  # -output_flow_last_fi: fi also at the last step
     output_last: bool = False          # -output_last: one more output after the loop
     supress_ic_output: bool = False    # -supress_ic_output: no output of the initial state
+    restart: bool = False              # -restart: fi from an earlier output
+    restart_counter: int = -1          # -restart_counter: its file number (else istep / kwrite)
     # fields of each output (FlowCreate defaults, lbm_flow.F90:137-142)
     output_rho: bool = True
     output_velocity: bool = True
@@ -344,6 +346,8 @@ def params_from_options(opts):
     run.output_flow_last_fi = _bool(get("output_flow_last_fi", "0"))
     run.output_last = _bool(get("output_last", "0"))
     run.supress_ic_output = _bool(get("supress_ic_output", "0"))
+    run.restart = _bool(get("restart", "0"))
+    run.restart_counter = int(get("restart_counter", -1))
     run.output_rho = _bool(get("output_rho", "1"))
     run.output_velocity = _bool(get("output_velocity", "1"))
     run.output_rhot = _bool(get("output_rhot", "0"))

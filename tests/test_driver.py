@@ -13,7 +13,7 @@ import pytest
 from taxila import options as O
 from taxila import params as P
 from taxila import petsc_io
-from taxila.lbm import LBM
+from taxila.lbm import LBM, main
 
 BASE = """
 -NX 4
@@ -39,6 +39,22 @@ class FakeHandle:
 
     def init(self):
         self.inited = True
+
+    def upload_walls(self, walls):
+        self.walls = np.array(walls)
+
+    def upload_state(self, rho, u=None):
+        self.rho = np.array(rho)
+
+    def upload_fi(self, fi):
+        self.fi = np.array(fi)
+
+    def upload_bc_values(self, face, vals):
+        self.bc = getattr(self, "bc", {})
+        self.bc[face] = np.array(vals)
+
+    def close(self):
+        self.closed = True
 
     def step(self, n):
         assert n > 0
@@ -162,3 +178,55 @@ def test_suppressed_initial_output_still_advances_the_counter(tmp_path):
     lbm.run()
     assert written(tmp_path, "walls", 0) is None and written(tmp_path, "rho", 0) is None
     assert int(written(tmp_path, "rho", 1)[0]) == 4
+
+
+def test_main_with_plugins(tmp_path):
+    deck = BASE + "-npasses 4\n-kwrite 2\n-output_file_prefix %s/o_\n" % tmp_path
+    seen = {}
+
+    def walls(p, run):
+        return np.zeros(p.nsites)
+
+    def state(p, run, w):
+        seen["rho"] = np.full(p.nsites, 1.25)
+        return seen["rho"]
+
+    def bcs(p, run):
+        return {1: np.ones(3)}
+
+    fake = FakeHandle(LBM.from_deck(deck).params)
+    main(deck, initialize_state=state, initialize_walls=walls, initialize_bcs=bcs, handle=fake)
+    assert fake.inited and fake.closed
+    assert np.array_equal(fake.rho, seen["rho"]) and np.array_equal(fake.walls, np.zeros(12))
+    assert 1 in fake.bc
+    assert fake.calls == [2, 2]
+    assert steps_of(tmp_path) == [0, 2, 4]
+
+
+def test_main_restart_reads_the_counter_file(tmp_path):
+    # -restart at istep 4 with -kwrite 2 reads fi002 and runs steps 5..6
+    deck = BASE + "-npasses 6\n-kwrite 2\n-restart\n-istep 4\n-output_file_prefix %s/o_\n" % tmp_path
+    p = LBM.from_deck(deck).params
+    fi = np.arange(p.nsites * p.Q, dtype=np.float64)
+    petsc_io.write_vec(petsc_io.output_name(str(tmp_path) + "/o_", "fi", 2), fi)
+    fake = FakeHandle(p)
+    main(deck, initialize_walls=lambda p, run: np.zeros(p.nsites), handle=fake)
+    assert np.array_equal(fake.fi, fi)
+    assert fake.calls == [2]
+    # the initial output rewrites file 002; step 6 goes to file 003 (the fake counts the 2 steps it ran)
+    assert int(written(tmp_path, "rho", 3)[0]) == 2
+
+
+def test_main_restart_needs_a_counter(tmp_path):
+    deck = BASE + "-npasses 6\n-restart\n-istep 4\n-output_file_prefix %s/o_\n" % tmp_path
+    fake = FakeHandle(LBM.from_deck(deck).params)
+    with pytest.raises(O.DeckError):
+        main(deck, initialize_walls=lambda p, run: np.zeros(p.nsites), handle=fake)
+    assert fake.closed
+
+
+def test_main_needs_an_initial_state(tmp_path):
+    deck = BASE + "-npasses 2\n-output_file_prefix %s/o_\n" % tmp_path
+    fake = FakeHandle(LBM.from_deck(deck).params)
+    with pytest.raises(O.DeckError):
+        main(deck, initialize_walls=lambda p, run: np.zeros(p.nsites), handle=fake)
