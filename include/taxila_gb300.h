@@ -209,6 +209,14 @@ int tx_init(tx_handle* h);
  * and of its transport part when the handle has species. */
 int tx_step(tx_handle* h, int32_t nsteps);
 
+/* nsteps iterations of the transport part of LBMRun2's loop body alone
+ * (TransportCollision, TransportStream and the species bounceback and moments,
+ * lbm.F90:290-370): the steady-flow mode of -steadystate_flow, in which the
+ * flow calls of the loop are skipped once the ramp-up steps are done
+ * (lbm.F90:283-363).  The flow state and its step count stay unchanged.
+ * TX_ERR_STATE without species. */
+int tx_step_species(tx_handle* h, int32_t nsteps);
+
 /* DistributionCalcDeltaNorm (lbm_distribution_function.F90:809-833):
  * ||(old - new)/new||_inf of TX_FIELD_RHO or TX_FIELD_FI against the values
  * saved by the previous call (first call: against zero).  Sites where new

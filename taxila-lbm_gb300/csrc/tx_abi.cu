@@ -608,6 +608,21 @@ int tx_step(tx_handle* h, int32_t nsteps) {
   return TX_OK;
 }
 
+int tx_step_species(tx_handle* h, int32_t nsteps) {
+  if (!h) return TX_ERR_ARG;
+  if (!h->inited) return fail(h, TX_ERR_STATE, "tx_init must come before tx_step_species");
+  if (nsteps < 0) return fail(h, TX_ERR_ARG, "nsteps must be >= 0");
+  if (h->NS == 0 || !h->have_species) return fail(h, TX_ERR_STATE, "the handle holds no species state");
+  for (int t = 0; t < nsteps; ++t) {
+    // the species part of tx_step alone: the flow state and its step count stay as they are
+    h->ss.step(species_args(h, h->gcur, 1 - h->gcur), h->stream);
+    h->gcur = 1 - h->gcur;
+    const int rc = check_launch(h, "k_species");
+    if (rc) return rc;
+  }
+  return TX_OK;
+}
+
 int tx_sync(tx_handle* h) {
   if (!h) return TX_ERR_ARG;
   return sync_stream(h);

@@ -50,6 +50,7 @@ def load():
         "tx_upload_bc_values": ([vp, i32, dp], C.c_int),
         "tx_init": ([vp], C.c_int),
         "tx_step": ([vp, i32], C.c_int),
+        "tx_step_species": ([vp, i32], C.c_int),
         "tx_delta_norm": ([vp, i32, dp], C.c_int),
         "tx_download": ([vp, i32, dp], C.c_int),
         "tx_conservation": ([vp, dp], C.c_int),
@@ -157,6 +158,10 @@ class Handle:
 
     def step(self, n=1):
         self._check(self.L.tx_step(self.h, int(n)))
+
+    def step_species(self, n=1):
+        """Transport only: the steady-flow mode's step."""
+        self._check(self.L.tx_step_species(self.h, int(n)))
 
     def sync(self):
         self._check(self.L.tx_sync(self.h))

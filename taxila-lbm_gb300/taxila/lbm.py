@@ -110,15 +110,28 @@ class LBM:
 
     # LBMOutput (lbm.F90:424-442) / FlowOutputDiagnostics (lbm_flow.F90:576-601)
     def output(self, istep, with_fi=None):
-        self._write_fields(with_fi)
+        ro = self.run_opts
+        # a flow held at steady state writes no flow fields after its ramp-up
+        flow = not ro.steadystate_flow or istep < ro.steadystate_rampup_steps
+        self._write_fields(with_fi, flow=flow)
         self.counter += 1
 
-    def _write_fields(self, with_fi=None):
+    def _write_fields(self, with_fi=None, flow=True):
         ro = self.run_opts
         pre = ro.output_prefix
         if pre and os.path.dirname(pre):
             os.makedirs(os.path.dirname(pre), exist_ok=True)
         h = self.handle
+        if flow:
+            self._write_flow(h, with_fi)
+        if self.params.nspecies > 0:
+            # TransportOutputDiagnostics (lbm_transport.F90:342-356): gi and psi
+            ns = self.params.nspecies
+            self._write("gi", h.download(P.FIELD_SPECIES_FI), ns * self.params.Q)
+            self._write("psi", h.download(P.FIELD_SPECIES_RHO), ns)
+
+    def _write_flow(self, h, with_fi):
+        ro = self.run_opts
         if with_fi if with_fi is not None else self.io_fi:
             self._write("fi", h.download(P.FIELD_FI), self.params.ncomponents * self.params.Q)
         if ro.output_rho:
@@ -135,11 +148,6 @@ class LBM:
             self._write("rhot", h.download(P.FIELD_RHOT), 1)
         if ro.output_pressure:
             self._write("prs", h.download(P.FIELD_PRS), 1)
-        if self.params.nspecies > 0:
-            # TransportOutputDiagnostics (lbm_transport.F90:342-356): gi and psi
-            ns = self.params.nspecies
-            self._write("gi", h.download(P.FIELD_SPECIES_FI), ns * self.params.Q)
-            self._write("psi", h.download(P.FIELD_SPECIES_RHO), ns)
 
     def _write(self, name, arr, dof):
         petsc_io.write_vec(petsc_io.output_name(self.run_opts.output_prefix, name, self.counter), arr, dof)
@@ -180,7 +188,15 @@ class LBM:
                     nxt = min(nxt, (step // kw + 1) * kw)
                 if self.waypoint < len(ro.waypoints) and ro.waypoints[self.waypoint] > step:
                     nxt = min(nxt, ro.waypoints[self.waypoint])
-            self.handle.step(nxt - step)
+            if ro.steadystate_flow and step + 1 >= ro.steadystate_rampup_steps:
+                # -steadystate_flow after the ramp-up: the flow calls of the
+                # loop are skipped (lbm.F90:283-363), the species step on
+                if self.params.nspecies > 0:
+                    self.handle.step_species(nxt - step)
+            else:
+                if ro.steadystate_flow:
+                    nxt = min(nxt, ro.steadystate_rampup_steps - 1)
+                self.handle.step(nxt - step)
             step = nxt
             if write_output:
                 self._output_check(step, kstep)

@@ -147,6 +147,11 @@ class RunOptions:
     supress_ic_output: bool = False    # -supress_ic_output: no output of the initial state
     restart: bool = False              # -restart: fi from an earlier output
     restart_counter: int = -1          # -restart_counter: its file number (else istep / kwrite)
+    # -steadystate_flow: the flow stops after steadystate_rampup_steps (0 with
+    # -steadystate_flow_file) and only the species step on
+    steadystate_flow: bool = False
+    steadystate_flow_file: str = ""
+    steadystate_rampup_steps: int = 0
     # fields of each output (FlowCreate defaults, lbm_flow.F90:137-142)
     output_rho: bool = True
     output_velocity: bool = True
@@ -348,6 +353,12 @@ def params_from_options(opts):
     run.supress_ic_output = _bool(get("supress_ic_output", "0"))
     run.restart = _bool(get("restart", "0"))
     run.restart_counter = int(get("restart_counter", -1))
+    # steady flow (lbm_options.F90:204-215): ramp-up steps only without a flow file
+    run.steadystate_flow = _bool(get("steadystate_flow", "0"))
+    if run.steadystate_flow:
+        run.steadystate_flow_file = (get("steadystate_flow_file") or "").strip()
+        if not has("steadystate_flow_file"):
+            run.steadystate_rampup_steps = int(get("steadystate_rampup_steps", 0))
     run.output_rho = _bool(get("output_rho", "1"))
     run.output_velocity = _bool(get("output_velocity", "1"))
     run.output_rhot = _bool(get("output_rhot", "0"))

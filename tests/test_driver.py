@@ -61,10 +61,16 @@ class FakeHandle:
         self.calls.append(n)
         self.t += n
 
+    def step_species(self, n):
+        assert n > 0
+        self.calls.append(("species", n))
+        self.t += n
+
     def download(self, field):
         p = self.p
         dof = {P.FIELD_FI: p.ncomponents * p.Q, P.FIELD_RHO: p.ncomponents, P.FIELD_VELT: p.ndims,
-               P.FIELD_PRS: 1, P.FIELD_RHOT: 1}[field]
+               P.FIELD_PRS: 1, P.FIELD_RHOT: 1, P.FIELD_SPECIES_FI: p.nspecies * p.Q,
+               P.FIELD_SPECIES_RHO: p.nspecies}[field]
         return np.full(p.nsites * dof, self.t + field / 100.0)
 
     def delta_norm(self, field):
@@ -230,3 +236,24 @@ def test_main_needs_an_initial_state(tmp_path):
     fake = FakeHandle(LBM.from_deck(deck).params)
     with pytest.raises(O.DeckError):
         main(deck, initialize_walls=lambda p, run: np.zeros(p.nsites), handle=fake)
+
+
+def test_steady_flow_after_rampup(tmp_path):
+    # the flow steps while lcv_step < rampup (steps 1..3), then only the
+    # species; flow fields are written only for outputs before the ramp-up ends
+    lbm = driver(tmp_path, "-npasses 10\n-kwrite 2\n-transport_discretization d2q9\n-nspecies 1\n"
+                           "-steadystate_flow\n-steadystate_rampup_steps 4")
+    ro = lbm.run_opts
+    assert ro.steadystate_flow and ro.steadystate_rampup_steps == 4
+    lbm.run()
+    assert lbm.handle.calls == [2, 1, ("species", 1), ("species", 2), ("species", 2), ("species", 2)]
+    assert steps_of(tmp_path, "rho") == [2]
+    assert steps_of(tmp_path, "psi") == [2, 4, 6, 8, 10]
+
+
+def test_steady_flow_file_means_no_rampup(tmp_path):
+    lbm = driver(tmp_path, "-npasses 4\n-transport_discretization d2q9\n-nspecies 1\n-steadystate_flow\n"
+                           "-steadystate_flow_file flow.dat\n-steadystate_rampup_steps 3")
+    assert lbm.run_opts.steadystate_rampup_steps == 0
+    lbm.run()
+    assert lbm.handle.calls == [("species", 4)]

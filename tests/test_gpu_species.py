@@ -59,3 +59,45 @@ def test_species_errors():
     h = Handle(p)
     with pytest.raises(Exception):
         h.upload_species(np.zeros(p.nsites))  # created without species
+
+
+@pytest.mark.parametrize("name,make,steps", cases.SPECIES, ids=[c[0] for c in cases.SPECIES])
+def test_species_only_steps(name, make, steps):
+    # the steady-flow mode (-steadystate_flow): after k full steps, m
+    # species-only steps leave the flow as it was and move the species exactly
+    # as m more full steps do, since the species feel no flow in this model
+    p, walls, rho, conc = make()
+    k, m = 3, 5
+
+    def started():
+        h = Handle(p)
+        h.upload_walls(walls)
+        h.upload_state(rho)
+        h.upload_species(conc)
+        h.init()
+        return h
+
+    a = started()
+    a.step(k)
+    flow_k = a.download(P.FIELD_FI)
+    a.step_species(m)
+    b = started()
+    b.step(k + m)
+    assert np.array_equal(a.download(P.FIELD_FI), flow_k)
+    for f in (P.FIELD_SPECIES_FI, P.FIELD_SPECIES_RHO, P.FIELD_SPECIES_FLUX):
+        assert np.array_equal(a.download(f), b.download(f)), f
+    a.close()
+    b.close()
+
+
+def test_species_only_step_needs_species():
+    from taxila._lib import TxError
+    p, walls, rho = cases.porous_case(P.D3Q19, (8, 8, 8))
+    h = Handle(p)
+    h.upload_walls(walls)
+    h.upload_state(rho)
+    h.init()
+    with pytest.raises(TxError) as e:
+        h.step_species(1)
+    assert e.value.code == 2
+    h.close()
