@@ -117,10 +117,6 @@ class LBM:
         self.counter += 1
 
     def _write_fields(self, with_fi=None, flow=True):
-        ro = self.run_opts
-        pre = ro.output_prefix
-        if pre and os.path.dirname(pre):
-            os.makedirs(os.path.dirname(pre), exist_ok=True)
         h = self.handle
         if flow:
             self._write_flow(h, with_fi)
@@ -150,7 +146,10 @@ class LBM:
             self._write("prs", h.download(P.FIELD_PRS), 1)
 
     def _write(self, name, arr, dof):
-        petsc_io.write_vec(petsc_io.output_name(self.run_opts.output_prefix, name, self.counter), arr, dof)
+        pre = self.run_opts.output_prefix
+        if pre and os.path.dirname(pre):
+            os.makedirs(os.path.dirname(pre), exist_ok=True)
+        petsc_io.write_vec(petsc_io.output_name(pre, name, self.counter), arr, dof)
 
     # the output check of LBMRun2 (lbm.F90:373-391): the next waypoint, else
     # the -kwrite cadence; at the last step -output_flow_last_fi adds fi
@@ -221,7 +220,7 @@ class LBM:
 
 
 def main(deck, initialize_state=None, initialize_walls=None, initialize_bcs=None, initialize_species=None,
-         handle=None):
+         handle=None, overrides=None):
     """One run of a deck, in the order of the reference's main program
     (src/lbm/main.F90:45-104).  The plugins are the reference's link-time
     externals as callables: initialize_walls(params, run) -> walls (else the
@@ -231,9 +230,10 @@ def main(deck, initialize_state=None, initialize_walls=None, initialize_bcs=None
     initialize_species(params, run, walls) -> conc or (conc, flux).  A restart
     (-restart) reads fi from the output file of -restart_counter (else
     istep / kwrite); -ic_file / -ic_file_rho read the initial state from
-    PETSc-binary files.  Returns the LBM object after its last step, with the
-    device handle released."""
-    lbm = LBM.from_deck(deck)
+    PETSc-binary files.  overrides: tx_params members to set after the deck
+    is read (e.g. {"exact": 1}).  Returns the LBM object after its last
+    step, with the device handle released."""
+    lbm = LBM.from_deck(deck, **(overrides or {}))
     ro = lbm.run_opts
     try:
         lbm.setup(initialize_walls, handle=handle)

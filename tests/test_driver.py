@@ -257,3 +257,58 @@ def test_steady_flow_file_means_no_rampup(tmp_path):
     assert lbm.run_opts.steadystate_rampup_steps == 0
     lbm.run()
     assert lbm.handle.calls == [("species", 4)]
+
+
+class OracleHandle:
+    """The CPU oracle behind the device handle's method names (test only)."""
+
+    def __init__(self, p):
+        from oracle import Oracle
+        self.o = Oracle(p)
+
+    def upload_walls(self, walls):
+        self.o.set_walls(walls)
+
+    def upload_state(self, rho, u=None):
+        self.o.set_state(rho, u)
+
+    def upload_fi(self, fi):
+        self.o.set_fi(fi)
+
+    def upload_bc_values(self, face, vals):
+        self.o.set_bc_values(face, vals)
+
+    def init(self):
+        self.o.init()
+
+    def step(self, n):
+        self.o.step(n)
+
+    def download(self, field):
+        return self.o.get(field)
+
+    def delta_norm(self, field):
+        return self.o.delta_norm(field)
+
+    def close(self):
+        self.o.close()
+
+
+def test_reference_bubble_2d_deck_through_main_on_the_oracle(tmp_path, monkeypatch):
+    # the reference's own test: its deck and initial state through main(),
+    # which writes test_solution/fi001.dat after 100 steps; its payload is the
+    # reference golden's bit for bit
+    import json
+
+    import cases
+    import test_options
+    from golden.make_golden import digest
+    monkeypatch.chdir(tmp_path)
+    p, _ = O.params_from_options(O.parse_deck_text(test_options.DECK_2D))
+    main(test_options.DECK_2D, initialize_state=lambda p, run, w: cases.bubble_2d_reference_state(p),
+         handle=OracleHandle(p))
+    assert os.path.exists(os.path.join("test_solution", "fi000.dat"))
+    fi = petsc_io.read_vec(os.path.join("test_solution", "fi001.dat"))
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "bubble_2D_fi001.json")) as f:
+        assert digest(fi) == json.load(f)["sha256_be"]
