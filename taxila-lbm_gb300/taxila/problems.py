@@ -90,3 +90,26 @@ def mineral_walls(solid, seed, nminerals=2):
     ids = rng.integers(1, nminerals + 1, size=solid.shape)
     walls[solid] = ids[solid]
     return walls.ravel()
+
+
+def bubble_plugin(only_pore=True):
+    """The reference tests' initialize_state plugin as a driver plugin
+    (plugin(params, run, walls) -> rho): reads -rho_inner and -rho_outer from
+    the deck (tests/bubble_2D/initialize_state.F90:80-95, :163-180) and fills
+    the box (N+1)/2 +- 10 in 3D, +- 26 in 2D (:104-109, :187-190).  The
+    bubble_2D plugin leaves wall sites at 0 (only_pore=True); the bubble_3D
+    and bubble_2D_hots plugins fill every site (only_pore=False)."""
+    def plugin(params, run, walls):
+        from .options import DeckError, _reals
+        s = params.ncomponents
+        vals = []
+        for key in ("rho_inner", "rho_outer"):
+            v = run.extra.get(key)
+            r = _reals(v) if v else []
+            if len(r) < s:
+                raise DeckError("-%s needs %d values" % (key, s))
+            vals.append(r[:s])
+        half = 10 if params.ndims == 3 else 26
+        nz = params.nz if params.ndims == 3 else 1
+        return bubble_box_state(params.nx, params.ny, nz, vals[0], vals[1], half, walls, only_pore)
+    return plugin

@@ -303,12 +303,31 @@ def test_reference_bubble_2d_deck_through_main_on_the_oracle(tmp_path, monkeypat
     import cases
     import test_options
     from golden.make_golden import digest
+    from taxila import problems
     monkeypatch.chdir(tmp_path)
-    p, _ = O.params_from_options(O.parse_deck_text(test_options.DECK_2D))
-    main(test_options.DECK_2D, initialize_state=lambda p, run, w: cases.bubble_2d_reference_state(p),
-         handle=OracleHandle(p))
+    p, run = O.params_from_options(O.parse_deck_text(test_options.DECK_2D))
+    plugin = problems.bubble_plugin()
+    walls = np.zeros(p.nsites)
+    assert np.array_equal(plugin(p, run, walls), cases.bubble_2d_reference_state(p))
+    main(test_options.DECK_2D, initialize_state=plugin, handle=OracleHandle(p))
     assert os.path.exists(os.path.join("test_solution", "fi000.dat"))
     fi = petsc_io.read_vec(os.path.join("test_solution", "fi001.dat"))
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "golden", "bubble_2D_fi001.json")) as f:
         assert digest(fi) == json.load(f)["sha256_be"]
+
+
+def test_bubble_plugin_on_the_reference_3d_deck():
+    # tests/bubble_3D of the reference: a 21^3 box of rho_inner (N+1)/2 +- 10
+    import cases
+    from taxila import problems
+    path = os.path.join(cases.REF, "tests", "bubble_3D", "input_data")
+    if not os.path.exists(path):
+        pytest.skip("reference test decks not present")
+    p, run = O.load_deck(path)
+    rho = problems.bubble_plugin(only_pore=False)(p, run, np.zeros(p.nsites)).reshape(p.shape + (p.ncomponents,))
+    inner = np.asarray(O._reals(run.extra["rho_inner"])[:p.ncomponents])
+    box = np.all(rho == inner, axis=-1)
+    assert box.sum() == 21 ** 3
+    c = (p.nx + 1) // 2 - 1  # 0-based index of the 1-based centre (N+1)/2
+    assert box[c - 10:c + 11, c - 10:c + 11, c - 10:c + 11].all()
