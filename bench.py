@@ -280,6 +280,71 @@ def traffic_from_profile():
         return None
 
 
+def bubble_2d_run(steps=1000, check_steps=200):
+    """The D2Q9 case the reference runs on its CPU build: two-component
+    Shan-Chen bubble, 200 x 200 fully periodic, FP64 BGK with tau = 1 for both
+    components, unit molecular masses, psi = rho, G = 0.9 (g_12 = G / c0 =
+    0.15), a centred disk of radius 30 at rho 2.0 in 0.06 (B reversed), zero
+    velocity, 1,000 steps.  Device-timed MLUPS of the plain FP64 form; the
+    oracle on the host cores over the first ``check_steps`` steps (a bounded
+    sample), whose densities the device's must match."""
+    import torch
+    from oracle import Oracle
+    from taxila._lib import Handle
+    p = P.default_params()
+    p.discretization = P.D2Q9
+    p.nx = p.ny = 200
+    p.nz = 1
+    p.ncomponents = 2
+    for f in range(4):
+        p.bc_flags[f] = P.BC_PERIODIC
+    p.g[0][1] = p.g[1][0] = 0.9 / 6.0
+    walls = np.zeros(p.nsites)
+    rho = problems.bubble_ball_state(p.nx, p.ny, 1, 30.0, [2.0, 0.06], [0.06, 2.0])
+
+    def started():
+        h = Handle(p)
+        h.upload_walls(walls)
+        h.upload_state(rho)
+        h.init()
+        return h
+
+    h = started()
+    h.step(5)
+    h.sync()
+    stream = torch.cuda.ExternalStream(h.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    h.close()
+    g = started()
+    g.step(check_steps)
+    r_dev = g.download(P.FIELD_RHO)
+    g.close()
+    threads = os.cpu_count() or 1
+    o = Oracle(p, threads=threads)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.init()
+    t0 = time.perf_counter()
+    o.step(check_steps)
+    dt = time.perf_counter() - t0
+    r_ref = o.get(P.FIELD_RHO)
+    o.close()
+    return {"workload": "D2Q9 200^2 2-component BGK Shan-Chen bubble (r=30, rho 2.0/0.06, G=0.9 -> g_12=0.15), "
+                        "periodic, FP64 plain form",
+            "steps": steps, "ms_per_step": round(ms / steps, 5),
+            "mlups": round(p.nsites * steps / (ms * 1e-3) / 1e6, 2),
+            "l2": "populations 5.8 MB stay in L2: MLUPS only, no HBM figure",
+            "cpu_oracle": {"mlups": round(p.nsites * check_steps / dt / 1e6, 3), "cores": threads,
+                           "sample": "first %d steps (%.1f s)" % (check_steps, dt)},
+            "rho_rel_err_vs_oracle_after_%d_steps" % check_steps:
+                float(np.max(np.abs(r_dev - r_ref)) / np.max(np.abs(r_ref)))}
+
+
 def batched_run(n_lat=96, steps=40, seed=4, compare=8, sides=(48, 192)):
     """Many uneven single-phase permeability lattices (D3Q19 BGK tau = 1, sides
     uniform in 48..192 per axis, seeded sphere packs with radii 4..10 and
@@ -528,7 +593,8 @@ def run_gpu(args):
             line["fp64_iso8"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
         except Exception as ex:
             line["fp64_iso8"] = {"error": str(ex)}
-        legs = (("batched", batched_run),
+        legs = (("bubble_2d", bubble_2d_run),
+                ("batched", batched_run),
                 ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
                 ("serving", serving_run))
         for key, fn in legs:
