@@ -113,3 +113,31 @@ def bubble_plugin(only_pore=True):
         nz = params.nz if params.ndims == 3 else 1
         return bubble_box_state(params.nx, params.ny, nz, vals[0], vals[1], half, walls, only_pore)
     return plugin
+
+
+def duct_walls(params, run):
+    """The stock initialize_walls_duct plugin as a driver plugin
+    (plugin(params, run) -> walls): walls of code 1 on the two faces normal to
+    -duct_normal_direction (1 = x, 2 = y (default), 3 = z; src/problem_specs/
+    initialize_walls_duct.F90:33-52, :63-77), in one process.  As written
+    there, the top z wall is set only when NZ equals NY (the test compares the
+    upper z index with NY), and a 2D lattice takes no z walls."""
+    normal = int(run.extra.get("duct_normal_direction") or 2)
+    nz, ny, nx = params.shape
+    w = np.zeros((nz, ny, nx))
+    if normal == 1:
+        w[:, :, 0] = 1.0
+        w[:, :, nx - 1] = 1.0
+    elif normal == 2:
+        w[:, 0, :] = 1.0
+        w[:, ny - 1, :] = 1.0
+    elif normal == 3 and params.ndims == 3:
+        w[0] = 1.0
+        if params.nz == params.ny:
+            w[nz - 1] = 1.0
+    return w.ravel()
+
+
+def no_walls(params, run):
+    """The stock initialize_walls_nowalls plugin: every site is pore."""
+    return np.zeros(params.nsites)

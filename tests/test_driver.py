@@ -331,3 +331,20 @@ def test_bubble_plugin_on_the_reference_3d_deck():
     assert box.sum() == 21 ** 3
     c = (p.nx + 1) // 2 - 1  # 0-based index of the 1-based centre (N+1)/2
     assert box[c - 10:c + 11, c - 10:c + 11, c - 10:c + 11].all()
+
+
+def test_duct_walls_plugin():
+    from taxila import problems
+    p, run = O.params_from_options(O.parse_deck_text(BASE))
+    w = problems.duct_walls(p, run).reshape(p.shape)
+    assert w[:, [0, -1], :].all() and not w[:, 1:-1, :].any()  # default normal: y
+    p3, run3 = O.params_from_options(O.parse_deck_text(
+        "-NX 4\n-NY 5\n-NZ 6\n-discretization d3q19\n-duct_normal_direction 3\n"))
+    w3 = problems.duct_walls(p3, run3).reshape(p3.shape)
+    # as in the reference, the top z wall needs NZ == NY
+    assert w3[0].all() and not w3[1:].any()
+    p4, run4 = O.params_from_options(O.parse_deck_text(
+        "-NX 4\n-NY 5\n-NZ 5\n-discretization d3q19\n-duct_normal_direction 1\n"))
+    w4 = problems.duct_walls(p4, run4).reshape(p4.shape)
+    assert w4[:, :, [0, -1]].all() and not w4[:, :, 1:-1].any()
+    assert not problems.no_walls(p, run).any()
