@@ -98,7 +98,9 @@ def bubble_plugin(only_pore=True):
     the deck (tests/bubble_2D/initialize_state.F90:80-95, :163-180) and fills
     the box (N+1)/2 +- 10 in 3D, +- 26 in 2D (:104-109, :187-190).  The
     bubble_2D plugin leaves wall sites at 0 (only_pore=True); the bubble_3D
-    and bubble_2D_hots plugins fill every site (only_pore=False)."""
+    and bubble_2D_hots plugins and the stock initialize_state_bubble
+    (src/problem_specs/initialize_state_bubble.F90) fill every site
+    (only_pore=False)."""
     def plugin(params, run, walls):
         from .options import DeckError, _reals
         s = params.ncomponents
@@ -141,3 +143,70 @@ def duct_walls(params, run):
 def no_walls(params, run):
     """The stock initialize_walls_nowalls plugin: every site is pore."""
     return np.zeros(params.nsites)
+
+
+def _singlephase_face(extra, face, direction):
+    # the first of pressure, flux, velocity given for the face (:95-120)
+    if ("bc_pressure_%s_value" % face) in extra:
+        return "pressure", float(extra["bc_pressure_%s_value" % face])
+    if ("bc_flux_%s_value" % face) in extra:
+        return "flux", float(extra["bc_flux_%s_value" % face])
+    if ("bc_velocity_%s_values" % face) in extra:
+        from .options import _reals
+        v = _reals(extra["bc_velocity_%s_values" % face] or "")
+        return "velocity", v[direction - 1] if len(v) >= direction else 0.0
+    return None, 0.0
+
+
+def singlephase_state(params, run, walls):
+    """The stock initialize_state_singlephase plugin as a driver plugin
+    (plugin(params, run, walls) -> (rho, u)), following
+    src/problem_specs/initialize_state_singlephase.F90:66-299 as written.
+    Along -flow_direction (1 = x default, 2 = y, 3 = z) the two faces' values
+    are read as pressure, flux or velocity (the first given).  Every
+    component starts at rho = 1, u = 0; the first component then gets: for
+    two pressures a linear profile 3 (p_left (1 - t) + p_right t), t = (i - 1)
+    / (N - 1) over the 1-based index along the axis; for pressure and flux
+    rho = 3 p, u = -flux / (3 p) (flux on the left: u = flux / (3 p)); for two
+    fluxes rho = 1, u = (flux_left - flux_right) / 2; for two velocities
+    rho = 1, u = mean; and the mixed velocity cases as in the source.  Every
+    site is set, walls included."""
+    nd, s = params.ndims, params.ncomponents
+    direction = int(run.extra.get("flow_direction") or 1)
+    rho = np.ones((params.nsites, s))
+    u = np.zeros((params.nsites, nd, s))
+    if not 1 <= direction <= nd:
+        return rho.ravel(), u.ravel()
+    ax = "xyz"[direction - 1]
+    (bl, vl), (br, vr) = (_singlephase_face(run.extra, ax + side, direction) for side in ("m", "p"))
+    r0, u0 = None, None
+    if bl == "pressure":
+        if br == "pressure":
+            n = (params.nx, params.ny, params.nz)[direction - 1]
+            i, j, k = _grid(params.nx, params.ny, params.nz if nd == 3 else 1)
+            idx = (i, j, k)[direction - 1].ravel()
+            t = (idx - 1.0) / (n - 1.0)
+            r0 = (vl * (1 - t) + vr * t) * 3.0
+        elif br == "flux":
+            r0, u0 = vl * 3.0, -vr / (vl * 3.0)
+        elif br == "velocity":
+            r0, u0 = vl * 3.0, vr
+    elif bl == "flux":
+        if br == "pressure":
+            r0, u0 = vr * 3.0, vl / (vr * 3.0)
+        elif br == "flux":
+            r0, u0 = 1.0, (vl - vr) / 2.0
+        elif br == "velocity":
+            r0, u0 = vl / vr, vr
+    elif bl == "velocity":
+        if br == "pressure":
+            r0, u0 = vr * 3.0, vl
+        elif br == "flux":
+            r0, u0 = -vr / vl, vl
+        elif br == "velocity":
+            r0, u0 = 1.0, (vl + vr) / 2.0
+    if r0 is not None:
+        rho[:, 0] = r0
+    if u0 is not None:
+        u[:, direction - 1, 0] = u0
+    return rho.ravel(), u.ravel()

@@ -348,3 +348,41 @@ def test_duct_walls_plugin():
     w4 = problems.duct_walls(p4, run4).reshape(p4.shape)
     assert w4[:, :, [0, -1]].all() and not w4[:, :, 1:-1].any()
     assert not problems.no_walls(p, run).any()
+
+
+SINGLE = """
+-NX 5
+-NY 3
+-NZ 4
+-discretization d3q19
+-ncomponents 1
+"""
+
+
+@pytest.mark.parametrize("faces,rho_expect,u_expect", [
+    ("-bc_pressure_xm\n-bc_pressure_xm_value 0.4\n-bc_pressure_xp\n-bc_pressure_xp_value 0.3",
+     lambda t: 3.0 * (0.4 * (1 - t) + 0.3 * t), 0.0),
+    ("-bc_pressure_xm\n-bc_pressure_xm_value 0.4\n-bc_flux_xp\n-bc_flux_xp_value 0.01",
+     lambda t: 1.2 + 0 * t, -0.01 / 1.2),
+    ("-bc_flux_xm\n-bc_flux_xm_value 0.02\n-bc_flux_xp\n-bc_flux_xp_value 0.01", lambda t: 1.0 + 0 * t, 0.005),
+    ("-bc_velocity_xm\n-bc_velocity_xm_values 0.02,0,0\n-bc_velocity_xp\n-bc_velocity_xp_values 0.04,0,0",
+     lambda t: 1.0 + 0 * t, 0.03),
+])
+def test_singlephase_plugin(faces, rho_expect, u_expect):
+    # initialize_state_singlephase: the first component along -flow_direction
+    # (x here): a linear pressure profile over the 1-based x index, or the
+    # closed forms of the mixed face kinds
+    from taxila import problems
+    p, run = O.params_from_options(O.parse_deck_text(SINGLE + faces))
+    rho, u = problems.singlephase_state(p, run, np.zeros(p.nsites))
+    x = np.tile(np.arange(p.nx), p.ny * p.nz)
+    assert np.allclose(rho, rho_expect(x / (p.nx - 1.0)), rtol=0, atol=1e-15)
+    u = u.reshape(p.nsites, 3)
+    assert np.allclose(u[:, 0], u_expect, rtol=0, atol=1e-15) and not u[:, 1:].any()
+
+
+def test_singlephase_plugin_without_faces_is_rest():
+    from taxila import problems
+    p, run = O.params_from_options(O.parse_deck_text(SINGLE + "-flow_direction 3\n"))
+    rho, u = problems.singlephase_state(p, run, np.zeros(p.nsites))
+    assert np.all(rho == 1.0) and not u.any()
