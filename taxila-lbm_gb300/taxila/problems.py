@@ -210,3 +210,9 @@ def singlephase_state(params, run, walls):
     if u0 is not None:
         u[:, direction - 1, 0] = u0
     return rho.ravel(), u.ravel()
+
+
+# The stock defaults: default_initialize_state.F90 is the single-phase plugin
+# (the two files are identical) and default_initialize_walls.F90 sets no walls.
+default_state = singlephase_state
+default_walls = no_walls
