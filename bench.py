@@ -46,6 +46,8 @@ UNIT = "MLUPS"
 N_SIDE = 128
 BYTES_PER_LUP_STEP = 2 * 19 * 2 * 8 + 1   # k_step: read + write 2x19 FP64 populations + mask
 BYTES_PER_LUP_DENSITY = 19 * 2 * 8 + 2 * 8 + 1  # k_density: read populations, write rho, mask
+# steps of the host-core baseline on the GPU line (about 10 s of CPU work)
+CPU_BASELINE_STEPS = 40
 
 
 FORMS = {"f64": P.PREC_F64, "f32": P.PREC_F32, "f16": P.PREC_F32_F16}
@@ -171,33 +173,53 @@ def cpu_oracle_mlups(p, walls, rho, steps, threads):
     return p.nsites * steps / dt / 1e6, dt
 
 
+def cpu_model():
+    """Host CPU model name (for the record beside the core count)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                    name = v.strip()
+                    if k.strip() == "CPU part":
+                        name = {"0xd4f": "Neoverse V2 (Grace)"}.get(name, "Arm CPU part " + name)
+                    return name
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def run_reference(args):
+    """The reference algorithm on the host cores: exactly --steps timed steps
+    of the full 128^3 lattice after --warmup untimed ones."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    from oracle import Oracle
     threads = os.cpu_count() or 1
     p = workload_params()
     walls, rho = workload_state(p)
-    sample = max(1, min(args.steps, 4))
-    vals = []
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_oracle_mlups(p, walls, rho, 1, threads)
-    total = 0.0
-    for _ in range(max(1, min(args.steps, 3))):
-        v, dt = cpu_oracle_mlups(p, walls, rho, sample, threads)
-        vals.append(v)
-        total += dt
-    v = statistics.median(vals)
+    o = Oracle(p, threads=threads)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.init()
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    v = p.nsites * args.steps / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(p.nsites / v / 1e3, 3),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "D3Q19 128^3 2-component MRT Shan-Chen bubble (r=24, rho 2.0/0.06, G=0.9 -> g_12=0.15), periodic, FP64",
                    "parallelism": "host OpenMP", "l2": "not applicable (CPU)"},
-        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d timed samples of %d steps of the full 128^3 lattice (%.1f s CPU); the reference "
-                                   "Fortran/PETSc 3.6 build is not buildable here, its C restatement runs instead"
-                                   % (len(vals), sample, total)},
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
+                         "sample": "%d timed steps of the full 128^3 lattice after %d warm-up steps (%.1f s); the "
+                                   "reference Fortran/PETSc 3.6 build is not buildable here, its C restatement runs "
+                                   "instead" % (args.steps, args.warmup, dt)},
         "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -475,6 +497,48 @@ def serving_run(n=30, rate=30.0, seed=1):
     return out
 
 
+def peaks_run(gpu):
+    """Measured issue rates of the FP64 (DFMA, DADD, DMUL) and FP32 (FFMA,
+    packed FFMA2) pipes over the whole GPU, with the SM clock sampled during
+    the probes: G operations per second and lanes per SM per cycle."""
+    import torch
+    from taxila import peaks
+    sms = torch.cuda.get_device_properties(gpu).multi_processor_count
+    with Clocks(gpu) as clk:
+        rates = peaks.pipe_rates(sms)
+    c = clk.summary()
+    mhz = c["sm_mhz"] or c["sm_max_mhz"]
+    out = {"sms": sms, "clocks": c, "unit": "G operations/s (DFMA/FFMA: one FMA per operation)"}
+    for op, r in rates.items():
+        out[op] = {"g_per_s": round(r["ops_per_s"] / 1e9, 2), "ms_per_launch": round(r["ms_per_launch"], 3),
+                   "per_sm_per_cycle": round(peaks.per_sm_cycle(r["ops_per_s"], sms, mhz), 3) if mhz else None}
+    out["fp64_tflops_dfma"] = round(2 * rates["dfma"]["ops_per_s"] / 1e12, 3)
+    return out
+
+
+def fp64_counts():
+    """FP64 instructions per lattice site of the FP64 k_step, from its ncu capture."""
+    with open(os.path.join(REPO, "profiles", "k_step_d3q19_2c_mrt_fp64_instr.json")) as f:
+        return json.load(f)
+
+
+def fp64_bound(pk, sites, k_ms):
+    """k_step of the FP64 form against the measured FP64 pipe: the time its
+    FP64 instructions need at the probes' rates, as a fraction of the
+    kernel's event-timed duration."""
+    c = fp64_counts()
+    n = {op: c["per_site"][op] for op in ("dadd", "dfma", "dmul")}
+    t_pipe = sum(sites * n[op] / (pk[op]["g_per_s"] * 1e9) for op in n)
+    instr = sum(n.values())
+    return {"pipe": "fp64", "fp64_instr_per_lup": instr, "per_lup": n,
+            "fp64_flop_per_lup": n["dadd"] + n["dmul"] + 2 * n["dfma"],
+            "achieved_g_instr_per_s": round(sites * instr / (k_ms * 1e-3) / 1e9, 1),
+            "peak_g_instr_per_s": round(pk["dfma"]["g_per_s"], 1),
+            "frac": round(t_pipe / (k_ms * 1e-3), 4),
+            "peak_source": "measured (peaks: DFMA/DADD/DMUL probes, this run)",
+            "counts_source": c["source"]}
+
+
 def conservation_mass(h):
     """Each component's mass from tx_conservation, or the error text."""
     try:
@@ -554,26 +618,37 @@ def run_gpu(args):
                      "kernel": "k_step (collide + push, %d B/LUP algorithmic)" % bpl,
                      "ms_per_launch": round(k_ms, 4), "ms_k_density": round(t_dens / nk, 4),
                      "peak_source": peak_kind,
-                     "compute_bound": ({"pipe": "fp64", "active_frac": 0.868, "fp64_instr_per_lup": 412,
-                                        "fp64_flop_per_lup": 539,
-                                        "fp64_instr_per_s": round(p.nsites * 412 / (k_ms * 1e-3) / 1e9, 1),
-                                        "fp64_instr_peak_per_s": round(2 * 152 * 2.07, 1),
-                                        "fp64_tflops": round(value / ws * 539 / 1e6, 3),
-                                        "source": "ncu sm__pipe_fp64_cycles_active and "
-                                                  "smsp__sass_thread_inst_executed_op_d{add,fma,mul} of k_step, 96^3 "
-                                                  "capture (profiles/k_step_d3q19_2c_mrt_96.md)"}
-                                       if args.form == "f64" else None),
-                     "note": "the FP64 form is bound by GB300's FP64 pipe (2 lanes per SM per cycle, "
-                             "fp64_instr_* in G instructions/s): its HBM fraction is low by construction; "
-                             "see the fp32/fp16 forms for the HBM-bound ones"},
+                     "compute_bound": None,
+                     "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM (compute_bound: its FP64 "
+                             "instructions per site against the measured FP64 instruction rate); the fp32/fp16 "
+                             "forms are the HBM-bound ones"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
+    small = {}
+    if args.form == "f64" and not args.quick:
+        # measured FP64 ceiling of the step kernel (pipe probes, sampled clock)
+        try:
+            small["peaks"] = peaks_run(gpu)
+            line["roofline"]["compute_bound"] = fp64_bound(small["peaks"], p.nsites, k_ms)
+        except Exception as ex:  # report, do not hide
+            small["peaks"] = {"error": str(ex)}
     if ws == 1 and not args.quick and args.form == "f64" and args.n == N_SIDE:
         try:
-            line["e2e"] = e2e_run(max(10, args.steps // 4), 2)
+            line["e2e"] = e2e_run(args.steps, 2)
         except Exception as ex:  # report, do not hide
             line["e2e"] = {"value": None, "unit": UNIT, "error": str(ex)}
+        # the long legs first: the end of the line (what a tail of the output
+        # keeps) holds the short per-form figures
+        legs = (("batched", batched_run),
+                ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
+                ("serving", serving_run),
+                ("bubble_2d", bubble_2d_run))
+        for key, fn in legs:
+            try:
+                line[key] = fn()
+            except Exception as ex:  # report, do not hide
+                line[key] = {"error": str(ex)}
         forms = {}
         for name, prec in (("fp32", P.PREC_F32), ("fp16_storage", P.PREC_F32_F16)):
             try:
@@ -584,32 +659,26 @@ def run_gpu(args):
                 forms[name] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
             except Exception as ex:
                 forms[name] = {"error": str(ex)}
-        line["precision_forms"] = forms
+        small["precision_forms"] = forms
         try:
             # the same workload with the isotropy-8 psi gradient (the higher-order variant)
             q8 = workload_params(P.PREC_F64)
             q8.isotropy_order = 8
             r = measure_form(P.PREC_F64, max(20, args.steps // 4), args.warmup, p=q8)
-            line["fp64_iso8"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
+            small["fp64_iso8"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
         except Exception as ex:
-            line["fp64_iso8"] = {"error": str(ex)}
-        legs = (("bubble_2d", bubble_2d_run),
-                ("batched", batched_run),
-                ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
-                ("serving", serving_run))
-        for key, fn in legs:
-            try:
-                line[key] = fn()
-            except Exception as ex:  # report, do not hide
-                line[key] = {"error": str(ex)}
+            small["fp64_iso8"] = {"error": str(ex)}
         try:
             threads = os.cpu_count() or 1
-            v, dt = cpu_oracle_mlups(p, walls, rho, 3, threads)
-            line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": "3 steps of the full 128^3 lattice (%.1f s), C restatement of the "
-                                              "reference step, OpenMP" % dt}
+            nb = CPU_BASELINE_STEPS
+            v, dt = cpu_oracle_mlups(p, walls, rho, nb, threads)
+            line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": threads, "cpu": cpu_model(),
+                                    "kind": "port",
+                                    "sample": "%d steps of the full 128^3 lattice (%.1f s), C restatement of the "
+                                              "reference step, OpenMP" % (nb, dt)}
         except Exception as ex:
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": str(ex)}
+    line.update(small)
     line["state_check"] = {"rho_delta_norm_last": rho_check}
     if isinstance(mass0, list) and isinstance(mass1, list):
         # each component's mass (FP64 device sums) after init and after every step of this run

@@ -168,7 +168,10 @@ int tx_create(const tx_params* p, tx_handle** out);
 /* LBMDestroy (src/lbm/lbm.F90:99-108). */
 int tx_destroy(tx_handle* h);
 
-/* Last error message of this handle (or of the last failed tx_create when h is NULL). */
+/* Last error message of this handle.  With h NULL: the message of the calling
+ * host thread's last failed call that has no handle (tx_create,
+ * tx_step_static, tx_batch_create); each host thread keeps its own, and the
+ * pointer stays valid until that thread's next such failure. */
 const char* tx_last_error(const tx_handle* h);
 
 /* WallsSetValues (src/lbm/lbm_walls.F90:151-177): natural-order wall codes,
@@ -258,9 +261,12 @@ int tx_sync(tx_handle* h);
  * (the reference's restart path) for the FP64 form.  All working storage comes
  * from one static device array of TX_STATIC_SCRATCH_BYTES; lattices that need
  * more return TX_ERR_ARG.  The first call on a device looks up that array's
- * address, so make it before any stream capture.  Calls share the array:
- * calls whose GPU work overlaps race.  The call is synchronous on `stream`
- * (a cudaStream_t; NULL = default stream).  Errors: tx_last_error(NULL). */
+ * address, so make it before any stream capture; after a cudaDeviceReset of
+ * that device the address is stale, so do not call this on a reset device in
+ * the same process.  Calls share the array: calls whose GPU work overlaps
+ * race.  Bad wall codes are rejected before any step, with fi_out untouched.
+ * The call is synchronous on `stream` (a cudaStream_t; NULL = default
+ * stream), also when it fails.  Errors: tx_last_error(NULL). */
 int tx_step_static(const tx_params* p, const double* walls, const double* fi_in, double* fi_out, int32_t nsteps,
                    void* stream);
 

@@ -21,7 +21,8 @@ import os
 import re
 import sys
 
-DEFAULT_SRC = "/root/reference/src/lbm/lbm_forcing.F90"
+# the reference checkout (TAXILA_REFERENCE overrides the default location)
+DEFAULT_SRC = os.path.join(os.environ.get("TAXILA_REFERENCE", "/root/reference"), "src/lbm/lbm_forcing.F90")
 AXIS = {"X_DIRECTION": 0, "Y_DIRECTION": 1, "Z_DIRECTION": 2}
 
 

@@ -15,6 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtaxila_gb300.so")
+# arithmetic-pipe throughput probes (measurement only, not part of the C ABI)
+PEAKS_SRC = os.path.join(CSRC, "peaks", "tx_peaks.cu")
+PEAKS_LIB = os.path.join(HERE, "libtx_peaks.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-I" + INCLUDE]
@@ -69,6 +72,9 @@ def build(verbose=True, jobs=None):
     objs.sort()
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        subprocess.run(cmd, check=True)
+    if not os.path.exists(PEAKS_LIB) or os.path.getmtime(PEAKS_LIB) < os.path.getmtime(PEAKS_SRC):
+        cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PEAKS_SRC, "-o", PEAKS_LIB]
         subprocess.run(cmd, check=True)
     if verbose:
         print("built", LIB)

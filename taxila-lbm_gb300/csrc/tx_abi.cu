@@ -13,7 +13,10 @@
 
 using namespace tx;
 
-static std::string g_create_error;
+// error text of the calling thread's last failed call without a handle
+// (tx_create, tx_step_static, batch creation): one string per host thread, so
+// failing calls on several threads at once do not race
+static thread_local std::string g_create_error;
 
 struct tx_handle {
   tx_params p{};

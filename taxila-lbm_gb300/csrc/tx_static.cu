@@ -12,10 +12,14 @@
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (the host-side name is only a stand-in and must never be
-// passed to a kernel); make that first call before any stream capture.  All
+// passed to a kernel) and keeps it for the life of the process; make that
+// first call before any stream capture.  A cudaDeviceReset unloads the
+// library's device code, so the kept address is stale afterwards: do not call
+// tx_step_static on a device after resetting it in the same process.  All
 // calls share the one array and leave its contents behind: each call clears
 // what has to start at zero, and calls whose GPU work overlaps (two streams,
-// two host threads) race on it.
+// two host threads) race on it.  A call that fails after queueing work waits
+// for that work before it returns, so a retry never overlaps it.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -163,10 +167,16 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   double* pb = (double*)(base + o_pb);
   unsigned* flag = (unsigned*)(base + o_flag);
 
-#define TX_SCHK(call)                                                                                   \
-  do {                                                                                                  \
-    const cudaError_t e_ = (call);                                                                      \
-    if (e_ != cudaSuccess) return static_fail(TX_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  // on an error after work was queued, wait for that work (ignoring the
+  // result) before returning, so that no kernel still writes the static area
+  // when the caller retries
+#define TX_SCHK(call)                                                                 \
+  do {                                                                                \
+    const cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                          \
+      (void)cudaStreamSynchronize(st);                                                \
+      return static_fail(TX_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    }                                                                                 \
   } while (0)
 
   // what must start at zero: the flag, the density and the second population buffer
@@ -194,6 +204,13 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
     faces.vals[f] = v;
   }
   TX_SCHK(cudaGetLastError());
+  // reject bad wall codes before any step touches fi_out
+  {
+    unsigned bad = 0;
+    TX_SCHK(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    TX_SCHK(cudaStreamSynchronize(st));
+    if (bad) return static_fail(TX_ERR_ARG, "wall codes must be 0 or positive; specular codes 900-902 are not supported");
+  }
 
   StepArgs a{};
   a.rho = rho;
@@ -228,10 +245,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   }
   ks.to_natural(cur, mask, N, shift_of(ph), fi_out, st);
   TX_SCHK(cudaGetLastError());
-  unsigned bad = 0;
-  TX_SCHK(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   TX_SCHK(cudaStreamSynchronize(st));
 #undef TX_SCHK
-  if (bad) return static_fail(TX_ERR_ARG, "wall codes must be 0 or positive; specular codes 900-902 are not supported");
   return TX_OK;
 }

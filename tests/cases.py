@@ -1,10 +1,12 @@
 """Parameter sets and initial states shared by the oracle and GPU tests."""
+import os
+
 import numpy as np
 
 from taxila import params as P
 from taxila import problems
 
-REF = "/root/reference"
+REF = os.environ.get("TAXILA_REFERENCE", "/root/reference")  # the reference checkout
 
 
 def base(disc, shape, ncomp=2, mode=P.SRT, iso=4, periodic=(1, 1, 1)):

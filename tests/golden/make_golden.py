@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-REF = "/root/reference"
+REF = os.environ.get("TAXILA_REFERENCE", "/root/reference")  # the reference checkout
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = {
     "bubble_2D": "tests/bubble_2D/reference_solution/fi001.dat",

@@ -91,3 +91,19 @@ def test_static_step_rejects_lattices_beyond_the_static_area():
     with pytest.raises(TxError) as e:
         step_static(p, d.data_ptr(), d.data_ptr(), d.data_ptr(), 1)
     assert e.value.code == 1 and "bytes of working storage" in str(e.value)
+
+
+def test_static_step_rejects_bad_wall_codes_before_stepping():
+    # a negative wall code is refused before any step: fi_out keeps what the caller put there
+    import torch
+    p, walls, rho = cases.porous_case(P.D3Q19, (12, 10, 14), mode=P.MRT, body=True)
+    bad = np.array(walls, dtype=np.float64)
+    bad[5] = -1.0
+    d_walls = torch.tensor(bad, dtype=torch.float64, device="cuda")
+    n = p.nsites * p.ncomponents * p.Q
+    d_in = torch.ones(n, dtype=torch.float64, device="cuda")
+    d_out = torch.full((n,), 7.0, dtype=torch.float64, device="cuda")
+    with pytest.raises(TxError) as e:
+        step_static(p, d_walls.data_ptr(), d_in.data_ptr(), d_out.data_ptr(), 3)
+    assert e.value.code == 1 and "wall codes" in str(e.value)
+    assert torch.all(d_out == 7.0).item()
