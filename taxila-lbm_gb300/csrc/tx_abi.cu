@@ -58,6 +58,7 @@ struct tx_handle {
   double* sflux = nullptr;
   bool have_species = false;
   bool have_walls = false, have_state = false, have_fi = false, inited = false;
+  int rest_pairs = -1;        // pairs for k_step_rest (paired FP32-arithmetic forms; counted at wall upload)
   bool timing = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double t_step_ms = 0.0, t_density_ms = 0.0;
@@ -109,7 +110,24 @@ StepArgs args(tx_handle* h, int in, int out) {
   a.g = h->g;
   a.faces = h->faces;
   a.step = h->steps_done;
+  a.rest = h->rest_pairs;
   return a;
+}
+
+// Pairs of the paired step that need the per-site kernel (none: it is not launched).
+int count_rest_pairs(tx_handle* h) {
+  h->rest_pairs = -1;
+  if (!h->ks.paired(h->g)) return TX_OK;
+  unsigned* cnt = reinterpret_cast<unsigned*>(h->red);
+  TX_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned), h->stream));
+  h->ks.count_rest(args(h, h->cur, h->cur), cnt, h->stream);
+  const int rc = check_launch(h, "k_count_rest");
+  if (rc) return rc;
+  unsigned n = 0;
+  TX_CUDA(h, cudaMemcpyAsync(&n, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+  TX_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->rest_pairs = (int)n;
+  return TX_OK;
 }
 
 long long field_dof(const tx_handle* h, int field) {
@@ -386,6 +404,10 @@ int tx_create(const tx_params* p, tx_handle** out) {
   }
   for (int i = 0; i < 4; ++i) cudaEventCreate(&h->ev[i]);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cleanup("stream sync failed", TX_ERR_CUDA);
+  if (count_rest_pairs(h) != TX_OK) {
+    const std::string why = h->err;
+    return cleanup(why, TX_ERR_CUDA);
+  }
   *out = h;
   return TX_OK;
 }
@@ -428,7 +450,9 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
     if (!wall_code(walls[i], h->p.nminerals, &h->host_mask[(size_t)i], &why)) return fail(h, TX_ERR_ARG, why);
   }
   TX_CUDA(h, cudaMemcpyAsync(h->mask, h->host_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
-  const int rc = update_links(h);
+  int rc = update_links(h);
+  if (rc != TX_OK) return rc;
+  rc = count_rest_pairs(h);
   if (rc != TX_OK) return rc;
   h->have_walls = true;
   return sync_stream(h);

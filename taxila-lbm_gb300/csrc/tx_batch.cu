@@ -52,6 +52,8 @@ struct Lattice {
   int NS = 0;
   long long bytes = 0;
   long long steps = 0;
+  bool paired = false;        // the paired step (FP32-arithmetic forms, even nx)
+  int rest = -1;              // its pairs for the per-site kernel
 };
 
 size_t pop_bytes(int precision) { return precision == TX_PREC_F64 ? 8 : (precision == TX_PREC_F32 ? 4 : 2); }
@@ -105,6 +107,16 @@ struct tx_batch {
   int4* d_otiles = nullptr;  // outlet-refresh tiles
   int otile_cap = 0;
   int* d_notiles = nullptr;
+  int4* d_stiles = nullptr;  // step tiles: per-site, pair and per-site-of-pairs
+  int stile_cap = 0;
+  int* d_nstiles = nullptr;
+  int4* d_ptiles = nullptr;
+  int ptile_cap = 0;
+  int* d_nptiles = nullptr;
+  int4* d_rtiles = nullptr;
+  int rtile_cap = 0;
+  int* d_nrtiles = nullptr;
+  unsigned* d_count = nullptr;  // pair count of a joining lattice
   bool need_faces = false, need_outlets = false;  // launched once a lattice needs them
   bool tables_ok = true;  // false after a failed rebuild_tables: launches and probes refuse until one succeeds
   // launch shape
@@ -184,6 +196,12 @@ BatchArgs bargs(const tx_batch* b) {
   a.nftiles = b->d_nftiles;
   a.otiles = b->d_otiles;
   a.notiles = b->d_notiles;
+  a.stiles = b->d_stiles;
+  a.nstiles = b->d_nstiles;
+  a.ptiles = b->d_ptiles;
+  a.nptiles = b->d_nptiles;
+  a.rtiles = b->d_rtiles;
+  a.nrtiles = b->d_nrtiles;
   return a;
 }
 
@@ -199,8 +217,27 @@ StepArgs lattice_args(const tx_batch* b, const Lattice* L, int in, int out) {
   a.g = L->g;
   a.faces = L->faces;
   a.steps_ptr = L->steps_dev;
+  a.rest = L->rest;
   (void)b;
   return a;
+}
+
+// Grows a device table to hold n entries (dropping the graph, whose launches
+// name the old address); entries are rewritten by the caller.
+template <class E>
+int grow_table(tx_batch* b, E** ptr, int* cap, int n);
+
+template <class E>
+int grow_table(tx_batch* b, E** ptr, int* cap, int n) {
+  if (n <= *cap) return TX_OK;
+  const int c = std::max(n, 2 * *cap);
+  drop_graph(b);
+  if (*ptr) cudaFreeAsync(*ptr, b->stream);
+  *ptr = nullptr;
+  *cap = 0;
+  TX_BCUDA(b, cudaMallocAsync((void**)ptr, (size_t)c * sizeof(E), b->stream));
+  *cap = c;
+  return TX_OK;
 }
 
 // Rewrites the descriptors and the tile table of the active lattices.
@@ -209,7 +246,7 @@ int rebuild_tables(tx_batch* b) {
   std::vector<LatDesc> descs;
   std::vector<int4> tiles;
   std::vector<int2> ltiles, ftiles;
-  std::vector<int4> otiles;
+  std::vector<int4> otiles, stiles, ptiles, rtiles;
   const long long run = 128LL * (long long)(16 / pop_bytes(b->form.precision));  // sites per density tile
   for (size_t s = 0; s < b->slots.size(); ++s) {
     Lattice* L = b->slots[s];
@@ -225,6 +262,16 @@ int rebuild_tables(tx_batch* b) {
       for (int y = 0; y < L->g.ny; y += b->by)
         for (int x = 0; x < L->g.nx; x += b->bx) tiles.push_back(make_int4((int)s, x, y, z));
     d.tile_count = (int)tiles.size() - d.tile_begin;
+    if (L->paired) {
+      for (int z = 0; z < L->g.nz; z += b->bz)
+        for (int y = 0; y < L->g.ny; y += b->by)
+          for (int x = 0; x < L->g.nx; x += 2 * b->bx) {
+            ptiles.push_back(make_int4((int)s, x, y, z));
+            if (L->rest != 0) rtiles.push_back(make_int4((int)s, x, y, z));
+          }
+    } else {
+      stiles.insert(stiles.end(), tiles.begin() + d.tile_begin, tiles.end());
+    }
     d.ltile_begin = (int)ltiles.size();
     for (long long c0 = 0; c0 < L->g.n; c0 += run) ltiles.push_back(make_int2((int)s, (int)c0));
     d.shell = L->shell;
@@ -291,6 +338,22 @@ int rebuild_tables(tx_batch* b) {
     b->otile_cap = 0;
     TX_BCUDA(b, cudaMallocAsync(&b->d_otiles, (size_t)cap * sizeof(int4), b->stream));
     b->otile_cap = cap;
+  }
+  // the step's tables
+  {
+    const int ns = (int)stiles.size(), np = (int)ptiles.size(), nr = (int)rtiles.size();
+    int rc = grow_table(b, &b->d_stiles, &b->stile_cap, ns);
+    if (!rc) rc = grow_table(b, &b->d_ptiles, &b->ptile_cap, np);
+    if (!rc) rc = grow_table(b, &b->d_rtiles, &b->rtile_cap, nr);
+    if (rc) return rc;
+    if (ns) TX_BCUDA(b, cudaMemcpyAsync(b->d_stiles, stiles.data(), (size_t)ns * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    if (np) TX_BCUDA(b, cudaMemcpyAsync(b->d_ptiles, ptiles.data(), (size_t)np * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    if (nr) TX_BCUDA(b, cudaMemcpyAsync(b->d_rtiles, rtiles.data(), (size_t)nr * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    TX_BCUDA(b, cudaMemcpyAsync(b->d_nstiles, &ns, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    TX_BCUDA(b, cudaMemcpyAsync(b->d_nptiles, &np, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    TX_BCUDA(b, cudaMemcpyAsync(b->d_nrtiles, &nr, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    // the counts are copied from the stack: wait for them before it goes
+    TX_BCUDA(b, cudaStreamSynchronize(b->stream));
   }
   if (nft) TX_BCUDA(b, cudaMemcpyAsync(b->d_ftiles, ftiles.data(), (size_t)nft * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   if (nov) TX_BCUDA(b, cudaMemcpyAsync(b->d_otiles, otiles.data(), (size_t)nov * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
@@ -436,7 +499,9 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
       cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&b->d_ntiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_nltiles, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&b->d_nftiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_notiles, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&b->d_nftiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_notiles, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&b->d_nstiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_nptiles, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&b->d_nrtiles, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_count, sizeof(unsigned)) != cudaSuccess) {
     tx::set_global_error("CUDA device setup failed");
     tx_batch_destroy(b);
     return TX_ERR_NODEVICE;
@@ -445,6 +510,9 @@ int tx_batch_create(const tx_params* form, int64_t hbm_budget_bytes, tx_batch** 
   cudaMemset(b->d_nltiles, 0, sizeof(int));
   cudaMemset(b->d_nftiles, 0, sizeof(int));
   cudaMemset(b->d_notiles, 0, sizeof(int));
+  cudaMemset(b->d_nstiles, 0, sizeof(int));
+  cudaMemset(b->d_nptiles, 0, sizeof(int));
+  cudaMemset(b->d_nrtiles, 0, sizeof(int));
   *out = b;
   return TX_OK;
 }
@@ -456,13 +524,17 @@ int tx_batch_destroy(tx_batch* b) {
   for (Lattice* L : b->slots) free_lattice(b, L);
   b->slots.clear();
   for (void* p : {(void*)b->d_lats, (void*)b->d_tiles, (void*)b->d_parts, (void*)b->d_res, (void*)b->d_ltiles,
-                 (void*)b->d_ftiles, (void*)b->d_otiles})
+                 (void*)b->d_ftiles, (void*)b->d_otiles, (void*)b->d_stiles, (void*)b->d_ptiles, (void*)b->d_rtiles})
     if (p) cudaFreeAsync(p, b->stream);
   if (b->stream) cudaStreamSynchronize(b->stream);
   cudaFree(b->d_ntiles);
   cudaFree(b->d_nltiles);
   cudaFree(b->d_nftiles);
   cudaFree(b->d_notiles);
+  cudaFree(b->d_nstiles);
+  cudaFree(b->d_nptiles);
+  cudaFree(b->d_nrtiles);
+  cudaFree(b->d_count);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return TX_OK;
@@ -626,6 +698,22 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
       k_links<3><<<l.grid, l.block, 0, st>>>(L->mask, L->g, L->links);
     else
       k_links<2><<<l.grid, l.block, 0, st>>>(L->mask, L->g, L->links);
+  }
+  // the paired step and its pairs for the per-site kernel
+  L->paired = b->ks.paired(L->g);
+  L->rest = -1;
+  if (L->paired) {
+    unsigned n = 0;
+    const bool okc = cudaMemsetAsync(b->d_count, 0, sizeof(unsigned), st) == cudaSuccess &&
+                     (b->ks.count_rest(lattice_args(b, L, b->flip, b->flip), b->d_count, st),
+                      cudaGetLastError() == cudaSuccess) &&
+                     cudaMemcpyAsync(&n, b->d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                     cudaStreamSynchronize(st) == cudaSuccess;
+    if (!okc) {
+      if (sconc) cudaFreeAsync(sconc, st);
+      return undo("pair count failed", TX_ERR_CUDA);
+    }
+    L->rest = (int)n;
   }
   // FlowFiInit + FlowUpdateMoments into the buffer that holds the state at the batch's flip
   const StepArgs a = lattice_args(b, L, b->flip, b->flip);

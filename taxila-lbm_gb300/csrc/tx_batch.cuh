@@ -20,6 +20,7 @@
 // LatDesc::a.fout.
 #pragma once
 #include "tx_kernels.cuh"
+#include "tx_pair.cuh"
 #include "tx_species.cuh"
 
 namespace tx {
@@ -61,6 +62,15 @@ struct BatchArgs {
   const int* nftiles;
   const int4* otiles; // outlet refresh: (lattice slot, face, first node, 0) of runs of 128 nodes
   const int* notiles;
+  // the step: per-site tiles of the lattices without the paired kernel; pair
+  // tiles (x extent twice the block's) of those with it, and the pair tiles
+  // of the lattices that have pairs for the per-site kernel
+  const int4* stiles;
+  const int* nstiles;
+  const int4* ptiles;
+  const int* nptiles;
+  const int4* rtiles;
+  const int* nrtiles;
 };
 
 __device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
@@ -74,12 +84,55 @@ __device__ __forceinline__ StepArgs flipped(const StepArgs& s, int flip) {
 
 template <int D, int S, int ISO, bool MRT, class T, class R, class RT>
 __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT)) k_step_tiles(BatchArgs b, int flip) {
-  const int nt = __ldg(b.ntiles);
+  const int nt = __ldg(b.nstiles);
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-    const int4 tl = __ldg(b.tiles + t);
+    const int4 tl = __ldg(b.stiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
     if (x < a.g.nx && y < a.g.ny && z < a.g.nz) step_site<D, S, ISO, MRT, false, T, R, RT>(a, x, y, z);
+  }
+}
+
+// The paired step of k_step_pair over the pair tiles (thread (i, j, k) of a
+// tile takes the pair at x = x0 + 2 i).
+template <int D, int S, int ISO, bool MRT, class T>
+__global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.nptiles);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.ptiles + t);
+    const StepArgs a = flipped(b.lats[tl.x].a, flip);
+    const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+    const int x0 = tl.y + 2 * (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    bool run = false, full = false;
+    uint2 ll = make_uint2(0u, 0u);
+    if (x0 < a.g.nx && y < a.g.ny && z < a.g.nz) {
+      const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+      ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+      run = pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 1;
+      constexpr uint32_t all = all_links<D>() | 1u;
+      full = (ll.x & all) == all && (ll.y & all) == all;
+    }
+    // every lane votes, so that the vote is uniform over the warp's running lanes
+    const bool warp_full = __all_sync(0xffffffffu, full || !run);
+    if (run) step_pair<D, S, ISO, MRT, T>(a, x0, y, z, ll.x, ll.y, warp_full);
+  }
+}
+
+// The per-site step of the pairs that k_step_pair_tiles leaves (k_step_rest).
+template <int D, int S, int ISO, bool MRT, class T>
+__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, float, MRT)) k_step_rest_tiles(BatchArgs b, int flip) {
+  const int nt = __ldg(b.nrtiles);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const int4 tl = __ldg(b.rtiles + t);
+    const StepArgs a = flipped(b.lats[tl.x].a, flip);
+    const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+    const int x0 = tl.y + 2 * (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    if (x0 < a.g.nx && y < a.g.ny && z < a.g.nz) {
+      const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+      const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+      if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 0)
+        for (int k = 0; k < 2; ++k) step_site<D, S, ISO, MRT, false, T, float, float>(a, x0 + k, y, z);
+    }
   }
 }
 

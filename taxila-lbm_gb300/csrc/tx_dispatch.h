@@ -7,6 +7,7 @@
 #include "tx_batch.cuh"
 #include "tx_host_params.h"
 #include "tx_kernels.cuh"
+#include "tx_pair.cuh"
 #include "tx_species.cuh"
 
 namespace tx {
@@ -29,6 +30,10 @@ struct KernelSet {
   // their batched forms (no-ops in the exact form)
   void (*faces_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   void (*outlet_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
+  // paired-site step (FP32-arithmetic forms, even nx): whether a lattice takes
+  // it, and how many of its pairs need the per-site kernel (counted into *count)
+  bool (*paired)(const Geo&);
+  void (*count_rest)(const StepArgs&, unsigned* count, cudaStream_t);
   const char* name;
 };
 
@@ -72,6 +77,13 @@ inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block 
 struct Launch3 {
   dim3 grid, block;
 };
+inline Launch3 launch3(const Geo& g, int threads);
+// the launch of the paired kernels: the sites' grid with x halved
+inline Launch3 launch_pairs(const Geo& g, int threads) {
+  Geo h = g;
+  h.nx = g.nx / 2;
+  return launch3(h, threads);
+}
 inline Launch3 launch3(const Geo& g, int threads) {
   int bx = ((g.nx + 31) / 32) * 32;
   if (bx > 128) bx = 128;
@@ -90,8 +102,24 @@ inline Launch3 launch3(const Geo& g, int threads) {
 #define TX_FORM_LAUNCHERS(D, S, ISO, MRT, EXACT, T, R, RT) TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)
 #define TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)                                                  \
   struct L_##S##_##ISO##_##MRT {                                                                             \
+    static constexpr bool kPairForm = !EXACT && std::is_same<R, float>::value;                                \
+    static bool paired(const Geo& g) { return kPairForm && g.nx % 2 == 0; }                                   \
     static void step(const StepArgs& a, cudaStream_t s) {                                                     \
+      if constexpr (kPairForm) {                                                                              \
+        if (paired(a.g)) {                                                                                    \
+          const Launch3 l = launch_pairs(a.g, 128);                                                           \
+          k_step_pair<D, S, ISO, MRT, T><<<l.grid, l.block, 0, s>>>(a);                                       \
+          if (a.rest != 0) k_step_rest<D, S, ISO, MRT, T><<<l.grid, l.block, 0, s>>>(a);                      \
+          return;                                                                                             \
+        }                                                                                                     \
+      }                                                                                                       \
       k_step<D, S, ISO, MRT, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a);                        \
+    }                                                                                                         \
+    static void count_rest(const StepArgs& a, unsigned* count, cudaStream_t s) {                              \
+      if constexpr (kPairForm) {                                                                              \
+        const Launch3 l = launch_pairs(a.g, 256);                                                             \
+        if (paired(a.g)) k_count_rest<D, ISO><<<l.grid, l.block, 0, s>>>(a, count);                           \
+      }                                                                                                       \
     }                                                                                                         \
     static void density(const StepArgs& a, int mode, cudaStream_t s) {                                        \
       constexpr int VW = 16 / (int)sizeof(T);                                                                 \
@@ -114,6 +142,10 @@ inline Launch3 launch3(const Geo& g, int threads) {
     }                                                                                                         \
     static void step_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {                \
       if constexpr (!EXACT) k_step_tiles<D, S, ISO, MRT, T, R, RT><<<grid, blk, 0, s>>>(b, flip);             \
+      if constexpr (kPairForm) {                                                                              \
+        k_step_pair_tiles<D, S, ISO, MRT, T><<<grid, blk, 0, s>>>(b, flip);                                   \
+        k_step_rest_tiles<D, S, ISO, MRT, T><<<grid, blk, 0, s>>>(b, flip);                                   \
+      }                                                                                                       \
     }                                                                                                         \
     static void density_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {             \
       if constexpr (!EXACT) k_density_tiles<D, S, T, R, RT><<<grid, blk, 0, s>>>(b, flip);                    \
@@ -147,6 +179,7 @@ inline Launch3 launch3(const Geo& g, int threads) {
                     &L_##S##_##ISO##_##MRT::probe_tiles, &L_##S##_##ISO##_##MRT::faces,                        \
                     &L_##S##_##ISO##_##MRT::outlet, &L_##S##_##ISO##_##MRT::faces_tiles,                          \
                     &L_##S##_##ISO##_##MRT::outlet_tiles,                                                         \
+                    &L_##S##_##ISO##_##MRT::paired, &L_##S##_##ISO##_##MRT::count_rest,                          \
                     MRT ? #S "c iso" #ISO " rates:any" : #S "c iso" #ISO " rates:bgk/s_nu"};                    \
     return true;                                                                                               \
   }

@@ -205,6 +205,9 @@ struct StepArgs {
   // counter that the density pass advances (so replayed graphs see it move).
   unsigned step;
   const unsigned* steps_ptr;
+  // FP32-arithmetic forms on lattices with an even nx (tx_pair.cuh): pairs
+  // that need the per-site kernel k_step_rest (-1: not counted, run it)
+  int rest;
 };
 
 // psi(rho) of one component: EOSApply_Rho / _SC / _Thermo / _PR
@@ -594,7 +597,10 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
 // rfd: stored forcing density of the site (rho - rho0); rf: rho itself;
 // psi: the psi(rho) field when the EOS is on (then the fluid-fluid force
 // differentiates psi and scales by psi(x), FlowCalcForces lbm_flow.F90:790-806).
-template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT>
+// BULK_ONLY: the caller guarantees that every stencil neighbour is pore
+// whenever the fluid-fluid force is on (the general wall-aware gradient is
+// then not compiled in).
+template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT, bool BULK_ONLY = false>
 __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P,
                                             const uint8_t* mask, const RT* rho, const RT* psi, long long N,
                                             const R rfd[S], const R rf[S], R F[S][D]) {
@@ -701,6 +707,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
       return;
     }
   }
+  if constexpr (BULK_ONLY) return;
   {
     R gr[S][D];
     R ws[D];

@@ -1,0 +1,530 @@
+// Paired-site step kernels of the FP32-arithmetic forms (FP32 or FP16
+// population storage).
+//
+// One thread updates two x-adjacent sites (x0 even, x0 + 1) of a lattice with
+// an even nx.  Every per-site quantity of the collision is a V2, the value at
+// both sites, and every V2 operation is one packed FP32x2 instruction of
+// sm_100+ (FADD2 / FMUL2 / FFMA2), so the collision costs half the FP32
+// instructions per site.  The two sites' populations of one direction are
+// adjacent in memory: they load with one 8-byte (FP32) or 4-byte (FP16) load,
+// and the rest population and the pushes along y and z store with one.  Site
+// indices, neighbourhoods and stream offsets are formed once per pair.
+//
+// k_step_pair takes the pairs whose pore sites are all "simple": not on a
+// Dirichlet-class face and, when the fluid-fluid force is on, with every
+// gradient-stencil neighbour pore (the bulk gradient).  k_step_rest runs the
+// per-site step (step_site) on the pore sites of every other pair.  Each pore
+// slot of the next state has exactly one writer, so the two launches are
+// independent.  The per-site arithmetic is the fast form of step_site, in the
+// same expression shapes; only the FMA contractions differ.
+#pragma once
+#include "tx_kernels.cuh"
+
+// Resident 128-thread blocks per SM that ptxas must make room for in
+// k_step_pair: 3 (168 registers) for one component, 2 (255) for two, whose
+// collision keeps both components' pair terms live; each thread carries two
+// sites, so two blocks keep as many sites in flight as four of step_site.
+#ifndef TX_PAIR_MIN_BLOCKS_S1
+#define TX_PAIR_MIN_BLOCKS_S1 3
+#endif
+#ifndef TX_PAIR_MIN_BLOCKS_S2
+#define TX_PAIR_MIN_BLOCKS_S2 2
+#endif
+#define TX_PAIR_MIN_BLOCKS(S) ((S) == 1 ? TX_PAIR_MIN_BLOCKS_S1 : TX_PAIR_MIN_BLOCKS_S2)
+
+namespace tx {
+
+// ------------------------------------------------------------ V2 arithmetic
+struct V2 {
+  float x, y;
+};
+__host__ __device__ __forceinline__ V2 v2(float a) { return V2{a, a}; }
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float2 f2_(V2 a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ V2 v2_(float2 a) { return V2{a.x, a.y}; }
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), f2_(b))); }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), make_float2(-b.x, -b.y))); }
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return v2_(__fmul2_rn(f2_(a), f2_(b))); }
+__device__ __forceinline__ V2 fma2(V2 a, V2 b, V2 c) { return v2_(__ffma2_rn(f2_(a), f2_(b), f2_(c))); }
+#else
+inline V2 operator+(V2 a, V2 b) { return V2{a.x + b.x, a.y + b.y}; }
+inline V2 operator-(V2 a, V2 b) { return V2{a.x - b.x, a.y - b.y}; }
+inline V2 operator*(V2 a, V2 b) { return V2{a.x * b.x, a.y * b.y}; }
+inline V2 fma2(V2 a, V2 b, V2 c) { return V2{__builtin_fmaf(a.x, b.x, c.x), __builtin_fmaf(a.y, b.y, c.y)}; }
+#endif
+__host__ __device__ __forceinline__ V2 operator-(V2 a) { return V2{-a.x, -a.y}; }
+
+// c_n . v over the nonzero components of c_n (no zero start: the first term seeds)
+template <int D, int n>
+__device__ __forceinline__ V2 cdot2(const V2 v[D]) {
+  V2 acc{0.f, 0.f};
+  bool first = true;
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    constexpr int c = Lat<D>::c(n, d);
+    if constexpr (c != 0) {
+      if (first)
+        acc = c > 0 ? v[d] : -v[d];
+      else
+        acc = c > 0 ? acc + v[d] : acc - v[d];
+      first = false;
+    }
+  });
+  return acc;
+}
+
+// ---------------------------------------------------------- storage pairs
+// Two floats to FP16, rounded toward zero, a in the low half (one cvt.rz.f16x2.f32).
+__device__ __forceinline__ uint32_t pack_half2_rz(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  uint32_t u;
+  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(u) : "f"(b), "f"(a));
+  return u;
+#else
+  const __half ha = __float2half_rz(a), hb = __float2half_rz(b);
+  uint16_t la, lb;
+  memcpy(&la, &ha, 2);
+  memcpy(&lb, &hb, 2);
+  return (uint32_t)la | ((uint32_t)lb << 16);
+#endif
+}
+
+// Population deviations of the two sites at p (p at an even cell of one stream).
+template <class T>
+__device__ __forceinline__ V2 ld_pair(const T* p, const PhysT<float>& P) {
+  if constexpr (std::is_same<T, __half>::value) {
+    const __half2 h = __ldg(reinterpret_cast<const __half2*>(p));
+    const float2 f = __half22float2(h);
+    return V2{f.x, f.y} * v2(P.inv_sscale);
+  } else {
+    const float2 f = __ldg(reinterpret_cast<const float2*>(p));
+    return V2{f.x, f.y};
+  }
+}
+
+// Both sites' values to the adjacent slots at p (FP16: stochastic rounding
+// with the per-site dithers d0, d1, exactly as st_dev_sr rounds each).
+template <class T>
+__device__ __forceinline__ void st_pair(T* p, V2 v, const PhysT<float>& P, uint32_t d0, uint32_t d1) {
+  if constexpr (std::is_same<T, __half>::value) {
+    const V2 s = v * v2(P.sscale);
+    const float a = __uint_as_float(__float_as_uint(s.x) + d0);
+    const float b = __uint_as_float(__float_as_uint(s.y) + d1);
+    *reinterpret_cast<uint32_t*>(p) = pack_half2_rz(a, b);
+  } else {
+    *reinterpret_cast<float2*>(p) = make_float2(v.x, v.y);
+  }
+}
+
+// One site's value (lane k of v) at p.
+template <class T>
+__device__ __forceinline__ void st_one(T* p, float v, const PhysT<float>& P, uint32_t d) {
+  st_dev_sr<T, float>(p, v, P, d);
+}
+
+// ------------------------------------------------------------- predicates
+// A pore site the paired kernel can update: not on a Dirichlet-class face and,
+// with the fluid-fluid force on, every gradient-stencil neighbour pore.
+template <int D, int ISO>
+__device__ __forceinline__ bool pair_simple_site(const StepArgs& a, const PhysT<float>& P, uint32_t links, int x, int y,
+                                                 int z) {
+  if (any_dirichlet<D>(a.g, a.faces, x, y, z)) return false;
+  if (!P.ff_on) return true;
+  constexpr int RB = stencil_reach<D, ISO>();
+  return stencil_is_links<D, ISO>() ? ((links | 1u) & (all_links<D>() | 1u)) == (all_links<D>() | 1u)
+         : RB == 2                ? (links & kBoxPore2) != 0u
+                                  : (links & kBoxPore3) != 0u;
+}
+
+// 1: the pair goes to k_step_pair; 0: to k_step_rest; -1: no pore site.
+template <int D, int ISO>
+__device__ __forceinline__ int pair_class(const StepArgs& a, const PhysT<float>& P, uint32_t l0, uint32_t l1, int x0,
+                                          int y, int z) {
+  const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
+  if (!p0 && !p1) return -1;
+  const bool s0 = !p0 || pair_simple_site<D, ISO>(a, P, l0, x0, y, z);
+  const bool s1 = !p1 || pair_simple_site<D, ISO>(a, P, l1, x0 + 1, y, z);
+  return (s0 && s1) ? 1 : 0;
+}
+
+// --------------------------------------------------------------- the pair
+// Pair (x0, x0 + 1) of a row; pairs are laid out like sites with x halved.
+__device__ __forceinline__ bool pair_of(const Geo& g, int& x0, int& y, int& z) {
+  x0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  z = (int)blockIdx.z;
+  return x0 < g.nx && y < g.ny && z < g.nz;
+}
+
+// Collision and push of one component of a simple pair.  FULL: both sites
+// pore with every link pore (no bounceback), so the pushes need no selects;
+// the caller takes FULL only when every active lane of the warp is full.
+template <int D, int S, bool MRT, bool FULL, class T, int RCH>
+struct PairPush {
+  using L = Lat<D>;
+  static constexpr int Q = L::Q;
+  T* fout;
+  unsigned N, c0;
+  uint32_t l0, l1;
+  bool p0, p1;
+  const Hood<D, RCH>* h0;
+  const Hood<D, RCH>* h1;
+  uint32_t seed0, seed1;
+  const PhysT<float>* P;
+
+  template <int n>
+  __device__ __forceinline__ void operator()(std::integral_constant<int, n>, int m, V2 v) const {
+    constexpr int o = opp<D>(n);
+    const uint32_t k = (uint32_t)(m * Q + n);
+    const uint32_t d0 = std::is_same<T, __half>::value ? sr_dither(seed0, k) : 0u;
+    const uint32_t d1 = std::is_same<T, __half>::value ? sr_dither(seed1, k) : 0u;
+    T* const sn = fout + (size_t)k * N;
+    if constexpr (n == 0) {
+      if (FULL || (p0 && p1)) {
+        st_pair<T>(sn + c0, v, *P, d0, d1);
+      } else {
+        if (p0) st_one<T>(sn + c0, v.x, *P, d0);
+        if (p1) st_one<T>(sn + c0 + 1, v.y, *P, d1);
+      }
+    } else {
+      constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
+      if constexpr (FULL) {
+        if constexpr (cx == 0) {
+          st_pair<T>(sn + h0->template at<0, cy, cz>(), v, *P, d0, d1);
+        } else {
+          st_one<T>(sn + h0->template at<cx, cy, cz>(), v.x, *P, d0);
+          st_one<T>(sn + h1->template at<cx, cy, cz>(), v.y, *P, d1);
+        }
+      } else {
+        T* const so = fout + (size_t)(m * Q + o) * N;
+        const bool q0 = ((l0 >> n) & 1u) != 0u, q1 = ((l1 >> n) & 1u) != 0u;
+        if (p0) st_one<T>(q0 ? sn + h0->template at<cx, cy, cz>() : so + c0, v.x, *P, d0);
+        if (p1) st_one<T>(q1 ? sn + h1->template at<cx, cy, cz>() : so + c0 + 1, v.y, *P, d1);
+      }
+    }
+  }
+};
+
+// Fast-form collision of step_site (see there) on V2 values, with the pushes.
+template <int D, int S, bool MRT, bool FULL, class T, int RCH>
+__device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, RCH>& push, const PhysT<float>& P,
+                                             const T* fin, unsigned N, unsigned c0, const V2 rc[S], const V2 rcd[S],
+                                             const V2 F[S][D], const V2 up[D]) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  constexpr int NP = npairs<D>();
+  V2 usqr = up[0] * up[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d) usqr = fma2(up[d], up[d], usqr);
+  const V2 cu_axis = v2(float(1.5 * L::w(1))) * usqr, cu_diag = v2(float(1.5 * L::w(Q - 1))) * usqr;
+  V2 Bo[NP], WBe[NP];
+  sfor<0, NP>([&](auto pp) {
+    constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+    constexpr double w = L::w(n);
+    const V2 ud = cdot2<D, n>(up);
+    Bo[p] = v2(float(3 * w)) * ud;
+    WBe[p] = fma2(v2(float(4.5 * w)) * ud, ud, -(n <= L::NAXIS ? cu_axis : cu_diag));
+  });
+  const V2 WB0 = v2(D == 3 ? -0.5f : float(-2.0 / 3.0)) * usqr;
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    const V2 r = rc[m], rd = rcd[m];
+    const V2 WA0 = v2(P.WAc[m][0]), WA1 = v2(P.WAc[m][1]), WA2 = v2(P.WAc[m][2]);
+    const V2 cA0 = v2(P.cA[m][0]), cA1 = v2(P.cA[m][1]), cA2 = v2(P.cA[m][2]);
+    const V2 s0 = v2(P.s0[m]);
+    const float kf = P.kfac[m];
+    const float keepf = P.keep[m];
+    const V2 keep = v2(keepf);
+    V2 Fu = F[m][0] * up[0], kF[D];
+#pragma unroll
+    for (int d = 1; d < D; ++d) Fu = fma2(F[m][d], up[d], Fu);
+#pragma unroll
+    for (int d = 0; d < D; ++d) kF[d] = v2(kf) * F[m][d];
+    const V2 kFu = v2(kf) * Fu;
+    const V2 G = fma2(s0, r, -kFu);
+    const unsigned spec = P.spec_mask[m];
+    const T* fm = fin + (size_t)m * Q * N + c0;
+    auto pop = [&](auto nn) -> V2 { return ld_pair<T>(fm + (size_t)decltype(nn)::value * N, P); };
+    const V2 E0 = WA0 + WB0;
+    // rest direction: g'_0 = keep g_0 + X0
+    const V2 X0 = s0 * fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * kFu;
+    auto pair_terms = [&](auto pp, V2& pe, V2& po) {
+      constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+      const V2 WA = n <= L::NAXIS ? WA1 : WA2;
+      const V2 Ae = WA + WBe[p];
+      const V2 h = cdot2<D, n>(kF);
+      const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
+      pe = fma2(s0, De, fma2(Bo[p], h, -(Ae * kFu)));
+      po = fma2(Bo[p], G, Ae * h);
+    };
+    if (spec == 0u && keepf == 0.f) {
+      // s0 = 1 (tau = 1): the relaxed populations are the forced equilibrium
+      push(std::integral_constant<int, 0>{}, m, X0);
+      sfor<0, NP>([&](auto pp) {
+        constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+        V2 pe, po;
+        pair_terms(pp, pe, po);
+        push(std::integral_constant<int, n>{}, m, pe + po);
+        push(std::integral_constant<int, nb>{}, m, pe - po);
+      });
+    } else if (spec == 0u) {
+      // every moment relaxes at s0 (BGK)
+      push(std::integral_constant<int, 0>{}, m, fma2(keep, pop(std::integral_constant<int, 0>{}), X0));
+      sfor<0, NP>([&](auto pp) {
+        constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+        V2 pe, po;
+        pair_terms(pp, pe, po);
+        push(std::integral_constant<int, n>{}, m, fma2(keep, pop(std::integral_constant<int, n>{}), pe + po));
+        push(std::integral_constant<int, nb>{}, m, fma2(keep, pop(std::integral_constant<int, nb>{}), pe - po));
+      });
+    } else if (spec == stress_mask<D>()) {
+      // s_nu != s0, every other rate s0: pair sums of the non-equilibrium
+      // part, the s_nu moments' corrections, then each pair relaxed
+      V2 F3[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) F3[d] = v2(3.f) * F[m][d];
+      const V2 hFu2 = v2(3.f) * Fu;
+      V2 Sp[NP];
+      sfor<0, NP>([&](auto pp) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+        const V2 WA = n <= L::NAXIS ? WA1 : WA2;
+        const V2 Ae = WA + WBe[p];
+        const V2 t2 = cdot2<D, n>(F3);
+        const V2 gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
+        const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
+        Sp[p] = fma2(Bo[p], t2, fma2(v2(-2.f), De, gs) - Ae * hFu2);
+      });
+      V2 ck[Q];
+      sfor<0, Q>([&](auto kk) {
+        constexpr int kq = decltype(kk)::value;
+        if constexpr (rate_of<D>(kq) == R_NU) {
+          V2 md{0.f, 0.f};
+          bool first = true;
+          sfor<0, NP>([&](auto pp) {
+            constexpr int p = decltype(pp)::value;
+            constexpr int v = L::mt(pair_n<D>(p), kq);
+            if constexpr (v != 0) {
+              if (first)
+                md = v == 1 ? Sp[p] : (v == -1 ? -Sp[p] : v2(float(v)) * Sp[p]);
+              else
+                md = v == 1 ? md + Sp[p] : (v == -1 ? md - Sp[p] : fma2(v2(float(v)), Sp[p], md));
+              first = false;
+            }
+          });
+          ck[kq] = v2(P.dspec[m][kq]) * md;
+        }
+      });
+      const bool k0 = keepf == 0.f;
+      push(std::integral_constant<int, 0>{}, m, k0 ? X0 : fma2(keep, pop(std::integral_constant<int, 0>{}), X0));
+      sfor<0, NP>([&](auto pp) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+        V2 pe, po;
+        pair_terms(pp, pe, po);
+        sfor<0, Q>([&](auto kk) {
+          constexpr int kq = decltype(kk)::value;
+          if constexpr (rate_of<D>(kq) == R_NU) {
+            constexpr int v = L::mt(n, kq);
+            if constexpr (v == 1) pe = pe - ck[kq];
+            else if constexpr (v == -1) pe = pe + ck[kq];
+            else if constexpr (v != 0) pe = fma2(v2(float(-v)), ck[kq], pe);
+          }
+        });
+        if (k0) {
+          push(std::integral_constant<int, n>{}, m, pe + po);
+          push(std::integral_constant<int, nb>{}, m, pe - po);
+        } else {
+          push(std::integral_constant<int, n>{}, m, fma2(keep, pop(std::integral_constant<int, n>{}), pe + po));
+          push(std::integral_constant<int, nb>{}, m, fma2(keep, pop(std::integral_constant<int, nb>{}), pe - po));
+        }
+      });
+    } else if constexpr (MRT) {
+      // general rate pattern: relax every moment at s0, then correct each
+      // moment whose rate differs by dspec_k times its projection of the
+      // deviation from the forced equilibrium
+      V2 fo[Q], dfi[Q];
+      fo[0] = fma2(keep, pop(std::integral_constant<int, 0>{}), X0);
+      const V2 hFu = v2(1.5f) * Fu;
+      V2 hF[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) hF[d] = v2(1.5f) * F[m][d];
+      dfi[0] = pop(std::integral_constant<int, 0>{}) - fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * hFu;
+      sfor<0, NP>([&](auto pp) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+        V2 pe, po;
+        pair_terms(pp, pe, po);
+        const V2 gn = pop(std::integral_constant<int, n>{}), gb = pop(std::integral_constant<int, nb>{});
+        fo[n] = fma2(keep, gn, pe + po);
+        fo[nb] = fma2(keep, gb, pe - po);
+        const V2 WA = n <= L::NAXIS ? WA1 : WA2;
+        const V2 t = cdot2<D, n>(hF);
+        const V2 En = WA + WBe[p] + Bo[p], Eb = WA + WBe[p] - Bo[p];
+        const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
+        dfi[n] = fma2(En, t - hFu, gn - fma2(Bo[p], r, De));
+        dfi[nb] = gb - fma2(Bo[p], -r, De) - Eb * (t + hFu);
+      });
+      sfor<0, Q>([&](auto kk) {
+        constexpr int kq = decltype(kk)::value;
+        if (spec & (1u << kq)) {
+          V2 md{0.f, 0.f};
+          sfor<0, Q>([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            constexpr int v = L::mt(i, kq);
+            if constexpr (v == 1) md = md + dfi[i];
+            else if constexpr (v == -1) md = md - dfi[i];
+            else if constexpr (v != 0) md = fma2(v2(float(v)), dfi[i], md);
+          });
+          const V2 ck = v2(P.dspec[m][kq]) * md;
+          sfor<0, Q>([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            constexpr int v = L::mt(i, kq);
+            if constexpr (v == 1) fo[i] = fo[i] - ck;
+            else if constexpr (v == -1) fo[i] = fo[i] + ck;
+            else if constexpr (v != 0) fo[i] = fma2(v2(float(-v)), ck, fo[i]);
+          });
+        }
+      });
+      sfor<0, Q>([&](auto nn) { push(nn, m, fo[decltype(nn)::value]); });
+    }
+  }
+}
+
+// One simple pair (x0, x0 + 1): forces per site, moments and collision on V2.
+template <int D, int S, int ISO, bool MRT, class T>
+__device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int z, uint32_t l0, uint32_t l1,
+                                          bool warp_full) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  constexpr int RCH = stencil_reach<D, ISO>();
+  const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+  const unsigned N = (unsigned)a.g.n;
+  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
+  const Hood<D, RCH> h0(a.g, x0, y, z), h1(a.g, x0 + 1, y, z);
+  uint32_t seed0 = 0, seed1 = 0;
+  if constexpr (std::is_same<T, __half>::value) {
+    const uint32_t st = 0x9E3779B9u * ((a.steps_ptr ? __ldg(a.steps_ptr) : a.step) + 1u);
+    seed0 = mix32(c0 ^ st);
+    seed1 = mix32((c0 + 1u) ^ st);
+  }
+  // forcing density of both sites, then each site's forces (step_site's cell_forces)
+  const float* rho = reinterpret_cast<const float*>(a.rho);
+  float rfd0[S], rfd1[S], rf0[S], rf1[S];
+  if constexpr (S == 2) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(rho) + (c0 >> 1));
+    rfd0[0] = t.x;
+    rfd0[1] = t.y;
+    rfd1[0] = t.z;
+    rfd1[1] = t.w;
+  } else {
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      rfd0[m] = __ldg(rho + (size_t)c0 * S + m);
+      rfd1[m] = __ldg(rho + (size_t)(c0 + 1) * S + m);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    rf0[m] = P.rho0[m] + rfd0[m];
+    rf1[m] = P.rho0[m] + rfd1[m];
+  }
+  float F0[S][D], F1[S][D];
+#pragma unroll
+  for (int m = 0; m < S; ++m)
+#pragma unroll
+    for (int d = 0; d < D; ++d) F0[m][d] = F1[m][d] = 0.f;
+  const float* psi = reinterpret_cast<const float*>(a.psi);
+  if (p0) cell_forces<D, S, ISO, false, RCH, float, float, true>(h0, l0, P, a.mask, rho, psi, a.g.n, rfd0, rf0, F0);
+  if (p1) cell_forces<D, S, ISO, false, RCH, float, float, true>(h1, l1, P, a.mask, rho, psi, a.g.n, rfd1, rf1, F1);
+  V2 F[S][D], rc[S], rcd[S];
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    rc[m] = V2{rf0[m], rf1[m]};
+    rcd[m] = V2{rfd0[m], rfd1[m]};
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[m][d] = V2{F0[m][d], F1[m][d]};
+  }
+  // moments: flux of each component from pair differences, common velocity
+  const T* fin = reinterpret_cast<const T*>(a.fin);
+  V2 up[D];
+  {
+    V2 num[D], den = v2(0.f);
+#pragma unroll
+    for (int d = 0; d < D; ++d) num[d] = v2(0.f);
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      V2 j[D];
+      bool seen[D] = {};
+      const T* fm = fin + (size_t)m * Q * N + c0;
+      sfor<0, npairs<D>()>([&](auto pp) {
+        constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+        const V2 dlt = ld_pair<T>(fm + (size_t)n * N, P) - ld_pair<T>(fm + (size_t)nb * N, P);
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          constexpr int c = L::c(n, d);
+          if constexpr (c != 0) {
+            const V2 t = c == 1 ? dlt : (c == -1 ? -dlt : v2(float(c)) * dlt);
+            j[d] = seen[d] ? j[d] + t : t;
+            seen[d] = true;
+          }
+        });
+      });
+      const V2 mm = v2(P.mmot[m]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) num[d] = fma2(fma2(v2(0.5f), F[m][d], j[d]), mm, num[d]);
+      den = fma2(rc[m], mm, den);
+    }
+    const V2 inv{__frcp_rn(den.x), __frcp_rn(den.y)};
+#pragma unroll
+    for (int d = 0; d < D; ++d) up[d] = num[d] * inv;
+  }
+  T* fout = reinterpret_cast<T*>(a.fout);
+  if (warp_full) {
+    const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, &h0, &h1, seed0, seed1, &P};
+    pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
+  } else {
+    const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, &h0, &h1, seed0, seed1, &P};
+    pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
+  }
+}
+
+// k_step_pair / k_step_rest blocks: 128 threads over pairs (x halved).
+template <int D, int S, int ISO, bool MRT, class T>
+__global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair(StepArgs a_in) {
+  const StepArgs a = a_in;
+  int x0, y, z;
+  if (!pair_of(a.g, x0, y, z)) return;
+  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) != 1) return;
+  constexpr uint32_t all = all_links<D>() | 1u;
+  const bool full = (ll.x & all) == all && (ll.y & all) == all;
+  const bool warp_full = __all_sync(__activemask(), full);
+  step_pair<D, S, ISO, MRT, T>(a, x0, y, z, ll.x, ll.y, warp_full);
+}
+
+template <int D, int S, int ISO, bool MRT, class T>
+__global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, float, MRT)) k_step_rest(StepArgs a_in) {
+  const StepArgs a = a_in;
+  int x0, y, z;
+  if (!pair_of(a.g, x0, y, z)) return;
+  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) != 0) return;
+  for (int k = 0; k < 2; ++k) step_site<D, S, ISO, MRT, false, T, float, float>(a, x0 + k, y, z);
+}
+
+// Pairs that need the per-site kernel (the count decides whether k_step_rest runs).
+template <int D, int ISO>
+__global__ void __launch_bounds__(256) k_count_rest(StepArgs a_in, unsigned* count) {
+  const StepArgs a = a_in;
+  int x0, y, z;
+  if (!pair_of(a.g, x0, y, z)) return;
+  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 0) atomicAdd(count, 1u);
+}
+
+}  // namespace tx

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "tx_host_params.h"
+#include "tx_pair.cuh"
 
 namespace emu {
 
@@ -113,6 +114,12 @@ std::string run(const Case& c, Result& out) {
   T* buf[2] = {f0.data(), f1.data()};
   int cur = 0;
   unsigned step = 0;
+  // the paired step of the FP32-arithmetic forms on lattices with an even nx
+  constexpr bool kPairForm = !EXACT && std::is_same<R, float>::value;
+  const bool paired = kPairForm && g.nx % 2 == 0;
+  Geo gp = g;
+  gp.nx = g.nx / 2;
+  int rest = -1;
   auto args = [&](int in, int o) {
     StepArgs a{};
     a.fin = buf[in];
@@ -125,8 +132,17 @@ std::string run(const Case& c, Result& out) {
     a.g = g;
     a.faces = faces;
     a.step = step;
+    a.rest = rest;
     return a;
   };
+  if constexpr (kPairForm) {
+    if (paired) {
+      unsigned cnt = 0;
+      const StepArgs a = args(cur, cur);
+      launch3(gp, 256, [&] { k_count_rest<D, ISO>(a, &cnt); });
+      rest = (int)cnt;
+    }
+  }
   const Shift sh = shift_of(ph);
   if (c.from_fi) {
     launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), mask.data(), N, sh, buf[cur]); });
@@ -189,7 +205,13 @@ std::string run(const Case& c, Result& out) {
           launch1(face_area_of(D, g.nx, g.ny, g.nz, f), 128, [&] {
             k_outlet<D, S, T, R, RT>(a, f, facevals[f].data(), p.bc_data[f][0], ph.c0, p.g[1][0]);
           });
-    launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
+    if (paired) {
+      // the library's paired step: k_step_pair, then k_step_rest when pairs need it
+      launch3(gp, 128, [&] { k_step_pair<D, S, ISO, MRT, T>(a); });
+      if (a.rest != 0) launch3(gp, 128, [&] { k_step_rest<D, S, ISO, MRT, T>(a); });
+    } else {
+      launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
+    }
     density(a, 0);
     if (faces.post) launch1(shell.start[shell.nf], 128, [&] { k_faces<D, S, ISO, EXACT, T, R, RT>(a, shell); });
     cur = 1 - cur;

@@ -19,3 +19,8 @@ inline __half __float2half_rz(float f) {
   }
   return __half{h};
 }
+
+struct alignas(4) __half2 {
+  __half x, y;
+};
+inline float2 __half22float2(__half2 h) { return float2{(float)h.x.v, (float)h.y.v}; }

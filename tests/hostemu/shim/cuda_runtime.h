@@ -1,8 +1,11 @@
 // Host stand-ins for the CUDA qualifiers and built-ins used by the flow
-// kernels (taxila-lbm_gb300/csrc/tx_kernels.cuh), so that the kernels compile
-// as plain C++ and run one thread at a time on the CPU.  The kernels use no
-// shared memory, barriers, warp operations or atomics, so a sequential walk
-// over the launch grid computes exactly what the device computes per thread.
+// kernels (taxila-lbm_gb300/csrc/tx_kernels.cuh, tx_pair.cuh), so that the
+// kernels compile as plain C++ and run one thread at a time on the CPU.  The
+// kernels use no shared memory or barriers, so a sequential walk over the
+// launch grid computes what the device computes per thread.  The one warp
+// vote (__all_sync, whether a whole warp takes the bounceback-free pushes of
+// the paired kernel) sees only the calling thread here: each thread then takes
+// that path when it alone qualifies, which the kernel must handle the same.
 #pragma once
 #include <cstdint>
 
@@ -17,9 +20,25 @@ struct dim3 {
 };
 inline dim3 threadIdx, blockIdx, blockDim, gridDim;
 
-struct float2 {
+struct alignas(8) float2 {
   float x, y;
 };
+struct alignas(16) float4 {
+  float x, y, z, w;
+};
+struct alignas(8) uint2 {
+  unsigned x, y;
+};
+inline float2 make_float2(float x, float y) { return float2{x, y}; }
+inline uint2 make_uint2(unsigned x, unsigned y) { return uint2{x, y}; }
+inline unsigned __activemask() { return 0xffffffffu; }
+inline bool __all_sync(unsigned, bool p) { return p; }
+inline unsigned atomicAdd(unsigned* p, unsigned v) {
+  const unsigned o = *p;
+  *p = o + v;
+  return o;
+}
+inline float __frcp_rn(float x) { return 1.0f / x; }
 struct alignas(16) double2 {
   double x, y;
 };
