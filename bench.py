@@ -539,6 +539,44 @@ def fp64_bound(pk, sites, k_ms):
             "counts_source": c["source"]}
 
 
+def serving_spec_run(n=40, seed=1):
+    """The specification's serving mix (serve.SPEC_MIX: 70% permeability
+    solves, sides 32-160, to a relative mean-flow change < 1e-7 per chunk; 30%
+    drainage with two minerals and a tracer, D2Q9 256^2-1024^2 or D3Q19
+    64^3-128^3, until the invader's mass levels off) with ``n`` seeded
+    requests: the FP16-storage form served at the Poisson arrival rate (p50 /
+    p99 latency) and with every request queued at once (capacity), the FP32
+    form at capacity, and the plain FP64 form one request at a time."""
+    from taxila import serve
+    reqs = serve.make_spec_mix(n, seed=seed)
+    sites = sum(r.params.nsites for r in reqs)
+    out = {"mix": "%d requests of the specification's mix, seed %d (%d perm, %d drain, %d sites): Poisson %.0f/s; "
+                  "perm sides %d-%d to mean-flow change < %g per chunk (cap %d steps); drainage D2Q9 %d-%d / D3Q19 "
+                  "%d-%d with 2 minerals and a tracer to invader-mass change < %g per chunk (cap %d steps)"
+                  % (n, seed, sum(r.kind == "perm" for r in reqs), sum(r.kind == "drain" for r in reqs), sites,
+                     serve.SPEC_MIX["rate"], *serve.SPEC_MIX["perm_sides"], serve.SPEC_MIX["perm_tol"],
+                     serve.SPEC_MIX["perm_max_steps"], *serve.SPEC_MIX["drain2_sides"], *serve.SPEC_MIX["drain3_sides"],
+                     serve.SPEC_MIX["drain_tol"], serve.SPEC_MIX["drain_steps"])}
+    runs = (("fp32_fp16_storage", P.PREC_F32_F16, None, True), ("fp32_fp16_storage_saturated", P.PREC_F32_F16, None, False),
+            ("fp32_saturated", P.PREC_F32, None, False), ("fp64_sequential_saturated", P.PREC_F64, 1, False))
+    values = {}
+    for name, prec, maxa, realtime in runs:
+        srv = serve.Server(precision=prec, max_active=maxa, chunk=100)
+        res = srv.run(reqs, realtime=realtime)
+        srv.close()
+        out[name] = serve.summary(res)
+        values[name] = {r.rid: r.value for r in res}
+    f, s = out["fp32_fp16_storage_saturated"], out["fp64_sequential_saturated"]
+    out["fp16_storage_vs_fp64_sequential_solves_saturated"] = round(f["solves_per_s"] / s["solves_per_s"], 2)
+    perm = [r.rid for r in reqs if r.kind == "perm"]
+    ref = values["fp64_sequential_saturated"]
+    for name in ("fp32_fp16_storage_saturated", "fp32_saturated"):
+        errs = [abs(values[name][i] / ref[i] - 1.0) for i in perm if ref.get(i)]
+        out[name]["perm_rel_err_max_vs_fp64"] = max(errs) if errs else None
+    out["saturated"] = "every request queued at once: solves/s is the server's capacity"
+    return out
+
+
 def conservation_mass(h):
     """Each component's mass from tx_conservation, or the error text."""
     try:
@@ -703,9 +741,10 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form, batched, serving and CPU legs")
     ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling runs use a smaller case)")
     ap.add_argument("--form", default="f64", choices=sorted(FORMS), help="storage/arithmetic form of the timed run")
-    ap.add_argument("--leg", default="all", choices=["all", "batched", "serving"],
+    ap.add_argument("--leg", default="all", choices=["all", "batched", "serving", "serving_spec"],
                     help="run one extra leg alone and print its JSON (profiling)")
     ap.add_argument("--lattices", type=int, default=96, help="lattices of the batched leg")
+    ap.add_argument("--requests", type=int, default=40, help="requests of the specification's serving mix")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -716,6 +755,9 @@ def main():
         return 0
     if args.leg == "serving":
         print(json.dumps(serving_run()))
+        return 0
+    if args.leg == "serving_spec":
+        print(json.dumps(serving_spec_run(n=args.requests)))
         return 0
     return run_gpu(args)
 

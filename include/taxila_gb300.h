@@ -284,7 +284,8 @@ typedef struct tx_batch tx_batch;
 /* Velocity statistics of one lattice from tx_batch_probe, over pore sites:
  * the largest change of any velocity component since the previous probe
  * (the first probe compares with zero), the largest component, the sum of
- * each component, the pore-site count and the steps taken so far. */
+ * each component, the pore-site count, the steps taken so far, and each
+ * component's mass (the sum of its density, as the collision sees it). */
 typedef struct {
   int32_t id;
   int32_t pad_;
@@ -293,6 +294,7 @@ typedef struct {
   double u_sum[3];
   int64_t pore_sites;
   int64_t steps;
+  double mass[TX_MAX_COMPONENTS];
 } tx_probe;
 
 /* form: discretization, ncomponents, relaxation_mode, isotropy_order,

@@ -133,34 +133,38 @@ namespace {
 // One block per lattice slot: its tiles' partials in a fixed order.
 __global__ void __launch_bounds__(256) k_probe_reduce(const LatDesc* lats, int nlat, const ProbePart* parts,
                                                       ProbePart* out) {
-  __shared__ double red[256][6];
+  constexpr int NV = 6 + MAXC;  // du, umax, usum x/y/z, npore, mass per component
+  __shared__ double red[256][NV];
   const int l = blockIdx.x;
   if (l >= nlat) return;
   const int t0 = lats[l].tile_begin, tn = lats[l].tile_count;
-  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double v[NV];
+  for (int k = 0; k < NV; ++k) v[k] = 0.0;
   for (int t = (int)threadIdx.x; t < tn; t += blockDim.x) {
     const ProbePart p = parts[t0 + t];
     v[0] = fmax(v[0], p.du);
     v[1] = fmax(v[1], p.umax);
     for (int d = 0; d < 3; ++d) v[2 + d] += p.usum[d];
     v[5] += p.npore;
+    for (int m = 0; m < MAXC; ++m) v[6 + m] += p.mass[m];
   }
-  for (int k = 0; k < 6; ++k) red[threadIdx.x][k] = v[k];
+  for (int k = 0; k < NV; ++k) red[threadIdx.x][k] = v[k];
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
     if ((int)threadIdx.x < s) {
       red[threadIdx.x][0] = fmax(red[threadIdx.x][0], red[threadIdx.x + s][0]);
       red[threadIdx.x][1] = fmax(red[threadIdx.x][1], red[threadIdx.x + s][1]);
-      for (int k = 2; k < 6; ++k) red[threadIdx.x][k] += red[threadIdx.x + s][k];
+      for (int k = 2; k < NV; ++k) red[threadIdx.x][k] += red[threadIdx.x + s][k];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    ProbePart r;
+    ProbePart r{};
     r.du = red[0][0];
     r.umax = red[0][1];
     for (int d = 0; d < 3; ++d) r.usum[d] = red[0][2 + d];
     r.npore = red[0][5];
+    for (int m = 0; m < MAXC; ++m) r.mass[m] = red[0][6 + m];
     out[l] = r;
   }
 }
@@ -824,6 +828,7 @@ int tx_batch_probe(tx_batch* b, int32_t cap, tx_probe* out, int32_t* n) {
     for (int d = 0; d < 3; ++d) o.u_sum[d] = res[(size_t)s].usum[d];
     o.pore_sites = (int64_t)res[(size_t)s].npore;
     o.steps = b->slots[(size_t)s]->steps;
+    for (int m = 0; m < TX_MAX_COMPONENTS && m < MAXC; ++m) o.mass[m] = res[(size_t)s].mass[m];
   }
   return TX_OK;
 }

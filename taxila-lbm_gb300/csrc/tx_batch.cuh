@@ -49,6 +49,7 @@ struct ProbePart {
   double umax;        // max over sites and axes of |u|
   double usum[3];     // sum of u per axis
   double npore;       // pore sites
+  double mass[MAXC];  // sum of each component's density
 };
 
 struct BatchArgs {
@@ -215,7 +216,8 @@ __global__ void __launch_bounds__(128) k_species_tiles(BatchArgs b, int flip) {
 // reduced in a fixed order so that the result depends only on the lattice.
 template <int D, int S, int ISO, class T, class R, class RT>
 __global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
-  __shared__ double red[4][6];
+  constexpr int NV = 6 + S;  // du, umax, usum x/y/z, npore, mass per component
+  __shared__ double red[4][NV];
   const int nt = __ldg(b.ntiles);
   const int tid = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
   const int lane = tid & 31, warp = tid >> 5;
@@ -224,7 +226,9 @@ __global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
     const LatDesc& L = b.lats[tl.x];
     const StepArgs a = flipped(L.a, flip);
     const int x = tl.y + (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
-    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // du, umax, usum x/y/z, npore
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
     if (x < a.g.nx && y < a.g.ny && z < a.g.nz) {
       const long long idx = (long long)x + (long long)a.g.nx * ((long long)y + (long long)a.g.ny * z);
       if (__ldg(a.mask + idx) == 0) {
@@ -243,6 +247,8 @@ __global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
           *uo = u;
         }
         v[5] = 1.0;
+#pragma unroll
+        for (int m = 0; m < S; ++m) v[6 + m] = double(rc[m]);
       }
     }
 #pragma unroll
@@ -250,17 +256,18 @@ __global__ void __launch_bounds__(128) k_probe_tiles(BatchArgs b, int flip) {
       v[0] = fmax(v[0], __shfl_xor_sync(0xffffffffu, v[0], o));
       v[1] = fmax(v[1], __shfl_xor_sync(0xffffffffu, v[1], o));
 #pragma unroll
-      for (int k = 2; k < 6; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      for (int k = 2; k < NV; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
     }
     if (lane == 0)
-      for (int k = 0; k < 6; ++k) red[warp][k] = v[k];
+      for (int k = 0; k < NV; ++k) red[warp][k] = v[k];
     __syncthreads();
     if (tid == 0) {
-      ProbePart p;
+      ProbePart p{};
       p.du = fmax(fmax(red[0][0], red[1][0]), fmax(red[2][0], red[3][0]));
       p.umax = fmax(fmax(red[0][1], red[1][1]), fmax(red[2][1], red[3][1]));
       for (int d = 0; d < 3; ++d) p.usum[d] = ((red[0][2 + d] + red[1][2 + d]) + red[2][2 + d]) + red[3][2 + d];
       p.npore = ((red[0][5] + red[1][5]) + red[2][5]) + red[3][5];
+      for (int m = 0; m < S; ++m) p.mass[m] = ((red[0][6 + m] + red[1][6 + m]) + red[2][6 + m]) + red[3][6 + m];
       b.parts[t] = p;
     }
     __syncthreads();

@@ -19,7 +19,8 @@ _lib = None
 class TxProbe(C.Structure):
     """tx_probe of include/taxila_gb300.h."""
     _fields_ = [("id", C.c_int32), ("pad_", C.c_int32), ("du_max", C.c_double), ("u_max", C.c_double),
-                ("u_sum", C.c_double * 3), ("pore_sites", C.c_int64), ("steps", C.c_int64)]
+                ("u_sum", C.c_double * 3), ("pore_sites", C.c_int64), ("steps", C.c_int64),
+                ("mass", C.c_double * P.MAXC)]
 
 
 class TxError(RuntimeError):

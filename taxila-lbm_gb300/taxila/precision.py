@@ -14,6 +14,7 @@ to 1e-12 after 1,000 steps (its exact variant bit for bit), so full-size
 runs that the CPU oracle cannot finish still have an FP64 anchor.
 
     python -m taxila.precision --n 256 --steps 20000 --out study.json
+    python -m taxila.precision --batch 96 --out batch.json   # the batched-permeability set
 """
 import argparse
 import json
@@ -121,6 +122,60 @@ def permeability_study(n, steps, seed=4321):
     return out
 
 
+def batch_lattices(n_lat=96, seed=4, sides=(48, 192), tol=1e-7, max_steps=40000, gz=1e-6):
+    """The batched-permeability workload: ``n_lat`` single-phase D3Q19 BGK
+    (tau = 1) lattices, each side uniform in ``sides``, seeded periodic sphere
+    packs (radii 4..10, porosity uniform 0.25..0.5), body force ``gz`` along
+    z, run until the mean flow changes by less than ``tol`` relative per
+    100-step chunk."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n_lat):
+        dims = [int(v) for v in rng.integers(sides[0], sides[1] + 1, size=3)]
+        reqs.append(serve.perm_request(i, 0.0, dims, int(rng.integers(0, 1 << 30)), tol, max_steps, gz=gz,
+                                       radii=(4.0, 10.0)))
+    return reqs
+
+
+def batch_permeability_study(n_lat=96, seed=4, tol=1e-7, max_steps=40000, chunk=100):
+    """Every lattice of the batched-permeability workload run to its stop
+    criterion in one batch per form (persistent tile-table launches replayed
+    as CUDA graphs, tuned tiles): time to solution of the whole set, and
+    each lattice's steps and permeability, with the FP32-arithmetic forms'
+    permeability errors against the FP64 form's."""
+    reqs = batch_lattices(n_lat, seed, tol=tol, max_steps=max_steps)
+    sites = sum(r.params.nsites for r in reqs)
+    out = {"case": "%d single-phase D3Q19 BGK periodic sphere packs, sides 48-192 per axis (%d sites), body force "
+                   "1e-6, stop at a relative change of the mean flow < %g per %d-step chunk (cap %d steps)"
+                   % (n_lat, sites, tol, chunk, max_steps), "forms": {}}
+    perms = {}
+    for name, prec, _ in FORMS:
+        srv = serve.Server(precision=prec, chunk=chunk, budget_bytes=200 << 30)
+        t = time.perf_counter()
+        res = srv.run(reqs, realtime=False)
+        span = time.perf_counter() - t
+        srv.close()
+        steps = {r.rid: r.steps for r in res}
+        perms[name] = {r.rid: r.value for r in res}
+        out["forms"][name] = {"time_to_solution_s": round(span, 2),
+                              "lattice_steps_mean": round(float(np.mean(list(steps.values()))), 1),
+                              "lattice_steps_max": int(max(steps.values())),
+                              "capped": int(sum(1 for v in steps.values() if v >= max_steps)),
+                              "gsite_steps": round(sum(r.sites * r.steps for r in res) / 1e9, 2)}
+    ref = perms["fp64"]
+    out["lattices"] = [{"rid": r.rid, "dims": [r.params.nx, r.params.ny, r.params.nz],
+                        "porosity": round(float(np.mean(np.asarray(r.walls) == 0)), 4),
+                        "k_fp64": ref[r.rid],
+                        "rel_err": {name: abs(perms[name][r.rid] / ref[r.rid] - 1.0)
+                                    for name in perms if name != "fp64"}} for r in reqs]
+    for name in perms:
+        if name != "fp64":
+            errs = [l["rel_err"][name] for l in out["lattices"]]
+            out["forms"][name]["perm_rel_err_max"] = max(errs)
+            out["forms"][name]["perm_rel_err_median"] = float(np.median(errs))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=256)
@@ -129,9 +184,14 @@ def main():
     ap.add_argument("--perm-n", type=int, default=96)
     ap.add_argument("--perm-steps", type=int, default=4000)
     ap.add_argument("--out", default="")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="run the batched-permeability study on this many lattices instead (96: the full set)")
     a = ap.parse_args()
-    cps = [a.steps * (i + 1) // a.checkpoints for i in range(a.checkpoints)]
-    res = {"drainage": drainage_study(a.n, a.steps, cps), "permeability": permeability_study(a.perm_n, a.perm_steps)}
+    if a.batch:
+        res = {"batched_permeability": batch_permeability_study(a.batch)}
+    else:
+        cps = [a.steps * (i + 1) // a.checkpoints for i in range(a.checkpoints)]
+        res = {"drainage": drainage_study(a.n, a.steps, cps), "permeability": permeability_study(a.perm_n, a.perm_steps)}
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

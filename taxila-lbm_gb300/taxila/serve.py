@@ -14,7 +14,10 @@ lattice and retires the ones whose stop criterion holds:
   max |u - u_prev| <= tol * max |u| over pore sites (criterion="max"; with
   FP16 storage the per-site rounding noise can keep this above small tol),
   or max_steps;
-* drainage: max_steps.
+* drainage: the invading component's mass (the sum of its density over pore
+  sites, from the same device probe) changed by at most tol relative over
+  the last chunk (the saturation has levelled off: breakthrough, or a front
+  held by capillary entry pressure), or max_steps.
 
 Admission happens only between chunks, so every lattice is probed at
 multiples of ``chunk`` of its own steps: its result does not depend on what
@@ -108,7 +111,7 @@ def perm_request(rid, arrival, sides, seed, tol, max_steps, gz=1e-5, radii=None)
     return Request(rid, "perm", arrival, p, walls, np.ones(p.nsites), tol=tol, max_steps=max_steps)
 
 
-def drain_request(rid, arrival, sides, seed, steps, dims=3):
+def drain_request(rid, arrival, sides, seed, steps, dims=3, tol=0.0):
     """Two-phase drainage: D3Q19 (or D2Q9) two-component BGK (tau = 1),
     seeded sphere (disk) pack of porosity 0.35 split into two minerals with
     adhesion (+a, -a) / (-a, +a); the pore starts with the wetting component 1
@@ -166,12 +169,13 @@ def drain_request(rid, arrival, sides, seed, steps, dims=3):
     p.species_relaxation_mode = P.SRT
     p.species_tau[0] = 0.8
     conc = np.where(pore & inlet, 1.0, 0.0)
-    return Request(rid, "drain", arrival, p, walls, rho.ravel(), max_steps=steps, invader=0, lo=0.03, hi=1.05,
+    return Request(rid, "drain", arrival, p, walls, rho.ravel(), tol=tol, max_steps=steps, invader=0, lo=0.03, hi=1.05,
                    conc=conc)
 
 
 def make_mix(seed=1, n=40, rate=30.0, perm_sides=(32, 64), drain3_sides=(32, 48), drain2_sides=(96, 192),
-             frac_perm=0.7, perm_tol=1e-5, perm_max_steps=6000, drain_steps=1500):
+             frac_perm=0.7, perm_tol=1e-5, perm_max_steps=6000, drain_steps=1500, drain_tol=0.0, perm_radii=None,
+             perm_gz=1e-5):
     """Seeded Poisson request stream: ``n`` requests at ``rate`` per second,
     70% permeability solves and 30% drainage runs (half D3Q19, half D2Q9),
     sides uniform in the given ranges (per axis for the 3D lattices)."""
@@ -182,12 +186,33 @@ def make_mix(seed=1, n=40, rate=30.0, perm_sides=(32, 64), drain3_sides=(32, 48)
         s = int(rng.integers(0, 1 << 30))
         u = rng.random()
         if u < frac_perm:
-            out.append(perm_request(i, t, _random_sides(rng, *perm_sides, 3), s, perm_tol, perm_max_steps))
+            out.append(perm_request(i, t, _random_sides(rng, *perm_sides, 3), s, perm_tol, perm_max_steps,
+                                    gz=perm_gz, radii=perm_radii))
         elif u < frac_perm + (1.0 - frac_perm) / 2:
-            out.append(drain_request(i, t, _random_sides(rng, *drain3_sides, 3), s, drain_steps, dims=3))
+            out.append(drain_request(i, t, _random_sides(rng, *drain3_sides, 3), s, drain_steps, dims=3, tol=drain_tol))
         else:
-            out.append(drain_request(i, t, _random_sides(rng, *drain2_sides, 2), s, drain_steps, dims=2))
+            out.append(drain_request(i, t, _random_sides(rng, *drain2_sides, 2), s, drain_steps, dims=2, tol=drain_tol))
     return out
+
+
+# The serving mix of the workload specification: 70% single-phase
+# permeability solves, sides 32-160 per axis, sphere radii 4-10, body force
+# 1e-6, run to a relative change of the mean flow below 1e-7 per 100-step
+# chunk; 30%
+# two-phase drainage with two minerals and one tracer, D2Q9 256^2-1024^2 or
+# D3Q19 64^3-128^3, run until the invader's mass changes by less than 1e-4
+# per chunk; Poisson arrivals at 30 per second.  The step caps bound a
+# request whose criterion is never met.
+SPEC_MIX = dict(rate=30.0, perm_sides=(32, 160), drain3_sides=(64, 128), drain2_sides=(256, 1024), frac_perm=0.7,
+                perm_tol=1e-7, perm_max_steps=20000, drain_steps=6000, drain_tol=1e-4, perm_radii=(4.0, 10.0),
+                perm_gz=1e-6)
+
+
+def make_spec_mix(n, seed=1, **overrides):
+    """``n`` requests of the specification's mix (SPEC_MIX, with overrides)."""
+    kw = dict(SPEC_MIX)
+    kw.update(overrides)
+    return make_mix(seed=seed, n=n, **kw)
 
 
 class Server:
@@ -281,13 +306,17 @@ class Server:
                 for lid, pr in b.probe().items():
                     slot = active[(key, lid)]
                     req, q, admitted, prev = slot
-                    slot[3] = pr.u_sum[2]
+                    # the probed quantity of the stop criterion: mean flow or invader mass
+                    cur = pr.u_sum[2] if req.kind == "perm" else pr.mass[req.invader]
+                    slot[3] = cur
                     done = pr.steps >= req.max_steps
                     if req.kind == "perm":
                         if self.criterion == "max":
                             done = done or (pr.u_max > 0.0 and pr.du_max <= req.tol * pr.u_max)
-                        elif prev is not None and pr.u_sum[2] != 0.0:
-                            done = done or abs(pr.u_sum[2] - prev) <= req.tol * abs(pr.u_sum[2])
+                        elif prev is not None and cur != 0.0:
+                            done = done or abs(cur - prev) <= req.tol * abs(cur)
+                    elif req.tol > 0.0 and prev is not None and cur != 0.0:
+                        done = done or abs(cur - prev) <= req.tol * abs(cur)
                     if not done:
                         continue
                     tracer = 0.0

@@ -61,10 +61,11 @@ def test_probe_struct_layout(tmp_path):
         pytest.skip("no C compiler")
     src = tmp_path / "probe.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "taxila_gb300.h"\n'
-                   'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(tx_probe), offsetof(tx_probe, du_max),'
-                   ' offsetof(tx_probe, u_sum), offsetof(tx_probe, pore_sites), offsetof(tx_probe, steps)); return 0; }\n')
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(tx_probe), offsetof(tx_probe, du_max),'
+                   ' offsetof(tx_probe, u_sum), offsetof(tx_probe, pore_sites), offsetof(tx_probe, steps),'
+                   ' offsetof(tx_probe, mass)); return 0; }\n')
     exe = tmp_path / "probe"
     subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == [ctypes.sizeof(TxProbe), TxProbe.du_max.offset, TxProbe.u_sum.offset,
-                   TxProbe.pore_sites.offset, TxProbe.steps.offset]
+                   TxProbe.pore_sites.offset, TxProbe.steps.offset, TxProbe.mass.offset]

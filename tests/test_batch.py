@@ -156,3 +156,20 @@ def test_batch_with_species_equals_alone():
         h.step(23)
         for f in (P.FIELD_FI, P.FIELD_SPECIES_FI, P.FIELD_SPECIES_RHO):
             assert np.array_equal(b.download(lid, f, h.L.tx_field_size(h.h, f)), h.download(f)), f
+
+
+def test_probe_mass_matches_downloaded_density():
+    # each component's mass in the probe is the sum of the downloaded density
+    # over pore sites (a periodic two-phase bubble: no density faces)
+    p, w, r = cases.sc_bubble(P.D3Q19, (16, 12, 14), P.MRT, 4)
+    q = form_of(p)
+    q.precision = P.PREC_F32
+    b = Batch(q)
+    lid = b.add(q, w, r)
+    b.step(8)
+    pr = b.probe()[lid]
+    rho = b.download(lid, P.FIELD_RHO, p.nsites * p.ncomponents).reshape(p.nsites, p.ncomponents)
+    pore = np.asarray(w) == 0
+    for m in range(p.ncomponents):
+        assert pr.mass[m] == pytest.approx(rho[pore, m].sum(), rel=1e-6)
+    b.close()

@@ -186,3 +186,22 @@ def test_eos_options():
     import pytest
     with pytest.raises(options.DeckError):
         options.params_from_options(options.parse_deck_text(deck.replace("-eos_component1 sc", "-eos_component1 vdw")))
+
+
+def test_spec_serving_mix_sizes():
+    # the specification's serving mix: request kinds and lattice sizes in range
+    from taxila import serve
+    reqs = serve.make_spec_mix(40, seed=1)
+    perm = [r for r in reqs if r.kind == "perm"]
+    drain = [r for r in reqs if r.kind == "drain"]
+    assert 0.5 < len(perm) / len(reqs) < 0.9 and drain
+    for r in perm:
+        assert all(32 <= v <= 160 for v in (r.params.nx, r.params.ny, r.params.nz))
+        assert r.tol == 1e-7 and r.params.gvt[2] == 1e-6
+    for r in drain:
+        if r.params.discretization == P.D2Q9:
+            assert all(256 <= v <= 1024 for v in (r.params.nx, r.params.ny))
+        else:
+            assert all(64 <= v <= 128 for v in (r.params.nx, r.params.ny, r.params.nz))
+        assert r.params.nspecies == 1 and r.params.nminerals == 2 and r.tol == 1e-4
+    assert all(a.arrival < b.arrival for a, b in zip(reqs, reqs[1:]))

@@ -90,3 +90,36 @@ def test_served_fp16_permeability_matches_fp64_oracle():
     o.step(600)
     k_ref = metrics.permeability(1.0, req.params.gvt[2], o.get(P.FIELD_FLUX), req.walls, req.params.nsites)
     assert abs(res.value / k_ref - 1.0) < 1e-3, (res.value, k_ref)
+
+
+def test_served_fp16_permeability_converged_matches_fp64_oracle():
+    # served to its stop criterion (relative change of the mean flow < 1e-7
+    # per chunk), the FP16-storage permeability is within 1e-3 of the FP64
+    # oracle run for the same number of steps
+    req = serve.perm_request(0, 0.0, (22, 18, 26), seed=23, tol=1e-7, max_steps=20000, gz=1e-6, radii=(2.5, 5.0))
+    srv = serve.Server(precision=P.PREC_F32_F16, storage_scale=4096.0, chunk=100)
+    (res,) = srv.run([req], realtime=False)
+    srv.close()
+    assert res.steps < 20000, "the stop criterion was never met"
+    o = Oracle(req.params)
+    o.set_walls(req.walls)
+    o.set_state(req.rho)
+    o.init()
+    o.step(res.steps)
+    k_ref = metrics.permeability(1.0, req.params.gvt[2], o.get(P.FIELD_FLUX), req.walls, req.params.nsites)
+    assert abs(res.value / k_ref - 1.0) < 1e-3, (res.steps, res.value, k_ref)
+
+
+def test_drainage_stops_when_the_invader_mass_levels_off():
+    # the drainage criterion ends a run before its step cap, and the run is
+    # the same alone and with a second request in flight
+    reqs = [serve.drain_request(0, 0.0, (16, 14, 20), 11, 20000, dims=3, tol=2e-3),
+            serve.perm_request(1, 0.0, (14, 16, 18), 12, tol=1e-4, max_steps=2000)]
+    srv = serve.Server(precision=P.PREC_F32, chunk=50)
+    mix = {r.rid: r for r in srv.run(reqs, realtime=False)}
+    srv.close()
+    one = serve.Server(precision=P.PREC_F32, chunk=50)
+    (alone,) = one.run(reqs[:1], realtime=False)
+    one.close()
+    assert mix[0].steps < 20000 and mix[0].steps % 50 == 0
+    assert (alone.steps, alone.value) == (mix[0].steps, mix[0].value)
