@@ -78,11 +78,12 @@ struct Launch3 {
   dim3 grid, block;
 };
 inline Launch3 launch3(const Geo& g, int threads);
-// the launch of the paired kernels: the sites' grid with x halved
+// the launch of the paired kernels: one thread per pair, one-dimensional
 inline Launch3 launch_pairs(const Geo& g, int threads) {
-  Geo h = g;
-  h.nx = g.nx / 2;
-  return launch3(h, threads);
+  Launch3 l;
+  l.block = dim3((unsigned)threads, 1, 1);
+  l.grid = dim3(grid_for(g.n / 2, threads), 1, 1);
+  return l;
 }
 inline Launch3 launch3(const Geo& g, int threads) {
   int bx = ((g.nx + 31) / 32) * 32;

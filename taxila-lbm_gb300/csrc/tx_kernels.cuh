@@ -264,6 +264,25 @@ __device__ __forceinline__ void st_dev(T* p, R v, const PhysT<R>& P) {
     St<T>::st(p, v);
 }
 
+// The FP16 storage scale and its inverse, read from the parameter block once
+// per thread: the compiler cannot tell that population stores leave the
+// parameter block alone, so a field read after a store is read again.
+template <class R>
+struct Scl {
+  R s, inv;
+};
+template <class R>
+__device__ __forceinline__ Scl<R> scl_of(const PhysT<R>& P) {
+  return Scl<R>{P.sscale, P.inv_sscale};
+}
+template <class T, class R>
+__device__ __forceinline__ R ld_dev_s(const T* p, Scl<R> sc) {
+  if constexpr (std::is_same<T, __half>::value)
+    return R(St<T>::ld(p)) * sc.inv;
+  else
+    return R(St<T>::ld(p));
+}
+
 // 32-bit integer finaliser (the "lowbias32" constants of C. Wellons' hash
 // prospector): a well-mixed hash of the site, direction and step.
 __host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
@@ -288,14 +307,18 @@ __host__ __device__ __forceinline__ uint32_t sr_dither(uint32_t seed, uint32_t k
   return (seed * (mix32(k + 1u) | 1u)) >> 19;
 }
 template <class T, class R>
-__device__ __forceinline__ void st_dev_sr(T* p, R v, const PhysT<R>& P, uint32_t dither) {
+__device__ __forceinline__ void st_dev_sr_s(T* p, R v, Scl<R> sc, uint32_t dither) {
   if constexpr (std::is_same<T, __half>::value) {
-    const float x = float(v * P.sscale);
+    const float x = float(v * sc.s);
     const uint32_t b = __float_as_uint(x) + dither;
     *p = __float2half_rz(__uint_as_float(b));
   } else {
-    st_dev<T, R>(p, v, P);
+    St<T>::st(p, v);
   }
+}
+template <class T, class R>
+__device__ __forceinline__ void st_dev_sr(T* p, R v, const PhysT<R>& P, uint32_t dither) {
+  st_dev_sr_s<T, R>(p, v, scl_of(P), dither);
 }
 
 // The forcing density is stored component-fastest, rho[cell * S + m], so that
@@ -920,6 +943,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   if (!(links & 1u)) return;  // wall site
   const long long N = a.g.n;
   const Hood<D, stencil_reach<D, ISO>()> h(a.g, x, y, z);
+  const Scl<R> sc = scl_of(P);
   // stochastic-rounding seed of this site and step (FP16 storage only)
   uint32_t sr_seed = 0;
   if constexpr (std::is_same<T, __half>::value)
@@ -985,7 +1009,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       T* const base = fout + (long long)(m * Q + (pore ? n : o)) * N;
       dst = base + (pore ? h.template at<cx, cy, cz>() : c);
     }
-    st_dev_sr<T, R>(dst, v, P, sr_dither(sr_seed, (uint32_t)(m * Q + n)));
+    st_dev_sr_s<T, R>(dst, v, sc, sr_dither(sr_seed, (uint32_t)(m * Q + n)));
   };
 
   if constexpr (EXACT) {
@@ -1102,7 +1126,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       const T* fm = fin + (long long)m * Q * N;
       auto pop = [&](auto nn) -> R {
         constexpr int n = decltype(nn)::value;
-        return ld_dev<T, R>(fm + (long long)n * N + c, P);
+        return ld_dev_s<T, R>(fm + (long long)n * N + c, sc);
       };
       const R E0 = WA0 + WB0;
       // rest direction: g'_0 = keep g_0 + X0

@@ -31,6 +31,9 @@
 #define TX_PAIR_MIN_BLOCKS_S2 2
 #endif
 #define TX_PAIR_MIN_BLOCKS(S) ((S) == 1 ? TX_PAIR_MIN_BLOCKS_S1 : TX_PAIR_MIN_BLOCKS_S2)
+#ifndef TX_PAIR_CALL
+#define TX_PAIR_CALL 0
+#endif
 
 namespace tx {
 
@@ -91,11 +94,11 @@ __device__ __forceinline__ uint32_t pack_half2_rz(float a, float b) {
 
 // Population deviations of the two sites at p (p at an even cell of one stream).
 template <class T>
-__device__ __forceinline__ V2 ld_pair(const T* p, const PhysT<float>& P) {
+__device__ __forceinline__ V2 ld_pair(const T* p, Scl<float> sc) {
   if constexpr (std::is_same<T, __half>::value) {
     const __half2 h = __ldg(reinterpret_cast<const __half2*>(p));
     const float2 f = __half22float2(h);
-    return V2{f.x, f.y} * v2(P.inv_sscale);
+    return V2{f.x, f.y} * v2(sc.inv);
   } else {
     const float2 f = __ldg(reinterpret_cast<const float2*>(p));
     return V2{f.x, f.y};
@@ -105,9 +108,9 @@ __device__ __forceinline__ V2 ld_pair(const T* p, const PhysT<float>& P) {
 // Both sites' values to the adjacent slots at p (FP16: stochastic rounding
 // with the per-site dithers d0, d1, exactly as st_dev_sr rounds each).
 template <class T>
-__device__ __forceinline__ void st_pair(T* p, V2 v, const PhysT<float>& P, uint32_t d0, uint32_t d1) {
+__device__ __forceinline__ void st_pair(T* p, V2 v, Scl<float> sc, uint32_t d0, uint32_t d1) {
   if constexpr (std::is_same<T, __half>::value) {
-    const V2 s = v * v2(P.sscale);
+    const V2 s = v * v2(sc.s);
     const float a = __uint_as_float(__float_as_uint(s.x) + d0);
     const float b = __uint_as_float(__float_as_uint(s.y) + d1);
     *reinterpret_cast<uint32_t*>(p) = pack_half2_rz(a, b);
@@ -118,8 +121,8 @@ __device__ __forceinline__ void st_pair(T* p, V2 v, const PhysT<float>& P, uint3
 
 // One site's value (lane k of v) at p.
 template <class T>
-__device__ __forceinline__ void st_one(T* p, float v, const PhysT<float>& P, uint32_t d) {
-  st_dev_sr<T, float>(p, v, P, d);
+__device__ __forceinline__ void st_one(T* p, float v, Scl<float> sc, uint32_t d) {
+  st_dev_sr_s<T, float>(p, v, sc, d);
 }
 
 // ------------------------------------------------------------- predicates
@@ -148,12 +151,16 @@ __device__ __forceinline__ int pair_class(const StepArgs& a, const PhysT<float>&
 }
 
 // --------------------------------------------------------------- the pair
-// Pair (x0, x0 + 1) of a row; pairs are laid out like sites with x halved.
+// Pair (x0, x0 + 1) of a row.  The pairs are numbered in storage order over
+// a one-dimensional grid, so that no lane idles at the end of a row.
 __device__ __forceinline__ bool pair_of(const Geo& g, int& x0, int& y, int& z) {
-  x0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
-  z = (int)blockIdx.z;
-  return x0 < g.nx && y < g.ny && z < g.nz;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned npx = (unsigned)g.nx >> 1;
+  const unsigned row = i / npx;
+  x0 = 2 * (int)(i - row * npx);
+  y = (int)(row % (unsigned)g.ny);
+  z = (int)(row / (unsigned)g.ny);
+  return z < g.nz;
 }
 
 // Collision and push of one component of a simple pair.  FULL: both sites
@@ -167,10 +174,9 @@ struct PairPush {
   unsigned N, c0;
   uint32_t l0, l1;
   bool p0, p1;
-  const Hood<D, RCH>* h0;
-  const Hood<D, RCH>* h1;
+  Hood<D, RCH> h0, h1;
   uint32_t seed0, seed1;
-  const PhysT<float>* P;
+  Scl<float> sc;
 
   template <int n>
   __device__ __forceinline__ void operator()(std::integral_constant<int, n>, int m, V2 v) const {
@@ -181,38 +187,56 @@ struct PairPush {
     T* const sn = fout + (size_t)k * N;
     if constexpr (n == 0) {
       if (FULL || (p0 && p1)) {
-        st_pair<T>(sn + c0, v, *P, d0, d1);
+        st_pair<T>(sn + c0, v, sc, d0, d1);
       } else {
-        if (p0) st_one<T>(sn + c0, v.x, *P, d0);
-        if (p1) st_one<T>(sn + c0 + 1, v.y, *P, d1);
+        if (p0) st_one<T>(sn + c0, v.x, sc, d0);
+        if (p1) st_one<T>(sn + c0 + 1, v.y, sc, d1);
       }
     } else {
       constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
       if constexpr (FULL) {
         if constexpr (cx == 0) {
-          st_pair<T>(sn + h0->template at<0, cy, cz>(), v, *P, d0, d1);
+          st_pair<T>(sn + h0.template at<0, cy, cz>(), v, sc, d0, d1);
         } else {
-          st_one<T>(sn + h0->template at<cx, cy, cz>(), v.x, *P, d0);
-          st_one<T>(sn + h1->template at<cx, cy, cz>(), v.y, *P, d1);
+          st_one<T>(sn + h0.template at<cx, cy, cz>(), v.x, sc, d0);
+          st_one<T>(sn + h1.template at<cx, cy, cz>(), v.y, sc, d1);
         }
       } else {
         T* const so = fout + (size_t)(m * Q + o) * N;
         const bool q0 = ((l0 >> n) & 1u) != 0u, q1 = ((l1 >> n) & 1u) != 0u;
-        if (p0) st_one<T>(q0 ? sn + h0->template at<cx, cy, cz>() : so + c0, v.x, *P, d0);
-        if (p1) st_one<T>(q1 ? sn + h1->template at<cx, cy, cz>() : so + c0 + 1, v.y, *P, d1);
+        if (p0) st_one<T>(q0 ? sn + h0.template at<cx, cy, cz>() : so + c0, v.x, sc, d0);
+        if (p1) st_one<T>(q1 ? sn + h1.template at<cx, cy, cz>() : so + c0 + 1, v.y, sc, d1);
       }
     }
   }
 };
 
-// Fast-form collision of step_site (see there) on V2 values, with the pushes.
+// Fast-form collision of step_site (see there) of component m on V2 values,
+// with the pushes.  With TX_PAIR_CALL each component's collision is a call
+// of its own, whose registers are allocated apart from the caller's: the
+// caller holds only what the next component needs across the call.
+template <int D>
+struct VecD {
+  V2 v[D];
+};
+#if TX_PAIR_CALL
+#define TX_PAIR_COLLIDE_INLINE __noinline__
+#else
+#define TX_PAIR_COLLIDE_INLINE __forceinline__
+#endif
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
-__device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, RCH>& push, const PhysT<float>& P,
-                                             const T* fin, unsigned N, unsigned c0, const V2 rc[S], const V2 rcd[S],
-                                             const V2 F[S][D], const V2 up[D]) {
+__device__ TX_PAIR_COLLIDE_INLINE void pair_collide_m(const PairPush<D, S, MRT, FULL, T, RCH> push,
+                                                      const PhysT<float>& P, const T* fin, unsigned N, unsigned c0,
+                                                      int m, V2 r, V2 rd, VecD<D> Fm_, VecD<D> up_) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   constexpr int NP = npairs<D>();
+  V2 F[S][D], up[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    F[m][d] = Fm_.v[d];
+    up[d] = up_.v[d];
+  }
   V2 usqr = up[0] * up[0];
 #pragma unroll
   for (int d = 1; d < D; ++d) usqr = fma2(up[d], up[d], usqr);
@@ -226,9 +250,7 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
     WBe[p] = fma2(v2(float(4.5 * w)) * ud, ud, -(n <= L::NAXIS ? cu_axis : cu_diag));
   });
   const V2 WB0 = v2(D == 3 ? -0.5f : float(-2.0 / 3.0)) * usqr;
-#pragma unroll
-  for (int m = 0; m < S; ++m) {
-    const V2 r = rc[m], rd = rcd[m];
+  {
     const V2 WA0 = v2(P.WAc[m][0]), WA1 = v2(P.WAc[m][1]), WA2 = v2(P.WAc[m][2]);
     const V2 cA0 = v2(P.cA[m][0]), cA1 = v2(P.cA[m][1]), cA2 = v2(P.cA[m][2]);
     const V2 s0 = v2(P.s0[m]);
@@ -244,7 +266,7 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
     const V2 G = fma2(s0, r, -kFu);
     const unsigned spec = P.spec_mask[m];
     const T* fm = fin + (size_t)m * Q * N + c0;
-    auto pop = [&](auto nn) -> V2 { return ld_pair<T>(fm + (size_t)decltype(nn)::value * N, P); };
+    auto pop = [&](auto nn) -> V2 { return ld_pair<T>(fm + (size_t)decltype(nn)::value * N, push.sc); };
     const V2 E0 = WA0 + WB0;
     // rest direction: g'_0 = keep g_0 + X0
     const V2 X0 = s0 * fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * kFu;
@@ -284,7 +306,9 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
 #pragma unroll
       for (int d = 0; d < D; ++d) F3[d] = v2(3.f) * F[m][d];
       const V2 hFu2 = v2(3.f) * Fu;
-      V2 Sp[NP];
+      // the s_nu moments of the pair sums, accumulated pair by pair
+      V2 ck[Q];
+      bool seen[Q] = {};
       sfor<0, NP>([&](auto pp) {
         constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
         const V2 WA = n <= L::NAXIS ? WA1 : WA2;
@@ -292,27 +316,24 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
         const V2 t2 = cdot2<D, n>(F3);
         const V2 gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
         const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
-        Sp[p] = fma2(Bo[p], t2, fma2(v2(-2.f), De, gs) - Ae * hFu2);
+        const V2 Sp = fma2(Bo[p], t2, fma2(v2(-2.f), De, gs) - Ae * hFu2);
+        sfor<0, Q>([&](auto kk) {
+          constexpr int kq = decltype(kk)::value;
+          if constexpr (rate_of<D>(kq) == R_NU) {
+            constexpr int v = L::mt(n, kq);
+            if constexpr (v != 0) {
+              if (!seen[kq])
+                ck[kq] = v == 1 ? Sp : (v == -1 ? -Sp : v2(float(v)) * Sp);
+              else
+                ck[kq] = v == 1 ? ck[kq] + Sp : (v == -1 ? ck[kq] - Sp : fma2(v2(float(v)), Sp, ck[kq]));
+              seen[kq] = true;
+            }
+          }
+        });
       });
-      V2 ck[Q];
       sfor<0, Q>([&](auto kk) {
         constexpr int kq = decltype(kk)::value;
-        if constexpr (rate_of<D>(kq) == R_NU) {
-          V2 md{0.f, 0.f};
-          bool first = true;
-          sfor<0, NP>([&](auto pp) {
-            constexpr int p = decltype(pp)::value;
-            constexpr int v = L::mt(pair_n<D>(p), kq);
-            if constexpr (v != 0) {
-              if (first)
-                md = v == 1 ? Sp[p] : (v == -1 ? -Sp[p] : v2(float(v)) * Sp[p]);
-              else
-                md = v == 1 ? md + Sp[p] : (v == -1 ? md - Sp[p] : fma2(v2(float(v)), Sp[p], md));
-              first = false;
-            }
-          });
-          ck[kq] = v2(P.dspec[m][kq]) * md;
-        }
+        if constexpr (rate_of<D>(kq) == R_NU) ck[kq] = v2(P.dspec[m][kq]) * ck[kq];
       });
       const bool k0 = keepf == 0.f;
       push(std::integral_constant<int, 0>{}, m, k0 ? X0 : fma2(keep, pop(std::integral_constant<int, 0>{}), X0));
@@ -388,6 +409,22 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
   }
 }
 
+template <int D, int S, bool MRT, bool FULL, class T, int RCH>
+__device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, RCH>& push, const PhysT<float>& P,
+                                             const T* fin, unsigned N, unsigned c0, const V2 rc[S], const V2 rcd[S],
+                                             const V2 F[S][D], const V2 up[D]) {
+  VecD<D> u;
+#pragma unroll
+  for (int d = 0; d < D; ++d) u.v[d] = up[d];
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    VecD<D> f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f.v[d] = F[m][d];
+    pair_collide_m<D, S, MRT, FULL, T, RCH>(push, P, fin, N, c0, m, rc[m], rcd[m], f, u);
+  }
+}
+
 // One simple pair (x0, x0 + 1): forces per site, moments and collision on V2.
 template <int D, int S, int ISO, bool MRT, class T>
 __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int z, uint32_t l0, uint32_t l1,
@@ -400,6 +437,7 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
   const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
   const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
   const Hood<D, RCH> h0(a.g, x0, y, z), h1(a.g, x0 + 1, y, z);
+  const Scl<float> sc = scl_of(P);
   uint32_t seed0 = 0, seed1 = 0;
   if constexpr (std::is_same<T, __half>::value) {
     const uint32_t st = 0x9E3779B9u * ((a.steps_ptr ? __ldg(a.steps_ptr) : a.step) + 1u);
@@ -457,7 +495,7 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
       const T* fm = fin + (size_t)m * Q * N + c0;
       sfor<0, npairs<D>()>([&](auto pp) {
         constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
-        const V2 dlt = ld_pair<T>(fm + (size_t)n * N, P) - ld_pair<T>(fm + (size_t)nb * N, P);
+        const V2 dlt = ld_pair<T>(fm + (size_t)n * N, sc) - ld_pair<T>(fm + (size_t)nb * N, sc);
         sfor<0, D>([&](auto dd) {
           constexpr int d = decltype(dd)::value;
           constexpr int c = L::c(n, d);
@@ -479,10 +517,10 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
   }
   T* fout = reinterpret_cast<T*>(a.fout);
   if (warp_full) {
-    const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, &h0, &h1, seed0, seed1, &P};
+    const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
     pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   } else {
-    const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, &h0, &h1, seed0, seed1, &P};
+    const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
     pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   }
 }

@@ -117,8 +117,6 @@ std::string run(const Case& c, Result& out) {
   // the paired step of the FP32-arithmetic forms on lattices with an even nx
   constexpr bool kPairForm = !EXACT && std::is_same<R, float>::value;
   const bool paired = kPairForm && g.nx % 2 == 0;
-  Geo gp = g;
-  gp.nx = g.nx / 2;
   int rest = -1;
   auto args = [&](int in, int o) {
     StepArgs a{};
@@ -139,7 +137,7 @@ std::string run(const Case& c, Result& out) {
     if (paired) {
       unsigned cnt = 0;
       const StepArgs a = args(cur, cur);
-      launch3(gp, 256, [&] { k_count_rest<D, ISO>(a, &cnt); });
+      launch1(N / 2, 256, [&] { k_count_rest<D, ISO>(a, &cnt); });
       rest = (int)cnt;
     }
   }
@@ -207,8 +205,8 @@ std::string run(const Case& c, Result& out) {
           });
     if (paired) {
       // the library's paired step: k_step_pair, then k_step_rest when pairs need it
-      launch3(gp, 128, [&] { k_step_pair<D, S, ISO, MRT, T>(a); });
-      if (a.rest != 0) launch3(gp, 128, [&] { k_step_rest<D, S, ISO, MRT, T>(a); });
+      launch1(N / 2, 128, [&] { k_step_pair<D, S, ISO, MRT, T>(a); });
+      if (a.rest != 0) launch1(N / 2, 128, [&] { k_step_rest<D, S, ISO, MRT, T>(a); });
     } else {
       launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     }
