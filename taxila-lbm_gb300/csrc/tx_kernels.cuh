@@ -264,6 +264,11 @@ __device__ __forceinline__ void st_dev(T* p, R v, const PhysT<R>& P) {
     St<T>::st(p, v);
 }
 
+// Correctly rounded reciprocal (the fast forms' 1/x): the hardware reciprocal
+// refined to round-to-nearest, without the general division's special-case path.
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+
 // The FP16 storage scale and its inverse, read from the parameter block once
 // per thread: the compiler cannot tell that population stores leave the
 // parameter block alone, so a field read after a store is read again.
@@ -849,6 +854,53 @@ __device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
   });
 }
 
+// The s_nu moments of the pair sums f_n + f_n~ (the traceless second
+// moments of the populations; only the R_NU entries of sn are written).
+template <int D, class R>
+__device__ __forceinline__ void nu_moments(const R f[Lat<D>::Q], R sn[Lat<D>::Q]) {
+  using L = Lat<D>;
+  R gs[npairs<D>()];
+  sfor<0, npairs<D>()>([&](auto pp) {
+    constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+    gs[p] = f[n] + f[opp<D>(n)];
+  });
+  sfor<0, L::Q>([&](auto kk) {
+    constexpr int k = decltype(kk)::value;
+    if constexpr (rate_of<D>(k) == R_NU) {
+      R acc = R(-0.0);
+      sfor<0, npairs<D>()>([&](auto pp) {
+        constexpr int p = decltype(pp)::value;
+        constexpr int v = L::mt(pair_n<D>(p), k);
+        if constexpr (v == 1) acc = acc + gs[p];
+        else if constexpr (v == -1) acc = acc - gs[p];
+        else if constexpr (v != 0) acc = acc + R(v) * gs[p];
+      });
+      sn[k] = acc;
+    }
+  });
+}
+
+// s_nu moment k of the pair sums of the non-equilibrium part (forced
+// equilibrium removed) from the populations' moment sn_k, the collision
+// density r, the velocity u and the component's force F:
+//   sn_k - (2 r + 3 F.u) * 4.5 sum_p v w (c.u)^2 + 9 sum_p v w (c.u)(c.F)
+// (the closed forms of nu_uu / nu_uf; the rest-density and weight-class
+// terms cancel on every s_nu moment).
+template <int D, int k, class R>
+__device__ __forceinline__ R nu_noneq(R sn_k, R q, const R u[D], const R F[D]) {
+  R e = R(-0.0), t = R(-0.0);
+  sfor<0, D>([&](auto aa) {
+    constexpr int a = decltype(aa)::value;
+    sfor<0, D>([&](auto bb) {
+      constexpr int b = decltype(bb)::value;
+      constexpr double cu = nu_uu<D>(k, a, b), cf = nu_uf<D>(k, a, b);
+      if constexpr (cu != 0.0) e = e + R(cu) * (u[a] * u[b]);
+      if constexpr (cf != 0.0) t = t + R(cf) * (u[a] * F[b]);
+    });
+  });
+  return sn_k - q * e + t;
+}
+
 // Density of the collision (Dirichlet nodes re-summed as in BCUpdateRho,
 // lbm_bc.F90:436-611) and the common velocity of FlowUpdateUED3/D2
 // (lbm_flow.F90:494-574) from the post-stream population deviations and the forces.
@@ -961,33 +1013,48 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   const T* fin = reinterpret_cast<const T*>(a.fin);
   // moments pass, one component's populations at a time; rcd = rc - rho0
   R rc[S], rcd[S], up[D];
+  // s_nu moments of the pair sums (FP32-arithmetic forms, s_nu-only rate
+  // patterns): the stress correction then takes their closed form and reloads
+  // no population.  The FP64 form keeps the pass over the pair sums, which
+  // costs fewer FP64 instructions.
+  constexpr bool kNuClosed = std::is_same<R, float>::value;
+  R snu[S][Q];
   {
     const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
     R jm[S][D];
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       R f1[1][Q];
-      load_pops<D, 1, T, R>(fin + (long long)m * Q * N, N, c, P, f1);
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        f1[0][n] = ld_dev_s<T, R>(fin + ((long long)(m * Q + n)) * N + c, sc);
+      });
       if constexpr (EXACT) {
 #pragma unroll
         for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
       } else {
         pop_flux_pairs<D, R>(f1[0], jm[m]);
+        // FP32 arithmetic: the s_nu moments of a component whose collision
+        // corrects them, while its populations are in registers
+        if constexpr (kNuClosed)
+          if (P.spec_mask[m] == stress_mask<D>()) nu_moments<D, R>(f1[0], snu[m]);
       }
       rcd[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rfd[m];
       rc[m] = dn ? P.rho0[m] + rcd[m] : rf[m];
     }
+    R den = EXACT ? R(0) : R(-0.0);
+#pragma unroll
+    for (int m = 0; m < S; ++m) den = den + rc[m] * R(P.mmot[m]);
+    const R inv = EXACT ? R(0) : rcp_rn(den);  // fast form: one correctly rounded reciprocal
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      R num = EXACT ? R(0) : R(-0.0), den = EXACT ? R(0) : R(-0.0);
+      R num = EXACT ? R(0) : R(-0.0);
 #pragma unroll
       for (int m = 0; m < S; ++m) num = num + (jm[m][d] + R(.5) * F[m][d]) * R(P.mmot[m]);
-#pragma unroll
-      for (int m = 0; m < S; ++m) den = den + rc[m] * R(P.mmot[m]);
       if constexpr (EXACT)
         up[d] = num / den;
       else
-        up[d] = num * (R(1) / den);
+        up[d] = num * inv;
     }
   }
   R usqr = EXACT ? R(0) : R(-0.0);
@@ -1170,43 +1237,55 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
           push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + (pe - po));
         });
       } else if (spec == stress_mask<D>()) {
-        // s_nu != s0, every other rate s0.  Pass 1: pair sums of the
-        // non-equilibrium part, S_p = g_n + g_n~ - 2 De - Ae (3 F.u) + Bo c_n.(3 F);
-        // then the s_nu moments and their corrections ck; pass 2 relaxes and
-        // pushes each pair with its correction (no per-pair arrays stay live).
-        R F3[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) F3[d] = R(3) * F[m][d];
-        const R hFu2 = R(3) * Fu;
-        R Sp[NP];
-        sfor<0, NP>([&](auto pp) {
-          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-          const R WA = n <= L::NAXIS ? WA1 : WA2;
-          const R Ae = WA + WBe[p];
-          const R t2 = cdot_z<D, n>(F3);
-          const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
-          if constexpr (kShifted<T>) {
-            const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
-            Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
-          } else {
-            Sp[p] = gs - Ae * (R(2) * r + hFu2) + Bo[p] * t2;
-          }
-        });
+        // s_nu != s0, every other rate s0: the s_nu moments of the pair sums
+        // of the non-equilibrium part, S_p = g_n + g_n~ - 2 De - Ae (3 F.u) +
+        // Bo c_n.(3 F), give the corrections ck; then each pair is relaxed
+        // and pushed with its correction.
         R ck[Q];
-        sfor<0, Q>([&](auto kk) {
-          constexpr int kq = decltype(kk)::value;
-          if constexpr (rate_of<D>(kq) == R_NU) {
-            R md = R(-0.0);
-            sfor<0, NP>([&](auto pp) {
-              constexpr int p = decltype(pp)::value;
-              constexpr int v = L::mt(pair_n<D>(p), kq);
-              if constexpr (v == 1) md = md + Sp[p];
-              else if constexpr (v == -1) md = md - Sp[p];
-              else if constexpr (v != 0) md = md + R(v) * Sp[p];
-            });
-            ck[kq] = P.dspec[m][kq] * md;
-          }
-        });
+        if constexpr (kNuClosed) {
+          // the s_nu moments of the non-equilibrium pair sums in closed form
+          // from the moments pass's snu (nu_noneq), then their corrections ck
+          const R q = R(2) * r + R(3) * Fu;
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU)
+              ck[kq] = P.dspec[m][kq] * nu_noneq<D, kq, R>(snu[m][kq], q, up, F[m]);
+          });
+        } else {
+          // pass 1: the pair sums of the non-equilibrium part, then their s_nu moments
+          R F3[D];
+#pragma unroll
+          for (int d = 0; d < D; ++d) F3[d] = R(3) * F[m][d];
+          const R hFu2 = R(3) * Fu;
+          R Sp[NP];
+          sfor<0, NP>([&](auto pp) {
+            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+            const R WA = n <= L::NAXIS ? WA1 : WA2;
+            const R Ae = WA + WBe[p];
+            const R t2 = cdot_z<D, n>(F3);
+            const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
+            if constexpr (kShifted<T>) {
+              const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+              Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
+            } else {
+              Sp[p] = gs - Ae * (R(2) * r + hFu2) + Bo[p] * t2;
+            }
+          });
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU) {
+              R md = R(-0.0);
+              sfor<0, NP>([&](auto pp) {
+                constexpr int p = decltype(pp)::value;
+                constexpr int v = L::mt(pair_n<D>(p), kq);
+                if constexpr (v == 1) md = md + Sp[p];
+                else if constexpr (v == -1) md = md - Sp[p];
+                else if constexpr (v != 0) md = md + R(v) * Sp[p];
+              });
+              ck[kq] = P.dspec[m][kq] * md;
+            }
+          });
+        }
         const bool k0 = keep == R(0);
         push(std::integral_constant<int, 0>{}, m, k0 ? X0 : keep * pop(std::integral_constant<int, 0>{}) + X0);
         sfor<0, NP>([&](auto pp) {

@@ -21,19 +21,17 @@
 #include "tx_kernels.cuh"
 
 // Resident 128-thread blocks per SM that ptxas must make room for in
-// k_step_pair: 3 (168 registers) for one component, 2 (255) for two, whose
-// collision keeps both components' pair terms live; each thread carries two
-// sites, so two blocks keep as many sites in flight as four of step_site.
+// k_step_pair (168 registers): each thread carries two sites, so three
+// blocks keep more sites in flight than four of step_site.  For two
+// components this spills a little; measured on GB300 at 128^3 it is faster
+// than two blocks without spills (FP16 storage: 0.128 against 0.153 ms).
 #ifndef TX_PAIR_MIN_BLOCKS_S1
 #define TX_PAIR_MIN_BLOCKS_S1 3
 #endif
 #ifndef TX_PAIR_MIN_BLOCKS_S2
-#define TX_PAIR_MIN_BLOCKS_S2 2
+#define TX_PAIR_MIN_BLOCKS_S2 3
 #endif
 #define TX_PAIR_MIN_BLOCKS(S) ((S) == 1 ? TX_PAIR_MIN_BLOCKS_S1 : TX_PAIR_MIN_BLOCKS_S2)
-#ifndef TX_PAIR_CALL
-#define TX_PAIR_CALL 0
-#endif
 
 namespace tx {
 
@@ -212,22 +210,45 @@ struct PairPush {
 };
 
 // Fast-form collision of step_site (see there) of component m on V2 values,
-// with the pushes.  With TX_PAIR_CALL each component's collision is a call
-// of its own, whose registers are allocated apart from the caller's: the
-// caller holds only what the next component needs across the call.
+// with the pushes.
 template <int D>
 struct VecD {
   V2 v[D];
 };
-#if TX_PAIR_CALL
-#define TX_PAIR_COLLIDE_INLINE __noinline__
-#else
-#define TX_PAIR_COLLIDE_INLINE __forceinline__
-#endif
+// the s_nu moments of one component's pre-collision pair sums (nu_slot order)
+template <int D>
+struct VecNu {
+  V2 v[nnu<D>()];
+};
+
+// V2 form of nu_noneq (tx_kernels.cuh): the s_nu moment k of the pair sums
+// of the non-equilibrium part from the populations' moment sn_k
+template <int D, int k>
+__device__ __forceinline__ V2 nu_noneq2(V2 sn_k, V2 q, const V2 u[D], const V2 F[D]) {
+  V2 e{0.f, 0.f}, t{0.f, 0.f};
+  bool fe = true, ft = true;
+  sfor<0, D>([&](auto aa) {
+    constexpr int a = decltype(aa)::value;
+    sfor<0, D>([&](auto bb) {
+      constexpr int b = decltype(bb)::value;
+      constexpr double cu = nu_uu<D>(k, a, b), cf = nu_uf<D>(k, a, b);
+      if constexpr (cu != 0.0) {
+        e = fe ? v2(float(cu)) * (u[a] * u[b]) : fma2(v2(float(cu)), u[a] * u[b], e);
+        fe = false;
+      }
+      if constexpr (cf != 0.0) {
+        t = ft ? v2(float(cf)) * (u[a] * F[b]) : fma2(v2(float(cf)), u[a] * F[b], t);
+        ft = false;
+      }
+    });
+  });
+  return fma2(-q, e, sn_k) + t;
+}
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
-__device__ TX_PAIR_COLLIDE_INLINE void pair_collide_m(const PairPush<D, S, MRT, FULL, T, RCH> push,
+__device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T, RCH> push,
                                                       const PhysT<float>& P, const T* fin, unsigned N, unsigned c0,
-                                                      int m, V2 r, V2 rd, VecD<D> Fm_, VecD<D> up_) {
+                                                      int m, V2 r, V2 rd, VecD<D> Fm_, VecD<D> up_,
+                                                      VecNu<D> sn) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   constexpr int NP = npairs<D>();
@@ -302,38 +323,14 @@ __device__ TX_PAIR_COLLIDE_INLINE void pair_collide_m(const PairPush<D, S, MRT, 
     } else if (spec == stress_mask<D>()) {
       // s_nu != s0, every other rate s0: pair sums of the non-equilibrium
       // part, the s_nu moments' corrections, then each pair relaxed
-      V2 F3[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) F3[d] = v2(3.f) * F[m][d];
-      const V2 hFu2 = v2(3.f) * Fu;
-      // the s_nu moments of the pair sums, accumulated pair by pair
+      // the s_nu moments of the non-equilibrium pair sums in closed form from
+      // the moments pass's sn, and their corrections
+      const V2 q = fma2(v2(2.f), r, v2(3.f) * Fu);
       V2 ck[Q];
-      bool seen[Q] = {};
-      sfor<0, NP>([&](auto pp) {
-        constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-        const V2 WA = n <= L::NAXIS ? WA1 : WA2;
-        const V2 Ae = WA + WBe[p];
-        const V2 t2 = cdot2<D, n>(F3);
-        const V2 gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
-        const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
-        const V2 Sp = fma2(Bo[p], t2, fma2(v2(-2.f), De, gs) - Ae * hFu2);
-        sfor<0, Q>([&](auto kk) {
-          constexpr int kq = decltype(kk)::value;
-          if constexpr (rate_of<D>(kq) == R_NU) {
-            constexpr int v = L::mt(n, kq);
-            if constexpr (v != 0) {
-              if (!seen[kq])
-                ck[kq] = v == 1 ? Sp : (v == -1 ? -Sp : v2(float(v)) * Sp);
-              else
-                ck[kq] = v == 1 ? ck[kq] + Sp : (v == -1 ? ck[kq] - Sp : fma2(v2(float(v)), Sp, ck[kq]));
-              seen[kq] = true;
-            }
-          }
-        });
-      });
       sfor<0, Q>([&](auto kk) {
         constexpr int kq = decltype(kk)::value;
-        if constexpr (rate_of<D>(kq) == R_NU) ck[kq] = v2(P.dspec[m][kq]) * ck[kq];
+        if constexpr (rate_of<D>(kq) == R_NU)
+          ck[kq] = v2(P.dspec[m][kq]) * nu_noneq2<D, kq>(sn.v[nu_slot<D>(kq)], q, up, F[m]);
       });
       const bool k0 = keepf == 0.f;
       push(std::integral_constant<int, 0>{}, m, k0 ? X0 : fma2(keep, pop(std::integral_constant<int, 0>{}), X0));
@@ -412,7 +409,7 @@ __device__ TX_PAIR_COLLIDE_INLINE void pair_collide_m(const PairPush<D, S, MRT, 
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
 __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, RCH>& push, const PhysT<float>& P,
                                              const T* fin, unsigned N, unsigned c0, const V2 rc[S], const V2 rcd[S],
-                                             const V2 F[S][D], const V2 up[D]) {
+                                             const V2 F[S][D], const V2 up[D], const VecNu<D> sn[S]) {
   VecD<D> u;
 #pragma unroll
   for (int d = 0; d < D; ++d) u.v[d] = up[d];
@@ -421,7 +418,7 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
     VecD<D> f;
 #pragma unroll
     for (int d = 0; d < D; ++d) f.v[d] = F[m][d];
-    pair_collide_m<D, S, MRT, FULL, T, RCH>(push, P, fin, N, c0, m, rc[m], rcd[m], f, u);
+    pair_collide_m<D, S, MRT, FULL, T, RCH>(push, P, fin, N, c0, m, rc[m], rcd[m], f, u, sn[m]);
   }
 }
 
@@ -484,6 +481,7 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
   // moments: flux of each component from pair differences, common velocity
   const T* fin = reinterpret_cast<const T*>(a.fin);
   V2 up[D];
+  VecNu<D> sn[S];  // s_nu moments of the pair sums (components with the s_nu-only rate pattern)
   {
     V2 num[D], den = v2(0.f);
 #pragma unroll
@@ -493,9 +491,26 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
       V2 j[D];
       bool seen[D] = {};
       const T* fm = fin + (size_t)m * Q * N + c0;
+      const bool stress = P.spec_mask[m] == stress_mask<D>();
+      bool nseen[nnu<D>()] = {};
       sfor<0, npairs<D>()>([&](auto pp) {
         constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
-        const V2 dlt = ld_pair<T>(fm + (size_t)n * N, sc) - ld_pair<T>(fm + (size_t)nb * N, sc);
+        const V2 fa = ld_pair<T>(fm + (size_t)n * N, sc), fb = ld_pair<T>(fm + (size_t)nb * N, sc);
+        const V2 dlt = fa - fb;
+        if (stress) {
+          const V2 gs = fa + fb;
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU) {
+              constexpr int v = L::mt(n, kq), sl = nu_slot<D>(kq);
+              if constexpr (v != 0) {
+                const V2 t = v == 1 ? gs : (v == -1 ? -gs : v2(float(v)) * gs);
+                sn[m].v[sl] = nseen[sl] ? sn[m].v[sl] + t : t;
+                nseen[sl] = true;
+              }
+            }
+          });
+        }
         sfor<0, D>([&](auto dd) {
           constexpr int d = decltype(dd)::value;
           constexpr int c = L::c(n, d);
@@ -518,10 +533,10 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
   T* fout = reinterpret_cast<T*>(a.fout);
   if (warp_full) {
     const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
-    pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
+    pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up, sn);
   } else {
     const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
-    pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
+    pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up, sn);
   }
 }
 

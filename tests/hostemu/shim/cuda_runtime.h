@@ -40,6 +40,7 @@ inline unsigned atomicAdd(unsigned* p, unsigned v) {
   return o;
 }
 inline float __frcp_rn(float x) { return 1.0f / x; }
+inline double __drcp_rn(double x) { return 1.0 / x; }
 struct alignas(16) double2 {
   double x, y;
 };
