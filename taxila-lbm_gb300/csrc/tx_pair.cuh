@@ -103,6 +103,19 @@ __device__ __forceinline__ V2 ld_pair(const T* p, Scl<float> sc) {
   }
 }
 
+// The stored values of the two sites at p as floats, the FP16 storage scale
+// not divided out (sums of them are scaled once).
+template <class T>
+__device__ __forceinline__ V2 ld_pair_raw(const T* p) {
+  if constexpr (std::is_same<T, __half>::value) {
+    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    return V2{f.x, f.y};
+  } else {
+    const float2 f = __ldg(reinterpret_cast<const float2*>(p));
+    return V2{f.x, f.y};
+  }
+}
+
 // Both sites' values to the adjacent slots at p (FP16: stochastic rounding
 // with the per-site dithers d0, d1, exactly as st_dev_sr rounds each).
 template <class T>
@@ -121,6 +134,24 @@ __device__ __forceinline__ void st_pair(T* p, V2 v, Scl<float> sc, uint32_t d0, 
 template <class T>
 __device__ __forceinline__ void st_one(T* p, float v, Scl<float> sc, uint32_t d) {
   st_dev_sr_s<T, float>(p, v, sc, d);
+}
+
+// Both sites' values to two separate slots (a push along x): one scale
+// multiply and one FP16 pack for the two, each half stored where it goes;
+// w0 / w1 say whether each is stored.
+template <class T>
+__device__ __forceinline__ void st_two(T* p0, T* p1, V2 v, Scl<float> sc, uint32_t d0, uint32_t d1, bool w0 = true,
+                                       bool w1 = true) {
+  if constexpr (std::is_same<T, __half>::value) {
+    const V2 s = v * v2(sc.s);
+    const uint32_t u = pack_half2_rz(__uint_as_float(__float_as_uint(s.x) + d0),
+                                     __uint_as_float(__float_as_uint(s.y) + d1));
+    if (w0) *reinterpret_cast<uint16_t*>(p0) = (uint16_t)(u & 0xffffu);
+    if (w1) *reinterpret_cast<uint16_t*>(p1) = (uint16_t)(u >> 16);
+  } else {
+    if (w0) *p0 = v.x;
+    if (w1) *p1 = v.y;
+  }
 }
 
 // ------------------------------------------------------------- predicates
@@ -187,8 +218,7 @@ struct PairPush {
       if (FULL || (p0 && p1)) {
         st_pair<T>(sn + c0, v, sc, d0, d1);
       } else {
-        if (p0) st_one<T>(sn + c0, v.x, sc, d0);
-        if (p1) st_one<T>(sn + c0 + 1, v.y, sc, d1);
+        st_two<T>(sn + c0, sn + c0 + 1, v, sc, d0, d1, p0, p1);
       }
     } else {
       constexpr int cx = L::c(n, 0), cy = L::c(n, 1), cz = D == 3 ? L::c(n, 2) : 0;
@@ -196,14 +226,13 @@ struct PairPush {
         if constexpr (cx == 0) {
           st_pair<T>(sn + h0.template at<0, cy, cz>(), v, sc, d0, d1);
         } else {
-          st_one<T>(sn + h0.template at<cx, cy, cz>(), v.x, sc, d0);
-          st_one<T>(sn + h1.template at<cx, cy, cz>(), v.y, sc, d1);
+          st_two<T>(sn + h0.template at<cx, cy, cz>(), sn + h1.template at<cx, cy, cz>(), v, sc, d0, d1);
         }
       } else {
         T* const so = fout + (size_t)(m * Q + o) * N;
         const bool q0 = ((l0 >> n) & 1u) != 0u, q1 = ((l1 >> n) & 1u) != 0u;
-        if (p0) st_one<T>(q0 ? sn + h0.template at<cx, cy, cz>() : so + c0, v.x, sc, d0);
-        if (p1) st_one<T>(q1 ? sn + h1.template at<cx, cy, cz>() : so + c0 + 1, v.y, sc, d1);
+        st_two<T>(q0 ? sn + h0.template at<cx, cy, cz>() : so + c0, q1 ? sn + h1.template at<cx, cy, cz>() : so + c0 + 1,
+                  v, sc, d0, d1, p0, p1);
       }
     }
   }
@@ -277,7 +306,7 @@ __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T
     const V2 s0 = v2(P.s0[m]);
     const float kf = P.kfac[m];
     const float keepf = P.keep[m];
-    const V2 keep = v2(keepf);
+    const V2 keep = v2(std::is_same<T, __half>::value ? keepf * push.sc.inv : keepf);
     V2 Fu = F[m][0] * up[0], kF[D];
 #pragma unroll
     for (int d = 1; d < D; ++d) Fu = fma2(F[m][d], up[d], Fu);
@@ -287,7 +316,8 @@ __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T
     const V2 G = fma2(s0, r, -kFu);
     const unsigned spec = P.spec_mask[m];
     const T* fm = fin + (size_t)m * Q * N + c0;
-    auto pop = [&](auto nn) -> V2 { return ld_pair<T>(fm + (size_t)decltype(nn)::value * N, push.sc); };
+    // the stored value (storage scale not divided out: keep carries it)
+    auto pop = [&](auto nn) -> V2 { return ld_pair_raw<T>(fm + (size_t)decltype(nn)::value * N); };
     const V2 E0 = WA0 + WB0;
     // rest direction: g'_0 = keep g_0 + X0
     const V2 X0 = s0 * fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * kFu;
@@ -360,19 +390,23 @@ __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T
       // moment whose rate differs by dspec_k times its projection of the
       // deviation from the forced equilibrium
       V2 fo[Q], dfi[Q];
-      fo[0] = fma2(keep, pop(std::integral_constant<int, 0>{}), X0);
+      // the deviations themselves (pop is the stored value, keep carries the scale)
+      const V2 inv = v2(std::is_same<T, __half>::value ? push.sc.inv : 1.f);
+      const V2 g0 = pop(std::integral_constant<int, 0>{});
+      fo[0] = fma2(keep, g0, X0);
       const V2 hFu = v2(1.5f) * Fu;
       V2 hF[D];
 #pragma unroll
       for (int d = 0; d < D; ++d) hF[d] = v2(1.5f) * F[m][d];
-      dfi[0] = pop(std::integral_constant<int, 0>{}) - fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * hFu;
+      dfi[0] = g0 * inv - fma2(WA0, rd, fma2(WB0, r, cA0)) - E0 * hFu;
       sfor<0, NP>([&](auto pp) {
         constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
         V2 pe, po;
         pair_terms(pp, pe, po);
-        const V2 gn = pop(std::integral_constant<int, n>{}), gb = pop(std::integral_constant<int, nb>{});
-        fo[n] = fma2(keep, gn, pe + po);
-        fo[nb] = fma2(keep, gb, pe - po);
+        const V2 sn_ = pop(std::integral_constant<int, n>{}), sb_ = pop(std::integral_constant<int, nb>{});
+        fo[n] = fma2(keep, sn_, pe + po);
+        fo[nb] = fma2(keep, sb_, pe - po);
+        const V2 gn = sn_ * inv, gb = sb_ * inv;
         const V2 WA = n <= L::NAXIS ? WA1 : WA2;
         const V2 t = cdot2<D, n>(hF);
         const V2 En = WA + WBe[p] + Bo[p], Eb = WA + WBe[p] - Bo[p];
@@ -495,7 +529,7 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
       bool nseen[nnu<D>()] = {};
       sfor<0, npairs<D>()>([&](auto pp) {
         constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
-        const V2 fa = ld_pair<T>(fm + (size_t)n * N, sc), fb = ld_pair<T>(fm + (size_t)nb * N, sc);
+        const V2 fa = ld_pair_raw<T>(fm + (size_t)n * N), fb = ld_pair_raw<T>(fm + (size_t)nb * N);
         const V2 dlt = fa - fb;
         if (stress) {
           const V2 gs = fa + fb;
@@ -521,6 +555,15 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
           }
         });
       });
+      if constexpr (std::is_same<T, __half>::value) {
+        // the storage scale out of the sums
+        const V2 inv = v2(sc.inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d) j[d] = j[d] * inv;
+        if (stress)
+#pragma unroll
+          for (int k = 0; k < nnu<D>(); ++k) sn[m].v[k] = sn[m].v[k] * inv;
+      }
       const V2 mm = v2(P.mmot[m]);
 #pragma unroll
       for (int d = 0; d < D; ++d) num[d] = fma2(fma2(v2(0.5f), F[m][d], j[d]), mm, num[d]);
