@@ -52,7 +52,7 @@ struct Lattice {
   int NS = 0;
   long long bytes = 0;
   long long steps = 0;
-  bool paired = false;        // the paired step (FP32-arithmetic forms, even nx)
+  bool paired = false;        // the paired step (FP32-arithmetic forms, even site count)
   int rest = -1;              // its pairs for the per-site kernel
 };
 
@@ -267,12 +267,10 @@ int rebuild_tables(tx_batch* b) {
         for (int x = 0; x < L->g.nx; x += b->bx) tiles.push_back(make_int4((int)s, x, y, z));
     d.tile_count = (int)tiles.size() - d.tile_begin;
     if (L->paired) {
-      for (int z = 0; z < L->g.nz; z += b->bz)
-        for (int y = 0; y < L->g.ny; y += b->by)
-          for (int x = 0; x < L->g.nx; x += 2 * b->bx) {
-            ptiles.push_back(make_int4((int)s, x, y, z));
-            if (L->rest != 0) rtiles.push_back(make_int4((int)s, x, y, z));
-          }
+      for (long long i0 = 0; 2 * i0 < L->g.n; i0 += 128) {
+        ptiles.push_back(make_int4((int)s, (int)i0, 0, 0));
+        if (L->rest != 0) rtiles.push_back(make_int4((int)s, (int)i0, 0, 0));
+      }
     } else {
       stiles.insert(stiles.end(), tiles.begin() + d.tile_begin, tiles.end());
     }

@@ -64,8 +64,8 @@ struct BatchArgs {
   const int4* otiles; // outlet refresh: (lattice slot, face, first node, 0) of runs of 128 nodes
   const int* notiles;
   // the step: per-site tiles of the lattices without the paired kernel; pair
-  // tiles (x extent twice the block's) of those with it, and the pair tiles
-  // of the lattices that have pairs for the per-site kernel
+  // tiles (lattice slot, first pair: runs of 128 pairs) of those with it, and
+  // the pair tiles of the lattices that have pairs for the per-site kernel
   const int4* stiles;
   const int* nstiles;
   const int4* ptiles;
@@ -94,28 +94,29 @@ __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT)) k_step_til
   }
 }
 
-// The paired step of k_step_pair over the pair tiles (thread (i, j, k) of a
-// tile takes the pair at x = x0 + 2 i).
+// The paired step of k_step_pair over the pair tiles: runs of 128 pairs
+// (lattice slot, first pair) of the lattices with an even site count.
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair_tiles(BatchArgs b, int flip) {
   const int nt = __ldg(b.nptiles);
+  const int lane = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const int4 tl = __ldg(b.ptiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-    const int x0 = tl.y + 2 * (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
+    const unsigned i = (unsigned)tl.y + (unsigned)lane;
     bool run = false, full = false;
     uint2 ll = make_uint2(0u, 0u);
-    if (x0 < a.g.nx && y < a.g.ny && z < a.g.nz) {
-      const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
-      ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
-      run = pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 1;
-      constexpr uint32_t all = all_links<D>() | 1u;
-      full = (ll.x & all) == all && (ll.y & all) == all;
+    PairSites ps{};
+    if ((long long)2 * i < a.g.n) {
+      ps = pair_sites(a.g, i);
+      ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
+      run = pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 1;
+      full = pair_full<D>(a.g, ps, ll.x, ll.y);
     }
     // every lane votes, so that the vote is uniform over the warp's running lanes
     const bool warp_full = __all_sync(0xffffffffu, full || !run);
-    if (run) step_pair<D, S, ISO, MRT, T>(a, x0, y, z, ll.x, ll.y, warp_full);
+    if (run) step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
   }
 }
 
@@ -123,16 +124,19 @@ __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair_tiles(
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, float, MRT)) k_step_rest_tiles(BatchArgs b, int flip) {
   const int nt = __ldg(b.nrtiles);
+  const int lane = (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z));
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const int4 tl = __ldg(b.rtiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-    const int x0 = tl.y + 2 * (int)threadIdx.x, y = tl.z + (int)threadIdx.y, z = tl.w + (int)threadIdx.z;
-    if (x0 < a.g.nx && y < a.g.ny && z < a.g.nz) {
-      const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
-      const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
-      if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 0)
-        for (int k = 0; k < 2; ++k) step_site<D, S, ISO, MRT, false, T, float, float>(a, x0 + k, y, z);
+    const unsigned i = (unsigned)tl.y + (unsigned)lane;
+    if ((long long)2 * i < a.g.n) {
+      const PairSites ps = pair_sites(a.g, i);
+      const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
+      if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 0) {
+        step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x0, ps.y0, ps.z0);
+        step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x1, ps.y1, ps.z1);
+      }
     }
   }
 }

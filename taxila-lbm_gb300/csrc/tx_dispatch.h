@@ -30,7 +30,7 @@ struct KernelSet {
   // their batched forms (no-ops in the exact form)
   void (*faces_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
   void (*outlet_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);
-  // paired-site step (FP32-arithmetic forms, even nx): whether a lattice takes
+  // paired-site step (FP32-arithmetic forms, even site count): whether a lattice takes
   // it, and how many of its pairs need the per-site kernel (counted into *count)
   bool (*paired)(const Geo&);
   void (*count_rest)(const StepArgs&, unsigned* count, cudaStream_t);
@@ -104,7 +104,7 @@ inline Launch3 launch3(const Geo& g, int threads) {
 #define TX_FORM_LAUNCHERS_(D, S, ISO, MRT, EXACT, T, R, RT)                                                  \
   struct L_##S##_##ISO##_##MRT {                                                                             \
     static constexpr bool kPairForm = !EXACT && std::is_same<R, float>::value;                                \
-    static bool paired(const Geo& g) { return kPairForm && g.nx % 2 == 0; }                                   \
+    static bool paired(const Geo& g) { return kPairForm && g.n % 2 == 0; }                                    \
     static void step(const StepArgs& a, cudaStream_t s) {                                                     \
       if constexpr (kPairForm) {                                                                              \
         if (paired(a.g)) {                                                                                    \

@@ -205,7 +205,7 @@ struct StepArgs {
   // counter that the density pass advances (so replayed graphs see it move).
   unsigned step;
   const unsigned* steps_ptr;
-  // FP32-arithmetic forms on lattices with an even nx (tx_pair.cuh): pairs
+  // FP32-arithmetic forms on lattices with an even site count (tx_pair.cuh): pairs
   // that need the per-site kernel k_step_rest (-1: not counted, run it)
   int rest;
 };

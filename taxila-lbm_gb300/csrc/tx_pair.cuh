@@ -1,8 +1,9 @@
 // Paired-site step kernels of the FP32-arithmetic forms (FP32 or FP16
 // population storage).
 //
-// One thread updates two x-adjacent sites (x0 even, x0 + 1) of a lattice with
-// an even nx.  Every per-site quantity of the collision is a V2, the value at
+// One thread updates two consecutive cells in storage order (c0 even, c0 + 1)
+// of a lattice with an even site count: usually x-neighbours of one row, at
+// odd nx one pair in two rows spans a row end.  Every per-site quantity of the collision is a V2, the value at
 // both sites, and every V2 operation is one packed FP32x2 instruction of
 // sm_100+ (FADD2 / FMUL2 / FFMA2), so the collision costs half the FP32
 // instructions per site.  The two sites' populations of one direction are
@@ -169,32 +170,56 @@ __device__ __forceinline__ bool pair_simple_site(const StepArgs& a, const PhysT<
 }
 
 // 1: the pair goes to k_step_pair; 0: to k_step_rest; -1: no pore site.
+// The two cells of pair i: c0 = 2 i and c0 + 1, with their coordinates.
+struct PairSites {
+  unsigned c0;
+  int x0, y0, z0, x1, y1, z1;
+  __device__ __forceinline__ bool same_row() const { return x1 == x0 + 1; }
+};
+__device__ __forceinline__ PairSites pair_sites(const Geo& g, unsigned i) {
+  PairSites ps;
+  ps.c0 = 2u * i;
+  const unsigned nx = (unsigned)g.nx, ny = (unsigned)g.ny;
+  unsigned row = ps.c0 / nx;
+  ps.x0 = (int)(ps.c0 - row * nx);
+  ps.y0 = (int)(row % ny);
+  ps.z0 = (int)(row / ny);
+  if (ps.x0 + 1 < g.nx) {
+    ps.x1 = ps.x0 + 1;
+    ps.y1 = ps.y0;
+    ps.z1 = ps.z0;
+  } else {
+    ++row;
+    ps.x1 = 0;
+    ps.y1 = (int)(row % ny);
+    ps.z1 = (int)(row / ny);
+  }
+  return ps;
+}
+
 template <int D, int ISO>
-__device__ __forceinline__ int pair_class(const StepArgs& a, const PhysT<float>& P, uint32_t l0, uint32_t l1, int x0,
-                                          int y, int z) {
+__device__ __forceinline__ int pair_class(const StepArgs& a, const PhysT<float>& P, uint32_t l0, uint32_t l1,
+                                          const PairSites& ps) {
   const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
   if (!p0 && !p1) return -1;
-  const bool s0 = !p0 || pair_simple_site<D, ISO>(a, P, l0, x0, y, z);
-  const bool s1 = !p1 || pair_simple_site<D, ISO>(a, P, l1, x0 + 1, y, z);
+  const bool s0 = !p0 || pair_simple_site<D, ISO>(a, P, l0, ps.x0, ps.y0, ps.z0);
+  const bool s1 = !p1 || pair_simple_site<D, ISO>(a, P, l1, ps.x1, ps.y1, ps.z1);
   return (s0 && s1) ? 1 : 0;
 }
 
 // --------------------------------------------------------------- the pair
-// Pair (x0, x0 + 1) of a row.  The pairs are numbered in storage order over
-// a one-dimensional grid, so that no lane idles at the end of a row.
-__device__ __forceinline__ bool pair_of(const Geo& g, int& x0, int& y, int& z) {
+// The pair of this thread in a one-dimensional launch over the pairs.
+__device__ __forceinline__ bool pair_of(const Geo& g, PairSites& ps) {
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned npx = (unsigned)g.nx >> 1;
-  const unsigned row = i / npx;
-  x0 = 2 * (int)(i - row * npx);
-  y = (int)(row % (unsigned)g.ny);
-  z = (int)(row / (unsigned)g.ny);
-  return z < g.nz;
+  if ((long long)2 * i >= g.n) return false;
+  ps = pair_sites(g, i);
+  return true;
 }
 
-// Collision and push of one component of a simple pair.  FULL: both sites
-// pore with every link pore (no bounceback), so the pushes need no selects;
-// the caller takes FULL only when every active lane of the warp is full.
+// Collision and push of one component of a simple pair.  FULL (pair_full):
+// both sites pore with every link pore (no bounceback), in one row of an
+// even-nx lattice, so the pushes need no selects; the caller takes FULL only
+// when every active lane of the warp is full.
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
 struct PairPush {
   using L = Lat<D>;
@@ -456,18 +481,18 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
   }
 }
 
-// One simple pair (x0, x0 + 1): forces per site, moments and collision on V2.
+// One simple pair: forces per site, moments and collision on V2.
 template <int D, int S, int ISO, bool MRT, class T>
-__device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int z, uint32_t l0, uint32_t l1,
+__device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps, uint32_t l0, uint32_t l1,
                                           bool warp_full) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   constexpr int RCH = stencil_reach<D, ISO>();
   const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
   const unsigned N = (unsigned)a.g.n;
-  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
+  const unsigned c0 = ps.c0;
   const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
-  const Hood<D, RCH> h0(a.g, x0, y, z), h1(a.g, x0 + 1, y, z);
+  const Hood<D, RCH> h0(a.g, ps.x0, ps.y0, ps.z0), h1(a.g, ps.x1, ps.y1, ps.z1);
   const Scl<float> sc = scl_of(P);
   uint32_t seed0 = 0, seed1 = 0;
   if constexpr (std::is_same<T, __half>::value) {
@@ -583,44 +608,49 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, int x0, int y, int 
   }
 }
 
-// k_step_pair / k_step_rest blocks: 128 threads over pairs (x halved).
+// Whether a pair goes the bounceback-free way (see PairPush): both sites pore
+// with every link pore, in one row of a lattice with an even nx (so that the
+// y and z neighbours' pair slots are aligned for one vector store).
+template <int D>
+__device__ __forceinline__ bool pair_full(const Geo& g, const PairSites& ps, uint32_t l0, uint32_t l1) {
+  constexpr uint32_t all = all_links<D>() | 1u;
+  return (g.nx & 1) == 0 && ps.same_row() && (l0 & all) == all && (l1 & all) == all;
+}
+
+// k_step_pair / k_step_rest / k_count_rest: one thread per pair, 1-D grid.
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair(StepArgs a_in) {
   const StepArgs a = a_in;
-  int x0, y, z;
-  if (!pair_of(a.g, x0, y, z)) return;
-  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
-  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  PairSites ps;
+  if (!pair_of(a.g, ps)) return;
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
   const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) != 1) return;
-  constexpr uint32_t all = all_links<D>() | 1u;
-  const bool full = (ll.x & all) == all && (ll.y & all) == all;
-  const bool warp_full = __all_sync(__activemask(), full);
-  step_pair<D, S, ISO, MRT, T>(a, x0, y, z, ll.x, ll.y, warp_full);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) != 1) return;
+  const bool warp_full = __all_sync(__activemask(), pair_full<D>(a.g, ps, ll.x, ll.y));
+  step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
 }
 
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, float, MRT)) k_step_rest(StepArgs a_in) {
   const StepArgs a = a_in;
-  int x0, y, z;
-  if (!pair_of(a.g, x0, y, z)) return;
-  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
-  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  PairSites ps;
+  if (!pair_of(a.g, ps)) return;
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
   const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) != 0) return;
-  for (int k = 0; k < 2; ++k) step_site<D, S, ISO, MRT, false, T, float, float>(a, x0 + k, y, z);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) != 0) return;
+  step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x0, ps.y0, ps.z0);
+  step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x1, ps.y1, ps.z1);
 }
 
 // Pairs that need the per-site kernel (the count decides whether k_step_rest runs).
 template <int D, int ISO>
 __global__ void __launch_bounds__(256) k_count_rest(StepArgs a_in, unsigned* count) {
   const StepArgs a = a_in;
-  int x0, y, z;
-  if (!pair_of(a.g, x0, y, z)) return;
-  const unsigned c0 = (unsigned)x0 + (unsigned)a.g.nx * ((unsigned)y + (unsigned)a.g.ny * (unsigned)z);
-  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (c0 >> 1));
+  PairSites ps;
+  if (!pair_of(a.g, ps)) return;
+  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
   const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-  if (pair_class<D, ISO>(a, P, ll.x, ll.y, x0, y, z) == 0) atomicAdd(count, 1u);
+  if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 0) atomicAdd(count, 1u);
 }
 
 }  // namespace tx

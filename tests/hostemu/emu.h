@@ -114,9 +114,9 @@ std::string run(const Case& c, Result& out) {
   T* buf[2] = {f0.data(), f1.data()};
   int cur = 0;
   unsigned step = 0;
-  // the paired step of the FP32-arithmetic forms on lattices with an even nx
+  // the paired step of the FP32-arithmetic forms on lattices with an even site count
   constexpr bool kPairForm = !EXACT && std::is_same<R, float>::value;
-  const bool paired = kPairForm && g.nx % 2 == 0;
+  const bool paired = kPairForm && N % 2 == 0;
   int rest = -1;
   auto args = [&](int in, int o) {
     StepArgs a{};

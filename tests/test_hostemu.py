@@ -130,8 +130,11 @@ def test_emulated_restart_from_fi(emu_exe, tmp_path):
 
 
 @pytest.mark.parametrize("prec", [P.PREC_F32, P.PREC_F32_F16], ids=["f32", "f32_f16"])
-def test_emulated_reduced_precision_forms(emu_exe, tmp_path, prec):
-    p, walls, rho = cases.sc_bubble(P.D3Q19, (12, 12, 14), P.MRT, 4, g=0.15)
+@pytest.mark.parametrize("shape,nu_only", [((12, 12, 14), False), ((12, 12, 13), False), ((12, 12, 13), True)],
+                         ids=["mixed_rates", "odd_nx", "odd_nx_s_nu_only"])
+def test_emulated_reduced_precision_forms(emu_exe, tmp_path, prec, shape, nu_only):
+    # odd nx: paired cells span row ends; s_nu only: the closed-form stress correction
+    p, walls, rho = cases.sc_bubble(P.D3Q19, shape, P.MRT, 4, g=0.15, nu_only=nu_only)
     ref = oracle_run(p, walls, rho, 20)
     q = P.copy_params(p)
     q.precision = prec
@@ -142,11 +145,12 @@ def test_emulated_reduced_precision_forms(emu_exe, tmp_path, prec):
 
 
 @pytest.mark.parametrize("prec,scale", [(P.PREC_F32, 1.0), (P.PREC_F32_F16, 4096.0)], ids=["f32", "f32_f16"])
-def test_emulated_permeability_precision(emu_exe, tmp_path, prec, scale):
+@pytest.mark.parametrize("shape", [(14, 12, 16), (14, 12, 15)], ids=["even_nx", "odd_nx"])
+def test_emulated_permeability_precision(emu_exe, tmp_path, prec, scale, shape):
     # single-phase body-force flow through a sphere pack, deviations stored
     # from rho0 = 1: the Darcy velocity (hence the permeability) within 1e-3 of
     # the FP64 oracle, populations and density far tighter
-    p, walls, rho = cases.permeability_case((14, 12, 16), seed=5)
+    p, walls, rho = cases.permeability_case(shape, seed=5)
     ref = oracle_run(p, walls, rho, 40)
     q = P.copy_params(p)
     q.precision = prec
