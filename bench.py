@@ -539,6 +539,17 @@ def fp64_bound(pk, sites, k_ms):
             "counts_source": c["source"]}
 
 
+def batched_converged_run(n_lat=16, seed=4):
+    """A bounded subset of the batched-permeability workload run to its stop
+    criterion (relative change of the mean flow < 1e-7 per 100-step chunk):
+    the first ``n_lat`` lattices of the 96 (sides 48-192, sphere packs, body
+    force 1e-6), one batch per form; time to solution and the permeability
+    errors of the FP32 and FP16-storage forms against the FP64 form."""
+    from taxila import precision
+    r = precision.batch_permeability_study(n_lat, seed)
+    return {"case": r["case"], "forms": r["forms"]}
+
+
 def serving_spec_run(n=40, seed=1):
     """The specification's serving mix (serve.SPEC_MIX: 70% permeability
     solves, sides 32-160, to a relative mean-flow change < 1e-7 per chunk; 30%
@@ -741,7 +752,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the e2e, precision-form, batched, serving and CPU legs")
     ap.add_argument("--n", type=int, default=N_SIDE, help="lattice side (profiling runs use a smaller case)")
     ap.add_argument("--form", default="f64", choices=sorted(FORMS), help="storage/arithmetic form of the timed run")
-    ap.add_argument("--leg", default="all", choices=["all", "batched", "serving", "serving_spec"],
+    ap.add_argument("--leg", default="all", choices=["all", "batched", "serving", "serving_spec", "batched_converged"],
                     help="run one extra leg alone and print its JSON (profiling)")
     ap.add_argument("--lattices", type=int, default=96, help="lattices of the batched leg")
     ap.add_argument("--requests", type=int, default=40, help="requests of the specification's serving mix")
@@ -758,6 +769,9 @@ def main():
         return 0
     if args.leg == "serving_spec":
         print(json.dumps(serving_spec_run(n=args.requests)))
+        return 0
+    if args.leg == "batched_converged":
+        print(json.dumps(batched_converged_run(n_lat=args.lattices)))
         return 0
     return run_gpu(args)
 

@@ -854,53 +854,6 @@ __device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
   });
 }
 
-// The s_nu moments of the pair sums f_n + f_n~ (the traceless second
-// moments of the populations; only the R_NU entries of sn are written).
-template <int D, class R>
-__device__ __forceinline__ void nu_moments(const R f[Lat<D>::Q], R sn[Lat<D>::Q]) {
-  using L = Lat<D>;
-  R gs[npairs<D>()];
-  sfor<0, npairs<D>()>([&](auto pp) {
-    constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
-    gs[p] = f[n] + f[opp<D>(n)];
-  });
-  sfor<0, L::Q>([&](auto kk) {
-    constexpr int k = decltype(kk)::value;
-    if constexpr (rate_of<D>(k) == R_NU) {
-      R acc = R(-0.0);
-      sfor<0, npairs<D>()>([&](auto pp) {
-        constexpr int p = decltype(pp)::value;
-        constexpr int v = L::mt(pair_n<D>(p), k);
-        if constexpr (v == 1) acc = acc + gs[p];
-        else if constexpr (v == -1) acc = acc - gs[p];
-        else if constexpr (v != 0) acc = acc + R(v) * gs[p];
-      });
-      sn[k] = acc;
-    }
-  });
-}
-
-// s_nu moment k of the pair sums of the non-equilibrium part (forced
-// equilibrium removed) from the populations' moment sn_k, the collision
-// density r, the velocity u and the component's force F:
-//   sn_k - (2 r + 3 F.u) * 4.5 sum_p v w (c.u)^2 + 9 sum_p v w (c.u)(c.F)
-// (the closed forms of nu_uu / nu_uf; the rest-density and weight-class
-// terms cancel on every s_nu moment).
-template <int D, int k, class R>
-__device__ __forceinline__ R nu_noneq(R sn_k, R q, const R u[D], const R F[D]) {
-  R e = R(-0.0), t = R(-0.0);
-  sfor<0, D>([&](auto aa) {
-    constexpr int a = decltype(aa)::value;
-    sfor<0, D>([&](auto bb) {
-      constexpr int b = decltype(bb)::value;
-      constexpr double cu = nu_uu<D>(k, a, b), cf = nu_uf<D>(k, a, b);
-      if constexpr (cu != 0.0) e = e + R(cu) * (u[a] * u[b]);
-      if constexpr (cf != 0.0) t = t + R(cf) * (u[a] * F[b]);
-    });
-  });
-  return sn_k - q * e + t;
-}
-
 // Density of the collision (Dirichlet nodes re-summed as in BCUpdateRho,
 // lbm_bc.F90:436-611) and the common velocity of FlowUpdateUED3/D2
 // (lbm_flow.F90:494-574) from the post-stream population deviations and the forces.
@@ -1013,12 +966,6 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   const T* fin = reinterpret_cast<const T*>(a.fin);
   // moments pass, one component's populations at a time; rcd = rc - rho0
   R rc[S], rcd[S], up[D];
-  // s_nu moments of the pair sums (FP32-arithmetic forms, s_nu-only rate
-  // patterns): the stress correction then takes their closed form and reloads
-  // no population.  The FP64 form keeps the pass over the pair sums, which
-  // costs fewer FP64 instructions.
-  constexpr bool kNuClosed = std::is_same<R, float>::value;
-  R snu[S][Q];
   {
     const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
     R jm[S][D];
@@ -1034,10 +981,6 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
       } else {
         pop_flux_pairs<D, R>(f1[0], jm[m]);
-        // FP32 arithmetic: the s_nu moments of a component whose collision
-        // corrects them, while its populations are in registers
-        if constexpr (kNuClosed)
-          if (P.spec_mask[m] == stress_mask<D>()) nu_moments<D, R>(f1[0], snu[m]);
       }
       rcd[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rfd[m];
       rc[m] = dn ? P.rho0[m] + rcd[m] : rf[m];
@@ -1242,16 +1185,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         // Bo c_n.(3 F), give the corrections ck; then each pair is relaxed
         // and pushed with its correction.
         R ck[Q];
-        if constexpr (kNuClosed) {
-          // the s_nu moments of the non-equilibrium pair sums in closed form
-          // from the moments pass's snu (nu_noneq), then their corrections ck
-          const R q = R(2) * r + R(3) * Fu;
-          sfor<0, Q>([&](auto kk) {
-            constexpr int kq = decltype(kk)::value;
-            if constexpr (rate_of<D>(kq) == R_NU)
-              ck[kq] = P.dspec[m][kq] * nu_noneq<D, kq, R>(snu[m][kq], q, up, F[m]);
-          });
-        } else {
+        {
           // pass 1: the pair sums of the non-equilibrium part, then their s_nu moments
           R F3[D];
 #pragma unroll
@@ -1468,6 +1402,28 @@ __device__ __forceinline__ void dirichlet_node(int f, const R pv[S], R fv[S][Lat
   }
 }
 
+// ------------------------------------------------------------ V2 arithmetic
+// Two FP32 lanes (two sites, or two consecutive cells) computed with the
+// packed FP32x2 instructions of sm_100+.
+struct V2 {
+  float x, y;
+};
+__host__ __device__ __forceinline__ V2 v2(float a) { return V2{a, a}; }
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float2 f2_(V2 a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ V2 v2_(float2 a) { return V2{a.x, a.y}; }
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), f2_(b))); }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), make_float2(-b.x, -b.y))); }
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return v2_(__fmul2_rn(f2_(a), f2_(b))); }
+__device__ __forceinline__ V2 fma2(V2 a, V2 b, V2 c) { return v2_(__ffma2_rn(f2_(a), f2_(b), f2_(c))); }
+#else
+inline V2 operator+(V2 a, V2 b) { return V2{a.x + b.x, a.y + b.y}; }
+inline V2 operator-(V2 a, V2 b) { return V2{a.x - b.x, a.y - b.y}; }
+inline V2 operator*(V2 a, V2 b) { return V2{a.x * b.x, a.y * b.y}; }
+inline V2 fma2(V2 a, V2 b, V2 c) { return V2{__builtin_fmaf(a.x, b.x, c.x), __builtin_fmaf(a.y, b.y, c.y)}; }
+#endif
+__host__ __device__ __forceinline__ V2 operator-(V2 a) { return V2{-a.x, -a.y}; }
+
 // -------------------------------------------------------------- density
 // mode 0 (after a step): forcing density = the face value on Dirichlet-class
 // face nodes (BCApplyDirichletToRho, lbm_bc.F90:252-434; the last such face in
@@ -1625,6 +1581,37 @@ __device__ __forceinline__ void density_group(const StepArgs& a, long long c0, i
     R acc[VW];
 #pragma unroll
     for (int v = 0; v < VW; ++v) acc[v] = R(0);
+    if constexpr (VEC && !std::is_same<T, double>::value) {
+      // FP32 arithmetic: the stored values of two cells per packed add, the
+      // FP16 storage scale applied once to each sum
+      V2 acc2[VW / 2];
+#pragma unroll
+      for (int v = 0; v < VW / 2; ++v) acc2[v] = v2(0.f);
+      sfor<0, Q>([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        const uint4 w = __ldg(reinterpret_cast<const uint4*>(fcur + (long long)(m * Q + n) * N + c0));
+        uint32_t wd[4];
+        memcpy(wd, &w, 16);
+#pragma unroll
+        for (int v = 0; v < VW / 2; ++v) {
+          float2 f;
+          if constexpr (std::is_same<T, __half>::value) {
+            __half2 h;
+            memcpy(&h, &wd[v], 4);
+            f = __half22float2(h);
+          } else {
+            memcpy(&f, &wd[2 * v], 8);
+          }
+          acc2[v] = acc2[v] + V2{f.x, f.y};
+        }
+      });
+      const float inv = std::is_same<T, __half>::value ? float(P.inv_sscale) : 1.f;
+#pragma unroll
+      for (int v = 0; v < VW / 2; ++v) {
+        acc[2 * v] = R(acc2[v].x * inv);
+        acc[2 * v + 1] = R(acc2[v].y * inv);
+      }
+    } else {
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       const T* src = fcur + (long long)(m * Q + n) * N + c0;
@@ -1640,6 +1627,7 @@ __device__ __forceinline__ void density_group(const StepArgs& a, long long c0, i
           if (v < cnt) acc[v] = acc[v] + from_dev<T, R>(__ldg(src + v), P);
       }
     });
+    }
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
       if (!pore[v]) continue;

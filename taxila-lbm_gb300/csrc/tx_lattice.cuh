@@ -176,68 +176,4 @@ __host__ __device__ constexpr bool moments_have_parity() {
 }
 static_assert(stress_even_traceless<3>() && stress_even_traceless<2>(), "s_nu moments must be even and traceless");
 
-// 36 w_n: integer weights (D3Q19 12 / 2 / 1, D2Q9 16 / 4 / 1)
-template <int D>
-__host__ __device__ constexpr int w36(int n) {
-  return D == 3 ? (n == 0 ? 12 : (n <= Lat<3>::NAXIS ? 2 : 1)) : (n == 0 ? 16 : (n <= Lat<2>::NAXIS ? 4 : 1));
-}
-
-// Closed forms of the equilibrium parts of the s_nu moments.  Over the
-// direction pairs p, with the pair-sum coefficients v_kp = mt(n_p, k),
-//   sum_p v_kp w_p         = 0  within each weight class (axis, diagonal),
-//   4.5 sum_p v_kp w_p (c_p.u)^2       = sum_{a<=b} nu_uu(k, a, b) u_a u_b,
-//   9   sum_p v_kp w_p (c_p.u)(c_p.F)  = sum_{a,b}  nu_uf(k, a, b) u_a F_b,
-// so a moment of the pair sums of the non-equilibrium part needs only the
-// moment of the pre-collision pair sums and these quadratic forms.  The
-// coefficients are eighths and quarters of integers: exact in any float type.
-template <int D>
-__host__ __device__ constexpr int nu_cc(int k, int a, int b) {
-  int s = 0;
-  for (int p = 0; p < npairs<D>(); ++p) {
-    const int n = pair_n<D>(p);
-    s += Lat<D>::mt(n, k) * w36<D>(n) * Lat<D>::c(n, a) * Lat<D>::c(n, b);
-  }
-  return s;
-}
-template <int D>
-__host__ __device__ constexpr double nu_uu(int k, int a, int b) {
-  return a == b ? nu_cc<D>(k, a, a) / 8.0 : (a < b ? 2 * nu_cc<D>(k, a, b) / 8.0 : 0.0);
-}
-template <int D>
-__host__ __device__ constexpr double nu_uf(int k, int a, int b) {
-  return nu_cc<D>(k, a, b) / 4.0;
-}
-template <int D>
-__host__ __device__ constexpr bool nu_class_sums_vanish() {
-  for (int k = 0; k < Lat<D>::Q; ++k) {
-    if (rate_of<D>(k) != R_NU) continue;
-    int sa = 0, sd = 0;
-    for (int p = 0; p < npairs<D>(); ++p) {
-      const int n = pair_n<D>(p);
-      (n <= Lat<D>::NAXIS ? sa : sd) += Lat<D>::mt(n, k);
-    }
-    if (sa != 0 || sd != 0) return false;
-  }
-  return true;
-}
-static_assert(nu_class_sums_vanish<3>() && nu_class_sums_vanish<2>(), "s_nu moments vanish on each weight class");
-// the s_nu moments in compact numbering: how many, and moment k's slot
-template <int D>
-__host__ __device__ constexpr int nnu() {
-  int c = 0;
-  for (int k = 0; k < Lat<D>::Q; ++k) c += rate_of<D>(k) == R_NU ? 1 : 0;
-  return c;
-}
-template <int D>
-__host__ __device__ constexpr int nu_slot(int k) {
-  int c = 0;
-  for (int j = 0; j < k; ++j) c += rate_of<D>(j) == R_NU ? 1 : 0;
-  return c;
-}
-static_assert(nu_uu<3>(9, 0, 0) == 1.0 && nu_uu<3>(9, 1, 1) == -0.5 && nu_uu<3>(13, 0, 1) == 0.5 &&
-                  nu_uf<3>(9, 0, 0) == 2.0 && nu_uf<3>(13, 0, 1) == 0.5 && nu_uu<2>(7, 0, 0) == 0.5,
-              "closed forms of the s_nu moments");
-static_assert(moments_have_parity<3>() && moments_have_parity<2>(), "MRT moments must have a parity");
-static_assert(npairs<3>() == 9 && pair_n<3>(8) > 0 && npairs<2>() == 4 && pair_n<2>(3) > 0, "direction pairs");
-
 }  // namespace tx

@@ -36,26 +36,6 @@
 
 namespace tx {
 
-// ------------------------------------------------------------ V2 arithmetic
-struct V2 {
-  float x, y;
-};
-__host__ __device__ __forceinline__ V2 v2(float a) { return V2{a, a}; }
-#if defined(__CUDA_ARCH__)
-__device__ __forceinline__ float2 f2_(V2 a) { return make_float2(a.x, a.y); }
-__device__ __forceinline__ V2 v2_(float2 a) { return V2{a.x, a.y}; }
-__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), f2_(b))); }
-__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return v2_(__fadd2_rn(f2_(a), make_float2(-b.x, -b.y))); }
-__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return v2_(__fmul2_rn(f2_(a), f2_(b))); }
-__device__ __forceinline__ V2 fma2(V2 a, V2 b, V2 c) { return v2_(__ffma2_rn(f2_(a), f2_(b), f2_(c))); }
-#else
-inline V2 operator+(V2 a, V2 b) { return V2{a.x + b.x, a.y + b.y}; }
-inline V2 operator-(V2 a, V2 b) { return V2{a.x - b.x, a.y - b.y}; }
-inline V2 operator*(V2 a, V2 b) { return V2{a.x * b.x, a.y * b.y}; }
-inline V2 fma2(V2 a, V2 b, V2 c) { return V2{__builtin_fmaf(a.x, b.x, c.x), __builtin_fmaf(a.y, b.y, c.y)}; }
-#endif
-__host__ __device__ __forceinline__ V2 operator-(V2 a) { return V2{-a.x, -a.y}; }
-
 // c_n . v over the nonzero components of c_n (no zero start: the first term seeds)
 template <int D, int n>
 __device__ __forceinline__ V2 cdot2(const V2 v[D]) {
@@ -202,6 +182,7 @@ __device__ __forceinline__ int pair_class(const StepArgs& a, const PhysT<float>&
                                           const PairSites& ps) {
   const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
   if (!p0 && !p1) return -1;
+  if (!ps.same_row()) return 0;  // spans a row end (odd nx): the per-site kernel
   const bool s0 = !p0 || pair_simple_site<D, ISO>(a, P, l0, ps.x0, ps.y0, ps.z0);
   const bool s1 = !p1 || pair_simple_site<D, ISO>(a, P, l1, ps.x1, ps.y1, ps.z1);
   return (s0 && s1) ? 1 : 0;
@@ -269,40 +250,10 @@ template <int D>
 struct VecD {
   V2 v[D];
 };
-// the s_nu moments of one component's pre-collision pair sums (nu_slot order)
-template <int D>
-struct VecNu {
-  V2 v[nnu<D>()];
-};
-
-// V2 form of nu_noneq (tx_kernels.cuh): the s_nu moment k of the pair sums
-// of the non-equilibrium part from the populations' moment sn_k
-template <int D, int k>
-__device__ __forceinline__ V2 nu_noneq2(V2 sn_k, V2 q, const V2 u[D], const V2 F[D]) {
-  V2 e{0.f, 0.f}, t{0.f, 0.f};
-  bool fe = true, ft = true;
-  sfor<0, D>([&](auto aa) {
-    constexpr int a = decltype(aa)::value;
-    sfor<0, D>([&](auto bb) {
-      constexpr int b = decltype(bb)::value;
-      constexpr double cu = nu_uu<D>(k, a, b), cf = nu_uf<D>(k, a, b);
-      if constexpr (cu != 0.0) {
-        e = fe ? v2(float(cu)) * (u[a] * u[b]) : fma2(v2(float(cu)), u[a] * u[b], e);
-        fe = false;
-      }
-      if constexpr (cf != 0.0) {
-        t = ft ? v2(float(cf)) * (u[a] * F[b]) : fma2(v2(float(cf)), u[a] * F[b], t);
-        ft = false;
-      }
-    });
-  });
-  return fma2(-q, e, sn_k) + t;
-}
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
 __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T, RCH> push,
                                                       const PhysT<float>& P, const T* fin, unsigned N, unsigned c0,
-                                                      int m, V2 r, V2 rd, VecD<D> Fm_, VecD<D> up_,
-                                                      VecNu<D> sn) {
+                                                      int m, V2 r, V2 rd, VecD<D> Fm_, VecD<D> up_) {
   using L = Lat<D>;
   constexpr int Q = L::Q;
   constexpr int NP = npairs<D>();
@@ -378,14 +329,40 @@ __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T
     } else if (spec == stress_mask<D>()) {
       // s_nu != s0, every other rate s0: pair sums of the non-equilibrium
       // part, the s_nu moments' corrections, then each pair relaxed
-      // the s_nu moments of the non-equilibrium pair sums in closed form from
-      // the moments pass's sn, and their corrections
-      const V2 q = fma2(v2(2.f), r, v2(3.f) * Fu);
+      V2 F3[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) F3[d] = v2(3.f) * F[m][d];
+      const V2 hFu2 = v2(3.f) * Fu;
+      const V2 inv = v2(std::is_same<T, __half>::value ? push.sc.inv : 1.f);
+      // the s_nu moments of the pair sums of the non-equilibrium part,
+      // S_p = g_n + g_n~ - 2 De - Ae (3 F.u) + Bo c_n.(3 F), accumulated pair by pair
       V2 ck[Q];
+      bool seen[Q] = {};
+      sfor<0, NP>([&](auto pp) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+        const V2 WA = n <= L::NAXIS ? WA1 : WA2;
+        const V2 Ae = WA + WBe[p];
+        const V2 t2 = cdot2<D, n>(F3);
+        const V2 gs = (pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{})) * inv;
+        const V2 De = fma2(WA, rd, fma2(WBe[p], r, n <= L::NAXIS ? cA1 : cA2));
+        const V2 Sp = fma2(Bo[p], t2, fma2(v2(-2.f), De, gs) - Ae * hFu2);
+        sfor<0, Q>([&](auto kk) {
+          constexpr int kq = decltype(kk)::value;
+          if constexpr (rate_of<D>(kq) == R_NU) {
+            constexpr int v = L::mt(n, kq);
+            if constexpr (v != 0) {
+              if (!seen[kq])
+                ck[kq] = v == 1 ? Sp : (v == -1 ? -Sp : v2(float(v)) * Sp);
+              else
+                ck[kq] = v == 1 ? ck[kq] + Sp : (v == -1 ? ck[kq] - Sp : fma2(v2(float(v)), Sp, ck[kq]));
+              seen[kq] = true;
+            }
+          }
+        });
+      });
       sfor<0, Q>([&](auto kk) {
         constexpr int kq = decltype(kk)::value;
-        if constexpr (rate_of<D>(kq) == R_NU)
-          ck[kq] = v2(P.dspec[m][kq]) * nu_noneq2<D, kq>(sn.v[nu_slot<D>(kq)], q, up, F[m]);
+        if constexpr (rate_of<D>(kq) == R_NU) ck[kq] = v2(P.dspec[m][kq]) * ck[kq];
       });
       const bool k0 = keepf == 0.f;
       push(std::integral_constant<int, 0>{}, m, k0 ? X0 : fma2(keep, pop(std::integral_constant<int, 0>{}), X0));
@@ -468,7 +445,7 @@ __device__ __forceinline__ void pair_collide_m(const PairPush<D, S, MRT, FULL, T
 template <int D, int S, bool MRT, bool FULL, class T, int RCH>
 __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, RCH>& push, const PhysT<float>& P,
                                              const T* fin, unsigned N, unsigned c0, const V2 rc[S], const V2 rcd[S],
-                                             const V2 F[S][D], const V2 up[D], const VecNu<D> sn[S]) {
+                                             const V2 F[S][D], const V2 up[D]) {
   VecD<D> u;
 #pragma unroll
   for (int d = 0; d < D; ++d) u.v[d] = up[d];
@@ -477,7 +454,7 @@ __device__ __forceinline__ void pair_collide(const PairPush<D, S, MRT, FULL, T, 
     VecD<D> f;
 #pragma unroll
     for (int d = 0; d < D; ++d) f.v[d] = F[m][d];
-    pair_collide_m<D, S, MRT, FULL, T, RCH>(push, P, fin, N, c0, m, rc[m], rcd[m], f, u, sn[m]);
+    pair_collide_m<D, S, MRT, FULL, T, RCH>(push, P, fin, N, c0, m, rc[m], rcd[m], f, u);
   }
 }
 
@@ -492,7 +469,8 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
   const unsigned N = (unsigned)a.g.n;
   const unsigned c0 = ps.c0;
   const bool p0 = (l0 & 1u) != 0u, p1 = (l1 & 1u) != 0u;
-  const Hood<D, RCH> h0(a.g, ps.x0, ps.y0, ps.z0), h1(a.g, ps.x1, ps.y1, ps.z1);
+  // the pair lies in one row (pair_class): x0 + 1, y0, z0
+  const Hood<D, RCH> h0(a.g, ps.x0, ps.y0, ps.z0), h1(a.g, ps.x0 + 1, ps.y0, ps.z0);
   const Scl<float> sc = scl_of(P);
   uint32_t seed0 = 0, seed1 = 0;
   if constexpr (std::is_same<T, __half>::value) {
@@ -540,7 +518,6 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
   // moments: flux of each component from pair differences, common velocity
   const T* fin = reinterpret_cast<const T*>(a.fin);
   V2 up[D];
-  VecNu<D> sn[S];  // s_nu moments of the pair sums (components with the s_nu-only rate pattern)
   {
     V2 num[D], den = v2(0.f);
 #pragma unroll
@@ -550,26 +527,9 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
       V2 j[D];
       bool seen[D] = {};
       const T* fm = fin + (size_t)m * Q * N + c0;
-      const bool stress = P.spec_mask[m] == stress_mask<D>();
-      bool nseen[nnu<D>()] = {};
       sfor<0, npairs<D>()>([&](auto pp) {
         constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
-        const V2 fa = ld_pair_raw<T>(fm + (size_t)n * N), fb = ld_pair_raw<T>(fm + (size_t)nb * N);
-        const V2 dlt = fa - fb;
-        if (stress) {
-          const V2 gs = fa + fb;
-          sfor<0, Q>([&](auto kk) {
-            constexpr int kq = decltype(kk)::value;
-            if constexpr (rate_of<D>(kq) == R_NU) {
-              constexpr int v = L::mt(n, kq), sl = nu_slot<D>(kq);
-              if constexpr (v != 0) {
-                const V2 t = v == 1 ? gs : (v == -1 ? -gs : v2(float(v)) * gs);
-                sn[m].v[sl] = nseen[sl] ? sn[m].v[sl] + t : t;
-                nseen[sl] = true;
-              }
-            }
-          });
-        }
+        const V2 dlt = ld_pair_raw<T>(fm + (size_t)n * N) - ld_pair_raw<T>(fm + (size_t)nb * N);
         sfor<0, D>([&](auto dd) {
           constexpr int d = decltype(dd)::value;
           constexpr int c = L::c(n, d);
@@ -585,9 +545,6 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
         const V2 inv = v2(sc.inv);
 #pragma unroll
         for (int d = 0; d < D; ++d) j[d] = j[d] * inv;
-        if (stress)
-#pragma unroll
-          for (int k = 0; k < nnu<D>(); ++k) sn[m].v[k] = sn[m].v[k] * inv;
       }
       const V2 mm = v2(P.mmot[m]);
 #pragma unroll
@@ -601,20 +558,20 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
   T* fout = reinterpret_cast<T*>(a.fout);
   if (warp_full) {
     const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
-    pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up, sn);
+    pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   } else {
     const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
-    pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up, sn);
+    pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   }
 }
 
-// Whether a pair goes the bounceback-free way (see PairPush): both sites pore
-// with every link pore, in one row of a lattice with an even nx (so that the
-// y and z neighbours' pair slots are aligned for one vector store).
+// Whether a pair of k_step_pair (one row) goes the bounceback-free way (see
+// PairPush): both sites pore with every link pore, on a lattice with an even
+// nx (so that the y and z neighbours' pair slots are aligned for one store).
 template <int D>
 __device__ __forceinline__ bool pair_full(const Geo& g, const PairSites& ps, uint32_t l0, uint32_t l1) {
   constexpr uint32_t all = all_links<D>() | 1u;
-  return (g.nx & 1) == 0 && ps.same_row() && (l0 & all) == all && (l1 & all) == all;
+  return (g.nx & 1) == 0 && (l0 & all) == all && (l1 & all) == all;
 }
 
 // k_step_pair / k_step_rest / k_count_rest: one thread per pair, 1-D grid.

@@ -26,7 +26,7 @@ from . import metrics
 from . import params as P
 from . import problems
 from . import serve
-from ._lib import Handle
+from ._lib import Batch, Handle
 
 
 def drainage_case(n, seed=1234):
@@ -145,19 +145,32 @@ def batch_permeability_study(n_lat=96, seed=4, tol=1e-7, max_steps=40000, chunk=
     permeability errors against the FP64 form's."""
     reqs = batch_lattices(n_lat, seed, tol=tol, max_steps=max_steps)
     sites = sum(r.params.nsites for r in reqs)
+    # tile shape and grid from the autotuner, on a batch of the same lattices
+    # that is then discarded (its trial steps would shift the probe chunks)
+    tiles = {}
+    for name, prec, _ in FORMS:
+        form = P.copy_params(reqs[0].params)
+        form.precision = prec
+        tb = Batch(form)
+        for r in reqs:
+            q = P.copy_params(r.params)
+            q.precision = prec
+            tb.add(q, r.walls, r.rho)
+        tiles[name] = tuple(tb.tune(2))
+        tb.close()
     out = {"case": "%d single-phase D3Q19 BGK periodic sphere packs, sides 48-192 per axis (%d sites), body force "
                    "1e-6, stop at a relative change of the mean flow < %g per %d-step chunk (cap %d steps)"
                    % (n_lat, sites, tol, chunk, max_steps), "forms": {}}
     perms = {}
     for name, prec, _ in FORMS:
-        srv = serve.Server(precision=prec, chunk=chunk, budget_bytes=200 << 30)
+        srv = serve.Server(precision=prec, chunk=chunk, budget_bytes=200 << 30, tiles=tiles[name])
         t = time.perf_counter()
         res = srv.run(reqs, realtime=False)
         span = time.perf_counter() - t
         srv.close()
         steps = {r.rid: r.steps for r in res}
         perms[name] = {r.rid: r.value for r in res}
-        out["forms"][name] = {"time_to_solution_s": round(span, 2),
+        out["forms"][name] = {"time_to_solution_s": round(span, 2), "tiles": list(tiles[name]),
                               "lattice_steps_mean": round(float(np.mean(list(steps.values()))), 1),
                               "lattice_steps_max": int(max(steps.values())),
                               "capped": int(sum(1 for v in steps.values() if v >= max_steps)),
