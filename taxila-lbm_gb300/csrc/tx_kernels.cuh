@@ -1576,14 +1576,13 @@ __device__ __forceinline__ void density_group(const StepArgs& a, long long c0, i
   if (!any) return;
   const T* fcur = reinterpret_cast<const T*>(a.fout);
   RT* rho = reinterpret_cast<RT*>(a.rho);
+  if constexpr (VEC && !std::is_same<T, double>::value) {
+    // FP32 arithmetic: the stored values of two cells per packed add, the FP16
+    // storage scale applied once to each sum; with two components and every
+    // site pore, each two sites' densities leave in one 16-byte store
+    float sum[S][VW];
 #pragma unroll
-  for (int m = 0; m < S; ++m) {
-    R acc[VW];
-#pragma unroll
-    for (int v = 0; v < VW; ++v) acc[v] = R(0);
-    if constexpr (VEC && !std::is_same<T, double>::value) {
-      // FP32 arithmetic: the stored values of two cells per packed add, the
-      // FP16 storage scale applied once to each sum
+    for (int m = 0; m < S; ++m) {
       V2 acc2[VW / 2];
 #pragma unroll
       for (int v = 0; v < VW / 2; ++v) acc2[v] = v2(0.f);
@@ -1608,10 +1607,38 @@ __device__ __forceinline__ void density_group(const StepArgs& a, long long c0, i
       const float inv = std::is_same<T, __half>::value ? float(P.inv_sscale) : 1.f;
 #pragma unroll
       for (int v = 0; v < VW / 2; ++v) {
-        acc[2 * v] = R(acc2[v].x * inv);
-        acc[2 * v + 1] = R(acc2[v].y * inv);
+        sum[m][2 * v] = acc2[v].x * inv;
+        sum[m][2 * v + 1] = acc2[v].y * inv;
       }
+    }
+    bool all = true;
+#pragma unroll
+    for (int v = 0; v < VW; ++v) all = all && pore[v];
+    if (S == 2 && all && !P.eos_on) {
+#pragma unroll
+      for (int v = 0; v < VW; v += 2)
+        *reinterpret_cast<float4*>(rho + (size_t)(c0 + v) * S) =
+            make_float4(sum[0][v], sum[S - 1][v], sum[0][v + 1], sum[S - 1][v + 1]);
     } else {
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        if (!pore[v]) continue;
+#pragma unroll
+        for (int m = 0; m < S; ++m) {
+          rho[(size_t)(c0 + v) * S + m] = RT(sum[m][v]);
+          if (P.eos_on)
+            reinterpret_cast<RT*>(a.psi)[(size_t)(c0 + v) * S + m] =
+                RT(eos_psi<R>(P.eos[m], P.eos_c[m], P.g[m][m], P.c0, P.rho0[m] + R(sum[m][v])));
+        }
+      }
+    }
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < S; ++m) {
+    R acc[VW];
+#pragma unroll
+    for (int v = 0; v < VW; ++v) acc[v] = R(0);
     sfor<0, Q>([&](auto nn) {
       constexpr int n = decltype(nn)::value;
       const T* src = fcur + (long long)(m * Q + n) * N + c0;
@@ -1627,7 +1654,6 @@ __device__ __forceinline__ void density_group(const StepArgs& a, long long c0, i
           if (v < cnt) acc[v] = acc[v] + from_dev<T, R>(__ldg(src + v), P);
       }
     });
-    }
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
       if (!pore[v]) continue;

@@ -56,6 +56,19 @@ __device__ __forceinline__ V2 cdot2(const V2 v[D]) {
 }
 
 // ---------------------------------------------------------- storage pairs
+// Whether k_step_pair prefetches the pair's population lines into L1 before
+// computing the forces.
+#ifndef TX_PAIR_PREFETCH
+#define TX_PAIR_PREFETCH 1
+#endif
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("prefetch.L1 [%0];" ::"l"(p));
+#else
+  (void)p;
+#endif
+}
+
 // Two floats to FP16, rounded toward zero, a in the low half (one cvt.rz.f16x2.f32).
 __device__ __forceinline__ uint32_t pack_half2_rz(float a, float b) {
 #if defined(__CUDA_ARCH__)
@@ -478,6 +491,15 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
     seed0 = mix32(c0 ^ st);
     seed1 = mix32((c0 + 1u) ^ st);
   }
+#if TX_PAIR_PREFETCH
+  // ask for the pair's population lines now, so that they arrive in L1 while
+  // the forces are computed (a hint: no register waits for it)
+  {
+    const T* fin0 = reinterpret_cast<const T*>(a.fin) + c0;
+#pragma unroll
+    for (int k = 0; k < S * Q; ++k) prefetch_l1(fin0 + (size_t)k * N);
+  }
+#endif
   // forcing density of both sites, then each site's forces (step_site's cell_forces)
   const float* rho = reinterpret_cast<const float*>(a.rho);
   float rfd0[S], rfd1[S], rf0[S], rf1[S];

@@ -31,6 +31,7 @@ struct alignas(8) uint2 {
   unsigned x, y;
 };
 inline float2 make_float2(float x, float y) { return float2{x, y}; }
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
 inline uint2 make_uint2(unsigned x, unsigned y) { return uint2{x, y}; }
 inline unsigned __activemask() { return 0xffffffffu; }
 inline bool __all_sync(unsigned, bool p) { return p; }

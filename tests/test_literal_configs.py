@@ -111,3 +111,34 @@ def test_served_drainage_values_stay_finite():
     p = r.params
     p.nspecies = 0
     assert first_nonfinite(p, r.walls, r.rho, 300, chunk=50) is None
+
+
+def test_specular_walls_leave_populations_in_wall_cells():
+    # Why the device rejects specular wall codes 900-902: in the reference's
+    # bounceback sweep (k-j-i order over the ghosted box, restated by the
+    # oracle) a specular wall moves a population along one axis only, possibly
+    # into a wall cell that the sweep has already cleared.  Those populations
+    # stay in wall cells, stream into pore cells on the next step and decide
+    # the result, so reproducing it needs every wall cell's populations and
+    # the sweep order; with ordinary walls alone, wall cells end every step empty.
+    rng = np.random.default_rng(0)
+    for codes, expect_left in (([1.0], False), ([1.0, 900.0, 901.0, 902.0], True)):
+        p = P.default_params()
+        p.discretization = P.D3Q19
+        p.nx, p.ny, p.nz = 14, 12, 10
+        p.ncomponents = 1
+        for f in range(6):
+            p.bc_flags[f] = P.BC_PERIODIC
+        p.body_forces = 1
+        p.gvt[0] = 1e-5
+        u = rng.random(p.nsites)
+        walls = np.where(u < 0.25, rng.choice(codes, size=p.nsites), 0.0)
+        o = Oracle(p)
+        o.set_walls(walls)
+        o.set_state(np.where(walls == 0, 1.0, 0.0))
+        o.init()
+        o.step(3)
+        fi = o.get(P.FIELD_FI).reshape(p.nsites, p.Q)
+        o.close()
+        left = np.abs(fi[walls > 0]).sum()
+        assert (left > 0.0) == expect_left, (codes, left)
