@@ -48,6 +48,10 @@ BYTES_PER_LUP_STEP = 2 * 19 * 2 * 8 + 1   # k_step: read + write 2x19 FP64 popul
 BYTES_PER_LUP_DENSITY = 19 * 2 * 8 + 2 * 8 + 1  # k_density: read populations, write rho, mask
 # steps of the host-core baseline on the GPU line (about 10 s of CPU work)
 CPU_BASELINE_STEPS = 40
+# lattices of the batched workload run to convergence, and requests of the
+# specification's serving mix, in the default run (each leg about a minute)
+CONVERGED_LATTICES = 8
+SPEC_REQUESTS = 16
 
 
 FORMS = {"f64": P.PREC_F64, "f32": P.PREC_F32, "f16": P.PREC_F32_F16}
@@ -691,7 +695,8 @@ def run_gpu(args):
         # keeps) holds the short per-form figures
         legs = (("batched", batched_run),
                 ("batched_small", lambda: batched_run(n_lat=192, steps=100, seed=5, sides=(16, 48))),
-                ("serving", serving_run),
+                ("batched_converged", lambda: batched_converged_run(n_lat=CONVERGED_LATTICES)),
+                ("serving_spec", lambda: serving_spec_run(n=SPEC_REQUESTS)),
                 ("bubble_2d", bubble_2d_run))
         for key, fn in legs:
             try:

@@ -628,7 +628,9 @@ __device__ __forceinline__ void ff_term(const Hood<D, RCH>& h, uint32_t links, c
 // BULK_ONLY: the caller guarantees that every stencil neighbour is pore
 // whenever the fluid-fluid force is on (the general wall-aware gradient is
 // then not compiled in).
-template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT, bool BULK_ONLY = false>
+// FF = false: fluid-solid and body forces only (the caller adds the
+// fluid-fluid force).
+template <int D, int S, int ISO, bool EXACT, int RCH, class R, class RT, bool BULK_ONLY = false, bool FF = true>
 __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t links, const PhysT<R>& P,
                                             const uint8_t* mask, const RT* rho, const RT* psi, long long N,
                                             const R rfd[S], const R rf[S], R F[S][D]) {
@@ -669,7 +671,7 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
 #pragma unroll
       for (int d = 0; d < D; ++d) F[m][d] = F[m][d] + R(P.gvt[d]) * R(P.mm[m]) * rf[m];
   }
-  if (!P.ff_on) return;
+  if (!FF || !P.ff_on) return;
   // the differentiated field, its value at x and the force's scale factor
   const RT* src = P.eos_on ? psi : rho;
   R selfv[S], mult[S];

@@ -210,6 +210,70 @@ __device__ __forceinline__ bool pair_of(const Geo& g, PairSites& ps) {
   return true;
 }
 
+// The value of field src (rho, or psi with the EOS on) at the two cells
+// (x0 + ex, x0 + 1 + ex) of row (ey, ez), per component.  With nx even, ex
+// even lands on an aligned pair of cells (one 16-byte load for two
+// components); ex odd takes each cell's own load.
+template <int D, int S, int RCH, int ex, int ey, int ez>
+__device__ __forceinline__ void field_pair(const Hood<D, RCH>& h0, const Hood<D, RCH>& h1, const float* src, V2 v[S]) {
+  const unsigned c = h0.template at<ex, ey, ez>();
+  if constexpr (S == 2 && (ex % 2 == 0)) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(src) + (c >> 1));
+    v[0] = V2{t.x, t.z};
+    v[1] = V2{t.y, t.w};
+  } else if constexpr (S == 2) {
+    const float2 a = __ldg(reinterpret_cast<const float2*>(src) + c);
+    const float2 b = __ldg(reinterpret_cast<const float2*>(src) + h1.template at<ex, ey, ez>());
+    v[0] = V2{a.x, b.x};
+    v[1] = V2{a.y, b.y};
+  } else {
+    const unsigned c1 = h1.template at<ex, ey, ez>();
+#pragma unroll
+    for (int m = 0; m < S; ++m) v[m] = V2{__ldg(src + (size_t)c * S + m), __ldg(src + (size_t)c1 * S + m)};
+  }
+}
+
+// The fluid-fluid force of both sites of a pair on a lattice with an even nx
+// whose pore sites see only pore stencil neighbours (cell_forces' bulk
+// gradient on V2 values): F -= psi(x) c0 sum_k g_mk grad_k, with
+// grad = sum over opposite stencil terms of w e (psi(x + e) - psi(x - e)).
+template <int D, int S, int ISO, int RCH>
+__device__ __forceinline__ void pair_ff_bulk(const Hood<D, RCH>& h0, const Hood<D, RCH>& h1, const PhysT<float>& P,
+                                             const float* src, const V2 mult[S], V2 F[S][D]) {
+  V2 gr[S][D];
+  bool seen[D] = {};
+  constexpr int NT = D == 3 ? FF_D3_COUNT : FF_D2_COUNT;
+  sfor<0, NT>([&](auto tt) {
+    constexpr int t = decltype(tt)::value;
+    constexpr FFTerm T = ffterm<D>(t);
+    if constexpr (T.level <= ISO && t < ff_opp<D>(t)) {
+      constexpr int ex = T.e[0], ey = T.e[1], ez = T.e[2], tw = T.w;
+      V2 vp[S], vm[S];
+      field_pair<D, S, RCH, ex, ey, ez>(h0, h1, src, vp);
+      field_pair<D, S, RCH, -ex, -ey, -ez>(h0, h1, src, vm);
+      sfor<0, D>([&](auto dd) {
+        constexpr int d = decltype(dd)::value;
+        constexpr int e = d == 0 ? ex : (d == 1 ? ey : ez);
+        if constexpr (e != 0) {
+          const V2 coef = v2(float(e) * P.ffwq[d][tw]);
+#pragma unroll
+          for (int m = 0; m < S; ++m) gr[m][d] = seen[d] ? fma2(coef, vp[m] - vm[m], gr[m][d]) : coef * (vp[m] - vm[m]);
+          seen[d] = true;
+        }
+      });
+    }
+  });
+#pragma unroll
+  for (int d = 0; d < D; ++d)
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      V2 acc = v2(P.c0g[m][0]) * gr[0][d];
+#pragma unroll
+      for (int k = 1; k < S; ++k) acc = fma2(v2(P.c0g[m][k]), gr[k][d], acc);
+      F[m][d] = F[m][d] - mult[m] * acc;
+    }
+}
+
 // Collision and push of one component of a simple pair.  FULL (pair_full):
 // both sites pore with every link pore (no bounceback), in one row of an
 // even-nx lattice, so the pushes need no selects; the caller takes FULL only
@@ -527,8 +591,16 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
 #pragma unroll
     for (int d = 0; d < D; ++d) F0[m][d] = F1[m][d] = 0.f;
   const float* psi = reinterpret_cast<const float*>(a.psi);
-  if (p0) cell_forces<D, S, ISO, false, RCH, float, float, true>(h0, l0, P, a.mask, rho, psi, a.g.n, rfd0, rf0, F0);
-  if (p1) cell_forces<D, S, ISO, false, RCH, float, float, true>(h1, l1, P, a.mask, rho, psi, a.g.n, rfd1, rf1, F1);
+  // with an even nx the fluid-fluid force of both sites comes from one pass
+  // over aligned cell pairs (pair_ff_bulk); otherwise each site's cell_forces
+  const bool pair_ff = (a.g.nx & 1) == 0;
+  if (pair_ff) {
+    if (p0) cell_forces<D, S, ISO, false, RCH, float, float, true, false>(h0, l0, P, a.mask, rho, psi, a.g.n, rfd0, rf0, F0);
+    if (p1) cell_forces<D, S, ISO, false, RCH, float, float, true, false>(h1, l1, P, a.mask, rho, psi, a.g.n, rfd1, rf1, F1);
+  } else {
+    if (p0) cell_forces<D, S, ISO, false, RCH, float, float, true>(h0, l0, P, a.mask, rho, psi, a.g.n, rfd0, rf0, F0);
+    if (p1) cell_forces<D, S, ISO, false, RCH, float, float, true>(h1, l1, P, a.mask, rho, psi, a.g.n, rfd1, rf1, F1);
+  }
   V2 F[S][D], rc[S], rcd[S];
 #pragma unroll
   for (int m = 0; m < S; ++m) {
@@ -536,6 +608,20 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
     rcd[m] = V2{rfd0[m], rfd1[m]};
 #pragma unroll
     for (int d = 0; d < D; ++d) F[m][d] = V2{F0[m][d], F1[m][d]};
+  }
+  if (pair_ff && P.ff_on) {
+    // psi(x) (EOS on) or rho(x) scales the force; wall lanes are discarded
+    V2 mult[S];
+    if (P.eos_on) {
+      V2 self[S];
+      field_pair<D, S, RCH, 0, 0, 0>(h0, h1, psi, self);
+#pragma unroll
+      for (int m = 0; m < S; ++m) mult[m] = self[m];
+    } else {
+#pragma unroll
+      for (int m = 0; m < S; ++m) mult[m] = rc[m];
+    }
+    pair_ff_bulk<D, S, ISO, RCH>(h0, h1, P, P.eos_on ? psi : rho, mult, F);
   }
   // moments: flux of each component from pair differences, common velocity
   const T* fin = reinterpret_cast<const T*>(a.fin);
