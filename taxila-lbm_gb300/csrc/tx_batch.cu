@@ -267,7 +267,7 @@ int rebuild_tables(tx_batch* b) {
         for (int x = 0; x < L->g.nx; x += b->bx) tiles.push_back(make_int4((int)s, x, y, z));
     d.tile_count = (int)tiles.size() - d.tile_begin;
     if (L->paired) {
-      for (long long i0 = 0; 2 * i0 < L->g.n; i0 += 128) {
+      for (long long i0 = 0; 2 * i0 < L->g.n; i0 += 128 * kPairTileRuns) {
         ptiles.push_back(make_int4((int)s, (int)i0, 0, 0));
         if (L->rest != 0) rtiles.push_back(make_int4((int)s, (int)i0, 0, 0));
       }

@@ -64,7 +64,7 @@ struct BatchArgs {
   const int4* otiles; // outlet refresh: (lattice slot, face, first node, 0) of runs of 128 nodes
   const int* notiles;
   // the step: per-site tiles of the lattices without the paired kernel; pair
-  // tiles (lattice slot, first pair: runs of 128 pairs) of those with it, and
+  // tiles (lattice slot, first pair: kPairTileRuns runs of 128 pairs) of those with it, and
   // the pair tiles of the lattices that have pairs for the per-site kernel
   const int4* stiles;
   const int* nstiles;
@@ -94,8 +94,11 @@ __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, R, MRT)) k_step_til
   }
 }
 
-// The paired step of k_step_pair over the pair tiles: runs of 128 pairs
-// (lattice slot, first pair) of the lattices with an even site count.
+// The paired step of k_step_pair over the pair tiles: runs of
+// kPairTileRuns x 128 pairs (lattice slot, first pair) of the lattices with an
+// even site count; a thread takes one pair of each run of 128, so the
+// lattice's arguments are read once per kPairTileRuns pairs.
+constexpr int kPairTileRuns = 4;
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair_tiles(BatchArgs b, int flip) {
   const int nt = __ldg(b.nptiles);
@@ -104,19 +107,21 @@ __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair_tiles(
     const int4 tl = __ldg(b.ptiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-    const unsigned i = (unsigned)tl.y + (unsigned)lane;
-    bool run = false, full = false;
-    uint2 ll = make_uint2(0u, 0u);
-    PairSites ps{};
-    if ((long long)2 * i < a.g.n) {
-      ps = pair_sites(a.g, i);
-      ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
-      run = pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 1;
-      full = pair_full<D>(a.g, ps, ll.x, ll.y);
+    for (int r = 0; r < kPairTileRuns; ++r) {
+      const unsigned i = (unsigned)tl.y + (unsigned)(128 * r + lane);
+      bool run = false, full = false;
+      uint2 ll = make_uint2(0u, 0u);
+      PairSites ps{};
+      if ((long long)2 * i < a.g.n) {
+        ps = pair_sites(a.g, i);
+        ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
+        run = pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 1;
+        full = pair_full<D>(a.g, ps, ll.x, ll.y);
+      }
+      // every lane votes, so that the vote is uniform over the warp's running lanes
+      const bool warp_full = __all_sync(0xffffffffu, full || !run);
+      if (run) step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
     }
-    // every lane votes, so that the vote is uniform over the warp's running lanes
-    const bool warp_full = __all_sync(0xffffffffu, full || !run);
-    if (run) step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
   }
 }
 
@@ -129,13 +134,15 @@ __global__ void __launch_bounds__(128, TX_STEP_MIN_BLOCKS(S, float, MRT)) k_step
     const int4 tl = __ldg(b.rtiles + t);
     const StepArgs a = flipped(b.lats[tl.x].a, flip);
     const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-    const unsigned i = (unsigned)tl.y + (unsigned)lane;
-    if ((long long)2 * i < a.g.n) {
-      const PairSites ps = pair_sites(a.g, i);
-      const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
-      if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 0) {
-        step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x0, ps.y0, ps.z0);
-        step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x1, ps.y1, ps.z1);
+    for (int r = 0; r < kPairTileRuns; ++r) {
+      const unsigned i = (unsigned)tl.y + (unsigned)(128 * r + lane);
+      if ((long long)2 * i < a.g.n) {
+        const PairSites ps = pair_sites(a.g, i);
+        const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
+        if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 0) {
+          step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x0, ps.y0, ps.z0);
+          step_site<D, S, ISO, MRT, false, T, float, float>(a, ps.x1, ps.y1, ps.z1);
+        }
       }
     }
   }

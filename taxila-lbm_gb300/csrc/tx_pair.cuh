@@ -287,15 +287,22 @@ struct PairPush {
   uint32_t l0, l1;
   bool p0, p1;
   Hood<D, RCH> h0, h1;
-  uint32_t seed0, seed1;
+  uint32_t seed0;  // the pair's stochastic-rounding seed (FP16)
   Scl<float> sc;
 
   template <int n>
   __device__ __forceinline__ void operator()(std::integral_constant<int, n>, int m, V2 v) const {
     constexpr int o = opp<D>(n);
     const uint32_t k = (uint32_t)(m * Q + n);
-    const uint32_t d0 = std::is_same<T, __half>::value ? sr_dither(seed0, k) : 0u;
-    const uint32_t d1 = std::is_same<T, __half>::value ? sr_dither(seed1, k) : 0u;
+    // FP16: both sites' 13-bit dithers from one multiply-shift product of the
+    // pair's seed (bits 31..19 and 18..6; both fields of the product of a
+    // uniform seed and an odd multiplier are uniform, so each rounding stays unbiased)
+    uint32_t d0 = 0u, d1 = 0u;
+    if constexpr (std::is_same<T, __half>::value) {
+      const uint32_t prod = seed0 * (mix32(k + 1u) | 1u);
+      d0 = prod >> 19;
+      d1 = (prod >> 6) & 0x1fffu;
+    }
     T* const sn = fout + (size_t)k * N;
     if constexpr (n == 0) {
       if (FULL || (p0 && p1)) {
@@ -549,11 +556,10 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
   // the pair lies in one row (pair_class): x0 + 1, y0, z0
   const Hood<D, RCH> h0(a.g, ps.x0, ps.y0, ps.z0), h1(a.g, ps.x0 + 1, ps.y0, ps.z0);
   const Scl<float> sc = scl_of(P);
-  uint32_t seed0 = 0, seed1 = 0;
+  uint32_t seed0 = 0;
   if constexpr (std::is_same<T, __half>::value) {
     const uint32_t st = 0x9E3779B9u * ((a.steps_ptr ? __ldg(a.steps_ptr) : a.step) + 1u);
-    seed0 = mix32(c0 ^ st);
-    seed1 = mix32((c0 + 1u) ^ st);
+    seed0 = mix32(c0 ^ st);  // one seed per pair (PairPush draws both sites' dithers from it)
   }
 #if TX_PAIR_PREFETCH
   // ask for the pair's population lines now, so that they arrive in L1 while
@@ -665,10 +671,10 @@ __device__ __forceinline__ void step_pair(const StepArgs& a, const PairSites& ps
   }
   T* fout = reinterpret_cast<T*>(a.fout);
   if (warp_full) {
-    const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
+    const PairPush<D, S, MRT, true, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, sc};
     pair_collide<D, S, MRT, true, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   } else {
-    const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, seed1, sc};
+    const PairPush<D, S, MRT, false, T, RCH> push{fout, N, c0, l0, l1, p0, p1, h0, h1, seed0, sc};
     pair_collide<D, S, MRT, false, T, RCH>(push, P, fin, N, c0, rc, rcd, F, up);
   }
 }
