@@ -264,9 +264,10 @@ __device__ __forceinline__ void st_dev(T* p, R v, const PhysT<R>& P) {
     St<T>::st(p, v);
 }
 
-// Correctly rounded reciprocal (the fast forms' 1/x): the hardware reciprocal
-// refined to round-to-nearest, without the general division's special-case path.
-__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+// The fast forms' 1/x: in FP32 the correctly rounded reciprocal (no general
+// division path); in FP64 the division 1/x, which measured fewer FP64
+// instructions per site than __drcp_rn (412 against 427) in k_step.
+__device__ __forceinline__ double rcp_rn(double x) { return 1.0 / x; }
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 
 // The FP16 storage scale and its inverse, read from the parameter block once

@@ -39,8 +39,11 @@ def gpu_after(q, walls, rho, steps):
 
 
 @pytest.mark.parametrize("prec,scale", [(P.PREC_F32, 1.0), (P.PREC_F32_F16, 4096.0)], ids=["f32", "f32_f16"])
-def test_permeability_reduced_precision(prec, scale):
-    p, walls, rho = cases.permeability_case((20, 18, 24), seed=9)
+@pytest.mark.parametrize("shape", [(20, 18, 24), (20, 18, 23), (19, 17, 23)], ids=["even_nx", "odd_nx", "odd_sites"])
+def test_permeability_reduced_precision(prec, scale, shape):
+    # even nx: the paired step everywhere; odd nx: pairs that span a row end
+    # take the per-site kernel; an odd site count: the per-site kernel alone
+    p, walls, rho = cases.permeability_case(shape, seed=9)
     steps = 300
     o = oracle_after(p, walls, rho, steps)
     q = P.copy_params(p)
@@ -61,8 +64,10 @@ def test_permeability_reduced_precision(prec, scale):
 
 
 @pytest.mark.parametrize("prec,tol", [(P.PREC_F32, 2e-5), (P.PREC_F32_F16, 2e-3)], ids=["f32", "f32_f16"])
-def test_bubble_reduced_precision(prec, tol):
-    p, walls, rho = cases.sc_bubble(P.D3Q19, (24, 24, 24), P.MRT, 4, g=0.15, r=6)
+@pytest.mark.parametrize("shape,nu_only", [((24, 24, 24), False), ((24, 24, 23), True)],
+                         ids=["mixed_rates", "odd_nx_s_nu_only"])
+def test_bubble_reduced_precision(prec, tol, shape, nu_only):
+    p, walls, rho = cases.sc_bubble(P.D3Q19, shape, P.MRT, 4, g=0.15, r=6, nu_only=nu_only)
     steps = 200
     o = oracle_after(p, walls, rho, steps)
     q = P.copy_params(p)
@@ -73,3 +78,8 @@ def test_bubble_reduced_precision(prec, tol):
     R_ref = metrics.equivalent_radius(r_ref, 2, 0, 0.06, 2.0, 3)
     R_gpu = metrics.equivalent_radius(r_gpu, 2, 0, 0.06, 2.0, 3)
     assert abs(R_gpu / R_ref - 1.0) < 1e-3, (R_gpu, R_ref)
+    # the same lattice in a batch of that form evolves identically
+    b = Batch(q)
+    lid = b.add(q, walls, rho)
+    b.step(steps)
+    assert np.array_equal(b.download(lid, P.FIELD_FI, p.nsites * 2 * 19), h.download(P.FIELD_FI))
