@@ -3,8 +3,9 @@
 // operations.  They give the measured compute ceiling that the FP64 step
 // kernels are held against (the HBM ceiling is a measured copy bandwidth).
 //
-// Each thread runs CHAINS independent dependency chains of one operation for
-// `iters` iterations; `blocks` x 256 threads cover the GPU.  The result is
+// Each thread runs CHAINS (16) independent dependency chains of one operation
+// for `iters` iterations (unrolled four times, so that loop bookkeeping is a
+// small share of the issued instructions); `blocks` x 256 threads cover the GPU.  The result is
 // written out so that nothing is optimised away.  Timed with CUDA events on
 // a private stream; the caller samples the SM clock.
 #include <cuda_runtime.h>
@@ -13,7 +14,7 @@
 
 namespace {
 
-constexpr int CHAINS = 8;
+constexpr int CHAINS = 16;
 
 enum : int { OP_DFMA = 0, OP_DADD = 1, OP_DMUL = 2, OP_FFMA = 3, OP_FFMA2 = 4 };
 
@@ -24,6 +25,7 @@ __global__ void __launch_bounds__(256) k_pipe(int iters, double b, double c, dou
     double a[CHAINS];
 #pragma unroll
     for (int k = 0; k < CHAINS; ++k) a[k] = 1.0 + 1e-9 * (tid + k);
+#pragma unroll 4
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
       for (int k = 0; k < CHAINS; ++k) {
@@ -41,6 +43,7 @@ __global__ void __launch_bounds__(256) k_pipe(int iters, double b, double c, dou
     const float bf = (float)b, cf = (float)c;
 #pragma unroll
     for (int k = 0; k < CHAINS; ++k) a[k] = 1.0f + 1e-6f * (float)(tid + k);
+#pragma unroll 4
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
       for (int k = 0; k < CHAINS; ++k) a[k] = fmaf(a[k], bf, cf);
@@ -55,6 +58,7 @@ __global__ void __launch_bounds__(256) k_pipe(int iters, double b, double c, dou
     const float2 bf = make_float2((float)b, (float)b), cf = make_float2((float)c, (float)c);
 #pragma unroll
     for (int k = 0; k < CHAINS; ++k) a[k] = make_float2(1.0f + 1e-6f * (float)(tid + k), 1.0f - 1e-6f * (float)k);
+#pragma unroll 4
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
       for (int k = 0; k < CHAINS; ++k) a[k] = __ffma2_rn(a[k], bf, cf);
