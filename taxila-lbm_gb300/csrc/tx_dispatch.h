@@ -78,11 +78,11 @@ struct Launch3 {
   dim3 grid, block;
 };
 inline Launch3 launch3(const Geo& g, int threads);
-// the launch of the paired kernels: one thread per pair, one-dimensional
-inline Launch3 launch_pairs(const Geo& g, int threads) {
+// the launch of the paired kernels: one-dimensional, `per` pairs per thread
+inline Launch3 launch_pairs(const Geo& g, int threads, int per = 1) {
   Launch3 l;
   l.block = dim3((unsigned)threads, 1, 1);
-  l.grid = dim3(grid_for(g.n / 2, threads), 1, 1);
+  l.grid = dim3(grid_for(g.n / 2, threads * per), 1, 1);
   return l;
 }
 inline Launch3 launch3(const Geo& g, int threads) {
@@ -108,8 +108,8 @@ inline Launch3 launch3(const Geo& g, int threads) {
     static void step(const StepArgs& a, cudaStream_t s) {                                                     \
       if constexpr (kPairForm) {                                                                              \
         if (paired(a.g)) {                                                                                    \
-          const Launch3 l = launch_pairs(a.g, 128);                                                           \
-          k_step_pair<D, S, ISO, MRT, T><<<l.grid, l.block, 0, s>>>(a);                                       \
+          const Launch3 lp = launch_pairs(a.g, 128, TX_PAIR_PER_THREAD), l = launch_pairs(a.g, 128);         \
+          k_step_pair<D, S, ISO, MRT, T><<<lp.grid, lp.block, 0, s>>>(a);                                     \
           if (a.rest != 0) k_step_rest<D, S, ISO, MRT, T><<<l.grid, l.block, 0, s>>>(a);                      \
           return;                                                                                             \
         }                                                                                                     \

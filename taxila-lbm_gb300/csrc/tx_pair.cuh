@@ -61,6 +61,10 @@ __device__ __forceinline__ V2 cdot2(const V2 v[D]) {
 #ifndef TX_PAIR_PREFETCH
 #define TX_PAIR_PREFETCH 1
 #endif
+// Pairs per thread of k_step_pair (its grid covers the pairs this many times over).
+#ifndef TX_PAIR_PER_THREAD
+#define TX_PAIR_PER_THREAD 2
+#endif
 __device__ __forceinline__ void prefetch_l1(const void* p) {
 #if defined(__CUDA_ARCH__)
   asm volatile("prefetch.L1 [%0];" ::"l"(p));
@@ -689,16 +693,36 @@ __device__ __forceinline__ bool pair_full(const Geo& g, const PairSites& ps, uin
 }
 
 // k_step_pair / k_step_rest / k_count_rest: one thread per pair, 1-D grid.
+// k_step_pair: each thread takes TX_PAIR_PER_THREAD pairs, one grid apart,
+// and asks for the next one's population lines before updating the current
+// one, so that the next pair's loads are in flight while this one computes.
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair(StepArgs a_in) {
   const StepArgs a = a_in;
-  PairSites ps;
-  if (!pair_of(a.g, ps)) return;
-  const uint2 ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
   const PhysT<float>& P = *reinterpret_cast<const PhysT<float>*>(a.phys);
-  if (pair_class<D, ISO>(a, P, ll.x, ll.y, ps) != 1) return;
-  const bool warp_full = __all_sync(__activemask(), pair_full<D>(a.g, ps, ll.x, ll.y));
-  step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
+  const unsigned stride = gridDim.x * blockDim.x;
+  const unsigned npairs = (unsigned)(a.g.n / 2);
+  constexpr int Q = Lat<D>::Q;
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int r = 0; r < TX_PAIR_PER_THREAD; ++r, i += stride) {
+    if (r + 1 < TX_PAIR_PER_THREAD && i + stride < npairs) {
+      const T* nxt = reinterpret_cast<const T*>(a.fin) + 2u * (i + stride);
+#pragma unroll
+      for (int k = 0; k < S * Q; ++k) prefetch_l1(nxt + (size_t)k * (size_t)a.g.n);
+    }
+    bool run = false, full = false;
+    uint2 ll = make_uint2(0u, 0u);
+    PairSites ps{};
+    if (i < npairs) {
+      ps = pair_sites(a.g, i);
+      ll = __ldg(reinterpret_cast<const uint2*>(a.links) + (ps.c0 >> 1));
+      run = pair_class<D, ISO>(a, P, ll.x, ll.y, ps) == 1;
+      full = pair_full<D>(a.g, ps, ll.x, ll.y);
+    }
+    // every lane votes, so that the vote is uniform over the warp's running lanes
+    const bool warp_full = __all_sync(0xffffffffu, full || !run);
+    if (run) step_pair<D, S, ISO, MRT, T>(a, ps, ll.x, ll.y, warp_full);
+  }
 }
 
 template <int D, int S, int ISO, bool MRT, class T>

@@ -205,7 +205,7 @@ std::string run(const Case& c, Result& out) {
           });
     if (paired) {
       // the library's paired step: k_step_pair, then k_step_rest when pairs need it
-      launch1(N / 2, 128, [&] { k_step_pair<D, S, ISO, MRT, T>(a); });
+      launch1((N / 2 + TX_PAIR_PER_THREAD - 1) / TX_PAIR_PER_THREAD, 128, [&] { k_step_pair<D, S, ISO, MRT, T>(a); });
       if (a.rest != 0) launch1(N / 2, 128, [&] { k_step_rest<D, S, ISO, MRT, T>(a); });
     } else {
       launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
