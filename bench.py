@@ -263,8 +263,13 @@ def measure_form(precision, steps, warmup, p=None):
     return res
 
 
-def e2e_run(steps, warmup):
-    """Through the C ABI with host buffers: upload, init, per-step host norm, final download."""
+def e2e_run(steps, warmup, repeats=5):
+    """Through the C ABI with host buffers: upload, init, per-step host norm, final download.
+
+    The timed region is taken ``repeats`` times on one handle; the value is the
+    median, with the spread and the median split into upload+init, steps and
+    download (each part closed by a stream synchronize, so the split adds up to
+    a little more than the unsplit region)."""
     import torch
     from taxila._lib import Handle
     p = workload_params()
@@ -278,22 +283,47 @@ def e2e_run(steps, warmup):
     h.init()
     h.step(warmup)
     h.delta_norm(P.FIELD_RHO)
+    h.download(P.FIELD_FI, fi_out)
     h.sync()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    h.upload_walls(walls_pinned)
-    h.upload_state(rho_pinned)
-    h.init()
-    for _ in range(steps):
-        h.step(1)
-        h.delta_norm(P.FIELD_RHO)
-    h.download(P.FIELD_FI, fi_out)
-    dt = time.perf_counter() - t0
+    whole, parts = [], []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        h.upload_walls(walls_pinned)
+        h.upload_state(rho_pinned)
+        h.init()
+        for _ in range(steps):
+            h.step(1)
+            h.delta_norm(P.FIELD_RHO)
+        h.download(P.FIELD_FI, fi_out)
+        whole.append(time.perf_counter() - t0)
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        h.upload_walls(walls_pinned)
+        h.upload_state(rho_pinned)
+        h.init()
+        h.sync()
+        t1 = time.perf_counter()
+        for _ in range(steps):
+            h.step(1)
+            h.delta_norm(P.FIELD_RHO)
+        h.sync()
+        t2 = time.perf_counter()
+        h.download(P.FIELD_FI, fi_out)
+        t3 = time.perf_counter()
+        parts.append((t1 - t0, t2 - t1, t3 - t2))
     h.close()
+    dt = statistics.median(whole)
+    split = [statistics.median(x[i] for x in parts) * 1e3 for i in range(3)]
     h2d = walls.nbytes + rho.nbytes
     d2h = 8 * steps + fi_out.nbytes
+    mlups = [p.nsites * steps / t / 1e6 for t in whole]
     return {"value": p.nsites * steps / dt / 1e6, "unit": UNIT,
-            "h2d_bytes_per_step": int(round(h2d / steps)), "d2h_bytes_per_step": int(round(d2h / steps))}
+            "h2d_bytes_per_step": int(round(h2d / steps)), "d2h_bytes_per_step": int(round(d2h / steps)),
+            "repeats": repeats, "min": round(min(mlups), 1), "max": round(max(mlups), 1),
+            "ms_upload_init": round(split[0], 3), "ms_steps": round(split[1], 3),
+            "ms_download": round(split[2], 3),
+            "download_gbs": round(fi_out.nbytes / split[2] / 1e6, 1)}
 
 
 def traffic_from_profile():

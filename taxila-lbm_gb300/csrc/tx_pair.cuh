@@ -61,9 +61,12 @@ __device__ __forceinline__ V2 cdot2(const V2 v[D]) {
 #ifndef TX_PAIR_PREFETCH
 #define TX_PAIR_PREFETCH 1
 #endif
-// Pairs per thread of k_step_pair (its grid covers the pairs this many times over).
+// Pairs per thread of k_step_pair (its grid covers the pairs this many times
+// over).  One is fastest on GB300: at 128^3 two pairs per thread with the next
+// pair's lines prefetched took 0.140 ms (FP16 storage) and 0.157 ms (FP32)
+// against 0.129 and 0.141 ms, and four pairs 0.149 and 0.172 ms.
 #ifndef TX_PAIR_PER_THREAD
-#define TX_PAIR_PER_THREAD 2
+#define TX_PAIR_PER_THREAD 1
 #endif
 __device__ __forceinline__ void prefetch_l1(const void* p) {
 #if defined(__CUDA_ARCH__)
@@ -693,9 +696,9 @@ __device__ __forceinline__ bool pair_full(const Geo& g, const PairSites& ps, uin
 }
 
 // k_step_pair / k_step_rest / k_count_rest: one thread per pair, 1-D grid.
-// k_step_pair: each thread takes TX_PAIR_PER_THREAD pairs, one grid apart,
-// and asks for the next one's population lines before updating the current
-// one, so that the next pair's loads are in flight while this one computes.
+// k_step_pair: each thread takes TX_PAIR_PER_THREAD pairs, one grid apart;
+// with more than one it asks for the next pair's population lines before
+// updating the current one.
 template <int D, int S, int ISO, bool MRT, class T>
 __global__ void __launch_bounds__(128, TX_PAIR_MIN_BLOCKS(S)) k_step_pair(StepArgs a_in) {
   const StepArgs a = a_in;
