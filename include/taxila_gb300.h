@@ -177,7 +177,14 @@ const char* tx_last_error(const tx_handle* h);
 /* WallsSetValues (src/lbm/lbm_walls.F90:151-177): natural-order wall codes,
  * NX*NY*NZ doubles.  0 = pore, 1..nminerals = mineral, other positive values
  * (e.g. 800, 999) = plain wall.  Ghost walls on non-periodic faces are added
- * by the library (WallsSetGhostNodes, lbm_walls.F90:179-231). */
+ * by the library (WallsSetGhostNodes, lbm_walls.F90:179-231).  The specular
+ * codes 900/901/902 (WALL_NORMAL_X/Y/Z, lbm_definitions.h; 902 is a plain
+ * wall in 2D) reflect as DistributionBounceback does
+ * (lbm_distribution_function.F90:668-784): their routes are resolved on the
+ * host at upload, and wall cells then hold populations, which tx_upload_fi,
+ * tx_download, tx_delta_norm and tx_conservation include.  They need the FP64
+ * forms and no species (TX_ERR_ARG otherwise); batches and tx_step_static
+ * refuse them.  A refused upload leaves the handle's walls unchanged. */
 int tx_upload_walls(tx_handle* h, const double* walls);
 
 /* The initialize_state plugin's output (src/lbm/lbm.F90:444-453): rho

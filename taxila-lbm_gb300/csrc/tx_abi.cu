@@ -10,6 +10,7 @@
 
 #include "../../include/taxila_gb300.h"
 #include "tx_dispatch.h"
+#include "tx_specular.cuh"
 
 using namespace tx;
 
@@ -48,6 +49,15 @@ struct tx_handle {
   unsigned long long* red = nullptr;  // [0] max bits, [1] non-finite count
   double* cons = nullptr;     // conservation-sum partials and per-population totals (first tx_conservation)
   std::vector<uint8_t> host_mask;
+  // specular walls (codes 900-902, FP64 forms): exceptions to the ordinary push
+  // (tx_specular.cuh), resolved at wall upload; wall cells then hold populations
+  bool spec = false;
+  std::vector<double> spec_walls;  // the uploaded wall values, for re-resolving at tx_upload_fi
+  long long spec_n = 0;
+  long long* spec_dst = nullptr;
+  long long* spec_src = nullptr;
+  double* spec_tmp = nullptr;
+  int spec_fresh = 0;              // steps whose output buffer still needs its wall slots cleared
   // passive species (transport): populations, parameters, initial state
   int NS = 0;
   SpeciesSet ss{};
@@ -86,6 +96,66 @@ int check_launch(tx_handle* h, const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(h, TX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
   return TX_OK;
+}
+
+// The wall mask the natural-order conversions zero wall cells with; with
+// specular walls wall cells hold populations, which pass through.
+const uint8_t* pop_mask(const tx_handle* h) { return h->spec ? nullptr : h->mask; }
+
+void free_spec(tx_handle* h) {
+  cudaFree(h->spec_dst);
+  cudaFree(h->spec_src);
+  cudaFree(h->spec_tmp);
+  h->spec_dst = h->spec_src = nullptr;
+  h->spec_tmp = nullptr;
+  h->spec_n = 0;
+}
+
+// Resolves the specular-wall routes of the uploaded walls (init_nz: wall slots
+// with non-zero initial content) and puts the exception list on the device.
+int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
+  SpecRoutes r;
+  const int n[3] = {h->g.nx, h->g.ny, h->g.nz};
+  bool pre[6];
+  for (int f = 0; f < 6; ++f) pre[f] = face_has_values(h->p, h->D, f);
+  const std::string why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, pre, init_nz, &r);
+  if (!why.empty()) return fail(h, TX_ERR_ARG, why);
+  free_spec(h);
+  const long long ne = (long long)r.dst.size();
+  if (ne > 0) {
+    long long *d = nullptr, *s = nullptr;
+    double* t = nullptr;
+    TX_CUDA(h, cudaMalloc(&d, (size_t)ne * sizeof(long long)));
+    h->spec_dst = d;
+    TX_CUDA(h, cudaMalloc(&s, (size_t)ne * sizeof(long long)));
+    h->spec_src = s;
+    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * h->S * sizeof(double)));
+    h->spec_tmp = t;
+    TX_CUDA(h, cudaMemcpy(h->spec_dst, r.dst.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
+    TX_CUDA(h, cudaMemcpy(h->spec_src, r.src.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
+  }
+  h->spec_n = ne;
+  return TX_OK;
+}
+
+// After the step kernels (push with ordinary bounceback), before the density
+// pass: the specular-wall exceptions.  The output buffer's wall slots are
+// cleared on the first two steps after an upload or init, so that wall slots
+// no exception writes hold zero in both state buffers.
+void spec_pass(tx_handle* h, int in, int out) {
+  double* fo = static_cast<double*>(h->f[out]);
+  const long long N = h->g.n;
+  if (h->spec_fresh > 0) {
+    k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, h->S * h->Q);
+    --h->spec_fresh;
+  }
+  const long long ne = h->spec_n;
+  if (ne == 0) return;
+  const unsigned grid = (unsigned)((ne + 255) / 256);
+  const long long QN = (long long)h->Q * N;
+  k_spec_gather<double><<<grid, 256, 0, h->stream>>>(static_cast<const double*>(h->f[in]), fo, h->spec_src, ne, h->S, QN,
+                                                     h->spec_tmp);
+  k_spec_scatter<double><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, h->S, QN, h->spec_tmp);
 }
 
 // link masks from the device wall mask (after every change of the mask)
@@ -234,7 +304,7 @@ int stage_field(tx_handle* h, int field) {
   if (field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) {
     h->ss.fields(species_args(h, h->gcur, h->gcur), field, h->stage, h->stream);
   } else if (field == TX_FIELD_FI) {
-    h->ks.to_natural(h->f[h->cur], h->mask, N, shift_of(h->ph), h->stage, h->stream);
+    h->ks.to_natural(h->f[h->cur], pop_mask(h), N, shift_of(h->ph), h->stage, h->stream);
   } else if (field == TX_FIELD_WALLS) {
     return TX_ERR_ARG;
   } else {
@@ -432,6 +502,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->uic);
   cudaFree(h->red);
   cudaFree(h->cons);
+  free_spec(h);
   cudaFree(h->d_phys);
   cudaFree(h->d_phys32);
   for (int f = 0; f < 6; ++f) cudaFree(h->faceval[f]);
@@ -445,10 +516,32 @@ int tx_destroy(tx_handle* h) {
 int tx_upload_walls(tx_handle* h, const double* walls) {
   if (!h || !walls) return TX_ERR_ARG;
   const long long N = h->g.n;
+  bool spec = false;
+  for (long long i = 0; i < N; ++i) spec = spec || specular_axis(walls[i], h->D) >= 0;
+  if (spec && h->p.precision != TX_PREC_F64)
+    return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 need the FP64 forms (precision TX_PREC_F64)");
+  if (spec && h->NS > 0)
+    return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 are not supported with species transport");
+  std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
-    if (!wall_code(walls[i], h->p.nminerals, &h->host_mask[(size_t)i], &why)) return fail(h, TX_ERR_ARG, why);
+    if (!wall_code(walls[i], h->p.nminerals, &mask[(size_t)i], &why, spec)) return fail(h, TX_ERR_ARG, why);
   }
+  if (spec) {
+    std::vector<double> prev(walls, walls + N);
+    h->spec_walls.swap(prev);
+    const int rc = upload_spec_routes(h, nullptr);
+    if (rc != TX_OK) {
+      h->spec_walls.swap(prev);  // a refused geometry leaves the handle as it was
+      return rc;
+    }
+  } else {
+    free_spec(h);
+    h->spec_walls.clear();
+  }
+  h->spec = spec;
+  h->spec_fresh = 2;
+  h->host_mask.swap(mask);
   TX_CUDA(h, cudaMemcpyAsync(h->mask, h->host_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
   int rc = update_links(h);
   if (rc != TX_OK) return rc;
@@ -537,8 +630,21 @@ int tx_upload_fi(tx_handle* h, const double* fi) {
   if (!h || !fi) return TX_ERR_ARG;
   const long long N = h->g.n;
   const size_t bytes = (size_t)N * h->S * h->Q * sizeof(double);
+  if (h->spec) {
+    // populations uploaded into wall cells travel on like those the sweep leaves there
+    std::vector<long long> nz;
+    for (int n = 0; n < h->Q; ++n)
+      for (long long i = 0; i < N; ++i) {
+        if (h->host_mask[(size_t)i] == 0) continue;
+        bool any = false;
+        for (int m = 0; m < h->S; ++m) any = any || fi[(i * h->Q + n) * h->S + m] != 0.0;
+        if (any) nz.push_back((long long)n * N + i);
+      }
+    const int rc = upload_spec_routes(h, nz.empty() ? nullptr : &nz);
+    if (rc != TX_OK) return rc;
+  }
   TX_CUDA(h, cudaMemcpyAsync(h->stage, fi, bytes, cudaMemcpyHostToDevice, h->stream));
-  h->ks.from_natural(h->stage, h->mask, N, shift_of(h->ph), h->f[h->cur], h->stream);
+  h->ks.from_natural(h->stage, pop_mask(h), N, shift_of(h->ph), h->f[h->cur], h->stream);
   int rc = check_launch(h, "k_pops_from_natural");
   if (rc) return rc;
   h->have_fi = true;
@@ -566,10 +672,17 @@ int tx_init(tx_handle* h) {
   if (!h->have_state && !h->have_fi) return fail(h, TX_ERR_STATE, "tx_upload_state or tx_upload_fi must come before tx_init");
   if (!h->have_fi) {
     // FlowFiInit: the state buffer becomes (1 - P/2) feq of the initial moments
+    if (h->spec) {
+      // wall cells start empty (the reference's VecSet(fi, 0))
+      const long long N = h->g.n;
+      k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(static_cast<double*>(h->f[h->cur]),
+                                                                                     h->mask, N, h->S * h->Q);
+    }
     h->ks.init(args(h, h->cur, h->cur), h->uic, h->stream);
     int rc = check_launch(h, "k_init");
     if (rc) return rc;
   }
+  h->spec_fresh = 2;
   // FlowUpdateMoments: the forcing density is the plain population sum
   h->ks.density(args(h, h->cur, h->cur), 1, h->stream);
   int rc = check_launch(h, "k_density");
@@ -606,6 +719,7 @@ int tx_step(tx_handle* h, int32_t nsteps) {
     }
     if (h->timing) cudaEventRecord(h->ev[0], h->stream);
     h->ks.step(a, h->stream);
+    if (h->spec) spec_pass(h, h->cur, nxt);
     if (h->timing) cudaEventRecord(h->ev[1], h->stream);
     h->ks.density(a, 0, h->stream);
     if (h->faces.post) {

@@ -2163,13 +2163,15 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
 }
 
 // Natural-order populations <-> SoA state (the shift and the FP16 scale are
-// applied in FP64).
+// applied in FP64).  Wall cells read and write as zero; with mask = null
+// (lattices with specular walls, whose wall cells hold populations) every
+// cell's populations pass through.
 template <int D, int S, class T, class R>
 __global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, Shift sh, double* out) {
   constexpr int Q = Lat<D>::Q;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N) return;
-  const bool wall = __ldg(mask + idx) != 0;
+  const bool wall = mask && __ldg(mask + idx) != 0;
   for (int n = 0; n < Q; ++n)
     for (int m = 0; m < S; ++m) {
       double v = 0.0;
@@ -2186,7 +2188,7 @@ __global__ void k_pops_from_natural(const double* in, const uint8_t* mask, long 
   constexpr int Q = Lat<D>::Q;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N) return;
-  const bool wall = __ldg(mask + idx) != 0;
+  const bool wall = mask && __ldg(mask + idx) != 0;
   for (int n = 0; n < Q; ++n)
     for (int m = 0; m < S; ++m) {
       double v = wall ? 0.0 : in[(idx * Q + n) * S + m];

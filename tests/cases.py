@@ -299,3 +299,43 @@ EOS = [
                                    rho_in=6.5, rho_out=0.4), 20),
     ("d3_eos_sc_mrt", lambda: eos_drop(P.D3Q19, (12, 14, 12), P.EOS_SC, (1.0,), -0.28, mode=P.MRT), 20),
 ]
+
+
+def specular_case(disc, shape, periodic, ncomp, codes, frac, seed):
+    """Seeded random walls mixing ordinary and specular (no-stick) codes:
+    900/901/902 reflect normal to x/y/z (902 is an ordinary wall in 2D); one
+    or two components with coupling, body force, slightly uneven densities."""
+    p = base(disc, shape, ncomp=ncomp, mode=P.SRT, periodic=periodic)
+    rng = np.random.default_rng(seed)
+    p.nminerals = 1
+    if ncomp == 2:
+        p.g[0][1] = p.g[1][0] = 0.1
+        p.tau[1] = 0.8
+    p.body_forces = 1
+    p.gvt[0], p.gvt[1] = 1e-4, -2e-4
+    walls = np.where(rng.random(p.nsites) < frac, rng.choice(codes, size=p.nsites), 0.0)
+    rho = np.repeat(np.where(walls == 0, 1.0, 0.0), ncomp) * (1.0 + 0.1 * rng.random(p.nsites * ncomp))
+    return p, walls, rho
+
+
+def specular_porous(disc, shape, iso, seed=7):
+    """porous_case (two minerals, density faces, body force, MRT) with half of
+    its wall cells turned into specular walls."""
+    p, walls, rho = porous_case(disc, shape, mode=P.MRT, iso=iso, body=True)
+    rng = np.random.default_rng(seed)
+    codes = [900.0, 901.0, 902.0] if disc == P.D3Q19 else [900.0, 901.0]
+    pick = (walls > 0) & (rng.random(p.nsites) < 0.5)
+    return p, np.where(pick, rng.choice(codes, size=p.nsites), walls), rho
+
+
+SPEC3 = [1.0, 900.0, 901.0, 902.0]
+# (name, case factory, steps): specular walls next to ordinary walls
+SPECULAR = [
+    ("d3_periodic_1c", lambda: specular_case(P.D3Q19, (10, 12, 14), (1, 1, 1), 1, SPEC3, 0.25, 0), 6),
+    ("d3_ghost_xy_2c", lambda: specular_case(P.D3Q19, (10, 12, 14), (0, 0, 1), 2, SPEC3, 0.25, 1), 6),
+    ("d3_ghost_xz_1c", lambda: specular_case(P.D3Q19, (9, 11, 13), (0, 1, 0), 1, SPEC3 + [999.0], 0.3, 2), 6),
+    ("d2_periodic_2c", lambda: specular_case(P.D2Q9, (1, 20, 24), (1, 1, 1), 2, SPEC3, 0.25, 3), 6),
+    ("d2_ghost_x_1c", lambda: specular_case(P.D2Q9, (1, 20, 24), (0, 1, 1), 1, SPEC3[:3], 0.3, 4), 6),
+    ("d3_porous_mrt_iso8_dirichlet", lambda: specular_porous(P.D3Q19, (12, 10, 11), 8), 30),
+    ("d2_porous_mrt_iso10_dirichlet", lambda: specular_porous(P.D2Q9, (1, 22, 18), 10), 8),
+]

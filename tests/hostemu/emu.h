@@ -11,6 +11,7 @@
 
 #include "tx_host_params.h"
 #include "tx_pair.cuh"
+#include "tx_specular.cuh"
 
 namespace emu {
 
@@ -83,11 +84,38 @@ std::string run(const Case& c, Result& out) {
   else
     convert_phys(ph, &P);
 
+  // specular walls: single-lattice FP64 handles without species (as tx_upload_walls)
+  bool spec = false;
+  for (long long i = 0; i < N; ++i) spec = spec || specular_axis(c.walls[(size_t)i], D) >= 0;
+  if (spec && (!std::is_same<T, double>::value || p.nspecies > 0))
+    return "specular (no-stick) wall codes 900-902 need the FP64 forms and no species";
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
-    if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why)) return why;
+    if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why, spec)) return why;
   }
+  SpecRoutes routes;
+  if (spec) {
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    std::vector<long long> init_nz;  // wall slots with uploaded content
+    if (c.from_fi)
+      for (long long i = 0; i < N; ++i)
+        if (mask[(size_t)i] != 0)
+          for (int n = 0; n < Q; ++n)
+            for (int m = 0; m < S; ++m)
+              if (c.init[(size_t)((i * Q + n) * S + m)] != 0.0) {
+                init_nz.push_back((long long)n * N + i);
+                break;
+              }
+    bool pre[6];
+    for (int f = 0; f < 6; ++f) pre[f] = face_has_values(p, D, f);
+    const std::string why = specular_routes(c.walls.data(), D, nn, g.per, pre, &init_nz, &routes);
+    if (!why.empty()) return why;
+  }
+  const long long ne = (long long)routes.dst.size();
+  std::vector<double> spec_tmp((size_t)(ne * S + 1));
+  const uint8_t* pop_mask = spec ? nullptr : mask.data();
+  int spec_fresh = 2;
   std::vector<uint32_t> links((size_t)N);
   launch3(g, 256, [&] { k_links<D>(mask.data(), g, links.data()); });
 
@@ -143,7 +171,7 @@ std::string run(const Case& c, Result& out) {
   }
   const Shift sh = shift_of(ph);
   if (c.from_fi) {
-    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), mask.data(), N, sh, buf[cur]); });
+    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), pop_mask, N, sh, buf[cur]); });
   } else {
     for (long long i = 0; i < N; ++i)
       for (int m = 0; m < S; ++m)
@@ -210,6 +238,21 @@ std::string run(const Case& c, Result& out) {
     } else {
       launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     }
+    if constexpr (std::is_same<T, double>::value) {
+      if (spec) {
+        // the library's specular-wall pass: clear the wall slots of a fresh buffer,
+        // then gather and scatter the exceptions to the ordinary push
+        double* fo = buf[1 - cur];
+        if (spec_fresh > 0) {
+          launch1(N, 256, [&] { k_spec_clear_walls<double>(fo, mask.data(), N, S * Q); });
+          --spec_fresh;
+        }
+        if (ne) {
+          launch1(ne, 256, [&] { k_spec_gather<double>(buf[cur], fo, routes.src.data(), ne, S, (long long)Q * N, spec_tmp.data()); });
+          launch1(ne, 256, [&] { k_spec_scatter<double>(fo, routes.dst.data(), ne, S, (long long)Q * N, spec_tmp.data()); });
+        }
+      }
+    }
     density(a, 0);
     if (faces.post) launch1(shell.start[shell.nf], 128, [&] { k_faces<D, S, ISO, EXACT, T, R, RT>(a, shell); });
     cur = 1 - cur;
@@ -233,7 +276,7 @@ std::string run(const Case& c, Result& out) {
     launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 11, out.sflux.data()); });
   }
   out.fi.assign((size_t)N * S * Q, 0.0);
-  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], mask.data(), N, sh, out.fi.data()); });
+  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], pop_mask, N, sh, out.fi.data()); });
   const StepArgs a = args(cur, cur);
   out.rho.assign((size_t)N * S, 0.0);
   out.flux.assign((size_t)N * S * D, 0.0);

@@ -159,6 +159,6 @@ def test_errors_are_status_codes():
         h.step(1)  # before init
     assert e.value.code == 2
     w = np.zeros(p.nsites)
-    w[3] = 900.0
+    w[3] = -1.0
     with pytest.raises(TxError):
         h.upload_walls(w)

@@ -1,0 +1,122 @@
+"""Specular (no-stick) walls 900/901/902 on the GPU against the oracle, through the C ABI.
+
+DistributionBouncebackD3/D2 (src/lbm/lbm_distribution_function.F90:668-784)
+sweeps the ghosted box in k-j-i order; a specular wall reflects only the
+component of c normal to it and may write into wall cells the sweep has
+already cleared, so wall cells end steps holding populations.  The library
+resolves every population slot's source once per wall upload and applies the
+exceptions to its ordinary push after the step kernel (csrc/tx_specular.cuh).
+
+* exact FP64 form: every cell's populations (wall cells included), densities,
+  velocities and forces identical to the oracle bit for bit;
+* fast FP64 form: within 1e-12 relative;
+* restarts with populations in wall cells, and the forms and paths that
+  refuse these codes.
+"""
+import numpy as np
+import pytest
+
+import cases
+from oracle import Oracle
+from taxila import params as P
+from taxila._lib import Batch, Handle, TxError
+
+pytestmark = pytest.mark.gpu
+FIELDS = (P.FIELD_FI, P.FIELD_RHO, P.FIELD_FLUX, P.FIELD_FORCES)
+
+
+def run_pair(p, walls, rho, steps, exact, fi=None):
+    o = Oracle(p)
+    o.set_walls(walls)
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    h = Handle(q)
+    h.upload_walls(walls)
+    if fi is not None:
+        o.set_fi(fi)
+        h.upload_fi(fi)
+    else:
+        o.set_state(rho)
+        h.upload_state(rho)
+    o.init()
+    h.init()
+    if steps:
+        o.step(steps)
+        h.step(steps)
+    return o, h
+
+
+def compare_all_cells(o, h, exact, rtol=1e-12):
+    for f in FIELDS:
+        a, b = o.get(f), h.download(f)
+        assert np.all(np.isfinite(a)), f
+        if exact:
+            bad = np.nonzero(a != b)[0]
+            assert bad.size == 0, "field %d: %d values differ, first %s: %r vs %r" % (f, bad.size, bad[:3], a[bad[:3]], b[bad[:3]])
+        else:
+            err = float(np.max(np.abs(a - b)) / (np.max(np.abs(a)) or 1.0))
+            assert err <= rtol, "field %d: max rel err %.3e > %.1e" % (f, err, rtol)
+
+
+def wall_content(o, p, walls):
+    return float(np.abs(o.get(P.FIELD_FI).reshape(p.nsites, -1)[np.asarray(walls) > 0]).sum())
+
+
+@pytest.mark.parametrize("name,make,steps", cases.SPECULAR, ids=[c[0] for c in cases.SPECULAR])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_specular_walls_match_oracle(name, make, steps, exact):
+    p, walls, rho = make()
+    o, h = run_pair(p, walls, rho, steps, exact)
+    assert wall_content(o, p, walls) > 0.0  # the case exercises populations left in wall cells
+    compare_all_cells(o, h, exact)
+    # the delta norms see the wall cells' populations as the reference's do
+    o.step(1)
+    h.step(1)
+    for field in (P.FIELD_RHO, P.FIELD_FI):
+        a, b = o.delta_norm(field), h.delta_norm(field)
+        assert (a == b) if exact else abs(a - b) <= 1e-10 * max(abs(a), 1e-300), (field, a, b)
+
+
+def test_specular_restart_with_wall_content():
+    p, walls, rho = cases.specular_porous(P.D3Q19, (12, 10, 11), 8)
+    o0 = Oracle(p)
+    o0.set_walls(walls)
+    o0.set_state(rho)
+    o0.init()
+    o0.step(3)
+    fi = o0.get(P.FIELD_FI)
+    o0.close()
+    assert np.abs(fi.reshape(p.nsites, -1)[walls > 0]).sum() > 0.0
+    o, h = run_pair(p, walls, None, 6, True, fi=fi)
+    compare_all_cells(o, h, True)
+
+
+def test_specular_larger_lattice_fast_form():
+    # more steps on a larger lattice: long wall-to-wall chains and many exceptions
+    p, walls, rho = cases.specular_case(P.D3Q19, (24, 28, 32), (1, 0, 1), 2, cases.SPEC3, 0.2, 11)
+    o, h = run_pair(p, walls, rho, 40, exact=False)
+    compare_all_cells(o, h, False)
+
+
+def test_specular_walls_refused_where_unsupported():
+    p, walls, rho = cases.SPECULAR[0][1]()
+    q = P.copy_params(p)
+    q.precision = P.PREC_F32
+    h = Handle(q)
+    with pytest.raises(TxError) as e:
+        h.upload_walls(walls)
+    assert e.value.code == 1 and "FP64" in str(e.value)
+    h.close()
+    # a refused upload leaves the handle usable with other walls
+    h = Handle(p)
+    h.upload_walls(np.where(walls >= 900.0, 1.0, walls))
+    h.upload_state(rho)
+    h.init()
+    h.step(2)
+    h.close()
+    form = P.copy_params(p)
+    form.exact = 0
+    b = Batch(form)
+    with pytest.raises(TxError):
+        b.add(p, walls, rho)
+    b.close()

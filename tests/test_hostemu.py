@@ -242,3 +242,67 @@ def test_emulated_exterior_bcs_fast_form_1000_steps(emu_exe, tmp_path, name):
     got = run_emu(emu_exe, q, walls, rho, 1000, False, tmp_path)
     errs = compare(ref, got, p, walls, 1e-12)
     print(name, errs)
+
+
+def compare_all_cells(ref, got, tol):
+    """Like compare, but every cell's populations count: with specular walls,
+    wall cells hold populations (the moments stay zero on walls)."""
+    for k in FIELDS:
+        a, b = ref[k], got[k]
+        assert np.all(np.isfinite(a)), k
+        if tol == 0.0:
+            bad = np.nonzero(a != b)[0]
+            assert bad.size == 0, "%s: %d values differ, first %s: %r vs %r" % (k, bad.size, bad[:3], a[bad[:3]], b[bad[:3]])
+        else:
+            err = float(np.max(np.abs(a - b)) / (np.max(np.abs(a)) or 1.0))
+            assert err <= tol, "%s: max rel err %.3e > %.1e" % (k, err, tol)
+
+
+@pytest.mark.parametrize("name,make,steps", cases.SPECULAR, ids=[c[0] for c in cases.SPECULAR])
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_emulated_specular_walls_match_oracle(emu_exe, tmp_path, name, make, steps, exact):
+    # specular walls 900/901/902 next to ordinary walls: the step kernels plus the
+    # route exceptions resolved at wall upload reproduce the reference's ordered
+    # bounceback sweep, wall cells' populations included
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    assert np.abs(ref["fi"].reshape(p.nsites, -1)[walls > 0]).sum() > 0.0  # wall cells do hold populations
+    q = P.copy_params(p)
+    q.exact = 1 if exact else 0
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    compare_all_cells(ref, got, 0.0 if exact else 1e-12)
+
+
+@pytest.mark.parametrize("name", ["d3_porous_mrt_iso8_dirichlet", "d2_periodic_2c"])
+def test_emulated_specular_restart_with_wall_content(emu_exe, tmp_path, name):
+    # populations uploaded into wall cells (a restart file) move on as the
+    # reference's sweep moves them
+    make = dict((c[0], c[1]) for c in cases.SPECULAR)[name]
+    p, walls, rho = make()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.init()
+    o.step(3)
+    fi = o.get(P.FIELD_FI)
+    o.close()
+    assert np.abs(fi.reshape(p.nsites, -1)[walls > 0]).sum() > 0.0
+    ref = oracle_run(p, walls, None, 5, fi=fi)
+    q = P.copy_params(p)
+    q.exact = 1
+    got = run_emu(emu_exe, q, walls, fi, 5, True, tmp_path)
+    compare_all_cells(ref, got, 0.0)
+
+
+def test_emulated_specular_walls_need_fp64(emu_exe, tmp_path):
+    p, walls, rho = cases.SPECULAR[0][1]()
+    q = P.copy_params(p)
+    q.precision = P.PREC_F32
+    case = os.path.join(str(tmp_path), "case.bin")
+    with open(case, "wb") as f:
+        f.write(C.string_at(C.addressof(q), C.sizeof(q)))
+        f.write(np.array([1, 0], dtype=np.int32).tobytes())
+        f.write(np.ascontiguousarray(walls, dtype=np.float64).tobytes())
+        f.write(np.ascontiguousarray(rho, dtype=np.float64).tobytes())
+    r = subprocess.run([emu_exe, case, case + ".out"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 2 and "FP64" in r.stderr

@@ -114,13 +114,13 @@ def test_served_drainage_values_stay_finite():
 
 
 def test_specular_walls_leave_populations_in_wall_cells():
-    # Why the device rejects specular wall codes 900-902: in the reference's
-    # bounceback sweep (k-j-i order over the ghosted box, restated by the
-    # oracle) a specular wall moves a population along one axis only, possibly
-    # into a wall cell that the sweep has already cleared.  Those populations
-    # stay in wall cells, stream into pore cells on the next step and decide
-    # the result, so reproducing it needs every wall cell's populations and
-    # the sweep order; with ordinary walls alone, wall cells end every step empty.
+    # Why the device keeps wall cells' populations when specular wall codes
+    # 900-902 are present: in the reference's bounceback sweep (k-j-i order
+    # over the ghosted box, restated by the oracle) a specular wall moves a
+    # population along one axis only, possibly into a wall cell that the sweep
+    # has already cleared.  Those populations stay in wall cells, stream into
+    # pore cells on the next step and decide the result; with ordinary walls
+    # alone, wall cells end every step empty.
     rng = np.random.default_rng(0)
     for codes, expect_left in (([1.0], False), ([1.0, 900.0, 901.0, 902.0], True)):
         p = P.default_params()
