@@ -103,6 +103,11 @@ struct PhysT {
   R c0g[MAXC][MAXC];
   R ffwq[3][12];
   int ff_on, fs_on, body_on;
+  // every component has the same W~A (equal molecular masses): the FP64 fast
+  // form computes the equilibrium weights E_n once per site
+  int wa_shared;
+  // two components coupled only to each other (g_11 = g_22 = 0)
+  int ff_cross;
 };
 using Phys = PhysT<double>;
 
@@ -127,6 +132,7 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   cp(&a.WAc[0][0], &b->WAc[0][0], MAXC * 3); cp(a.keep, b->keep, MAXC); cp(a.kfac, b->kfac, MAXC);
   cp(&a.c0g[0][0], &b->c0g[0][0], MAXC * MAXC); cp(&a.ffwq[0][0], &b->ffwq[0][0], 36);
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
+  b->wa_shared = a.wa_shared; b->ff_cross = a.ff_cross;
 }
 
 // Classes of the exterior BC kinds, as bc%flags holds them next to
@@ -725,7 +731,15 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
           });
         }
       });
-      // F -= psi(x) c0 sum_k g_mk grad_k (the weight sum is folded into ffwq)
+      // F -= psi(x) c0 sum_k g_mk grad_k (the weight sum is folded into ffwq);
+      // with two components coupled only to each other, the one cross term
+      if (S == 2 && std::is_same<R, double>::value && P.ff_cross) {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int m = 0; m < S; ++m) F[m][d] = F[m][d] - mult[m] * (P.c0g[m][S - 1 - m] * gr[S - 1 - m][d]);
+        return;
+      }
 #pragma unroll
       for (int d = 0; d < D; ++d)
 #pragma unroll
@@ -1083,15 +1097,199 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         });
       }
     }
+  } else if constexpr (!kShifted<T>) {
+    // Fast form, FP64 (plain storage), with c_s^2 = 1/3 and E_n = W~_n (A_m,n + B_n)
+    // (W~_0 = 1, B_n the velocity terms):
+    //   feq_n   = rho E_n
+    //   P feq_n = 3 E_n (F.c_n - F.u)          (He forcing)
+    //   f'_n    = (1 - s0) f_n + E_n (G + c_n.kF),  G = s0 rho - k F.u,  k = 3 - 1.5 s0,
+    // i.e. f - s0 (f - feq + P feq / 2) + P feq, every moment relaxed at s0;
+    // moments whose MRT rate differs from s0 are corrected afterwards.
+    // Directions come in pairs (n, n~ = opp(n)); with t = c_n.u and, per
+    // direction class, WAu = W~A - 1.5 w u^2,
+    //   E_n = WAu + t (3w + 4.5w t),   E_n~ = WAu - t (3w - 4.5w t),
+    // two FMAs each, and the pair relaxes to E_n (G + h) and E_n~ (G - h) with
+    // h = c_n.kF.  E depends on the component only through W~A = w/mm (d_k at
+    // rest): it is computed for the first component, and a component with
+    // another molecular mass shifts it by the difference of W~A
+    // (P.wa_shared: none does).
+    constexpr int NP = npairs<D>();
+    R En[NP], Eb[NP], E0;
+    {
+      E0 = P.WAc[0][0] + (D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr);
+      const R WAu1 = P.WAc[0][1] - R(1.5 * L::w(1)) * usqr, WAu2 = P.WAc[0][2] - R(1.5 * L::w(Q - 1)) * usqr;
+      sfor<0, NP>([&](auto pp) {
+        constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+        constexpr double w = L::w(n);
+        const R t = cdot_z<D, n>(up);
+        const R WAu = n <= L::NAXIS ? WAu1 : WAu2;
+        En[p] = t * (R(3 * w) + R(4.5 * w) * t) + WAu;
+        Eb[p] = WAu - t * (R(3 * w) - R(4.5 * w) * t);
+      });
+    }
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+      if (m > 0 && !P.wa_shared) {
+        const R d0 = P.WAc[m][0] - P.WAc[m - 1][0], d1 = P.WAc[m][1] - P.WAc[m - 1][1],
+                d2 = P.WAc[m][2] - P.WAc[m - 1][2];
+        E0 = E0 + d0;
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+          En[p] = En[p] + (n <= L::NAXIS ? d1 : d2);
+          Eb[p] = Eb[p] + (n <= L::NAXIS ? d1 : d2);
+        });
+      }
+      const R r = rc[m];
+      const R s0 = P.s0[m];
+      const R k = P.kfac[m];
+      const R keep = P.keep[m];
+      R Fu = R(-0.0), kF[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        Fu = Fu + F[m][d] * up[d];
+        kF[d] = k * F[m][d];
+      }
+      const R G = s0 * r - k * Fu;
+      const unsigned spec = P.spec_mask[m];
+      const T* fm = fin + (long long)m * Q * N;
+      auto pop = [&](auto nn) -> R {
+        constexpr int n = decltype(nn)::value;
+        return ld_dev_s<T, R>(fm + (long long)n * N + c, sc);
+      };
+      const R X0 = E0 * G;
+      if (spec == 0u && keep == R(0)) {
+        // s0 = 1 (tau = 1): the relaxed populations are the forced equilibrium
+        push(std::integral_constant<int, 0>{}, m, X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          const R h = cdot_z<D, n>(kF);
+          push(std::integral_constant<int, n>{}, m, En[p] * (G + h));
+          push(std::integral_constant<int, nb>{}, m, Eb[p] * (G - h));
+        });
+      } else if (spec == 0u) {
+        // every moment relaxes at s0 (BGK): one pair at a time
+        push(std::integral_constant<int, 0>{}, m, keep * pop(std::integral_constant<int, 0>{}) + X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          const R h = cdot_z<D, n>(kF);
+          push(std::integral_constant<int, n>{}, m, keep * pop(std::integral_constant<int, n>{}) + En[p] * (G + h));
+          push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + Eb[p] * (G - h));
+        });
+      } else if (spec == stress_mask<D>()) {
+        // s_nu != s0, every other rate s0: the s_nu moments of the pair sums of
+        // the non-equilibrium part, S_p = f_n + f_n~ - E_n (r + 1.5 F.u - c_n.1.5F)
+        // - E_n~ (r + 1.5 F.u + c_n.1.5F), give the corrections ck; each pair
+        // is relaxed and pushed less its correction.
+        R ck[Q];
+        {
+          R hF[D];
+#pragma unroll
+          for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
+          const R Xh = r + R(1.5) * Fu;
+          R Sp[NP];
+          sfor<0, NP>([&](auto pp) {
+            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+            const R th = cdot_z<D, n>(hF);
+            const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
+            Sp[p] = gs - En[p] * (Xh - th) - Eb[p] * (Xh + th);
+          });
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU) {
+              R md = R(-0.0);
+              sfor<0, NP>([&](auto pp) {
+                constexpr int p = decltype(pp)::value;
+                constexpr int v = L::mt(pair_n<D>(p), kq);
+                if constexpr (v == 1) md = md + Sp[p];
+                else if constexpr (v == -1) md = md - Sp[p];
+                else if constexpr (v != 0) md = md + R(v) * Sp[p];
+              });
+              ck[kq] = P.dspec[m][kq] * md;
+            }
+          });
+        }
+        const bool k0 = keep == R(0);
+        push(std::integral_constant<int, 0>{}, m, k0 ? X0 : keep * pop(std::integral_constant<int, 0>{}) + X0);
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          R corr = R(-0.0);
+          sfor<0, Q>([&](auto kk) {
+            constexpr int kq = decltype(kk)::value;
+            if constexpr (rate_of<D>(kq) == R_NU) {
+              constexpr int v = L::mt(n, kq);
+              if constexpr (v == 1) corr = corr + ck[kq];
+              else if constexpr (v == -1) corr = corr - ck[kq];
+              else if constexpr (v != 0) corr = corr + R(v) * ck[kq];
+            }
+          });
+          const R h = cdot_z<D, n>(kF);
+          const R vn = En[p] * (G + h) - corr, vb = Eb[p] * (G - h) - corr;
+          if (k0) {
+            push(std::integral_constant<int, n>{}, m, vn);
+            push(std::integral_constant<int, nb>{}, m, vb);
+          } else {
+            push(std::integral_constant<int, n>{}, m, keep * pop(std::integral_constant<int, n>{}) + vn);
+            push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + vb);
+          }
+        });
+      } else if constexpr (MRT) {
+        // General rate pattern, compiled into the MRT kernels only (the host
+        // runs the others when every component is BGK-like or s_nu-only):
+        // relax every moment at s0, then correct each moment k whose rate
+        // differs by dspec_k times its projection of the deviation from the
+        // forced equilibrium, f - E_n (r + 1.5 F.u - 1.5 F.c_n)
+        R fo[Q], dfi[Q];
+        const R hFu = R(1.5) * Fu;
+        R hF[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
+        {
+          const R g0 = pop(std::integral_constant<int, 0>{});
+          fo[0] = keep * g0 + X0;
+          dfi[0] = g0 - E0 * (r + hFu);
+        }
+        sfor<0, NP>([&](auto pp) {
+          constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+          const R h = cdot_z<D, n>(kF), t = cdot_z<D, n>(hF);
+          const R gn = pop(std::integral_constant<int, n>{}), gb = pop(std::integral_constant<int, nb>{});
+          fo[n] = keep * gn + En[p] * (G + h);
+          fo[nb] = keep * gb + Eb[p] * (G - h);
+          dfi[n] = gn - En[p] * (r + hFu - t);
+          dfi[nb] = gb - Eb[p] * (r + hFu + t);
+        });
+        sfor<0, Q>([&](auto kk) {
+          constexpr int kq = decltype(kk)::value;
+          if (spec & (1u << kq)) {
+            R md = R(-0.0);
+            sfor<0, Q>([&](auto ii) {
+              constexpr int i = decltype(ii)::value;
+              constexpr int v = L::mt(i, kq);
+              if constexpr (v == 1) md = md + dfi[i];
+              else if constexpr (v == -1) md = md - dfi[i];
+              else if constexpr (v != 0) md = md + R(v) * dfi[i];
+            });
+            const R ckq = P.dspec[m][kq] * md;
+            sfor<0, Q>([&](auto ii) {
+              constexpr int i = decltype(ii)::value;
+              constexpr int v = L::mt(i, kq);
+              if constexpr (v == 1) fo[i] = fo[i] - ckq;
+              else if constexpr (v == -1) fo[i] = fo[i] + ckq;
+              else if constexpr (v != 0) fo[i] = fo[i] - ckq * R(v);
+            });
+          }
+        });
+        sfor<0, Q>([&](auto nn) { push(nn, m, fo[decltype(nn)::value]); });
+      }
+    }
   } else {
-    // Fast form, with c_s^2 = 1/3 and E_n = W~_n (A_m,n + B_n) (W~_0 = 1):
+    // Fast form of the FP32-arithmetic forms, with c_s^2 = 1/3 and E_n = W~_n (A_m,n + B_n) (W~_0 = 1):
     //   feq_n   = rho E_n                      (B_n holds the velocity terms)
     //   P feq_n = 3 E_n (F.c_n - F.u)          (He forcing)
     //   f'_n    = (1 - s0) f_n + s0 feq_n + (3 - 1.5 s0) E_n (F.c_n - F.u),
     // i.e. f - s0 (f - feq + P feq / 2) + P feq, every moment relaxed at s0;
     // moments whose MRT rate differs from s0 are corrected afterwards.
-    // Everything is computed on deviations from the rest state, g = f - w rho0
-    // (rho0 = 0 in the FP64 form): g'_n = (1 - s0) g_n + s0 dE_n + k E_n (F.c_n - F.u)
+    // Everything is computed on deviations from the rest state, g = f - w rho0:
+    // g'_n = (1 - s0) g_n + s0 dE_n + k E_n (F.c_n - F.u)
     // with dE_n = feq_n - w_n rho0 = W~A (rho - rho0) + W~B rho + (W~A - w) rho0,
     // so that FP32 arithmetic keeps the precision of the small deviations.
     // WB_n = W~_n B_n is shared by the components.
@@ -1102,8 +1300,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
     // h = c_n.kF the relaxed pair is
     //   g'_n = keep g_n + Pe + Po,   g'_n~ = keep g_n~ + Pe - Po,
     //   Pe = s0 De + Bo h - Ae kFu,  Po = Bo G + Ae h,  G = s0 rho - kFu,
-    // where Ae = W~A + WBe and De = W~A (rho - rho0) + WBe rho + cA (in the
-    // FP64 form Pe = Ae G + Bo h).  Moments relaxed at s_nu != s0 (the
+    // where Ae = W~A + WBe and De = W~A (rho - rho0) + WBe rho + cA.  Moments relaxed at s_nu != s0 (the
     // traceless second moments, even in c) correct Pe through the pair sums of
     // the non-equilibrium part, S_p = dfi_n + dfi_n~.  Other rate patterns take
     // the general path below.
@@ -1143,23 +1340,15 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       };
       const R E0 = WA0 + WB0;
       // rest direction: g'_0 = keep g_0 + X0
-      R X0;
-      if constexpr (kShifted<T>)
-        X0 = s0 * (WA0 * rd + (WB0 * r + cA0)) - E0 * kFu;
-      else
-        X0 = E0 * G;
+      const R X0 = s0 * (WA0 * rd + (WB0 * r + cA0)) - E0 * kFu;
       // the even and odd parts of pair p
       auto pair_terms = [&](auto pp, R& pe, R& po) {
         constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
         const R WA = n <= L::NAXIS ? WA1 : WA2;
         const R Ae = WA + WBe[p];
         const R h = cdot_z<D, n>(kF);
-        if constexpr (kShifted<T>) {
-          const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
-          pe = s0 * De + (Bo[p] * h - Ae * kFu);
-        } else {
-          pe = Ae * G + Bo[p] * h;
-        }
+        const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+        pe = s0 * De + (Bo[p] * h - Ae * kFu);
         po = Bo[p] * G + Ae * h;
       };
       if (spec == 0u && keep == R(0)) {
@@ -1201,12 +1390,8 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
             const R Ae = WA + WBe[p];
             const R t2 = cdot_z<D, n>(F3);
             const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
-            if constexpr (kShifted<T>) {
-              const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
-              Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
-            } else {
-              Sp[p] = gs - Ae * (R(2) * r + hFu2) + Bo[p] * t2;
-            }
+            const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+            Sp[p] = (gs - R(2) * De) - Ae * hFu2 + Bo[p] * t2;
           });
           sfor<0, Q>([&](auto kk) {
             constexpr int kq = decltype(kk)::value;
@@ -1260,10 +1445,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
         {
           const R g0 = pop(std::integral_constant<int, 0>{});
-          if constexpr (kShifted<T>)
-            dfi[0] = g0 - (WA0 * rd + (WB0 * r + cA0)) - E0 * hFu;
-          else
-            dfi[0] = g0 - E0 * (r + hFu);
+          dfi[0] = g0 - (WA0 * rd + (WB0 * r + cA0)) - E0 * hFu;
         }
         sfor<0, NP>([&](auto pp) {
           constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
@@ -1275,14 +1457,9 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
           const R WA = n <= L::NAXIS ? WA1 : WA2;
           const R t = cdot_z<D, n>(hF);
           const R En = WA + WBe[p] + Bo[p], Eb = WA + WBe[p] - Bo[p];
-          if constexpr (kShifted<T>) {
-            const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
-            dfi[n] = gn - (De + Bo[p] * r) + En * (t - hFu);
-            dfi[nb] = gb - (De - Bo[p] * r) - Eb * (t + hFu);
-          } else {
-            dfi[n] = gn - En * (r + hFu - t);
-            dfi[nb] = gb - Eb * (r + hFu + t);
-          }
+          const R De = WA * rd + (WBe[p] * r + (n <= L::NAXIS ? cA1 : cA2));
+          dfi[n] = gn - (De + Bo[p] * r) + En * (t - hFu);
+          dfi[nb] = gb - (De - Bo[p] * r) - Eb * (t + hFu);
         });
         sfor<0, Q>([&](auto kk) {
           constexpr int kq = decltype(kk)::value;
