@@ -853,6 +853,29 @@ __device__ __forceinline__ R cdot_z(const R v[D]) {
   return acc;
 }
 
+// The bilinear form stress_coef(k, ., .) of s_nu moment k at (a, b); the two
+// off-diagonal terms of a symmetric coefficient share one multiplication.
+template <int D, int k, class R>
+__device__ __forceinline__ R stress_form(const R a[D], const R b[D]) {
+  R acc = R(-0.0);
+  sfor<0, D>([&](auto dd) {
+    constexpr int d = decltype(dd)::value;
+    sfor<d, D>([&](auto ee) {
+      constexpr int e = decltype(ee)::value;
+      constexpr double Cde = stress_coef<D>(k, d, e), Ced = stress_coef<D>(k, e, d);
+      if constexpr (d == e) {
+        if constexpr (Cde != 0.0) acc = acc + R(Cde) * (a[d] * b[d]);
+      } else if constexpr (Cde == Ced) {
+        if constexpr (Cde != 0.0) acc = acc + R(Cde) * (a[d] * b[e] + a[e] * b[d]);
+      } else {
+        if constexpr (Cde != 0.0) acc = acc + R(Cde) * (a[d] * b[e]);
+        if constexpr (Ced != 0.0) acc = acc + R(Ced) * (a[e] * b[d]);
+      }
+    });
+  });
+  return acc;
+}
+
 // Fast-form flux of one component from pair differences f_n - f_opp(n).
 template <int D, class R>
 __device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
@@ -1176,23 +1199,25 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
           push(std::integral_constant<int, nb>{}, m, keep * pop(std::integral_constant<int, nb>{}) + Eb[p] * (G - h));
         });
       } else if (spec == stress_mask<D>()) {
-        // s_nu != s0, every other rate s0: the s_nu moments of the pair sums of
-        // the non-equilibrium part, S_p = f_n + f_n~ - E_n (r + 1.5 F.u - c_n.1.5F)
-        // - E_n~ (r + 1.5 F.u + c_n.1.5F), give the corrections ck; each pair
-        // is relaxed and pushed less its correction.
+        // s_nu != s0, every other rate s0: the corrections ck = dspec md_k come
+        // from the s_nu moments md_k of the pair sums of the non-equilibrium
+        // part, S_p = f_n + f_n~ - (E_n + E_n~)(r + 1.5 F.u) + (E_n - E_n~) c_n.1.5F.
+        // With E_n + E_n~ = 2 WAu + 9w t^2 and E_n - E_n~ = 6w t, the class
+        // constants WAu drop out of these moments (stress_class_free), so
+        //   md_k = M_k(f_n + f_n~) + T_k(u, F - (r + 1.5 F.u) u),
+        // T_k the bilinear form stress_coef.  Each pair is then relaxed and
+        // pushed less its correction.
         R ck[Q];
         {
-          R hF[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) hF[d] = R(1.5) * F[m][d];
-          const R Xh = r + R(1.5) * Fu;
-          R Sp[NP];
+          R gs[NP];
           sfor<0, NP>([&](auto pp) {
             constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-            const R th = cdot_z<D, n>(hF);
-            const R gs = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
-            Sp[p] = gs - En[p] * (Xh - th) - Eb[p] * (Xh + th);
+            gs[p] = pop(std::integral_constant<int, n>{}) + pop(std::integral_constant<int, nb>{});
           });
+          const R Xh = r + R(1.5) * Fu;
+          R vF[D];
+#pragma unroll
+          for (int d = 0; d < D; ++d) vF[d] = F[m][d] - Xh * up[d];
           sfor<0, Q>([&](auto kk) {
             constexpr int kq = decltype(kk)::value;
             if constexpr (rate_of<D>(kq) == R_NU) {
@@ -1200,10 +1225,11 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
               sfor<0, NP>([&](auto pp) {
                 constexpr int p = decltype(pp)::value;
                 constexpr int v = L::mt(pair_n<D>(p), kq);
-                if constexpr (v == 1) md = md + Sp[p];
-                else if constexpr (v == -1) md = md - Sp[p];
-                else if constexpr (v != 0) md = md + R(v) * Sp[p];
+                if constexpr (v == 1) md = md + gs[p];
+                else if constexpr (v == -1) md = md - gs[p];
+                else if constexpr (v != 0) md = md + R(v) * gs[p];
               });
+              md = md + stress_form<D, kq, R>(up, vF);
               ck[kq] = P.dspec[m][kq] * md;
             }
           });

@@ -176,4 +176,44 @@ __host__ __device__ constexpr bool moments_have_parity() {
 }
 static_assert(stress_even_traceless<3>() && stress_even_traceless<2>(), "s_nu moments must be even and traceless");
 
+// 9 w_n for the direction classes, exactly (axis, diagonal): 1/2, 1/4 in D3Q19;
+// 1, 1/4 in D2Q9.
+template <int D>
+__host__ __device__ constexpr double nine_w(int n) {
+  return n <= Lat<D>::NAXIS ? (D == 3 ? 0.5 : 1.0) : 0.25;
+}
+
+// Bilinear form of an s_nu moment over direction pairs: the moment k of the
+// pair values 9 w_n (c_n.a)(c_n.b) is sum_de stress_coef(k, d, e) a_d b_e,
+// stress_coef(k, d, e) = sum over pairs of mt(n, k) 9 w_n c_n,d c_n,e.
+template <int D>
+__host__ __device__ constexpr double stress_coef(int k, int d, int e) {
+  double acc = 0.0;
+  for (int p = 0; p < npairs<D>(); ++p) {
+    const int n = pair_n<D>(p);
+    acc += Lat<D>::mt(n, k) * nine_w<D>(n) * Lat<D>::c(n, d) * Lat<D>::c(n, e);
+  }
+  return acc;
+}
+
+// The s_nu moments see no constant per direction class: over the axis pairs
+// and over the diagonal pairs the coefficients mt(n, k) sum to zero.
+template <int D>
+__host__ __device__ constexpr bool stress_class_free() {
+  for (int k = 0; k < Lat<D>::Q; ++k) {
+    if (rate_of<D>(k) != R_NU) continue;
+    int axis = 0, diag = 0;
+    for (int p = 0; p < npairs<D>(); ++p) {
+      const int n = pair_n<D>(p);
+      if (n <= Lat<D>::NAXIS)
+        axis += Lat<D>::mt(n, k);
+      else
+        diag += Lat<D>::mt(n, k);
+    }
+    if (axis != 0 || diag != 0) return false;
+  }
+  return true;
+}
+static_assert(stress_class_free<3>() && stress_class_free<2>(), "s_nu moments must vanish on class constants");
+
 }  // namespace tx
