@@ -158,6 +158,40 @@ void spec_pass(tx_handle* h, int in, int out) {
   k_spec_scatter<double><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, h->S, QN, h->spec_tmp);
 }
 
+// Reference wall values -> device mask codes on the device (the rules of
+// wall_code): flags[0] counts values the library refuses (negative or not
+// finite), flags[1] counts specular codes, whose routes the host resolves.
+__global__ void __launch_bounds__(256) k_wall_codes(const double* walls, long long N, int nminerals, int D,
+                                                    uint8_t* mask, unsigned* flags) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double v = walls[i];
+  uint8_t code = 255;
+  if (v == 0.0) {
+    code = 0;
+  } else if (!(v > 0.0) || !isfinite(v)) {
+    atomicAdd(&flags[0], 1u);
+  } else if (specular_axis(v, D) >= 0) {
+    atomicAdd(&flags[1], 1u);
+  } else if (v < 998.0) {
+    const int mineral = (int)v;
+    if (mineral >= 1 && mineral <= nminerals) code = (uint8_t)mineral;
+  }
+  mask[i] = code;
+}
+
+// The forcing density from natural-order densities (component fastest, the
+// device layout too): rho - rho0 on pore cells, zero on walls.
+template <class RT>
+__global__ void __launch_bounds__(256) k_rho_from_natural(const double* rho, const uint8_t* mask, long long N, int S,
+                                                          Shift sh, RT* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N * S) return;
+  const long long c = i / S;
+  const int m = (int)(i - c * S);
+  out[i] = RT(mask[c] == 0 ? rho[i] - sh.rho0[m] : 0.0);
+}
+
 // link masks from the device wall mask (after every change of the mask)
 int update_links(tx_handle* h) {
   const Launch3 l = launch3(h->g, 256);
@@ -233,11 +267,13 @@ namespace {
 
 void fill_phys(tx_handle* h) { fill_phys_impl(h->p, h->D, h->S, h->Q, h->ph); }
 
-__global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red) {
+// mask (with dof values per cell): the field is read in place, and walls read as zero
+__global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red,
+                             const uint8_t* mask = nullptr, int dof = 1) {
   double mx = 0.0;
   unsigned long long bad = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double c = cur[i];
+    const double c = mask && mask[i / dof] != 0 ? 0.0 : cur[i];
     if (!isfinite(c)) ++bad;
     const double v = c != 0.0 ? fabs((old[i] - c) / c) : 0.0;
     if (v > mx) mx = v;
@@ -516,8 +552,37 @@ int tx_destroy(tx_handle* h) {
 int tx_upload_walls(tx_handle* h, const double* walls) {
   if (!h || !walls) return TX_ERR_ARG;
   const long long N = h->g.n;
-  bool spec = false;
-  for (long long i = 0; i < N; ++i) spec = spec || specular_axis(walls[i], h->D) >= 0;
+  // codes on the device, into the staging area (the walls, then the new mask),
+  // so that a refused upload leaves the handle's walls as they were
+  double* dw = h->stage;
+  uint8_t* dmask = reinterpret_cast<uint8_t*>(h->stage + N);
+  unsigned* flags = reinterpret_cast<unsigned*>(h->red);
+  TX_CUDA(h, cudaMemcpyAsync(dw, walls, (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TX_CUDA(h, cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), h->stream));
+  k_wall_codes<<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(dw, N, h->p.nminerals, h->D, dmask, flags);
+  int rc0 = check_launch(h, "k_wall_codes");
+  if (rc0) return rc0;
+  unsigned fl[2] = {0u, 0u};
+  TX_CUDA(h, cudaMemcpyAsync(fl, flags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream));
+  rc0 = sync_stream(h);
+  if (rc0) return rc0;
+  if (fl[0]) return fail(h, TX_ERR_ARG, "wall codes must be 0 (pore) or positive");
+  const bool spec = fl[1] != 0;
+  if (!spec) {
+    TX_CUDA(h, cudaMemcpyAsync(h->mask, dmask, (size_t)N, cudaMemcpyDeviceToDevice, h->stream));
+    TX_CUDA(h, cudaMemcpyAsync(h->host_mask.data(), dmask, (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+    free_spec(h);
+    h->spec_walls.clear();
+    h->spec = false;
+    h->spec_fresh = 2;
+    int rc = update_links(h);
+    if (rc != TX_OK) return rc;
+    rc = count_rest_pairs(h);
+    if (rc != TX_OK) return rc;
+    h->have_walls = true;
+    return sync_stream(h);
+  }
+  // specular walls: codes and routes on the host
   if (spec && h->p.precision != TX_PREC_F64)
     return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 need the FP64 forms (precision TX_PREC_F64)");
   if (spec && h->NS > 0)
@@ -525,7 +590,7 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
-    if (!wall_code(walls[i], h->p.nminerals, &mask[(size_t)i], &why, spec)) return fail(h, TX_ERR_ARG, why);
+    if (!wall_code(walls[i], h->p.nminerals, &mask[(size_t)i], &why, h->D, spec)) return fail(h, TX_ERR_ARG, why);
   }
   if (spec) {
     std::vector<double> prev(walls, walls + N);
@@ -555,19 +620,19 @@ int tx_upload_state(tx_handle* h, const double* rho, const double* u) {
   if (!h || !rho) return TX_ERR_ARG;
   const long long N = h->g.n;
   const int S = h->S, D = h->D;
-  // rho - rho0: natural order (component fastest, the device layout too), zero on walls
-  std::vector<double> rt((size_t)N * S);
-  for (long long i = 0; i < N; ++i)
-    for (int m = 0; m < S; ++m)
-      rt[(size_t)(i * S + m)] = h->host_mask[(size_t)i] == 0 ? rho[i * S + m] - h->ph.rho0[m] : 0.0;
-  if (h->rho_bytes == 8) {
-    TX_CUDA(h, cudaMemcpyAsync(h->rho, rt.data(), rt.size() * 8, cudaMemcpyHostToDevice, h->stream));
-    TX_CUDA(h, cudaStreamSynchronize(h->stream));
-  } else {
-    std::vector<float> rf(rt.begin(), rt.end());
-    TX_CUDA(h, cudaMemcpyAsync(h->rho, rf.data(), rf.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    TX_CUDA(h, cudaStreamSynchronize(h->stream));
-  }
+  // rho - rho0 on the device: natural order (component fastest, the device
+  // layout too), zero on walls
+  TX_CUDA(h, cudaMemcpyAsync(h->stage, rho, (size_t)N * S * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  const unsigned grid = (unsigned)((N * S + 255) / 256);
+  if (h->rho_bytes == 8)
+    k_rho_from_natural<double><<<grid, 256, 0, h->stream>>>(h->stage, h->mask, N, S, shift_of(h->ph),
+                                                            static_cast<double*>(h->rho));
+  else
+    k_rho_from_natural<float><<<grid, 256, 0, h->stream>>>(h->stage, h->mask, N, S, shift_of(h->ph),
+                                                           static_cast<float*>(h->rho));
+  int rc0 = check_launch(h, "k_rho_from_natural");
+  if (rc0) return rc0;
+  TX_CUDA(h, cudaStreamSynchronize(h->stream));
   if (h->psi) {
     // psi(rho) of the initial density, for the forces of FlowFiInit
     std::vector<double> ps((size_t)N * S, 0.0);
@@ -807,10 +872,17 @@ int tx_delta_norm(tx_handle* h, int32_t field, double* norm) {
     old = fresh;
     TX_CUDA(h, cudaMemsetAsync(old, 0, (size_t)n * sizeof(double), h->stream));
   }
-  int rc = stage_field(h, field);
+  // In the FP64 form without face nodes that re-sum their density, the
+  // density field is the stored forcing density itself (zero on walls)
+  bool in_place = field == TX_FIELD_RHO && h->p.precision == TX_PREC_F64;
+  for (int f = 0; f < 6; ++f) in_place = in_place && !h->faces.on[f];
+  int rc = in_place ? TX_OK : stage_field(h, field);
   if (rc) return rc;
   TX_CUDA(h, cudaMemsetAsync(h->red, 0, 2 * sizeof(unsigned long long), h->stream));
-  k_delta_norm<<<1216, 256, 0, h->stream>>>(h->stage, old, n, h->red);
+  if (in_place)
+    k_delta_norm<<<1216, 256, 0, h->stream>>>(static_cast<const double*>(h->rho), old, n, h->red, h->mask, h->S);
+  else
+    k_delta_norm<<<1216, 256, 0, h->stream>>>(h->stage, old, n, h->red);
   rc = check_launch(h, "k_delta_norm");
   if (rc) return rc;
   unsigned long long r[2];

@@ -584,7 +584,7 @@ int tx_batch_add(tx_batch* b, const tx_params* p, const double* walls, const dou
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* w = nullptr;
-    if (!wall_code(walls[i], p->nminerals, &mask[(size_t)i], &w)) {
+    if (!wall_code(walls[i], p->nminerals, &mask[(size_t)i], &w, D)) {
       delete L;
       return bfail(b, TX_ERR_ARG, w);
     }

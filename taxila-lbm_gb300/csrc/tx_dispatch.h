@@ -136,10 +136,10 @@ inline Launch3 launch3(const Geo& g, int threads) {
       k_moments<D, S, ISO, EXACT, T, R, RT><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a, what, out);               \
     }                                                                                                         \
     static void to_nat(const void* f, const uint8_t* m, long long N, Shift sh, double* o, cudaStream_t s) {   \
-      k_pops_to_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, sh, o); \
+      k_pops_to_natural<D, S, T, R><<<grid_for(N, kNatTile), 256, 0, s>>>(reinterpret_cast<const T*>(f), m, N, sh, o); \
     }                                                                                                         \
     static void from_nat(const double* i, const uint8_t* m, long long N, Shift sh, void* f, cudaStream_t s) { \
-      k_pops_from_natural<D, S, T, R><<<grid_for(N, 256), 256, 0, s>>>(i, m, N, sh, reinterpret_cast<T*>(f)); \
+      k_pops_from_natural<D, S, T, R><<<grid_for(N, kNatTile), 256, 0, s>>>(i, m, N, sh, reinterpret_cast<T*>(f)); \
     }                                                                                                         \
     static void step_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {                \
       if constexpr (!EXACT) k_step_tiles<D, S, ISO, MRT, T, R, RT><<<grid, blk, 0, s>>>(b, flip);             \

@@ -376,9 +376,10 @@ inline void convert_species(const SpeciesPhysT<double>& a, SpeciesPhysT<R>* b) {
 // Reference wall value (lbm_walls.F90:151-177) -> device mask code:
 // 0 pore, 1..nminerals mineral, 255 any other wall (codes >= 998, unknown
 // minerals, and the specular codes 900-902 where the caller resolves their
-// routes: specular_ok).  Returns false, with the reason, for values the device
-// path rejects: negative or non-finite values, and specular codes elsewhere.
-inline bool wall_code(double v, int nminerals, uint8_t* code, const char** why, bool specular_ok = false) {
+// routes: specular_ok; 902 is a plain wall in 2D).  Returns false, with the
+// reason, for values the device path rejects: negative or non-finite values,
+// and specular codes elsewhere.
+inline bool wall_code(double v, int nminerals, uint8_t* code, const char** why, int D = 3, bool specular_ok = false) {
   if (v == 0.0) {
     *code = 0;
     return true;
@@ -387,12 +388,12 @@ inline bool wall_code(double v, int nminerals, uint8_t* code, const char** why, 
     *why = "wall codes must be 0 (pore) or positive";
     return false;
   }
-  if ((v == 900.0 || v == 901.0 || v == 902.0) && !specular_ok) {
+  if ((v == 900.0 || v == 901.0 || (v == 902.0 && D == 3)) && !specular_ok) {
     *why = "specular (no-stick) wall codes 900-902 need a single-lattice FP64 handle";
     return false;
   }
-  const int mineral = (int)v;
-  *code = (v < 998.0 && mineral >= 1 && mineral <= nminerals) ? (uint8_t)mineral : (uint8_t)255;
+  const int mineral = v < 998.0 ? (int)v : 0;
+  *code = (mineral >= 1 && mineral <= nminerals) ? (uint8_t)mineral : (uint8_t)255;
   return true;
 }
 

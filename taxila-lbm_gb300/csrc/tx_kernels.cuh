@@ -2223,9 +2223,31 @@ __device__ __forceinline__ void init_site(const StepArgs& a, int x, int y, int z
         feq_pf<D, n, EXACT, R>(P, m, rf[m], u, usqr, F[m], feq, pf);
         St<T>::st(fout + (long long)(m * Q + n) * N + idx, (R(1.) - R(0.5) * pf) * feq);
       });
+    } else if constexpr (!kShifted<T>) {
+      // FP64 fast form: (1 - P/2) feq_n = E_n (rho + 1.5 F.u - 1.5 F.c_n), with the
+      // pair weights E_n, E_n~ of step_site (two FMAs each)
+      const R WAu1 = P.WAc[m][1] - R(1.5 * L::w(1)) * usqr, WAu2 = P.WAc[m][2] - R(1.5 * L::w(Q - 1)) * usqr;
+      R Fu = R(-0.0), hF[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        Fu = Fu + F[m][d] * u[d];
+        hF[d] = R(1.5) * F[m][d];
+      }
+      const R Y = rf[m] + R(1.5) * Fu;
+      const R E0 = P.WAc[m][0] + (D == 3 ? R(-0.5) * usqr : R(-2.0 / 3.0) * usqr);
+      St<T>::st(fout + (long long)(m * Q) * N + idx, E0 * Y);
+      sfor<0, npairs<D>()>([&](auto pp) {
+        constexpr int n = pair_n<D>(decltype(pp)::value), nb = opp<D>(n);
+        constexpr double w = L::w(n);
+        const R t = cdot_z<D, n>(u), h = cdot_z<D, n>(hF);
+        const R WAu = n <= L::NAXIS ? WAu1 : WAu2;
+        const R En = t * (R(3 * w) + R(4.5 * w) * t) + WAu, Eb = WAu - t * (R(3 * w) - R(4.5 * w) * t);
+        St<T>::st(fout + (long long)(m * Q + n) * N + idx, En * (Y - h));
+        St<T>::st(fout + (long long)(m * Q + nb) * N + idx, Eb * (Y + h));
+      });
     } else {
-      // the fast forms: the deviation (1 - P/2) feq - w rho0 = dE_n - 1.5 E_n (F.c_n - F.u), as in
-      // step_site (rho0 = 0 and the deviation is f itself in the FP64 form)
+      // the FP32-arithmetic forms: the deviation (1 - P/2) feq - w rho0 = dE_n - 1.5 E_n (F.c_n - F.u),
+      // as in step_site
       const R A0 = P.A0[m], An = P.An[m];
       R Fu = R(0);
 #pragma unroll
@@ -2368,39 +2390,59 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
 // Natural-order populations <-> SoA state (the shift and the FP16 scale are
 // applied in FP64).  Wall cells read and write as zero; with mask = null
 // (lattices with specular walls, whose wall cells hold populations) every
-// cell's populations pass through.
+// cell's populations pass through.  A block moves kNatTile consecutive sites
+// through shared memory, so that both the SoA side (one row per population)
+// and the natural side (s*Q consecutive values per site) are read and written
+// in whole lines.
+constexpr int kNatTile = 64;
+
 template <int D, int S, class T, class R>
-__global__ void k_pops_to_natural(const T* f, const uint8_t* mask, long long N, Shift sh, double* out) {
-  constexpr int Q = Lat<D>::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= N) return;
-  const bool wall = mask && __ldg(mask + idx) != 0;
-  for (int n = 0; n < Q; ++n)
-    for (int m = 0; m < S; ++m) {
-      double v = 0.0;
-      if (!wall) {
-        v = double(St<T>::ld(f + (long long)(m * Q + n) * N + idx));
-        if constexpr (kShifted<T>) v = v / sh.scale + Lat<D>::w(n) * sh.rho0[m];
-      }
-      out[(idx * Q + n) * S + m] = v;
+__global__ void __launch_bounds__(256) k_pops_to_natural(const T* f, const uint8_t* mask, long long N, Shift sh,
+                                                         double* out) {
+  constexpr int Q = Lat<D>::Q, SQ = S * Q;
+  __shared__ double tile[kNatTile * SQ];
+  const long long c0 = (long long)blockIdx.x * kNatTile;
+  const int cnt = (int)(N - c0 < kNatTile ? N - c0 : kNatTile);
+  for (int i = threadIdx.x; i < SQ * kNatTile; i += blockDim.x) {
+    const int q = i / kNatTile, v = i - q * kNatTile;  // q = m * Q + n, the SoA row
+    if (v >= cnt) continue;
+    const long long idx = c0 + v;
+    const int m = q / Q, n = q - m * Q;
+    double x = 0.0;
+    if (!(mask && __ldg(mask + idx) != 0)) {
+      x = double(St<T>::ld(f + (long long)q * N + idx));
+      if constexpr (kShifted<T>) x = x / sh.scale + Lat<D>::w(n) * sh.rho0[m];
     }
+    tile[v * SQ + n * S + m] = x;
+  }
+  __syncthreads();
+  double* o = out + c0 * SQ;
+  for (int i = threadIdx.x; i < cnt * SQ; i += blockDim.x) o[i] = tile[i];
 }
 
 template <int D, int S, class T, class R>
-__global__ void k_pops_from_natural(const double* in, const uint8_t* mask, long long N, Shift sh, T* f) {
-  constexpr int Q = Lat<D>::Q;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= N) return;
-  const bool wall = mask && __ldg(mask + idx) != 0;
-  for (int n = 0; n < Q; ++n)
-    for (int m = 0; m < S; ++m) {
-      double v = wall ? 0.0 : in[(idx * Q + n) * S + m];
-      if constexpr (kShifted<T>) v = wall ? 0.0 : (v - Lat<D>::w(n) * sh.rho0[m]) * sh.scale;
-      if constexpr (std::is_same<T, double>::value)
-        f[(long long)(m * Q + n) * N + idx] = v;
-      else
-        St<T>::st(f + (long long)(m * Q + n) * N + idx, R(v));
-    }
+__global__ void __launch_bounds__(256) k_pops_from_natural(const double* in, const uint8_t* mask, long long N, Shift sh,
+                                                           T* f) {
+  constexpr int Q = Lat<D>::Q, SQ = S * Q;
+  __shared__ double tile[kNatTile * SQ];
+  const long long c0 = (long long)blockIdx.x * kNatTile;
+  const int cnt = (int)(N - c0 < kNatTile ? N - c0 : kNatTile);
+  const double* src = in + c0 * SQ;
+  for (int i = threadIdx.x; i < cnt * SQ; i += blockDim.x) tile[i] = src[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < SQ * kNatTile; i += blockDim.x) {
+    const int q = i / kNatTile, v = i - q * kNatTile;
+    if (v >= cnt) continue;
+    const long long idx = c0 + v;
+    const int m = q / Q, n = q - m * Q;
+    const bool wall = mask && __ldg(mask + idx) != 0;
+    double x = wall ? 0.0 : tile[v * SQ + n * S + m];
+    if constexpr (kShifted<T>) x = wall ? 0.0 : (x - Lat<D>::w(n) * sh.rho0[m]) * sh.scale;
+    if constexpr (std::is_same<T, double>::value)
+      f[(long long)q * N + idx] = x;
+    else
+      St<T>::st(f + (long long)q * N + idx, R(x));
+  }
 }
 
 }  // namespace tx

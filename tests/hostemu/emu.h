@@ -64,6 +64,40 @@ void launch1(long long n, int bs, F&& f) {
     }
 }
 
+// The library's natural-order conversions move tiles of sites through shared
+// memory with a barrier between the two halves, which a one-thread-at-a-time
+// walk cannot run; here they are plain loops with the same arithmetic (the GPU
+// tests compare every download of the kernels with the oracle).
+template <int D, int S, class T, class R>
+void pops_from_natural(const double* in, const uint8_t* mask, long long N, Shift sh, T* f) {
+  constexpr int Q = Lat<D>::Q;
+  for (long long idx = 0; idx < N; ++idx)
+    for (int n = 0; n < Q; ++n)
+      for (int m = 0; m < S; ++m) {
+        const bool wall = mask && mask[idx] != 0;
+        double x = wall ? 0.0 : in[(idx * Q + n) * S + m];
+        if constexpr (kShifted<T>) x = wall ? 0.0 : (x - Lat<D>::w(n) * sh.rho0[m]) * sh.scale;
+        if constexpr (std::is_same<T, double>::value)
+          f[(long long)(m * Q + n) * N + idx] = x;
+        else
+          St<T>::st(f + (long long)(m * Q + n) * N + idx, R(x));
+      }
+}
+template <int D, int S, class T, class R>
+void pops_to_natural(const T* f, const uint8_t* mask, long long N, Shift sh, double* out) {
+  constexpr int Q = Lat<D>::Q;
+  for (long long idx = 0; idx < N; ++idx)
+    for (int n = 0; n < Q; ++n)
+      for (int m = 0; m < S; ++m) {
+        double x = 0.0;
+        if (!(mask && mask[idx] != 0)) {
+          x = double(St<T>::ld(f + (long long)(m * Q + n) * N + idx));
+          if constexpr (kShifted<T>) x = x / sh.scale + Lat<D>::w(n) * sh.rho0[m];
+        }
+        out[(idx * Q + n) * S + m] = x;
+      }
+}
+
 template <int D, int S, int ISO, bool MRT, bool EXACT, class T, class R, class RT>
 std::string run(const Case& c, Result& out) {
   constexpr int Q = Lat<D>::Q;
@@ -92,7 +126,7 @@ std::string run(const Case& c, Result& out) {
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
-    if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why, spec)) return why;
+    if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why, D, spec)) return why;
   }
   SpecRoutes routes;
   if (spec) {
@@ -171,7 +205,7 @@ std::string run(const Case& c, Result& out) {
   }
   const Shift sh = shift_of(ph);
   if (c.from_fi) {
-    launch1(N, 256, [&] { k_pops_from_natural<D, S, T, R>(c.init.data(), pop_mask, N, sh, buf[cur]); });
+    pops_from_natural<D, S, T, R>(c.init.data(), pop_mask, N, sh, buf[cur]);
   } else {
     for (long long i = 0; i < N; ++i)
       for (int m = 0; m < S; ++m)
@@ -276,7 +310,7 @@ std::string run(const Case& c, Result& out) {
     launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 11, out.sflux.data()); });
   }
   out.fi.assign((size_t)N * S * Q, 0.0);
-  launch1(N, 256, [&] { k_pops_to_natural<D, S, T, R>(buf[cur], pop_mask, N, sh, out.fi.data()); });
+  pops_to_natural<D, S, T, R>(buf[cur], pop_mask, N, sh, out.fi.data());
   const StepArgs a = args(cur, cur);
   out.rho.assign((size_t)N * S, 0.0);
   out.flux.assign((size_t)N * S * D, 0.0);

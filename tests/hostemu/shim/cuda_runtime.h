@@ -1,8 +1,10 @@
 // Host stand-ins for the CUDA qualifiers and built-ins used by the flow
 // kernels (taxila-lbm_gb300/csrc/tx_kernels.cuh, tx_pair.cuh), so that the
 // kernels compile as plain C++ and run one thread at a time on the CPU.  The
-// kernels use no shared memory or barriers, so a sequential walk over the
-// launch grid computes what the device computes per thread.  The one warp
+// kernels the emulation launches use no shared memory or barriers, so a
+// sequential walk over the launch grid computes what the device computes per
+// thread (the natural-order conversions, which tile through shared memory,
+// are not launched here).  The one warp
 // vote (__all_sync, whether a whole warp takes the bounceback-free pushes of
 // the paired kernel) sees only the calling thread here: each thread then takes
 // that path when it alone qualifies, which the kernel must handle the same.
@@ -15,6 +17,10 @@
 #define __forceinline__ inline
 #define __noinline__ __attribute__((noinline))
 #define __launch_bounds__(...)
+// parsed only: a kernel that reaches a barrier cannot run one thread at a
+// time, so the emulation stops loudly if it ever launches one
+#define __shared__ static
+[[noreturn]] inline void __syncthreads() { __builtin_trap(); }
 
 struct dim3 {
   unsigned x, y, z;
