@@ -846,7 +846,12 @@ int tx_download(tx_handle* h, int32_t field, double* out) {
   if (dof < 0) return fail(h, TX_ERR_ARG, "unknown field");
   const long long N = h->g.n;
   if (field == TX_FIELD_WALLS) {
-    // the uploaded codes are kept on the host in mask form; report them as the reference walls vector
+    // the uploaded codes are kept on the host in mask form (with specular
+    // walls, as uploaded); report them as the reference walls vector
+    if (h->spec) {
+      std::memcpy(out, h->spec_walls.data(), (size_t)N * sizeof(double));
+      return TX_OK;
+    }
     for (long long i = 0; i < N; ++i) {
       const uint8_t c = h->host_mask[(size_t)i];
       out[i] = c == 255 ? 999.0 : (double)c;

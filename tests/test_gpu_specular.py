@@ -120,3 +120,11 @@ def test_specular_walls_refused_where_unsupported():
     with pytest.raises(TxError):
         b.add(p, walls, rho)
     b.close()
+
+
+def test_specular_walls_download_as_uploaded():
+    p, walls, _ = cases.SPECULAR[3][1]()
+    h = Handle(p)
+    h.upload_walls(walls)
+    assert np.array_equal(h.download(P.FIELD_WALLS), walls)
+    h.close()
