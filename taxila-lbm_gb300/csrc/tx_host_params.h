@@ -214,6 +214,9 @@ inline void fill_phys_impl(const tx_params& p, int D, int S, int Q, Phys& P) {
     for (int q = 0; q < 3; ++q)
       if (P.WAc[m][q] != P.WAc[0][q]) P.wa_shared = 0;
   P.ff_cross = S == 2 && P.c0g[0][0] == 0.0 && P.c0g[1][1] == 0.0;
+  P.mmot_shared = 1;
+  for (int m = 1; m < S; ++m)
+    if (P.mmot[m] != P.mmot[0]) P.mmot_shared = 0;
 }
 
 // Whether the fast MRT step needs its general rate path: some component has

@@ -108,6 +108,8 @@ struct PhysT {
   int wa_shared;
   // two components coupled only to each other (g_11 = g_22 = 0)
   int ff_cross;
+  // every component has the same mm s_c: it cancels from the common velocity
+  int mmot_shared;
 };
 using Phys = PhysT<double>;
 
@@ -132,7 +134,7 @@ inline void convert_phys(const PhysT<Src>& a, PhysT<R>* b) {
   cp(&a.WAc[0][0], &b->WAc[0][0], MAXC * 3); cp(a.keep, b->keep, MAXC); cp(a.kfac, b->kfac, MAXC);
   cp(&a.c0g[0][0], &b->c0g[0][0], MAXC * MAXC); cp(&a.ffwq[0][0], &b->ffwq[0][0], 36);
   b->ff_on = a.ff_on; b->fs_on = a.fs_on; b->body_on = a.body_on;
-  b->wa_shared = a.wa_shared; b->ff_cross = a.ff_cross;
+  b->wa_shared = a.wa_shared; b->ff_cross = a.ff_cross; b->mmot_shared = a.mmot_shared;
 }
 
 // Classes of the exterior BC kinds, as bc%flags holds them next to
@@ -735,9 +737,11 @@ __device__ __forceinline__ void cell_forces(const Hood<D, RCH>& h, uint32_t link
       // with two components coupled only to each other, the one cross term
       if (S == 2 && std::is_same<R, double>::value && P.ff_cross) {
 #pragma unroll
-        for (int d = 0; d < D; ++d)
+        for (int m = 0; m < S; ++m) {
+          const R fac = mult[m] * P.c0g[m][S - 1 - m];
 #pragma unroll
-          for (int m = 0; m < S; ++m) F[m][d] = F[m][d] - mult[m] * (P.c0g[m][S - 1 - m] * gr[S - 1 - m][d]);
+          for (int d = 0; d < D; ++d) F[m][d] = F[m][d] - fac * gr[S - 1 - m][d];
+        }
         return;
       }
 #pragma unroll
@@ -876,6 +880,22 @@ __device__ __forceinline__ R stress_form(const R a[D], const R b[D]) {
   return acc;
 }
 
+// sum_p c_n,d v_p over the direction pairs (v_p = f_n - f_opp(n) gives the flux)
+template <int D, class R>
+__device__ __forceinline__ void pair_axis_sums(const R v[npairs<D>()], R j[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) j[d] = R(-0.0);
+  sfor<0, npairs<D>()>([&](auto pp) {
+    constexpr int p = decltype(pp)::value, n = pair_n<D>(p);
+    sfor<0, D>([&](auto dd) {
+      constexpr int d = decltype(dd)::value;
+      constexpr int c = Lat<D>::c(n, d);
+      if constexpr (c == 1) j[d] = j[d] + v[p];
+      if constexpr (c == -1) j[d] = j[d] - v[p];
+    });
+  });
+}
+
 // Fast-form flux of one component from pair differences f_n - f_opp(n).
 template <int D, class R>
 __device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
@@ -1009,6 +1029,12 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
   {
     const bool dn = any_dirichlet<D>(a.g, a.faces, x, y, z);
     R jm[S][D];
+    // FP64 fast form with every component's mm s_c equal (P.mmot_shared): that
+    // factor cancels from the common velocity, u = (sum_m j_m + F_m / 2) / sum_m rho_m,
+    // and the components' pair differences are summed before the axis sums
+    constexpr bool kShare = !EXACT && !kShifted<T>;
+    const bool share = kShare && P.mmot_shared;
+    R jp[npairs<D>()];
 #pragma unroll
     for (int m = 0; m < S; ++m) {
       R f1[1][Q];
@@ -1019,12 +1045,36 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
       if constexpr (EXACT) {
 #pragma unroll
         for (int d = 0; d < D; ++d) jm[m][d] = pop_flux<D, 1, R>(f1, 0, d);
+      } else if constexpr (kShare) {
+        if (share) {
+          sfor<0, npairs<D>()>([&](auto pp) {
+            constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
+            const R dlt = f1[0][n] - f1[0][nb];
+            jp[p] = m == 0 ? dlt : jp[p] + dlt;
+          });
+        } else {
+          pop_flux_pairs<D, R>(f1[0], jm[m]);
+        }
       } else {
         pop_flux_pairs<D, R>(f1[0], jm[m]);
       }
       rcd[m] = dn ? pop_sum<D, 1, R>(f1, 0) : rfd[m];
       rc[m] = dn ? P.rho0[m] + rcd[m] : rf[m];
     }
+    if (share) {
+      R den = R(-0.0), J[D];
+#pragma unroll
+      for (int m = 0; m < S; ++m) den = den + rc[m];
+      const R inv = rcp_rn(den);
+      pair_axis_sums<D, R>(jp, J);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        R Fs = R(-0.0);
+#pragma unroll
+        for (int m = 0; m < S; ++m) Fs = Fs + F[m][d];
+        up[d] = (J[d] + R(.5) * Fs) * inv;
+      }
+    } else {
     R den = EXACT ? R(0) : R(-0.0);
 #pragma unroll
     for (int m = 0; m < S; ++m) den = den + rc[m] * R(P.mmot[m]);
@@ -1038,6 +1088,7 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
         up[d] = num / den;
       else
         up[d] = num * inv;
+    }
     }
   }
   R usqr = EXACT ? R(0) : R(-0.0);
