@@ -47,6 +47,7 @@ struct tx_handle {
   double* old_fi = nullptr;
   double* uic = nullptr;
   unsigned long long* red = nullptr;  // [0] max bits, [1] non-finite count
+  unsigned long long* red_host = nullptr;  // pinned copy of red (the per-step norm's read-back)
   double* cons = nullptr;     // conservation-sum partials and per-population totals (first tx_conservation)
   std::vector<uint8_t> host_mask;
   // specular walls (codes 900-902, FP64 forms): exceptions to the ordinary push
@@ -267,17 +268,35 @@ namespace {
 
 void fill_phys(tx_handle* h) { fill_phys_impl(h->p, h->D, h->S, h->Q, h->ph); }
 
-// mask (with dof values per cell): the field is read in place, and walls read as zero
+// max |(old - cur) / cur| over the field (DistributionCalcDeltaNorm), and old <- cur.
+// mask (with dof values per cell): the field is read in place, and walls read as zero.
+// The FP64 division runs only for values that may reach the thread's running
+// maximum: a single-precision screen (|old - cur| and |cur| rounded to float,
+// against the maximum less 2^-10, which covers the roundings) passes every
+// value that can, and every value whose magnitudes leave float's normal range
+// or whose running maximum lies outside [1e-30, 1e30]; so the result is the
+// exact maximum of the FP64 quotients.
 __global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red,
                              const uint8_t* mask = nullptr, int dof = 1) {
+  constexpr float kMin = 1.17549435e-38f, kMax = 3.40282347e38f;
   double mx = 0.0;
+  float thr = 0.f;  // float(mx) (1 - 2^-10), or 0 (screen off)
   unsigned long long bad = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double c = mask && mask[i / dof] != 0 ? 0.0 : cur[i];
     if (!isfinite(c)) ++bad;
-    const double v = c != 0.0 ? fabs((old[i] - c) / c) : 0.0;
-    if (v > mx) mx = v;
+    const double o = old[i];
     old[i] = c;
+    if (c == 0.0) continue;
+    const double a = fabs(o - c), b = fabs(c);
+    if (a == 0.0) continue;  // a zero quotient never raises the maximum
+    const float af = (float)a, bf = (float)b;
+    if ((af >= kMin && af <= kMax) && (bf >= kMin && bf <= kMax) && !(af > thr * bf)) continue;
+    const double v = a / b;  // NaN (a NaN input) never raises it either
+    if (v > mx) {
+      mx = v;
+      thr = (mx >= 1e-30 && mx < 1e30) ? (float)mx * (1.f - 0.0009765625f) : 0.f;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -454,6 +473,7 @@ int tx_create(const tx_params* p, tx_handle** out) {
       cudaMalloc(&h->mask, (size_t)N) != cudaSuccess || cudaMalloc(&h->links, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&h->stage, stageb) != cudaSuccess ||
       cudaMalloc(&h->red, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&h->red_host, 2 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&h->d_phys, sizeof(Phys)) != cudaSuccess ||
       cudaMalloc(&h->d_phys32, sizeof(PhysT<float>)) != cudaSuccess)
     return cleanup("device allocation failed", TX_ERR_NOMEM);
@@ -537,6 +557,7 @@ int tx_destroy(tx_handle* h) {
   cudaFree(h->old_fi);
   cudaFree(h->uic);
   cudaFree(h->red);
+  cudaFreeHost(h->red_host);
   cudaFree(h->cons);
   free_spec(h);
   cudaFree(h->d_phys);
@@ -890,8 +911,8 @@ int tx_delta_norm(tx_handle* h, int32_t field, double* norm) {
     k_delta_norm<<<1216, 256, 0, h->stream>>>(h->stage, old, n, h->red);
   rc = check_launch(h, "k_delta_norm");
   if (rc) return rc;
-  unsigned long long r[2];
-  TX_CUDA(h, cudaMemcpyAsync(r, h->red, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long* r = h->red_host;
+  TX_CUDA(h, cudaMemcpyAsync(r, h->red, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   rc = sync_stream(h);
   if (rc) return rc;
   double v;

@@ -137,12 +137,18 @@ def test_diagnostics_match_oracle():
         assert np.array_equal(a, b), f
 
 
-def test_delta_norm_matches_oracle():
-    p, walls, rho = cases.sc_bubble(P.D2Q9, (1, 32, 32), P.SRT, 4)
+@pytest.mark.parametrize("make", [lambda: cases.sc_bubble(P.D2Q9, (1, 32, 32), P.SRT, 4),
+                                  lambda: cases.sc_bubble(P.D3Q19, (12, 14, 16), P.MRT, 4),
+                                  lambda: cases.porous_case(P.D3Q19, (10, 12, 14), mode=P.MRT, body=True)],
+                         ids=["d2_periodic", "d3_periodic", "d3_porous_density_faces"])
+def test_delta_norm_matches_oracle(make):
+    # periodic lattices read the density in place, density faces stage it; both
+    # screen the FP64 divisions and must return the oracle's norm bit for bit
+    p, walls, rho = make()
     o, h = run_pair(p, walls, rho, 0, exact=True)
-    for _ in range(4):
-        o.step(2)
-        h.step(2)
+    for k in range(6):
+        o.step(1 + k % 2)
+        h.step(1 + k % 2)
         assert o.delta_norm(P.FIELD_RHO) == h.delta_norm(P.FIELD_RHO)
         assert o.delta_norm(P.FIELD_FI) == h.delta_norm(P.FIELD_FI)
 
@@ -162,3 +168,26 @@ def test_errors_are_status_codes():
     w[3] = -1.0
     with pytest.raises(TxError):
         h.upload_walls(w)
+
+
+def test_refused_wall_codes_leave_the_walls():
+    # wall codes are converted on the device; a refused upload (negative, NaN,
+    # infinite) changes nothing, and the next run equals the oracle
+    p, walls, rho = cases.porous_case(P.D3Q19, (10, 12, 8), body=True)
+    o, h = run_pair(p, walls, rho, 0, exact=True)
+    for bad in (-1.0, float("nan"), float("inf"), -float("inf")):
+        w = np.array(walls, dtype=np.float64)
+        w[17] = bad
+        with pytest.raises(TxError) as e:
+            h.upload_walls(w)
+        assert e.value.code == 1
+        assert np.array_equal(h.download(P.FIELD_WALLS), np.where(walls >= 998.0, 999.0, walls))
+    h.step(5)
+    o.step(5)
+    compare(o, h, p, walls, exact=True)
+    # an unknown mineral or a code at or above 998 is a plain wall
+    w = np.array(walls, dtype=np.float64)
+    w[w == 2.0] = 7.0
+    w[w == 1.0] = 1e300
+    h.upload_walls(w)
+    assert set(np.unique(h.download(P.FIELD_WALLS))) <= {0.0, 999.0}
