@@ -54,15 +54,16 @@ int static_fail(int code, const std::string& msg) {
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-// walls (reference codes, natural order) -> mask; records the first bad code
-__global__ void k_static_mask(const double* walls, long long n, int nminerals, uint8_t* mask, unsigned* bad) {
+// walls (reference codes, natural order) -> mask; records a bad code (the
+// specular codes too: 900, 901 and, in 3D, 902; in 2D 902 is a plain wall)
+__global__ void k_static_mask(const double* walls, long long n, int nminerals, int D, uint8_t* mask, unsigned* bad) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double v = walls[i];
   uint8_t code;
   if (v == 0.0) {
     code = 0;
-  } else if (!(v > 0.0) || v == 900.0 || v == 901.0 || v == 902.0 || !isfinite(v)) {
+  } else if (!(v > 0.0) || v == 900.0 || v == 901.0 || (v == 902.0 && D == 3) || !isfinite(v)) {
     atomicOr(bad, 1u);
     code = 255;
   } else {
@@ -184,7 +185,7 @@ extern "C" int tx_step_static(const tx_params* p, const double* walls, const dou
   TX_SCHK(cudaMemsetAsync(flag, 0, sizeof(unsigned), st));
   TX_SCHK(cudaMemsetAsync(rho, 0, (size_t)N * S * sizeof(double), st));
   TX_SCHK(cudaMemsetAsync(pb, 0, pop_bytes, st));
-  k_static_mask<<<grid_for(N, 256), 256, 0, st>>>(walls, N, p->nminerals, mask, flag);
+  k_static_mask<<<grid_for(N, 256), 256, 0, st>>>(walls, N, p->nminerals, D, mask, flag);
   {
     const Launch3 l = launch3(g, 256);
     if (D == 3)
