@@ -268,36 +268,20 @@ namespace {
 
 void fill_phys(tx_handle* h) { fill_phys_impl(h->p, h->D, h->S, h->Q, h->ph); }
 
-// max |(old - cur) / cur| over the field (DistributionCalcDeltaNorm), and old <- cur.
-// mask (with dof values per cell): the field is read in place, and walls read as zero.
-// The FP64 division runs only for values that may reach the thread's running
-// maximum: a single-precision screen (|old - cur| and |cur| rounded to float,
-// against the maximum less 2^-10, which covers the roundings) passes every
-// value that can, and every value whose magnitudes leave float's normal range
-// or whose running maximum lies outside [1e-30, 1e30]; so the result is the
-// exact maximum of the FP64 quotients.
+// max |(old - cur) / cur| over the field (DistributionCalcDeltaNorm), and old <- cur
+// (NormMax screens the FP64 divisions).  mask (with dof values per cell): the
+// field is read in place, and walls read as zero.
 __global__ void k_delta_norm(const double* cur, double* old, long long n, unsigned long long* red,
                              const uint8_t* mask = nullptr, int dof = 1) {
-  constexpr float kMin = 1.17549435e-38f, kMax = 3.40282347e38f;
-  double mx = 0.0;
-  float thr = 0.f;  // float(mx) (1 - 2^-10), or 0 (screen off)
+  NormMax acc;
   unsigned long long bad = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double c = mask && mask[i / dof] != 0 ? 0.0 : cur[i];
     if (!isfinite(c)) ++bad;
-    const double o = old[i];
+    acc.add(old[i], c);
     old[i] = c;
-    if (c == 0.0) continue;
-    const double a = fabs(o - c), b = fabs(c);
-    if (a == 0.0) continue;  // a zero quotient never raises the maximum
-    const float af = (float)a, bf = (float)b;
-    if ((af >= kMin && af <= kMax) && (bf >= kMin && bf <= kMax) && !(af > thr * bf)) continue;
-    const double v = a / b;  // NaN (a NaN input) never raises it either
-    if (v > mx) {
-      mx = v;
-      thr = (mx >= 1e-30 && mx < 1e30) ? (float)mx * (1.f - 0.0009765625f) : 0.f;
-    }
   }
+  double mx = acc.mx;
   for (int o = 16; o > 0; o >>= 1) {
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     bad += __shfl_xor_sync(0xffffffffu, bad, o);

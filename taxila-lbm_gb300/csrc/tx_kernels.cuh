@@ -2438,6 +2438,31 @@ __global__ void __launch_bounds__(128) k_moments(StepArgs a_in, int what, double
   moments_site<D, S, ISO, EXACT, T, R, RT>(a, x, y, z, what, out);
 }
 
+// Running maximum of |(old - cur) / cur| (DistributionCalcDeltaNorm) over a
+// sequence of values, with the FP64 division only for values that may reach
+// it: a single-precision screen (|old - cur| and |cur| rounded to float,
+// against the maximum less 2^-10, which covers the roundings) passes every
+// value that can, and every value whose magnitudes leave float's normal range
+// or whose running maximum lies outside [1e-30, 1e30].  The result is the
+// exact maximum of the FP64 quotients; zero and NaN quotients never raise it.
+struct NormMax {
+  double mx = 0.0;
+  float thr = 0.f;  // float(mx) (1 - 2^-10), or 0 (screen off)
+  __host__ __device__ __forceinline__ void add(double o, double c) {
+    constexpr float kMin = 1.17549435e-38f, kMax = 3.40282347e38f;
+    if (c == 0.0) return;
+    const double a = fabs(o - c), b = fabs(c);
+    if (a == 0.0) return;
+    const float af = (float)a, bf = (float)b;
+    if ((af >= kMin && af <= kMax) && (bf >= kMin && bf <= kMax) && !(af > thr * bf)) return;
+    const double v = a / b;
+    if (v > mx) {
+      mx = v;
+      thr = (mx >= 1e-30 && mx < 1e30) ? (float)mx * (1.f - 0.0009765625f) : 0.f;
+    }
+  }
+};
+
 // Natural-order populations <-> SoA state (the shift and the FP16 scale are
 // applied in FP64).  Wall cells read and write as zero; with mask = null
 // (lattices with specular walls, whose wall cells hold populations) every

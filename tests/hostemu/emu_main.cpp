@@ -7,7 +7,11 @@
 //             species gi [N*ns*Q] | concentration [N*ns] | flux [N*D*ns], f64
 // Exit status 0 on success, 2 for parameters the library rejects (message on
 // stderr), 3 when the combination is not compiled into the emulation.
+#include <cmath>
 #include <cstdio>
+#include <cstring>
+#include <limits>
+#include <random>
 
 #include "emu.h"
 
@@ -15,7 +19,54 @@ using namespace emu;
 
 static bool read_all(FILE* f, void* p, size_t bytes) { return fread(p, 1, bytes, f) == bytes; }
 
+// emu norm: NormMax (the delta norm's screened running maximum) against the
+// plain maximum of every FP64 quotient, on seeded sequences that mix ordinary
+// values with zeros, ties, tiny and huge magnitudes, subnormals, NaN and inf.
+static int norm_selftest() {
+  std::mt19937_64 g(12345);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::uniform_int_distribution<int> e(-320, 300), pick(0, 15);
+  const double inf = std::numeric_limits<double>::infinity(), qnan = std::numeric_limits<double>::quiet_NaN();
+  int bad = 0;
+  for (int trial = 0; trial < 4000; ++trial) {
+    const int n = 1 + (int)(g() % 400);
+    const int mode = trial % 4;
+    NormMax acc;
+    double ref = 0.0;
+    for (int i = 0; i < n; ++i) {
+      double c, o;
+      const int k = pick(g);
+      if (mode == 0) {  // a converging field: relative changes around 1e-7 .. 1e-3
+        c = 1.0 + u(g);
+        o = c * (1.0 + u(g) * std::pow(10.0, -3 - (int)(g() % 5)));
+      } else if (mode == 1) {  // magnitudes over the whole double range
+        c = u(g) * std::ldexp(1.0, e(g));
+        o = u(g) * std::ldexp(1.0, e(g));
+      } else if (mode == 2) {  // near-ties of the quotient
+        c = 1.0 + u(g);
+        o = c * (1.0 + 1e-6 * (1.0 + 1e-9 * u(g)));
+      } else {  // specials
+        c = k == 0 ? 0.0 : k == 1 ? qnan : k == 2 ? inf : k == 3 ? 4.9e-324 : k == 4 ? 1e-310 : u(g) * 1e-30;
+        o = k == 5 ? c : k == 6 ? qnan : k == 7 ? -inf : k == 8 ? 1e308 : u(g);
+      }
+      acc.add(o, c);
+      const double v = c != 0.0 ? std::fabs((o - c) / c) : 0.0;
+      if (v > ref) ref = v;
+    }
+    uint64_t a, b;
+    std::memcpy(&a, &acc.mx, 8);
+    std::memcpy(&b, &ref, 8);
+    if (a != b) {
+      if (bad < 5) fprintf(stderr, "trial %d mode %d: screened %.17g, plain %.17g\n", trial, mode, acc.mx, ref);
+      ++bad;
+    }
+  }
+  if (bad) fprintf(stderr, "%d of 4000 sequences differ\n", bad);
+  return bad ? 1 : 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 2 && std::strcmp(argv[1], "norm") == 0) return norm_selftest();
   if (argc != 3) {
     fprintf(stderr, "usage: emu case.bin result.bin\n");
     return 1;

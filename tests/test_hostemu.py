@@ -306,3 +306,12 @@ def test_emulated_specular_walls_need_fp64(emu_exe, tmp_path):
         f.write(np.ascontiguousarray(rho, dtype=np.float64).tobytes())
     r = subprocess.run([emu_exe, case, case + ".out"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 2 and "FP64" in r.stderr
+
+
+def test_delta_norm_screen_is_exact(emu_exe):
+    # the delta norm divides in FP64 only where a single-precision screen says
+    # the quotient may reach the running maximum; on sequences of ordinary,
+    # near-tied, extreme and special values the result equals the plain
+    # maximum of every FP64 quotient bit for bit
+    r = subprocess.run([emu_exe, "norm"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
