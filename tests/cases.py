@@ -339,3 +339,18 @@ SPECULAR = [
     ("d3_porous_mrt_iso8_dirichlet", lambda: specular_porous(P.D3Q19, (12, 10, 11), 8), 30),
     ("d2_porous_mrt_iso10_dirichlet", lambda: specular_porous(P.D2Q9, (1, 22, 18), 10), 8),
 ]
+
+
+def with_specular(make, seed=5):
+    """A case factory whose wall cells turn half into specular walls."""
+    def made():
+        p, walls, rho = make()
+        rng = np.random.default_rng(seed)
+        codes = [900.0, 901.0, 902.0] if p.ndims == 3 else [900.0, 901.0]
+        pick = (walls > 0) & (rng.random(p.nsites) < 0.5)
+        return p, np.where(pick, rng.choice(codes, size=p.nsites), walls), rho
+    return made
+
+
+# (name, case factory, steps): every exterior BC kind with specular walls among the grains
+SPECULAR_BCS = [(name, with_specular(make), steps) for name, make, steps in BCS]

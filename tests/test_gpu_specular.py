@@ -77,6 +77,13 @@ def test_specular_walls_match_oracle(name, make, steps, exact):
         assert (a == b) if exact else abs(a - b) <= 1e-10 * max(abs(a), 1e-300), (field, a, b)
 
 
+@pytest.mark.parametrize("name,make,steps", cases.SPECULAR_BCS, ids=[c[0] for c in cases.SPECULAR_BCS])
+def test_specular_walls_with_exterior_bcs(name, make, steps):
+    p, walls, rho = make()
+    o, h = run_pair(p, walls, rho, steps, True)
+    compare_all_cells(o, h, True)
+
+
 def test_specular_restart_with_wall_content():
     p, walls, rho = cases.specular_porous(P.D3Q19, (12, 10, 11), 8)
     o0 = Oracle(p)

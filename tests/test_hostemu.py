@@ -315,3 +315,15 @@ def test_delta_norm_screen_is_exact(emu_exe):
     # maximum of every FP64 quotient bit for bit
     r = subprocess.run([emu_exe, "norm"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("name,make,steps", cases.SPECULAR_BCS, ids=[c[0] for c in cases.SPECULAR_BCS])
+def test_emulated_specular_walls_with_exterior_bcs(emu_exe, tmp_path, name, make, steps):
+    # specular walls next to every exterior BC kind: the faces' pre-stream
+    # copies and corrections act on the populations the sweep leaves
+    p, walls, rho = make()
+    ref = oracle_run(p, walls, rho, steps)
+    q = P.copy_params(p)
+    q.exact = 1
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path)
+    compare_all_cells(ref, got, 0.0)
