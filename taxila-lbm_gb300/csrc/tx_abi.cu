@@ -275,8 +275,10 @@ __global__ void k_delta_norm(const double* cur, double* old, long long n, unsign
                              const uint8_t* mask = nullptr, int dof = 1) {
   NormMax acc;
   unsigned long long bad = 0;
+  const bool small = n <= 0xffffffffLL;  // the cell index by a 32-bit division
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double c = mask && mask[i / dof] != 0 ? 0.0 : cur[i];
+    const long long cell = !mask ? 0 : small ? (long long)((unsigned)i / (unsigned)dof) : i / dof;
+    const double c = mask && mask[cell] != 0 ? 0.0 : cur[i];
     if (!isfinite(c)) ++bad;
     acc.add(old[i], c);
     old[i] = c;
