@@ -79,9 +79,11 @@ def test_specular_walls_match_oracle(name, make, steps, exact):
 
 @pytest.mark.parametrize("name,make,steps", cases.SPECULAR_BCS, ids=[c[0] for c in cases.SPECULAR_BCS])
 def test_specular_walls_with_exterior_bcs(name, make, steps):
+    # bit for bit, except where an equation of state calls exp (the device's
+    # and the host libm's may differ by an ulp): there within 1e-12
     p, walls, rho = make()
     o, h = run_pair(p, walls, rho, steps, True)
-    compare_all_cells(o, h, True)
+    compare_all_cells(o, h, not p.use_nonideal_eos)
 
 
 def test_specular_restart_with_wall_content():
