@@ -59,6 +59,7 @@ struct tx_handle {
   long long* spec_src = nullptr;
   double* spec_tmp = nullptr;
   int spec_fresh = 0;              // steps whose output buffer still needs its wall slots cleared
+  int spec_fresh_sp = 0;           // the same for the species buffers
   // passive species (transport): populations, parameters, initial state
   int NS = 0;
   SpeciesSet ss{};
@@ -130,7 +131,7 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
     h->spec_dst = d;
     TX_CUDA(h, cudaMalloc(&s, (size_t)ne * sizeof(long long)));
     h->spec_src = s;
-    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * h->S * sizeof(double)));
+    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * (h->S > h->NS ? h->S : h->NS) * sizeof(double)));
     h->spec_tmp = t;
     TX_CUDA(h, cudaMemcpy(h->spec_dst, r.dst.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
     TX_CUDA(h, cudaMemcpy(h->spec_src, r.src.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
@@ -140,23 +141,29 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
 }
 
 // After the step kernels (push with ordinary bounceback), before the density
-// pass: the specular-wall exceptions.  The output buffer's wall slots are
-// cleared on the first two steps after an upload or init, so that wall slots
-// no exception writes hold zero in both state buffers.
-void spec_pass(tx_handle* h, int in, int out) {
-  double* fo = static_cast<double*>(h->f[out]);
+// pass: the specular-wall exceptions, for the ncomp components of state
+// buffers fin -> fout (the flow's, or the species', which stream and bounce
+// back alike).  The output buffer's wall slots are cleared on the first two
+// steps after an upload or init (fresh), so that wall slots no exception
+// writes hold zero in both state buffers.
+void spec_apply(tx_handle* h, const void* fin, void* fout, int ncomp, int& fresh) {
+  double* fo = static_cast<double*>(fout);
   const long long N = h->g.n;
-  if (h->spec_fresh > 0) {
-    k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, h->S * h->Q);
-    --h->spec_fresh;
+  if (fresh > 0) {
+    k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, ncomp * h->Q);
+    --fresh;
   }
   const long long ne = h->spec_n;
   if (ne == 0) return;
   const unsigned grid = (unsigned)((ne + 255) / 256);
   const long long QN = (long long)h->Q * N;
-  k_spec_gather<double><<<grid, 256, 0, h->stream>>>(static_cast<const double*>(h->f[in]), fo, h->spec_src, ne, h->S, QN,
+  k_spec_gather<double><<<grid, 256, 0, h->stream>>>(static_cast<const double*>(fin), fo, h->spec_src, ne, ncomp, QN,
                                                      h->spec_tmp);
-  k_spec_scatter<double><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, h->S, QN, h->spec_tmp);
+  k_spec_scatter<double><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, ncomp, QN, h->spec_tmp);
+}
+void spec_pass(tx_handle* h, int in, int out) { spec_apply(h, h->f[in], h->f[out], h->S, h->spec_fresh); }
+void spec_pass_species(tx_handle* h, int in, int out) {
+  spec_apply(h, h->sg[in], h->sg[out], h->NS, h->spec_fresh_sp);
 }
 
 // Reference wall values -> device mask codes on the device (the rules of
@@ -343,7 +350,9 @@ SpeciesArgs species_args(tx_handle* h, int in, int out) {
 int stage_field(tx_handle* h, int field) {
   const long long N = h->g.n;
   if (field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) {
-    h->ss.fields(species_args(h, h->gcur, h->gcur), field, h->stage, h->stream);
+    SpeciesArgs sa = species_args(h, h->gcur, h->gcur);
+    if (h->spec && field == TX_FIELD_SPECIES_FI) sa.mask = nullptr;  // wall cells' populations too
+    h->ss.fields(sa, field, h->stage, h->stream);
   } else if (field == TX_FIELD_FI) {
     h->ks.to_natural(h->f[h->cur], pop_mask(h), N, shift_of(h->ph), h->stage, h->stream);
   } else if (field == TX_FIELD_WALLS) {
@@ -581,7 +590,7 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
     free_spec(h);
     h->spec_walls.clear();
     h->spec = false;
-    h->spec_fresh = 2;
+    h->spec_fresh = h->spec_fresh_sp = 2;
     int rc = update_links(h);
     if (rc != TX_OK) return rc;
     rc = count_rest_pairs(h);
@@ -592,8 +601,10 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
   // specular walls: codes and routes on the host
   if (spec && h->p.precision != TX_PREC_F64)
     return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 need the FP64 forms (precision TX_PREC_F64)");
-  if (spec && h->NS > 0)
-    return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 are not supported with species transport");
+  if (spec && h->NS > 0 && h->D == 2)
+    return fail(h, TX_ERR_ARG,
+                "specular (no-stick) wall codes 900-901 are not supported with species transport in 2D "
+                "(the reference's 2D transport collides wall cells)");
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
@@ -612,7 +623,7 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
     h->spec_walls.clear();
   }
   h->spec = spec;
-  h->spec_fresh = 2;
+  h->spec_fresh = h->spec_fresh_sp = 2;
   h->host_mask.swap(mask);
   TX_CUDA(h, cudaMemcpyAsync(h->mask, h->host_mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
   int rc = update_links(h);
@@ -754,7 +765,7 @@ int tx_init(tx_handle* h) {
     int rc = check_launch(h, "k_init");
     if (rc) return rc;
   }
-  h->spec_fresh = 2;
+  h->spec_fresh = h->spec_fresh_sp = 2;
   // FlowUpdateMoments: the forcing density is the plain population sum
   h->ks.density(args(h, h->cur, h->cur), 1, h->stream);
   int rc = check_launch(h, "k_density");
@@ -801,6 +812,7 @@ int tx_step(tx_handle* h, int32_t nsteps) {
     if (h->timing) cudaEventRecord(h->ev[2], h->stream);
     if (h->NS > 0 && h->have_species) {
       h->ss.step(species_args(h, h->gcur, 1 - h->gcur), h->stream);
+      if (h->spec) spec_pass_species(h, h->gcur, 1 - h->gcur);
       h->gcur = 1 - h->gcur;
     }
     int rc = check_launch(h, "k_step/k_density");
@@ -829,6 +841,7 @@ int tx_step_species(tx_handle* h, int32_t nsteps) {
   for (int t = 0; t < nsteps; ++t) {
     // the species part of tx_step alone: the flow state and its step count stay as they are
     h->ss.step(species_args(h, h->gcur, 1 - h->gcur), h->stream);
+    if (h->spec) spec_pass_species(h, h->gcur, 1 - h->gcur);
     h->gcur = 1 - h->gcur;
     const int rc = check_launch(h, "k_species");
     if (rc) return rc;

@@ -260,7 +260,9 @@ __global__ void __launch_bounds__(128) k_species_init(SpeciesArgs a_in, const do
 }
 
 // Species fields in natural order: what 9 populations, 10 concentration,
-// 11 flux (zero on walls, as TransportUpdateMoments).
+// 11 flux (zero on walls, as TransportUpdateMoments).  With a.mask null every
+// cell's populations are read (wall cells hold populations next to specular
+// walls); the moments need the mask.
 template <int D, class T, class R>
 __global__ void __launch_bounds__(128) k_species_fields(SpeciesArgs a_in, int what, double* out) {
   using L = Lat<D>;
@@ -270,7 +272,7 @@ __global__ void __launch_bounds__(128) k_species_fields(SpeciesArgs a_in, int wh
   int x, y, z;
   long long idx;
   if (!site_of(a.g, x, y, z, idx)) return;
-  const bool pore = __ldg(a.mask + idx) == 0;
+  const bool pore = !a.mask || __ldg(a.mask + idx) == 0;
   const T* gin = reinterpret_cast<const T*>(a.gin);
   const int ns = a.ns;
   for (int s = 0; s < ns; ++s) {

@@ -354,3 +354,18 @@ def with_specular(make, seed=5):
 
 # (name, case factory, steps): every exterior BC kind with specular walls among the grains
 SPECULAR_BCS = [(name, with_specular(make), steps) for name, make, steps in BCS]
+
+
+def _sp_specular(make, mode, ns=1, seed=6):
+    """_sp with half of the wall cells specular (3D: the species stream and
+    bounce back through the same sweep)."""
+    def f():
+        p, w, r = with_specular(make, seed)()
+        return p, w, r, with_species(p, w, mode=mode, ns=ns)
+    return f
+
+
+SPECIES_SPECULAR = [
+    ("d3_srt_species_specular", _sp_specular(lambda: porous_case(P.D3Q19, (12, 10, 14), body=True), P.SRT), 20),
+    ("d3_mrt_two_species_specular", _sp_specular(lambda: porous_case(P.D3Q19, (10, 12, 12), mode=P.MRT), P.MRT, ns=2), 15),
+]

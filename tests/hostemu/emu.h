@@ -118,11 +118,11 @@ std::string run(const Case& c, Result& out) {
   else
     convert_phys(ph, &P);
 
-  // specular walls: single-lattice FP64 handles without species (as tx_upload_walls)
+  // specular walls: single-lattice FP64 handles, species only in 3D (as tx_upload_walls)
   bool spec = false;
   for (long long i = 0; i < N; ++i) spec = spec || specular_axis(c.walls[(size_t)i], D) >= 0;
-  if (spec && (!std::is_same<T, double>::value || p.nspecies > 0))
-    return "specular (no-stick) wall codes 900-902 need the FP64 forms and no species";
+  if (spec && (!std::is_same<T, double>::value || (p.nspecies > 0 && D == 2)))
+    return "specular (no-stick) wall codes 900-902 need the FP64 forms (and no species in 2D)";
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
@@ -149,7 +149,7 @@ std::string run(const Case& c, Result& out) {
   const long long ne = (long long)routes.dst.size();
   std::vector<double> spec_tmp((size_t)(ne * S + 1));
   const uint8_t* pop_mask = spec ? nullptr : mask.data();
-  int spec_fresh = 2;
+  int spec_fresh = 2, spec_fresh_sp = 2;
   std::vector<uint32_t> links((size_t)N);
   launch3(g, 256, [&] { k_links<D>(mask.data(), g, links.data()); });
 
@@ -297,6 +297,21 @@ std::string run(const Case& c, Result& out) {
         launch3(g, 128, [&] { k_species<D, true, EXACT, T, R>(sa); });
       else
         launch3(g, 128, [&] { k_species<D, false, EXACT, T, R>(sa); });
+      if constexpr (std::is_same<T, double>::value) {
+        if (spec) {
+          // the species stream and bounce back as the flow does: the same exceptions
+          double* go = gbuf[1 - gcur];
+          if (spec_fresh_sp > 0) {
+            launch1(N, 256, [&] { k_spec_clear_walls<double>(go, mask.data(), N, NS * Q); });
+            --spec_fresh_sp;
+          }
+          if (ne) {
+            std::vector<double> stmp((size_t)(ne * NS + 1));
+            launch1(ne, 256, [&] { k_spec_gather<double>(gbuf[gcur], go, routes.src.data(), ne, NS, (long long)Q * N, stmp.data()); });
+            launch1(ne, 256, [&] { k_spec_scatter<double>(go, routes.dst.data(), ne, NS, (long long)Q * N, stmp.data()); });
+          }
+        }
+      }
       gcur = 1 - gcur;
     }
   }
@@ -305,7 +320,9 @@ std::string run(const Case& c, Result& out) {
     out.sfi.assign((size_t)N * NS * Q, 0.0);
     out.srho.assign((size_t)N * NS, 0.0);
     out.sflux.assign((size_t)N * NS * D, 0.0);
-    launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 9, out.sfi.data()); });
+    SpeciesArgs sa9 = sa;
+    if (spec) sa9.mask = nullptr;  // wall cells' populations too
+    launch3(g, 128, [&] { k_species_fields<D, T, R>(sa9, 9, out.sfi.data()); });
     launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 10, out.srho.data()); });
     launch3(g, 128, [&] { k_species_fields<D, T, R>(sa, 11, out.sflux.data()); });
   }

@@ -86,6 +86,32 @@ def test_specular_walls_with_exterior_bcs(name, make, steps):
     compare_all_cells(o, h, not p.use_nonideal_eos)
 
 
+@pytest.mark.parametrize("name,make,steps", cases.SPECIES_SPECULAR, ids=[c[0] for c in cases.SPECIES_SPECULAR])
+def test_species_with_specular_walls(name, make, steps):
+    # 3D species stream and bounce back through the same sweep as the flow
+    p, walls, rho, conc = make()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.set_species(conc)
+    o.init()
+    o.step(steps)
+    q = P.copy_params(p)
+    q.exact = 1
+    h = Handle(q)
+    h.upload_walls(walls)
+    h.upload_state(rho)
+    h.upload_species(conc)
+    h.init()
+    h.step(steps)
+    for f in (P.FIELD_FI, P.FIELD_SPECIES_FI, P.FIELD_SPECIES_RHO, P.FIELD_SPECIES_FLUX):
+        a, b = o.get(f), h.download(f)
+        assert np.all(np.isfinite(a)), f
+        assert np.array_equal(a, b), (f, int(np.sum(a != b)))
+    h.close()
+    o.close()
+
+
 def test_specular_restart_with_wall_content():
     p, walls, rho = cases.specular_porous(P.D3Q19, (12, 10, 11), 8)
     o0 = Oracle(p)
@@ -122,6 +148,13 @@ def test_specular_walls_refused_where_unsupported():
     h.upload_state(rho)
     h.init()
     h.step(2)
+    h.close()
+    # species in 2D: the reference's 2D transport collides wall cells
+    p2, walls2, rho2, _ = cases._sp(cases.with_specular(lambda: cases.porous_case(P.D2Q9, (1, 30, 26))), P.SRT)()
+    h = Handle(p2)
+    with pytest.raises(TxError) as e:
+        h.upload_walls(walls2)
+    assert e.value.code == 1 and "2D" in str(e.value)
     h.close()
     form = P.copy_params(p)
     form.exact = 0
