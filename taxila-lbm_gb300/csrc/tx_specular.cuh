@@ -28,8 +28,10 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -115,7 +117,9 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
   out->dst.clear();
   out->src.clear();
   const long long kInf = 1LL << 62;
-  for (int z = 1; z <= n[2]; ++z)
+  // One z-layer of owned slots (the chains only read the walls, so layers are
+  // independent); the error of a refused geometry, else null.
+  auto layer = [&](int z, std::vector<long long>& ldst, std::vector<long long>& lsrc) -> const char* {
     for (int y = 1; y <= n[1]; ++y)
       for (int x = 1; x <= n[0]; ++x) {
         const int T0[3] = {x, y, z};
@@ -215,11 +219,11 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
           }
           if (zero && std_zero) continue;
           if (!zero && !std_zero && sn == stdn && S[0] == stdX[0] && S[1] == stdX[1] && S[2] == stdX[2]) continue;
-          out->dst.push_back((long long)m * N + cell(T0));
+          ldst.push_back((long long)m * N + cell(T0));
           if (zero) {
-            out->src.push_back(-1);
+            lsrc.push_back(-1);
           } else if (walls[cell(S)] != 0.0) {
-            out->src.push_back((((long long)sn * N + cell(S)) << 1) | 1);  // a wall cell's content
+            lsrc.push_back((((long long)sn * N + cell(S)) << 1) | 1);  // a wall cell's content
           } else {
             // where the step kernel pushed P(sn, S): to S + c_sn when that is pore, else back into S as opp(sn)
             int Y[3], Yw[3];
@@ -229,10 +233,33 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
               slot = (long long)sn * N + cell(Yw);
             else
               slot = (long long)opp[sn] * N + cell(S);
-            out->src.push_back(slot << 1);
+            lsrc.push_back(slot << 1);
           }
         }
       }
+    return nullptr;
+  };
+  // The layers run on host threads; their lists are joined in layer order,
+  // the order one thread would produce.
+  const int nz = n[2];
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = (int)std::max(1u, std::min(hw ? hw : 1u, (unsigned)std::min(nz, 32)));
+  std::vector<std::vector<long long>> ld((size_t)nz), ls((size_t)nz);
+  std::vector<const char*> err((size_t)nz, nullptr);
+  std::atomic<int> next{0};
+  auto run_layers = [&]() {
+    for (int z = next.fetch_add(1); z < nz; z = next.fetch_add(1)) err[(size_t)z] = layer(z + 1, ld[(size_t)z], ls[(size_t)z]);
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nt; ++i) pool.emplace_back(run_layers);
+  run_layers();
+  for (std::thread& t : pool) t.join();
+  for (int z = 0; z < nz; ++z)
+    if (err[(size_t)z]) return err[(size_t)z];
+  for (int z = 0; z < nz; ++z) {
+    out->dst.insert(out->dst.end(), ld[(size_t)z].begin(), ld[(size_t)z].end());
+    out->src.insert(out->src.end(), ls[(size_t)z].begin(), ls[(size_t)z].end());
+  }
   // Keep the exceptions into pore cells, and those into wall slots that a chain
   // of wall-content moves links to a pore cell's P or to non-zero initial content.
   const size_t E = out->dst.size();
