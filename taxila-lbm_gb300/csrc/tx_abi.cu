@@ -57,7 +57,7 @@ struct tx_handle {
   long long spec_n = 0;
   long long* spec_dst = nullptr;
   long long* spec_src = nullptr;
-  double* spec_tmp = nullptr;
+  void* spec_tmp = nullptr;       // [exception][component], storage type
   int spec_fresh = 0;              // steps whose output buffer still needs its wall slots cleared
   int spec_fresh_sp = 0;           // the same for the species buffers
   // passive species (transport): populations, parameters, initial state
@@ -126,12 +126,12 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
   const long long ne = (long long)r.dst.size();
   if (ne > 0) {
     long long *d = nullptr, *s = nullptr;
-    double* t = nullptr;
+    void* t = nullptr;
     TX_CUDA(h, cudaMalloc(&d, (size_t)ne * sizeof(long long)));
     h->spec_dst = d;
     TX_CUDA(h, cudaMalloc(&s, (size_t)ne * sizeof(long long)));
     h->spec_src = s;
-    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * (h->S > h->NS ? h->S : h->NS) * sizeof(double)));
+    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * (h->S > h->NS ? h->S : h->NS) * h->pop_bytes));
     h->spec_tmp = t;
     TX_CUDA(h, cudaMemcpy(h->spec_dst, r.dst.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
     TX_CUDA(h, cudaMemcpy(h->spec_src, r.src.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
@@ -143,27 +143,52 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
 // After the step kernels (push with ordinary bounceback), before the density
 // pass: the specular-wall exceptions, for the ncomp components of state
 // buffers fin -> fout (the flow's, or the species', which stream and bounce
-// back alike).  The output buffer's wall slots are cleared on the first two
-// steps after an upload or init (fresh), so that wall slots no exception
-// writes hold zero in both state buffers.
-void spec_apply(tx_handle* h, const void* fin, void* fout, int ncomp, int& fresh) {
-  double* fo = static_cast<double*>(fout);
+// back alike; sh: their storage's rest state and scale).  The output buffer's
+// wall slots are emptied on the first two steps after an upload or init
+// (fresh), so that wall slots no exception writes are empty in both state buffers.
+// fin null: only empty the wall cells of fout.
+template <int D, class T>
+void spec_launch(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+  T* fo = static_cast<T*>(fout);
   const long long N = h->g.n;
   if (fresh > 0) {
-    k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, ncomp * h->Q);
+    k_spec_clear_walls<D, T><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, ncomp, sh);
     --fresh;
   }
   const long long ne = h->spec_n;
-  if (ne == 0) return;
+  if (ne == 0 || !fin) return;
   const unsigned grid = (unsigned)((ne + 255) / 256);
-  const long long QN = (long long)h->Q * N;
-  k_spec_gather<double><<<grid, 256, 0, h->stream>>>(static_cast<const double*>(fin), fo, h->spec_src, ne, ncomp, QN,
-                                                     h->spec_tmp);
-  k_spec_scatter<double><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, ncomp, QN, h->spec_tmp);
+  T* tmp = static_cast<T*>(h->spec_tmp);
+  k_spec_gather<D, T><<<grid, 256, 0, h->stream>>>(static_cast<const T*>(fin), fo, h->spec_src, h->spec_dst, ne, ncomp, N,
+                                                   sh, tmp);
+  k_spec_scatter<T><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, ncomp, (long long)h->Q * N, tmp);
 }
-void spec_pass(tx_handle* h, int in, int out) { spec_apply(h, h->f[in], h->f[out], h->S, h->spec_fresh); }
+template <int D>
+void spec_apply_d(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+  if (h->p.precision == TX_PREC_F64)
+    spec_launch<D, double>(h, fin, fout, ncomp, sh, fresh);
+  else if (h->p.precision == TX_PREC_F32)
+    spec_launch<D, float>(h, fin, fout, ncomp, sh, fresh);
+  else
+    spec_launch<D, __half>(h, fin, fout, ncomp, sh, fresh);
+}
+void spec_apply(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+  if (h->D == 3)
+    spec_apply_d<3>(h, fin, fout, ncomp, sh, fresh);
+  else
+    spec_apply_d<2>(h, fin, fout, ncomp, sh, fresh);
+}
+// the species' storage has no rest state
+Shift species_shift() {
+  Shift sh{};
+  sh.scale = 1.0;
+  return sh;
+}
+void spec_pass(tx_handle* h, int in, int out) {
+  spec_apply(h, h->f[in], h->f[out], h->S, shift_of(h->ph), h->spec_fresh);
+}
 void spec_pass_species(tx_handle* h, int in, int out) {
-  spec_apply(h, h->sg[in], h->sg[out], h->NS, h->spec_fresh_sp);
+  spec_apply(h, h->sg[in], h->sg[out], h->NS, species_shift(), h->spec_fresh_sp);
 }
 
 // Reference wall values -> device mask codes on the device (the rules of
@@ -599,8 +624,6 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
     return sync_stream(h);
   }
   // specular walls: codes and routes on the host
-  if (spec && h->p.precision != TX_PREC_F64)
-    return fail(h, TX_ERR_ARG, "specular (no-stick) wall codes 900-902 need the FP64 forms (precision TX_PREC_F64)");
   if (spec && h->NS > 0 && h->D == 2)
     return fail(h, TX_ERR_ARG,
                 "specular (no-stick) wall codes 900-901 are not supported with species transport in 2D "
@@ -757,9 +780,8 @@ int tx_init(tx_handle* h) {
     // FlowFiInit: the state buffer becomes (1 - P/2) feq of the initial moments
     if (h->spec) {
       // wall cells start empty (the reference's VecSet(fi, 0))
-      const long long N = h->g.n;
-      k_spec_clear_walls<double><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(static_cast<double*>(h->f[h->cur]),
-                                                                                     h->mask, N, h->S * h->Q);
+      int once = 1;
+      spec_apply(h, nullptr, h->f[h->cur], h->S, shift_of(h->ph), once);
     }
     h->ks.init(args(h, h->cur, h->cur), h->uic, h->stream);
     int rc = check_launch(h, "k_init");

@@ -35,7 +35,7 @@
 #include <utility>
 #include <vector>
 
-#include "tx_lattice.cuh"
+#include "tx_kernels.cuh"
 
 namespace tx {
 
@@ -305,17 +305,39 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
   return "";
 }
 
-// Every exception's source value, per component (pops: [(m * Q + n) * N + cell]).
-// Specular walls come with the FP64 forms only (plain, unshifted storage): T = double.
-template <class T>
-__global__ void __launch_bounds__(256) k_spec_gather(const T* fin, const T* fout, const long long* src, long long ne,
-                                                     int S, long long QN, T* tmp) {
+// The stored value of an empty population slot (f = 0): its deviation
+// (0 - w_n rho0_m) times the storage scale in the FP32/FP16 forms, zero in the
+// FP64 form (and for species, whose storage has no rest state: sh.rho0 = 0).
+template <int D, class T>
+__host__ __device__ inline T empty_slot(int m, int n, const Shift& sh) {
+  if constexpr (std::is_same<T, double>::value) {
+    return 0.0;
+  } else {
+    const double x = (0.0 - Lat<D>::w(n) * sh.rho0[m]) * sh.scale;
+    if constexpr (std::is_same<T, float>::value)
+      return (float)x;
+    else
+      return __float2half_rn((float)x);
+  }
+}
+
+// Every exception's source value, per component (pops: [(m * Q + n) * N + cell]):
+// a copy of the stored value (a slot of the same speed |c|, so of the same
+// weight and rest-state offset), or the empty value of the destination slot.
+template <int D, class T>
+__global__ void __launch_bounds__(256) k_spec_gather(const T* fin, const T* fout, const long long* src,
+                                                     const long long* dst, long long ne, int S, long long N, Shift sh,
+                                                     T* tmp) {
+  constexpr int Q = Lat<D>::Q;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const long long s = src[e];
   for (int m = 0; m < S; ++m) {
-    T v = T(0);
-    if (s >= 0) v = ((s & 1) ? fin : fout)[(long long)m * QN + (s >> 1)];
+    T v;
+    if (s >= 0)
+      v = ((s & 1) ? fin : fout)[(long long)m * Q * N + (s >> 1)];
+    else
+      v = empty_slot<D, T>(m, (int)(dst[e] / N), sh);
     tmp[e * S + m] = v;
   }
 }
@@ -328,13 +350,15 @@ __global__ void __launch_bounds__(256) k_spec_scatter(T* fout, const long long* 
   for (int m = 0; m < S; ++m) fout[(long long)m * QN + dst[e]] = tmp[e * S + m];
 }
 
-// Clears every wall cell's slots (after an upload or init, before the state
+// Empties every wall cell's slots (after an upload or init, before the state
 // buffers have both been written by a step with the routes above).
-template <class T>
-__global__ void __launch_bounds__(256) k_spec_clear_walls(T* f, const uint8_t* mask, long long N, int SQ) {
+template <int D, class T>
+__global__ void __launch_bounds__(256) k_spec_clear_walls(T* f, const uint8_t* mask, long long N, int S, Shift sh) {
+  constexpr int Q = Lat<D>::Q;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N || mask[i] == 0) return;
-  for (int q = 0; q < SQ; ++q) f[(long long)q * N + i] = T(0);
+  for (int m = 0; m < S; ++m)
+    for (int n = 0; n < Q; ++n) f[(long long)(m * Q + n) * N + i] = empty_slot<D, T>(m, n, sh);
 }
 
 }  // namespace tx

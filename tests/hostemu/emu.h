@@ -118,11 +118,10 @@ std::string run(const Case& c, Result& out) {
   else
     convert_phys(ph, &P);
 
-  // specular walls: single-lattice FP64 handles, species only in 3D (as tx_upload_walls)
+  // specular walls: single-lattice handles, species only in 3D (as tx_upload_walls)
   bool spec = false;
   for (long long i = 0; i < N; ++i) spec = spec || specular_axis(c.walls[(size_t)i], D) >= 0;
-  if (spec && (!std::is_same<T, double>::value || (p.nspecies > 0 && D == 2)))
-    return "specular (no-stick) wall codes 900-902 need the FP64 forms (and no species in 2D)";
+  if (spec && p.nspecies > 0 && D == 2) return "specular (no-stick) wall codes 900-901 with species need a 3D lattice";
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
@@ -147,7 +146,7 @@ std::string run(const Case& c, Result& out) {
     if (!why.empty()) return why;
   }
   const long long ne = (long long)routes.dst.size();
-  std::vector<double> spec_tmp((size_t)(ne * S + 1));
+  std::vector<T> spec_tmp((size_t)(ne * S + 1));
   const uint8_t* pop_mask = spec ? nullptr : mask.data();
   int spec_fresh = 2, spec_fresh_sp = 2;
   std::vector<uint32_t> links((size_t)N);
@@ -218,6 +217,7 @@ std::string run(const Case& c, Result& out) {
                 RT(eos_psi<double>(ph.eos[m], ph.eos_c[m], ph.g[m][m], ph.c0, c.init[(size_t)(i * S + m)]));
     const StepArgs a = args(cur, cur);
     launch3(g, 128, [&] { k_init<D, S, ISO, EXACT, T, R, RT>(a, nullptr); });
+    if (spec) launch1(N, 256, [&] { k_spec_clear_walls<D, T>(buf[cur], mask.data(), N, S, sh); });  // empty wall cells
   }
   // the density pass as the library launches it (16-byte loads when N allows)
   auto density = [&](const StepArgs& a, int mode) {
@@ -272,19 +272,17 @@ std::string run(const Case& c, Result& out) {
     } else {
       launch3(g, 128, [&] { k_step<D, S, ISO, MRT, EXACT, T, R, RT>(a); });
     }
-    if constexpr (std::is_same<T, double>::value) {
-      if (spec) {
-        // the library's specular-wall pass: clear the wall slots of a fresh buffer,
-        // then gather and scatter the exceptions to the ordinary push
-        double* fo = buf[1 - cur];
-        if (spec_fresh > 0) {
-          launch1(N, 256, [&] { k_spec_clear_walls<double>(fo, mask.data(), N, S * Q); });
-          --spec_fresh;
-        }
-        if (ne) {
-          launch1(ne, 256, [&] { k_spec_gather<double>(buf[cur], fo, routes.src.data(), ne, S, (long long)Q * N, spec_tmp.data()); });
-          launch1(ne, 256, [&] { k_spec_scatter<double>(fo, routes.dst.data(), ne, S, (long long)Q * N, spec_tmp.data()); });
-        }
+    if (spec) {
+      // the library's specular-wall pass: empty the wall slots of a fresh buffer,
+      // then gather and scatter the exceptions to the ordinary push
+      T* fo = buf[1 - cur];
+      if (spec_fresh > 0) {
+        launch1(N, 256, [&] { k_spec_clear_walls<D, T>(fo, mask.data(), N, S, sh); });
+        --spec_fresh;
+      }
+      if (ne) {
+        launch1(ne, 256, [&] { k_spec_gather<D, T>(buf[cur], fo, routes.src.data(), routes.dst.data(), ne, S, N, sh, spec_tmp.data()); });
+        launch1(ne, 256, [&] { k_spec_scatter<T>(fo, routes.dst.data(), ne, S, (long long)Q * N, spec_tmp.data()); });
       }
     }
     density(a, 0);
@@ -297,19 +295,20 @@ std::string run(const Case& c, Result& out) {
         launch3(g, 128, [&] { k_species<D, true, EXACT, T, R>(sa); });
       else
         launch3(g, 128, [&] { k_species<D, false, EXACT, T, R>(sa); });
-      if constexpr (std::is_same<T, double>::value) {
-        if (spec) {
-          // the species stream and bounce back as the flow does: the same exceptions
-          double* go = gbuf[1 - gcur];
-          if (spec_fresh_sp > 0) {
-            launch1(N, 256, [&] { k_spec_clear_walls<double>(go, mask.data(), N, NS * Q); });
-            --spec_fresh_sp;
-          }
-          if (ne) {
-            std::vector<double> stmp((size_t)(ne * NS + 1));
-            launch1(ne, 256, [&] { k_spec_gather<double>(gbuf[gcur], go, routes.src.data(), ne, NS, (long long)Q * N, stmp.data()); });
-            launch1(ne, 256, [&] { k_spec_scatter<double>(go, routes.dst.data(), ne, NS, (long long)Q * N, stmp.data()); });
-          }
+      if (spec) {
+        // the species stream and bounce back as the flow does: the same exceptions
+        // (their storage has no rest state)
+        Shift ssh{};
+        ssh.scale = 1.0;
+        T* go = gbuf[1 - gcur];
+        if (spec_fresh_sp > 0) {
+          launch1(N, 256, [&] { k_spec_clear_walls<D, T>(go, mask.data(), N, NS, ssh); });
+          --spec_fresh_sp;
+        }
+        if (ne) {
+          std::vector<T> stmp((size_t)(ne * NS + 1));
+          launch1(ne, 256, [&] { k_spec_gather<D, T>(gbuf[gcur], go, routes.src.data(), routes.dst.data(), ne, NS, N, ssh, stmp.data()); });
+          launch1(ne, 256, [&] { k_spec_scatter<T>(go, routes.dst.data(), ne, NS, (long long)Q * N, stmp.data()); });
         }
       }
       gcur = 1 - gcur;

@@ -10,8 +10,9 @@ exceptions to its ordinary push after the step kernel (csrc/tx_specular.cuh).
 * exact FP64 form: every cell's populations (wall cells included), densities,
   velocities and forces identical to the oracle bit for bit;
 * fast FP64 form: within 1e-12 relative;
-* restarts with populations in wall cells, and the forms and paths that
-  refuse these codes.
+* the FP32/FP16 forms within their bounds of the FP64 oracle;
+* restarts with populations in wall cells, and the paths that refuse these
+  codes (species in 2D, batches).
 """
 import numpy as np
 import pytest
@@ -112,6 +113,37 @@ def test_species_with_specular_walls(name, make, steps):
     o.close()
 
 
+FORM_TOL = {P.PREC_F32: 2e-5, P.PREC_F32_F16: 2e-3}
+
+
+@pytest.mark.parametrize("prec,rho0,scale", [(P.PREC_F32, 1.0, 1.0), (P.PREC_F32_F16, 1.0, 4096.0)],
+                         ids=["f32", "f32_f16"])
+def test_specular_walls_reduced_precision(prec, rho0, scale):
+    # deviation storage: exceptions copy stored values between slots of one
+    # speed, empty slots take the stored value of f = 0
+    p, walls, rho = cases.SPECULAR[0][1]()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.init()
+    o.step(6)
+    q = P.copy_params(p)
+    q.precision = prec
+    q.rho0[0] = rho0
+    q.storage_scale = scale
+    h = Handle(q)
+    h.upload_walls(walls)
+    h.upload_state(rho)
+    h.init()
+    h.step(6)
+    for f in (P.FIELD_FI, P.FIELD_RHO):
+        a, b = o.get(f), h.download(f)
+        err = float(np.max(np.abs(a - b)) / np.max(np.abs(a)))
+        assert err <= FORM_TOL[prec], (f, err)
+    h.close()
+    o.close()
+
+
 def test_specular_restart_with_wall_content():
     p, walls, rho = cases.specular_porous(P.D3Q19, (12, 10, 11), 8)
     o0 = Oracle(p)
@@ -135,15 +167,12 @@ def test_specular_larger_lattice_fast_form():
 
 def test_specular_walls_refused_where_unsupported():
     p, walls, rho = cases.SPECULAR[0][1]()
-    q = P.copy_params(p)
-    q.precision = P.PREC_F32
-    h = Handle(q)
-    with pytest.raises(TxError) as e:
-        h.upload_walls(walls)
-    assert e.value.code == 1 and "FP64" in str(e.value)
-    h.close()
-    # a refused upload leaves the handle usable with other walls
+    # a refused upload (a negative code) leaves the handle usable with other walls
     h = Handle(p)
+    bad = np.array(walls)
+    bad[0] = -3.0
+    with pytest.raises(TxError):
+        h.upload_walls(bad)
     h.upload_walls(np.where(walls >= 900.0, 1.0, walls))
     h.upload_state(rho)
     h.init()
