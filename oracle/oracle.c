@@ -388,6 +388,21 @@ static orc* orc_create_transport(const tx_params* p) {
   return t;
 }
 
+int orc_lattice(const tx_params* p, int* ci, double* w, int* mt, int* mmt, double* ffw, double* rate) {
+  orc* o = orc_create(p);
+  if (!o) return TX_ERR_ARG;
+  for (int n = 0; n < o->Q; ++n) {
+    for (int a = 0; a < 3; ++a) ci[n * 3 + a] = o->ci[n][a];
+    w[n] = o->w[n];
+    mmt[n] = o->mmt[n];
+    rate[n] = o->tau_mrt[0][n];
+    for (int k = 0; k < o->Q; ++k) mt[n * o->Q + k] = o->mt[n][k];
+  }
+  for (int i = 0; i < 12; ++i) ffw[i] = o->ffw[i];
+  orc_destroy(o);
+  return 0;
+}
+
 void orc_destroy(orc* o) {
   if (!o) return;
   orc_destroy(o->tr);

@@ -27,6 +27,11 @@ int orc_init(orc* o);
 int orc_step(orc* o, int nsteps);
 double orc_delta_norm(orc* o, int field);
 int orc_get(orc* o, int field, double* out);
+/* The lattice tables of an oracle built from p, for the tests that pin them
+ * to the reference source: ci[Q*3], w[Q], mt[Q*Q] (M^T(i,k) at i*Q+k),
+ * mmt[Q], ffw[12] (isotropy weights by |e|^2) and the MRT rate of every
+ * moment of component 0, rate[Q] (tau_mrt). */
+int orc_lattice(const tx_params* p, int* ci, double* w, int* mt, int* mmt, double* ffw, double* rate);
 long orc_field_size(const orc* o, int field);
 int orc_set_threads(int n);
 int orc_set_species(orc* o, const double* conc, const double* flux);

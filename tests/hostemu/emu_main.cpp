@@ -9,6 +9,7 @@
 // stderr), 3 when the combination is not compiled into the emulation.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <random>
@@ -65,8 +66,51 @@ static int norm_selftest() {
   return bad ? 1 : 0;
 }
 
+// emu lattice D iso: the library's lattice tables as it compiles them (Lat<D>)
+// and as fill_phys_impl sets them up (isotropy weights, MRT rate of every
+// moment with the seven rates told apart), one JSON object.
+static int lattice_dump(int D, int iso) {
+  tx_params p;
+  std::memset(&p, 0, sizeof(p));
+  p.discretization = D == 3 ? TX_D3Q19 : TX_D2Q9;
+  p.nx = p.ny = p.nz = 4;
+  p.ncomponents = 1;
+  p.relaxation_mode = TX_RELAX_MRT;
+  p.isotropy_order = iso;
+  p.tau[0] = 1.0;
+  p.mm[0] = 1.0;
+  p.s_c[0] = 1.01; p.s_e[0] = 1.02; p.s_e2[0] = 1.03; p.s_q[0] = 1.04;
+  p.s_nu[0] = 1.05; p.s_pi[0] = 1.06; p.s_m[0] = 1.07;
+  const int Q = D == 3 ? 19 : 9;
+  Phys P{};
+  fill_phys_impl(p, D, 1, Q, P);
+  auto c = [&](int n, int a) { return D == 3 ? Lat<3>::c(n, a) : Lat<2>::c(n, a); };
+  auto w = [&](int n) { return D == 3 ? Lat<3>::w(n) : Lat<2>::w(n); };
+  auto mt = [&](int i, int k) { return D == 3 ? Lat<3>::mt(i, k) : Lat<2>::mt(i, k); };
+  auto mmt = [&](int k) { return D == 3 ? Lat<3>::mmt(k) : Lat<2>::mmt(k); };
+  printf("{\"ci\": [");
+  for (int n = 0; n < Q; ++n) printf("%s[%d, %d, %d]", n ? ", " : "", c(n, 0), c(n, 1), c(n, 2));
+  printf("], \"w\": [");
+  for (int n = 0; n < Q; ++n) printf("%s%.17g", n ? ", " : "", w(n));
+  printf("], \"mt\": [");
+  for (int i = 0; i < Q; ++i) {
+    printf("%s[", i ? ", " : "");
+    for (int k = 0; k < Q; ++k) printf("%s%d", k ? ", " : "", mt(i, k));
+    printf("]");
+  }
+  printf("], \"mmt\": [");
+  for (int k = 0; k < Q; ++k) printf("%s%d", k ? ", " : "", mmt(k));
+  printf("], \"rate\": [");
+  for (int k = 0; k < Q; ++k) printf("%s%.17g", k ? ", " : "", P.srate[0][k]);
+  printf("], \"ffw\": [");
+  for (int i = 0; i < 12; ++i) printf("%s%.17g", i ? ", " : "", P.ffw[i]);
+  printf("]}\n");
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc == 2 && std::strcmp(argv[1], "norm") == 0) return norm_selftest();
+  if (argc == 4 && std::strcmp(argv[1], "lattice") == 0) return lattice_dump(std::atoi(argv[2]), std::atoi(argv[3]));
   if (argc != 3) {
     fprintf(stderr, "usage: emu case.bin result.bin\n");
     return 1;
