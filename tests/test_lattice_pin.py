@@ -127,3 +127,19 @@ def test_mrt_basis_is_orthogonal():
         mt = np.array(t["mt"])
         assert np.array_equal(mt.T @ mt, np.diag(t["mmt"]))
         assert np.all(mt[:, 0] == 1)
+
+
+def test_abi_constants_match_reference():
+    # the boundary-condition kinds and relaxation modes cross the C ABI as the
+    # reference's own integer codes (include/lbm_definitions.h)
+    defs = os.path.join(cases.REF, "include/lbm_definitions.h")
+    if not os.path.exists(defs):
+        pytest.skip("reference tree not present")
+    ref = {m.group(1): int(m.group(2))
+           for m in re.finditer(r"PetscInt,\s*parameter\s*::\s*(\w+)\s*=\s*(-?\d+)", open(defs).read())}
+    header = open(os.path.join(os.path.dirname(HERE), "include", "taxila_gb300.h")).read()
+    ours = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+TX_(BC_\w+|RELAX_\w+)\s+(-?\d+)", header)}
+    names = {k: ("RELAXATION_MODE_" + k[6:] if k.startswith("RELAX_") else k) for k in ours}
+    assert len(ours) >= 14
+    for k, v in ours.items():
+        assert ref[names[k]] == v, (k, v, ref.get(names[k]))
