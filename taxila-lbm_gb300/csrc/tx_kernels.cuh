@@ -896,6 +896,48 @@ __device__ __forceinline__ void pair_axis_sums(const R v[npairs<D>()], R j[D]) {
   });
 }
 
+// The pair (index p of pair_n) of direction n, and the axis pairs (a, b) of
+// the diagonal directions: ab 0 = (x, y), 1 = (x, z), 2 = (y, z).
+template <int D>
+__host__ __device__ constexpr int pair_of(int n) {
+  for (int p = 0; p < npairs<D>(); ++p)
+    if (pair_n<D>(p) == n || opp<D>(pair_n<D>(p)) == n) return p;
+  return -1;
+}
+__host__ __device__ constexpr int ab_a(int ab) { return ab == 2 ? 1 : 0; }
+__host__ __device__ constexpr int ab_b(int ab) { return ab == 0 ? 1 : 2; }
+template <int D>
+__host__ __device__ constexpr int n_ab() { return D == 3 ? 3 : 1; }
+
+// sum over the s_nu moments k of coef(k) ck[k], coef a compile-time function
+// of k given by CF::at (zero and unit coefficients cost nothing).
+template <int D, class CF, class R>
+__device__ __forceinline__ R snu_lincomb(const R ck[Lat<D>::Q]) {
+  R acc = R(-0.0);
+  sfor<0, Lat<D>::Q>([&](auto kk) {
+    constexpr int k = decltype(kk)::value;
+    if constexpr (rate_of<D>(k) == R_NU) {
+      constexpr double c = CF::at(k);
+      if constexpr (c == 1.0) acc = acc + ck[k];
+      else if constexpr (c == -1.0) acc = acc - ck[k];
+      else if constexpr (c != 0.0) acc = acc + R(c) * ck[k];
+    }
+  });
+  return acc;
+}
+template <int D, int d>
+struct SnuAxis {  // B_k(d, d): the correction of the axis pair along d
+  static constexpr double at(int k) { return stress_b<D>(k, d, d); }
+};
+template <int D, int ab>
+struct SnuDiagSum {  // B_k(a, a) + B_k(b, b)
+  static constexpr double at(int k) { return stress_b<D>(k, ab_a(ab), ab_a(ab)) + stress_b<D>(k, ab_b(ab), ab_b(ab)); }
+};
+template <int D, int ab>
+struct SnuDiagOff {  // 2 B_k(a, b)
+  static constexpr double at(int k) { return 2.0 * stress_b<D>(k, ab_a(ab), ab_b(ab)); }
+};
+
 // Fast-form flux of one component from pair differences f_n - f_opp(n).
 template <int D, class R>
 __device__ __forceinline__ void pop_flux_pairs(const R f[Lat<D>::Q], R j[D]) {
@@ -1269,36 +1311,70 @@ __device__ __forceinline__ void step_site(const StepArgs& a, int x, int y, int z
           R vF[D];
 #pragma unroll
           for (int d = 0; d < D; ++d) vF[d] = F[m][d] - Xh * up[d];
+          // each s_nu moment is a quadratic form B_k of c (stress_b): over the
+          // axis pairs B_k(d, d), over the two diagonal pairs of axes (a, b)
+          // B_k(a, a) + B_k(b, b) times their sum and 2 B_k(a, b) times their difference
+          R sg[n_ab<D>()], dg[n_ab<D>()];
+          sfor<0, n_ab<D>()>([&](auto ii) {
+            constexpr int ab = decltype(ii)::value;
+            constexpr int pp = pair_of<D>(diag_dir<D>(ab_a(ab), ab_b(ab), 1));
+            constexpr int pm = pair_of<D>(diag_dir<D>(ab_a(ab), ab_b(ab), -1));
+            sg[ab] = gs[pp] + gs[pm];
+            dg[ab] = gs[pp] - gs[pm];
+          });
           sfor<0, Q>([&](auto kk) {
             constexpr int kq = decltype(kk)::value;
             if constexpr (rate_of<D>(kq) == R_NU) {
               R md = R(-0.0);
-              sfor<0, NP>([&](auto pp) {
-                constexpr int p = decltype(pp)::value;
-                constexpr int v = L::mt(pair_n<D>(p), kq);
-                if constexpr (v == 1) md = md + gs[p];
-                else if constexpr (v == -1) md = md - gs[p];
-                else if constexpr (v != 0) md = md + R(v) * gs[p];
+              sfor<0, D>([&](auto dd) {
+                constexpr int d = decltype(dd)::value;
+                constexpr double c = stress_b<D>(kq, d, d);
+                if constexpr (c == 1.0) md = md + gs[pair_of<D>(axis_dir<D>(d))];
+                else if constexpr (c == -1.0) md = md - gs[pair_of<D>(axis_dir<D>(d))];
+                else if constexpr (c != 0.0) md = md + R(c) * gs[pair_of<D>(axis_dir<D>(d))];
+              });
+              sfor<0, n_ab<D>()>([&](auto ii) {
+                constexpr int ab = decltype(ii)::value;
+                constexpr double cs = SnuDiagSum<D, ab>::at(kq), cd = SnuDiagOff<D, ab>::at(kq);
+                if constexpr (cs == 1.0) md = md + sg[ab];
+                else if constexpr (cs == -1.0) md = md - sg[ab];
+                else if constexpr (cs != 0.0) md = md + R(cs) * sg[ab];
+                if constexpr (cd == 1.0) md = md + dg[ab];
+                else if constexpr (cd == -1.0) md = md - dg[ab];
+                else if constexpr (cd != 0.0) md = md + R(cd) * dg[ab];
               });
               md = md + stress_form<D, kq, R>(up, vF);
               ck[kq] = P.dspec[m][kq] * md;
             }
           });
         }
+        // the correction of each pair, sum_k ck_k mt(n, k): B(d, d) on the axis
+        // pairs; on a diagonal pair e_a + s e_b, (B(a, a) + B(b, b)) + s 2 B(a, b)
+        R cax[D], csum[n_ab<D>()], coff[n_ab<D>()];
+        sfor<0, D>([&](auto dd) {
+          constexpr int d = decltype(dd)::value;
+          cax[d] = snu_lincomb<D, SnuAxis<D, d>, R>(ck);
+        });
+        sfor<0, n_ab<D>()>([&](auto ii) {
+          constexpr int ab = decltype(ii)::value;
+          csum[ab] = snu_lincomb<D, SnuDiagSum<D, ab>, R>(ck);
+          coff[ab] = snu_lincomb<D, SnuDiagOff<D, ab>, R>(ck);
+        });
         const bool k0 = keep == R(0);
         push(std::integral_constant<int, 0>{}, m, k0 ? X0 : keep * pop(std::integral_constant<int, 0>{}) + X0);
         sfor<0, NP>([&](auto pp) {
           constexpr int p = decltype(pp)::value, n = pair_n<D>(p), nb = opp<D>(n);
-          R corr = R(-0.0);
-          sfor<0, Q>([&](auto kk) {
-            constexpr int kq = decltype(kk)::value;
-            if constexpr (rate_of<D>(kq) == R_NU) {
-              constexpr int v = L::mt(n, kq);
-              if constexpr (v == 1) corr = corr + ck[kq];
-              else if constexpr (v == -1) corr = corr - ck[kq];
-              else if constexpr (v != 0) corr = corr + R(v) * ck[kq];
-            }
-          });
+          R corr;
+          if constexpr (n <= L::NAXIS) {
+            constexpr int d = L::c(n, 0) != 0 ? 0 : (L::c(n, 1) != 0 ? 1 : 2);
+            corr = cax[d];
+          } else {
+            constexpr int a = L::c(n, 0) != 0 ? 0 : 1;
+            constexpr int b = (a == 0 && L::c(n, 1) != 0) ? 1 : 2;
+            constexpr int ab = a == 0 ? (b == 1 ? 0 : 1) : 2;
+            constexpr int sgn = L::c(n, a) * L::c(n, b);
+            corr = sgn > 0 ? csum[ab] + coff[ab] : csum[ab] - coff[ab];
+          }
           const R h = cdot_z<D, n>(kF);
           const R vn = En[p] * (G + h) - corr, vb = Eb[p] * (G - h) - corr;
           if (k0) {

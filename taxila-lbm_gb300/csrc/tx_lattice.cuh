@@ -216,4 +216,47 @@ __host__ __device__ constexpr bool stress_class_free() {
 }
 static_assert(stress_class_free<3>() && stress_class_free<2>(), "s_nu moments must vanish on class constants");
 
+// The direction with velocity (x, y, z), -1 if none.
+template <int D>
+__host__ __device__ constexpr int dir_of(int x, int y, int z) {
+  for (int n = 0; n < Lat<D>::Q; ++n)
+    if (Lat<D>::c(n, 0) == x && Lat<D>::c(n, 1) == y && (D == 3 ? Lat<D>::c(n, 2) : 0) == z) return n;
+  return -1;
+}
+template <int D>
+__host__ __device__ constexpr int axis_dir(int d) {
+  return dir_of<D>(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0);
+}
+// The direction e_a + s e_b (a != b, s = +-1).
+template <int D>
+__host__ __device__ constexpr int diag_dir(int a, int b, int s) {
+  int v[3] = {0, 0, 0};
+  v[a] = 1;
+  v[b] = s;
+  return dir_of<D>(v[0], v[1], v[2]);
+}
+
+// An s_nu moment k is a quadratic form of the velocity: mt(n, k) =
+// sum_de stress_b(k, d, e) c_n,d c_n,e, with the diagonal from the axis
+// directions and the off-diagonal from the diagonal directions.
+template <int D>
+__host__ __device__ constexpr double stress_b(int k, int d, int e) {
+  if (d == e) return Lat<D>::mt(axis_dir<D>(d), k);
+  return 0.5 * (Lat<D>::mt(diag_dir<D>(d, e, 1), k) - Lat<D>::mt(axis_dir<D>(d), k) - Lat<D>::mt(axis_dir<D>(e), k));
+}
+template <int D>
+__host__ __device__ constexpr bool stress_quadratic() {
+  for (int k = 0; k < Lat<D>::Q; ++k) {
+    if (rate_of<D>(k) != R_NU) continue;
+    for (int n = 0; n < Lat<D>::Q; ++n) {
+      double q = 0.0;
+      for (int d = 0; d < D; ++d)
+        for (int e = 0; e < D; ++e) q += stress_b<D>(k, d, e) * Lat<D>::c(n, d) * Lat<D>::c(n, e);
+      if (q != Lat<D>::mt(n, k)) return false;
+    }
+  }
+  return true;
+}
+static_assert(stress_quadratic<3>() && stress_quadratic<2>(), "s_nu moments must be quadratic forms of c");
+
 }  // namespace tx
