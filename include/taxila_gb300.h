@@ -183,9 +183,9 @@ const char* tx_last_error(const tx_handle* h);
  * (lbm_distribution_function.F90:668-784): their routes are resolved on the
  * host at upload, and wall cells then hold populations, which tx_upload_fi,
  * tx_download, tx_delta_norm and tx_conservation include (species
- * populations too, which stream through the same sweep).  With species they
- * need a 3D lattice (TX_ERR_ARG otherwise); batches and tx_step_static refuse
- * them.  A refused upload leaves the handle's walls unchanged. */
+ * populations too, which stream through the same sweep).  Batches and
+ * tx_step_static refuse them (TX_ERR_ARG).  A refused upload leaves the
+ * handle's walls unchanged. */
 int tx_upload_walls(tx_handle* h, const double* walls);
 
 /* The initialize_state plugin's output (src/lbm/lbm.F90:444-453): rho

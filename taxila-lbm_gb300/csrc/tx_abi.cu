@@ -178,6 +178,18 @@ void spec_apply(tx_handle* h, const void* fin, void* fout, int ncomp, const Shif
   else
     spec_apply_d<2>(h, fin, fout, ncomp, sh, fresh);
 }
+// the species kernels' arguments: populations read from state in, written to state out
+SpeciesArgs species_args(tx_handle* h, int in, int out) {
+  SpeciesArgs a{};
+  a.gin = h->sg[in];
+  a.gout = h->sg[out];
+  a.links = h->links;
+  a.mask = h->mask;
+  a.phys = h->d_sphys;
+  a.g = h->g;
+  a.ns = h->NS;
+  return a;
+}
 // the species' storage has no rest state
 Shift species_shift() {
   Shift sh{};
@@ -188,6 +200,8 @@ void spec_pass(tx_handle* h, int in, int out) {
   spec_apply(h, h->f[in], h->f[out], h->S, shift_of(h->ph), h->spec_fresh);
 }
 void spec_pass_species(tx_handle* h, int in, int out) {
+  // in 2D the reference collides wall cells, which hold populations here
+  if (h->D == 2) h->ss.wall_collide(species_args(h, in, in), h->stream);
   spec_apply(h, h->sg[in], h->sg[out], h->NS, species_shift(), h->spec_fresh_sp);
 }
 
@@ -360,18 +374,6 @@ int sync_stream(tx_handle* h) {
 }
 
 // populations of state cur -> natural order staging
-SpeciesArgs species_args(tx_handle* h, int in, int out) {
-  SpeciesArgs a{};
-  a.gin = h->sg[in];
-  a.gout = h->sg[out];
-  a.links = h->links;
-  a.mask = h->mask;
-  a.phys = h->d_sphys;
-  a.g = h->g;
-  a.ns = h->NS;
-  return a;
-}
-
 int stage_field(tx_handle* h, int field) {
   const long long N = h->g.n;
   if (field >= TX_FIELD_SPECIES_FI && field <= TX_FIELD_SPECIES_FLUX) {
@@ -624,10 +626,6 @@ int tx_upload_walls(tx_handle* h, const double* walls) {
     return sync_stream(h);
   }
   // specular walls: codes and routes on the host
-  if (spec && h->NS > 0 && h->D == 2)
-    return fail(h, TX_ERR_ARG,
-                "specular (no-stick) wall codes 900-901 are not supported with species transport in 2D "
-                "(the reference's 2D transport collides wall cells)");
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;

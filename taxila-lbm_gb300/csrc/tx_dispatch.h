@@ -43,6 +43,7 @@ struct SpeciesSet {
   void (*init)(const SpeciesArgs&, const double* conc, const double* flux, cudaStream_t);
   void (*fields)(const SpeciesArgs&, int what, double* out, cudaStream_t);
   void (*step_tiles)(const BatchArgs&, int flip, int grid, dim3 block, cudaStream_t);  // no-op in the exact form
+  void (*wall_collide)(const SpeciesArgs&, cudaStream_t);  // 2D with specular walls: collide wall cells in gout
 };
 bool species_d3_exact(bool mrt, SpeciesSet* ss);
 bool species_d2_exact(bool mrt, SpeciesSet* ss);

@@ -33,16 +33,19 @@ struct SpeciesLaunch {
   static void step_tiles(const BatchArgs& b, int flip, int grid, dim3 blk, cudaStream_t s) {
     if constexpr (!TX_EXACT) k_species_tiles<TX_D, MRT, TX_T, TX_R><<<grid, blk, 0, s>>>(b, flip);
   }
+  static void wall_collide(const SpeciesArgs& a, cudaStream_t s) {
+    k_species_wall_collide<TX_D, MRT, TX_T, TX_R><<<launch3(a.g, 128).grid, launch3(a.g, 128).block, 0, s>>>(a);
+  }
 };
 }  // namespace
 
 bool TX_SPECIES_FN(bool mrt, SpeciesSet* ss) {
   if (mrt)
     *ss = SpeciesSet{&SpeciesLaunch<true>::step, &SpeciesLaunch<true>::init, &SpeciesLaunch<true>::fields,
-                     &SpeciesLaunch<true>::step_tiles};
+                     &SpeciesLaunch<true>::step_tiles, &SpeciesLaunch<true>::wall_collide};
   else
     *ss = SpeciesSet{&SpeciesLaunch<false>::step, &SpeciesLaunch<false>::init, &SpeciesLaunch<false>::fields,
-                     &SpeciesLaunch<false>::step_tiles};
+                     &SpeciesLaunch<false>::step_tiles, &SpeciesLaunch<false>::wall_collide};
   return true;
 }
 #endif

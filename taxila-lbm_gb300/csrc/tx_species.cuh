@@ -259,6 +259,60 @@ __global__ void __launch_bounds__(128) k_species_init(SpeciesArgs a_in, const do
   }
 }
 
+// TransportCollisionD2 collides the cells with walls > 0 (lbm_transport.F90:450)
+// toward the equilibrium of their moments, which are zero on walls, so their
+// equilibrium is zero too.  Wall cells hold populations only next to specular
+// walls; this is their collision there, in the operation order of the exact
+// form (SRT g - (g - 0) / tau; MRT with the differences g - 0), in place in
+// a.gout, before the specular exceptions read them.
+template <int D, bool MRT, class T, class R>
+__global__ void __launch_bounds__(128) k_species_wall_collide(SpeciesArgs a_in) {
+  using L = Lat<D>;
+  constexpr int Q = L::Q;
+  const SpeciesArgs a = a_in;
+  const SpeciesPhysT<R>& P = *reinterpret_cast<const SpeciesPhysT<R>*>(a.phys);
+  int x, y, z;
+  long long idx;
+  if (!site_of(a.g, x, y, z, idx)) return;
+  if (__ldg(a.mask + idx) == 0) return;
+  T* g0 = reinterpret_cast<T*>(a.gout);
+  for (int s = 0; s < a.ns; ++s) {
+    const SpecieRelax<R>& sr = P.sp[s];
+    R g[Q];
+#pragma unroll
+    for (int n = 0; n < Q; ++n) g[n] = ld_sp<T, R>(g0 + (long long)(s * Q + n) * a.g.n + idx, P);
+    if constexpr (!MRT) {
+#pragma unroll
+      for (int n = 0; n < Q; ++n) g[n] = g[n] - (g[n] - R(0)) / sr.tau;
+    } else {
+      R dfi[Q];
+#pragma unroll
+      for (int n = 0; n < Q; ++n) dfi[n] = g[n] - R(0);
+      sfor<0, Q>([&](auto kk) {
+        constexpr int k = decltype(kk)::value;
+        R md = R(0);
+        sfor<0, Q>([&](auto ii) {
+          constexpr int i = decltype(ii)::value;
+          constexpr int v = L::mt(i, k);
+          if constexpr (v == 1) md = md + dfi[i];
+          else if constexpr (v == -1) md = md - dfi[i];
+          else if constexpr (v != 0) md = md + R(v) * dfi[i];
+        });
+        const R coef = sr.srate[k] * md / R(L::mmt(k));
+        sfor<0, Q>([&](auto ii) {
+          constexpr int i = decltype(ii)::value;
+          constexpr int v = L::mt(i, k);
+          if constexpr (v == 1) g[i] = g[i] - coef;
+          else if constexpr (v == -1) g[i] = g[i] + coef;
+          else if constexpr (v != 0) g[i] = g[i] - coef * R(v);
+        });
+      });
+    }
+#pragma unroll
+    for (int n = 0; n < Q; ++n) st_sp<T, R>(g0 + (long long)(s * Q + n) * a.g.n + idx, g[n], P);
+  }
+}
+
 // Species fields in natural order: what 9 populations, 10 concentration,
 // 11 flux (zero on walls, as TransportUpdateMoments).  With a.mask null every
 // cell's populations are read (wall cells hold populations next to specular

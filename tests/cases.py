@@ -368,4 +368,6 @@ def _sp_specular(make, mode, ns=1, seed=6):
 SPECIES_SPECULAR = [
     ("d3_srt_species_specular", _sp_specular(lambda: porous_case(P.D3Q19, (12, 10, 14), body=True), P.SRT), 20),
     ("d3_mrt_two_species_specular", _sp_specular(lambda: porous_case(P.D3Q19, (10, 12, 12), mode=P.MRT), P.MRT, ns=2), 15),
+    # 2D: the reference collides wall cells, and the species near the walls move on within a few steps
+    ("d2_species_specular", _sp_specular(lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), P.SRT), 3),
 ]

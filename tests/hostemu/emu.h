@@ -118,10 +118,9 @@ std::string run(const Case& c, Result& out) {
   else
     convert_phys(ph, &P);
 
-  // specular walls: single-lattice handles, species only in 3D (as tx_upload_walls)
+  // specular walls (as tx_upload_walls)
   bool spec = false;
   for (long long i = 0; i < N; ++i) spec = spec || specular_axis(c.walls[(size_t)i], D) >= 0;
-  if (spec && p.nspecies > 0 && D == 2) return "specular (no-stick) wall codes 900-901 with species need a 3D lattice";
   std::vector<uint8_t> mask((size_t)N);
   for (long long i = 0; i < N; ++i) {
     const char* why = nullptr;
@@ -300,6 +299,14 @@ std::string run(const Case& c, Result& out) {
         // (their storage has no rest state)
         Shift ssh{};
         ssh.scale = 1.0;
+        if (D == 2) {
+          // the reference's 2D transport collides wall cells, which hold populations here
+          SpeciesArgs wa = sargs(gcur, gcur);
+          if (p.species_relaxation_mode == TX_RELAX_MRT)
+            launch3(g, 128, [&] { k_species_wall_collide<D, true, T, R>(wa); });
+          else
+            launch3(g, 128, [&] { k_species_wall_collide<D, false, T, R>(wa); });
+        }
         T* go = gbuf[1 - gcur];
         if (spec_fresh_sp > 0) {
           launch1(N, 256, [&] { k_spec_clear_walls<D, T>(go, mask.data(), N, NS, ssh); });
