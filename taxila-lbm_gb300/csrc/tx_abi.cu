@@ -120,7 +120,9 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
   const int n[3] = {h->g.nx, h->g.ny, h->g.nz};
   bool pre[6];
   for (int f = 0; f < 6; ++f) pre[f] = face_has_values(h->p, h->D, f);
-  const std::string why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, pre, init_nz, &r);
+  // 2D species under MRT: their wall cells' collision mixes the cells' slots
+  const bool mix = h->D == 2 && h->NS > 0 && h->p.species_relaxation_mode == TX_RELAX_MRT;
+  const std::string why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, pre, init_nz, mix, &r);
   if (!why.empty()) return fail(h, TX_ERR_ARG, why);
   free_spec(h);
   const long long ne = (long long)r.dst.size();

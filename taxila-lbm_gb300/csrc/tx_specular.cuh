@@ -61,7 +61,10 @@ struct SpecRoutes {
 // per: periodic axes; prestream: faces XM..ZP whose boundary condition copies
 // populations into the ghost layer before the stream (BCPreStream,
 // lbm_bc.F90:613-779); init_nz: sorted slots (n * N + cell) of wall cells
-// whose initial content is not zero (uploaded populations), or null.  Returns
+// whose initial content is not zero (uploaded populations), or null;
+// cell_mix: wall cells are collided, and a collision that mixes their slots
+// (the 2D species' MRT toward a zero equilibrium) makes every slot of a wall
+// cell live once one of them is.  Returns
 // "" or the reason the geometry is refused (a slot whose value would come
 // from outside what the reference defines).
 //
@@ -71,7 +74,7 @@ struct SpecRoutes {
 // they do with ordinary walls alone; their exceptions are dropped, so the
 // list stays proportional to the specular walls' neighbourhood.
 inline std::string specular_routes(const double* walls, int D, const int n[3], const int per[3], const bool prestream[6],
-                                   const std::vector<long long>* init_nz, SpecRoutes* out) {
+                                   const std::vector<long long>* init_nz, bool cell_mix, SpecRoutes* out) {
   const int Q = D == 3 ? 19 : 9;
   int c[19][3], opp[19], refl[3][19];
   for (int q = 0; q < Q; ++q)
@@ -217,7 +220,9 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
               stdn = opp[m];
             }
           }
-          if (zero && std_zero) continue;
+          // (with cell_mix a wall cell's zero slots are listed too: its
+          // collision may have written them in place)
+          if (zero && std_zero && !cell_mix) continue;
           if (!zero && !std_zero && sn == stdn && S[0] == stdX[0] && S[1] == stdX[1] && S[2] == stdX[2]) continue;
           ldst.push_back((long long)m * N + cell(T0));
           if (zero) {
@@ -278,13 +283,32 @@ inline std::string specular_routes(const double* walls, int D, const int n[3], c
     if (s >= 0 && (s & 1) && is_wall_slot(out->dst[e])) readers.emplace_back(s >> 1, e);
   }
   std::sort(readers.begin(), readers.end());
-  auto wake = [&](long long slot) {
+  auto wake_slot = [&](long long slot) {
     auto it = std::lower_bound(readers.begin(), readers.end(), std::make_pair(slot, (size_t)0));
     for (; it != readers.end() && it->first == slot; ++it)
       if (!live[it->second]) {
         live[it->second] = 1;
         work.push_back(it->second);
       }
+  };
+  // cell_mix: liveness per wall cell; a live cell keeps the exceptions read
+  // from any of its slots and those into all of its slots (the zero ones too)
+  std::vector<std::pair<long long, size_t>> writers;  // (wall cell written, exception)
+  std::vector<char> cell_live;
+  if (cell_mix) {
+    cell_live.assign((size_t)N, 0);
+    for (size_t e = 0; e < E; ++e)
+      if (is_wall_slot(out->dst[e])) writers.emplace_back(out->dst[e] % N, e);
+    std::sort(writers.begin(), writers.end());
+  }
+  auto wake = [&](long long slot) {
+    if (!cell_mix) return wake_slot(slot);
+    const long long cell = slot % N;
+    if (cell_live[(size_t)cell]) return;
+    cell_live[(size_t)cell] = 1;
+    for (int q = 0; q < Q; ++q) wake_slot((long long)q * N + cell);
+    auto it = std::lower_bound(writers.begin(), writers.end(), std::make_pair(cell, (size_t)0));
+    for (; it != writers.end() && it->first == cell; ++it) live[it->second] = 1;
   };
   if (init_nz)
     for (long long s : *init_nz) wake(s);

@@ -357,8 +357,8 @@ SPECULAR_BCS = [(name, with_specular(make), steps) for name, make, steps in BCS]
 
 
 def _sp_specular(make, mode, ns=1, seed=6):
-    """_sp with half of the wall cells specular (3D: the species stream and
-    bounce back through the same sweep)."""
+    """_sp with half of the wall cells specular (the species stream and bounce
+    back through the same sweep; in 2D their wall cells are also collided)."""
     def f():
         p, w, r = with_specular(make, seed)()
         return p, w, r, with_species(p, w, mode=mode, ns=ns)
@@ -370,4 +370,5 @@ SPECIES_SPECULAR = [
     ("d3_mrt_two_species_specular", _sp_specular(lambda: porous_case(P.D3Q19, (10, 12, 12), mode=P.MRT), P.MRT, ns=2), 15),
     # 2D: the reference collides wall cells, and the species near the walls move on within a few steps
     ("d2_species_specular", _sp_specular(lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), P.SRT), 3),
+    ("d2_mrt_species_specular", _sp_specular(lambda: porous_case(P.D2Q9, (1, 28, 30), mode=P.MRT, iso=8), P.MRT, seed=9), 12),
 ]

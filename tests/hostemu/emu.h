@@ -141,7 +141,8 @@ std::string run(const Case& c, Result& out) {
               }
     bool pre[6];
     for (int f = 0; f < 6; ++f) pre[f] = face_has_values(p, D, f);
-    const std::string why = specular_routes(c.walls.data(), D, nn, g.per, pre, &init_nz, &routes);
+    const bool mix = D == 2 && p.nspecies > 0 && p.species_relaxation_mode == TX_RELAX_MRT;
+    const std::string why = specular_routes(c.walls.data(), D, nn, g.per, pre, &init_nz, mix, &routes);
     if (!why.empty()) return why;
   }
   const long long ne = (long long)routes.dst.size();

@@ -317,8 +317,9 @@ def test_emulated_specular_walls_with_exterior_bcs(emu_exe, tmp_path, name, make
 
 @pytest.mark.parametrize("name,make,steps", cases.SPECIES_SPECULAR, ids=[c[0] for c in cases.SPECIES_SPECULAR])
 def test_emulated_species_with_specular_walls(emu_exe, tmp_path, name, make, steps):
-    # in 3D the species stream and bounce back through the flow's sweep: the
-    # same exceptions move their populations, wall cells included
+    # the species stream and bounce back through the flow's sweep: the same
+    # exceptions move their populations, wall cells included; in 2D the wall
+    # cells are also collided (under MRT that mixes their slots)
     p, walls, rho, conc = make()
     o = Oracle(p)
     o.set_walls(walls)
