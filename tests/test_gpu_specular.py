@@ -192,3 +192,38 @@ def test_specular_walls_download_as_uploaded():
     h.upload_walls(walls)
     assert np.array_equal(h.download(P.FIELD_WALLS), walls)
     h.close()
+
+
+SPECIES_FORM_CASES = [("d3_mrt_two_species_specular", P.PREC_F32, 6), ("d3_mrt_two_species_specular", P.PREC_F32_F16, 6),
+                      ("d2_species_specular", P.PREC_F32, 10), ("d2_mrt_species_specular", P.PREC_F32, 12)]
+
+
+@pytest.mark.parametrize("name,prec,steps", SPECIES_FORM_CASES, ids=["d3_mrt_f32", "d3_mrt_f16", "d2_srt_f32", "d2_mrt_f32"])
+def test_species_specular_reduced_precision(name, prec, steps):
+    # species (no rest state: empty slots store zero) next to the flow's
+    # deviation storage, each component's rest density at its mean
+    p, walls, rho, conc = dict((c[0], c[1]) for c in cases.SPECIES_SPECULAR)[name]()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.set_species(conc)
+    o.init()
+    o.step(steps)
+    q = P.copy_params(p)
+    q.exact = 0
+    q.precision = prec
+    q.storage_scale = 4096.0 if prec == P.PREC_F32_F16 else 1.0
+    for m in range(p.ncomponents):
+        q.rho0[m] = float(np.mean(np.asarray(rho).reshape(-1, p.ncomponents)[:, m]))
+    h = Handle(q)
+    h.upload_walls(walls)
+    h.upload_state(rho)
+    h.upload_species(conc)
+    h.init()
+    h.step(steps)
+    for f in (P.FIELD_FI, P.FIELD_SPECIES_FI, P.FIELD_SPECIES_RHO):
+        a, b = o.get(f), h.download(f)
+        err = float(np.max(np.abs(a - b)) / np.max(np.abs(a)))
+        assert err <= FORM_TOL[prec], (f, err)
+    h.close()
+    o.close()

@@ -363,3 +363,35 @@ def test_emulated_specular_walls_reduced_precision(emu_exe, tmp_path, name, prec
         a, b = ref[k], got[k]
         err = float(np.max(np.abs(a - b)) / np.max(np.abs(a)))
         assert err <= FORM_TOL[prec][k], "%s: max rel err %.3e" % (k, err)
+
+
+SPECIES_FORM_CASES = [("d3_mrt_two_species_specular", P.PREC_F32, 6), ("d3_mrt_two_species_specular", P.PREC_F32_F16, 6),
+                      ("d2_species_specular", P.PREC_F32, 10)]
+
+
+@pytest.mark.parametrize("name,prec,steps", SPECIES_FORM_CASES, ids=["d3_mrt_f32", "d3_mrt_f16", "d2_srt_f32"])
+def test_emulated_species_specular_reduced_precision(emu_exe, tmp_path, name, prec, steps):
+    # species in the FP32/FP16 forms (no rest state: their empty slots store
+    # zero) next to the flow's deviation storage, with each component's rest
+    # density at its mean; species and flow populations within the forms' bounds
+    p, walls, rho, conc = dict((c[0], c[1]) for c in cases.SPECIES_SPECULAR)[name]()
+    o = Oracle(p)
+    o.set_walls(walls)
+    o.set_state(rho)
+    o.set_species(conc)
+    o.init()
+    o.step(steps)
+    ref = {"fi": o.get(P.FIELD_FI), "sfi": o.get(P.FIELD_SPECIES_FI), "srho": o.get(P.FIELD_SPECIES_RHO)}
+    o.close()
+    assert np.abs(ref["sfi"].reshape(p.nsites, -1)[np.asarray(walls) > 0]).sum() > 0.0
+    q = P.copy_params(p)
+    q.exact = 0
+    q.precision = prec
+    q.storage_scale = 4096.0 if prec == P.PREC_F32_F16 else 1.0
+    for m in range(p.ncomponents):
+        q.rho0[m] = float(np.mean(np.asarray(rho).reshape(-1, p.ncomponents)[:, m]))
+    got = run_emu(emu_exe, q, walls, rho, steps, False, tmp_path, conc=conc)
+    tol = FORM_TOL[prec]["fi"]
+    for k, v in ref.items():
+        err = float(np.max(np.abs(v - got[k])) / np.max(np.abs(v)))
+        assert err <= tol, "%s: max rel err %.3e" % (k, err)
