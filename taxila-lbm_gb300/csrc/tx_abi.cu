@@ -54,10 +54,10 @@ struct tx_handle {
   // (tx_specular.cuh), resolved at wall upload; wall cells then hold populations
   bool spec = false;
   std::vector<double> spec_walls;  // the uploaded wall values, for re-resolving at tx_upload_fi
-  long long spec_n = 0;
-  long long* spec_dst = nullptr;
-  long long* spec_src = nullptr;
-  void* spec_tmp = nullptr;       // [exception][component], storage type
+  // the flow's exceptions, and the species' (no BCPreStream copies: their
+  // transport applies no boundary condition; 2D MRT: wall cells' slots mix)
+  SpecList spec_fl, spec_sp;
+  void* spec_tmp = nullptr;       // [exception][component], storage type, shared
   int spec_fresh = 0;              // steps whose output buffer still needs its wall slots cleared
   int spec_fresh_sp = 0;           // the same for the species buffers
   // passive species (transport): populations, parameters, initial state
@@ -105,40 +105,43 @@ int check_launch(tx_handle* h, const char* what) {
 const uint8_t* pop_mask(const tx_handle* h) { return h->spec ? nullptr : h->mask; }
 
 void free_spec(tx_handle* h) {
-  cudaFree(h->spec_dst);
-  cudaFree(h->spec_src);
+  for (SpecList* l : {&h->spec_fl, &h->spec_sp}) {
+    cudaFree(l->dst);
+    cudaFree(l->src);
+    *l = SpecList{};
+  }
   cudaFree(h->spec_tmp);
-  h->spec_dst = h->spec_src = nullptr;
   h->spec_tmp = nullptr;
-  h->spec_n = 0;
 }
 
 // Resolves the specular-wall routes of the uploaded walls (init_nz: wall slots
 // with non-zero initial content) and puts the exception list on the device.
 int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
-  SpecRoutes r;
+  SpecRoutes r, rs;
   const int n[3] = {h->g.nx, h->g.ny, h->g.nz};
   bool pre[6];
+  const bool none[6] = {false, false, false, false, false, false};
   for (int f = 0; f < 6; ++f) pre[f] = face_has_values(h->p, h->D, f);
-  // 2D species under MRT: their wall cells' collision mixes the cells' slots
-  const bool mix = h->D == 2 && h->NS > 0 && h->p.species_relaxation_mode == TX_RELAX_MRT;
-  const std::string why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, pre, init_nz, mix, &r);
+  std::string why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, pre, init_nz, false, &r);
+  if (why.empty() && h->NS > 0) {
+    // the species start from their equilibrium (empty wall cells); in 2D under
+    // MRT their wall cells' collision mixes the cells' slots
+    const bool mix = h->D == 2 && h->p.species_relaxation_mode == TX_RELAX_MRT;
+    why = specular_routes(h->spec_walls.data(), h->D, n, h->g.per, none, nullptr, mix, &rs);
+  }
   if (!why.empty()) return fail(h, TX_ERR_ARG, why);
   free_spec(h);
-  const long long ne = (long long)r.dst.size();
-  if (ne > 0) {
-    long long *d = nullptr, *s = nullptr;
-    void* t = nullptr;
-    TX_CUDA(h, cudaMalloc(&d, (size_t)ne * sizeof(long long)));
-    h->spec_dst = d;
-    TX_CUDA(h, cudaMalloc(&s, (size_t)ne * sizeof(long long)));
-    h->spec_src = s;
-    TX_CUDA(h, cudaMalloc(&t, (size_t)ne * (h->S > h->NS ? h->S : h->NS) * h->pop_bytes));
-    h->spec_tmp = t;
-    TX_CUDA(h, cudaMemcpy(h->spec_dst, r.dst.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
-    TX_CUDA(h, cudaMemcpy(h->spec_src, r.src.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
+  const long long tmp_n = std::max((long long)r.dst.size() * h->S, (long long)rs.dst.size() * h->NS);
+  if (tmp_n > 0) TX_CUDA(h, cudaMalloc(&h->spec_tmp, (size_t)tmp_n * h->pop_bytes));
+  for (auto [l, rr] : {std::make_pair(&h->spec_fl, &r), std::make_pair(&h->spec_sp, &rs)}) {
+    const long long ne = (long long)rr->dst.size();
+    if (ne == 0) continue;
+    TX_CUDA(h, cudaMalloc(&l->dst, (size_t)ne * sizeof(long long)));
+    TX_CUDA(h, cudaMalloc(&l->src, (size_t)ne * sizeof(long long)));
+    l->n = ne;
+    TX_CUDA(h, cudaMemcpy(l->dst, rr->dst.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
+    TX_CUDA(h, cudaMemcpy(l->src, rr->src.data(), (size_t)ne * sizeof(long long), cudaMemcpyHostToDevice));
   }
-  h->spec_n = ne;
   return TX_OK;
 }
 
@@ -150,35 +153,34 @@ int upload_spec_routes(tx_handle* h, const std::vector<long long>* init_nz) {
 // (fresh), so that wall slots no exception writes are empty in both state buffers.
 // fin null: only empty the wall cells of fout.
 template <int D, class T>
-void spec_launch(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+void spec_launch(tx_handle* h, const SpecList& L, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
   T* fo = static_cast<T*>(fout);
   const long long N = h->g.n;
   if (fresh > 0) {
     k_spec_clear_walls<D, T><<<(unsigned)((N + 255) / 256), 256, 0, h->stream>>>(fo, h->mask, N, ncomp, sh);
     --fresh;
   }
-  const long long ne = h->spec_n;
+  const long long ne = L.n;
   if (ne == 0 || !fin) return;
   const unsigned grid = (unsigned)((ne + 255) / 256);
   T* tmp = static_cast<T*>(h->spec_tmp);
-  k_spec_gather<D, T><<<grid, 256, 0, h->stream>>>(static_cast<const T*>(fin), fo, h->spec_src, h->spec_dst, ne, ncomp, N,
-                                                   sh, tmp);
-  k_spec_scatter<T><<<grid, 256, 0, h->stream>>>(fo, h->spec_dst, ne, ncomp, (long long)h->Q * N, tmp);
+  k_spec_gather<D, T><<<grid, 256, 0, h->stream>>>(static_cast<const T*>(fin), fo, L.src, L.dst, ne, ncomp, N, sh, tmp);
+  k_spec_scatter<T><<<grid, 256, 0, h->stream>>>(fo, L.dst, ne, ncomp, (long long)h->Q * N, tmp);
 }
 template <int D>
-void spec_apply_d(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+void spec_apply_d(tx_handle* h, const SpecList& L, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
   if (h->p.precision == TX_PREC_F64)
-    spec_launch<D, double>(h, fin, fout, ncomp, sh, fresh);
+    spec_launch<D, double>(h, L, fin, fout, ncomp, sh, fresh);
   else if (h->p.precision == TX_PREC_F32)
-    spec_launch<D, float>(h, fin, fout, ncomp, sh, fresh);
+    spec_launch<D, float>(h, L, fin, fout, ncomp, sh, fresh);
   else
-    spec_launch<D, __half>(h, fin, fout, ncomp, sh, fresh);
+    spec_launch<D, __half>(h, L, fin, fout, ncomp, sh, fresh);
 }
-void spec_apply(tx_handle* h, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
+void spec_apply(tx_handle* h, const SpecList& L, const void* fin, void* fout, int ncomp, const Shift& sh, int& fresh) {
   if (h->D == 3)
-    spec_apply_d<3>(h, fin, fout, ncomp, sh, fresh);
+    spec_apply_d<3>(h, L, fin, fout, ncomp, sh, fresh);
   else
-    spec_apply_d<2>(h, fin, fout, ncomp, sh, fresh);
+    spec_apply_d<2>(h, L, fin, fout, ncomp, sh, fresh);
 }
 // the species kernels' arguments: populations read from state in, written to state out
 SpeciesArgs species_args(tx_handle* h, int in, int out) {
@@ -199,12 +201,12 @@ Shift species_shift() {
   return sh;
 }
 void spec_pass(tx_handle* h, int in, int out) {
-  spec_apply(h, h->f[in], h->f[out], h->S, shift_of(h->ph), h->spec_fresh);
+  spec_apply(h, h->spec_fl, h->f[in], h->f[out], h->S, shift_of(h->ph), h->spec_fresh);
 }
 void spec_pass_species(tx_handle* h, int in, int out) {
   // in 2D the reference collides wall cells, which hold populations here
   if (h->D == 2) h->ss.wall_collide(species_args(h, in, in), h->stream);
-  spec_apply(h, h->sg[in], h->sg[out], h->NS, species_shift(), h->spec_fresh_sp);
+  spec_apply(h, h->spec_sp, h->sg[in], h->sg[out], h->NS, species_shift(), h->spec_fresh_sp);
 }
 
 // Reference wall values -> device mask codes on the device (the rules of
@@ -781,7 +783,7 @@ int tx_init(tx_handle* h) {
     if (h->spec) {
       // wall cells start empty (the reference's VecSet(fi, 0))
       int once = 1;
-      spec_apply(h, nullptr, h->f[h->cur], h->S, shift_of(h->ph), once);
+      spec_apply(h, h->spec_fl, nullptr, h->f[h->cur], h->S, shift_of(h->ph), once);
     }
     h->ks.init(args(h, h->cur, h->cur), h->uic, h->stream);
     int rc = check_launch(h, "k_init");

@@ -55,6 +55,12 @@ __host__ __device__ inline int specular_axis(double v, int D) {
 struct SpecRoutes {
   std::vector<long long> dst, src;
 };
+// an exception list on the device
+struct SpecList {
+  long long n = 0;
+  long long* dst = nullptr;
+  long long* src = nullptr;
+};
 
 // Resolves every owned slot (see the file comment).  walls: the reference's
 // wall values in natural order (x fastest); n: lattice sides (n[2] = 1 in 2D);

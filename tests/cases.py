@@ -372,3 +372,11 @@ SPECIES_SPECULAR = [
     ("d2_species_specular", _sp_specular(lambda: porous_case(P.D2Q9, (1, 30, 26), body=True), P.SRT), 3),
     ("d2_mrt_species_specular", _sp_specular(lambda: porous_case(P.D2Q9, (1, 28, 30), mode=P.MRT, iso=8), P.MRT, seed=9), 12),
 ]
+
+# species with specular walls next to exterior BCs: the flow's BCPreStream
+# copies fill its ghost layer, the species' transport applies no boundary
+# condition, so their exceptions differ there
+_SPB = dict((c[0], c) for c in BCS)
+SPECIES_SPECULAR_BCS = [(name + ("_mrt" if mode == P.MRT else "_srt") + "_species", _sp_specular(_SPB[name][1], mode), _SPB[name][2])
+                        for name, mode in (("d3_reflect_momentum", P.SRT), ("d3_reflect_momentum", P.MRT),
+                                           ("d3_flux_velocity_mrt", P.MRT), ("d2_momentum_flux_eos", P.MRT))]

@@ -126,7 +126,7 @@ std::string run(const Case& c, Result& out) {
     const char* why = nullptr;
     if (!wall_code(c.walls[(size_t)i], p.nminerals, &mask[(size_t)i], &why, D, spec)) return why;
   }
-  SpecRoutes routes;
+  SpecRoutes routes, sroutes;  // the flow's, and the species' (no BCPreStream copies)
   if (spec) {
     const int nn[3] = {g.nx, g.ny, g.nz};
     std::vector<long long> init_nz;  // wall slots with uploaded content
@@ -141,8 +141,12 @@ std::string run(const Case& c, Result& out) {
               }
     bool pre[6];
     for (int f = 0; f < 6; ++f) pre[f] = face_has_values(p, D, f);
-    const bool mix = D == 2 && p.nspecies > 0 && p.species_relaxation_mode == TX_RELAX_MRT;
-    const std::string why = specular_routes(c.walls.data(), D, nn, g.per, pre, &init_nz, mix, &routes);
+    std::string why = specular_routes(c.walls.data(), D, nn, g.per, pre, &init_nz, false, &routes);
+    if (why.empty() && p.nspecies > 0) {
+      const bool none[6] = {false, false, false, false, false, false};
+      const bool mix = D == 2 && p.species_relaxation_mode == TX_RELAX_MRT;
+      why = specular_routes(c.walls.data(), D, nn, g.per, none, nullptr, mix, &sroutes);
+    }
     if (!why.empty()) return why;
   }
   const long long ne = (long long)routes.dst.size();
@@ -296,8 +300,8 @@ std::string run(const Case& c, Result& out) {
       else
         launch3(g, 128, [&] { k_species<D, false, EXACT, T, R>(sa); });
       if (spec) {
-        // the species stream and bounce back as the flow does: the same exceptions
-        // (their storage has no rest state)
+        // the species stream and bounce back as the flow does, through their own
+        // exception list (their storage has no rest state)
         Shift ssh{};
         ssh.scale = 1.0;
         if (D == 2) {
@@ -313,10 +317,11 @@ std::string run(const Case& c, Result& out) {
           launch1(N, 256, [&] { k_spec_clear_walls<D, T>(go, mask.data(), N, NS, ssh); });
           --spec_fresh_sp;
         }
-        if (ne) {
-          std::vector<T> stmp((size_t)(ne * NS + 1));
-          launch1(ne, 256, [&] { k_spec_gather<D, T>(gbuf[gcur], go, routes.src.data(), routes.dst.data(), ne, NS, N, ssh, stmp.data()); });
-          launch1(ne, 256, [&] { k_spec_scatter<T>(go, routes.dst.data(), ne, NS, (long long)Q * N, stmp.data()); });
+        const long long nes = (long long)sroutes.dst.size();
+        if (nes) {
+          std::vector<T> stmp((size_t)(nes * NS + 1));
+          launch1(nes, 256, [&] { k_spec_gather<D, T>(gbuf[gcur], go, sroutes.src.data(), sroutes.dst.data(), nes, NS, N, ssh, stmp.data()); });
+          launch1(nes, 256, [&] { k_spec_scatter<T>(go, sroutes.dst.data(), nes, NS, (long long)Q * N, stmp.data()); });
         }
       }
       gcur = 1 - gcur;
