@@ -380,3 +380,45 @@ _SPB = dict((c[0], c) for c in BCS)
 SPECIES_SPECULAR_BCS = [(name + ("_mrt" if mode == P.MRT else "_srt") + "_species", _sp_specular(_SPB[name][1], mode), _SPB[name][2])
                         for name, mode in (("d3_reflect_momentum", P.SRT), ("d3_reflect_momentum", P.MRT),
                                            ("d3_flux_velocity_mrt", P.MRT), ("d2_momentum_flux_eos", P.MRT))]
+
+
+def random_specular(seed):
+    """A seeded random configuration with specular walls: D2Q9 or D3Q19, random
+    periodic axes, wall fraction and codes, one or two components, SRT or MRT,
+    optional exterior BCs (one component), optional species (SRT or MRT, one or
+    two) and a random step count.  Returns (p, walls, rho, conc or None, steps,
+    restart_steps): restart_steps > 0 asks for a restart from the populations
+    after that many steps."""
+    rng = np.random.default_rng(1000 + seed)
+    D = 3 if rng.random() < 0.5 else 2
+    disc = P.D3Q19 if D == 3 else P.D2Q9
+    shape = tuple(int(v) for v in rng.integers(5, 12, size=3)) if D == 3 else (1, int(rng.integers(6, 22)), int(rng.integers(6, 22)))
+    per = tuple(int(v) for v in rng.integers(0, 2, size=3))
+    ncomp = int(rng.integers(1, 3))
+    codes = [1.0, 900.0, 901.0, 902.0] if D == 3 else [1.0, 2.0, 900.0, 901.0]
+    p, walls, rho = specular_case(disc, shape, per, ncomp, codes, float(rng.uniform(0.1, 0.45)), int(rng.integers(0, 10**6)))
+    p.nminerals = 2
+    if D == 3 and rng.random() < 0.4:
+        p.relaxation_mode = P.MRT
+    elif D == 2 and ncomp == 2 and rng.random() < 0.4:
+        p.relaxation_mode, p.isotropy_order = P.MRT, 8
+    if ncomp == 1 and rng.random() < 0.6:
+        for a in range(D):
+            if per[a]:
+                continue
+            for f in (2 * a, 2 * a + 1):
+                r = rng.random()
+                if r < 0.25:
+                    p.bc_flags[f], p.bc_data[f][0] = P.BC_DENSITY, 1.0 + 0.02 * rng.random()
+                elif r < 0.45:
+                    p.bc_flags[f], p.bc_data[f][0] = P.BC_FLUX, 0.001 * (1 if f % 2 == 0 else -1)
+                elif r < 0.6 and not (D == 2 and f == 0):
+                    p.bc_flags[f] = P.BC_REFLECTING
+    sp = int(rng.integers(0, 3))
+    conc = None
+    if sp:
+        conc = with_species(p, walls, mode=P.SRT if sp == 1 else P.MRT, ns=int(rng.integers(1, 3)),
+                            front=int(rng.integers(1, 5)))
+    steps = int(rng.integers(1, 14))
+    restart = int(rng.integers(1, 5)) if rng.random() < 0.5 else 0
+    return p, walls, rho, conc, steps, restart

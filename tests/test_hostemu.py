@@ -420,3 +420,42 @@ def test_emulated_species_specular_with_exterior_bcs(emu_exe, tmp_path, name, ma
         assert np.all(np.isfinite(v)), k
         bad = int(np.sum(np.abs(v - got[k]) > tol * np.max(np.abs(v))))
         assert bad == 0, "%s: %d values differ" % (k, bad)
+
+
+@pytest.mark.parametrize("seed", range(32))
+def test_emulated_specular_random_configurations(emu_exe, tmp_path, seed):
+    # seeded random lattices with specular walls among ordinary ones: periodic
+    # axes, components, relaxation, exterior BCs, species and restarts with
+    # wall content drawn at random; every cell bit for bit
+    p, walls, rho, conc, steps, restart = cases.random_specular(seed)
+    init, from_fi = rho, False
+    if restart:
+        o0 = Oracle(p)
+        o0.set_walls(walls)
+        o0.set_state(rho)
+        o0.init()
+        o0.step(restart)
+        init, from_fi = o0.get(P.FIELD_FI), True
+        o0.close()
+    o = Oracle(p)
+    o.set_walls(walls)
+    if from_fi:
+        o.set_fi(init)
+    else:
+        o.set_state(rho)
+    if conc is not None:
+        o.set_species(conc)
+    o.init()
+    o.step(steps)
+    fields = {"fi": P.FIELD_FI, "rho": P.FIELD_RHO, "flux": P.FIELD_FLUX}
+    if conc is not None:
+        fields.update({"sfi": P.FIELD_SPECIES_FI, "srho": P.FIELD_SPECIES_RHO})
+    ref = {k: o.get(f) for k, f in fields.items()}
+    o.close()
+    q = P.copy_params(p)
+    q.exact = 1
+    got = run_emu(emu_exe, q, walls, init, steps, from_fi, tmp_path, conc=conc)
+    for k, v in ref.items():
+        assert np.all(np.isfinite(v)), k
+        bad = int(np.sum(v != got[k]))
+        assert bad == 0, "%s: %d values differ" % (k, bad)
