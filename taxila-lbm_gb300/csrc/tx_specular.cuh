@@ -25,6 +25,14 @@
 // source (a pore cell's P sits where the step kernel pushed it; a wall cell's
 // content sits in the previous state buffer), then k_spec_scatter writes them,
 // so no exception reads a slot another one overwrites.
+//
+// Passive species stream and bounce back through the same sweep with a list
+// of their own: the transport applies no boundary condition (LBMRun2,
+// src/lbm/lbm.F90:348-352), so their chains never end at a face's BCPreStream
+// copy.  In 2D the transport also collides the wall cells toward a zero
+// equilibrium (TransportCollisionD2, src/lbm/lbm_transport.F90:433-458);
+// under MRT that mixes a wall cell's slots, and their list then keeps every
+// slot of a wall cell that can hold content (cell_mix).
 #pragma once
 
 #include <algorithm>
